@@ -1,0 +1,55 @@
+#!/usr/bin/env bash
+# Regenerates the mechanism and gas-model fixtures under tests/golden/mech/.
+#
+# It builds the reference's own vendored Lua 5.4.3 + lpeg (extern/lua-5.4.3) in a
+# scratch directory, assembles the species database exactly as
+# src/gas/species-database/makefile does, and runs the reference's pre-processors
+# prep_gas.lua and prep_chem.lua on the mechanism inputs.  The machine-readable
+# files it writes are what the reference's D code reads at run time
+# (src/kinetics/chemistry_update.d:42-137, src/gas/composite_gas.d:37-120).
+# The reference's own sample data used by its unit tests is copied verbatim.
+#
+# Usage: tests/golden/make_fixtures.sh [REFERENCE_DIR]   (needs gcc and make)
+set -euo pipefail
+REF=${1:-/root/reference}
+HERE=$(cd "$(dirname "$0")" && pwd)
+OUT=$HERE/mech
+WORK=$(mktemp -d /tmp/gdtk_fixtures.XXXXXX)
+trap 'rm -rf "$WORK"' EXIT
+
+cp -r "$REF/extern/lua-5.4.3" "$WORK/lua"
+chmod -R u+w "$WORK/lua"
+(cd "$WORK/lua" && make linux local > "$WORK/lua-build.log" 2>&1)
+LUA=$WORK/lua/install/bin/dgd-lua
+
+mkdir -p "$WORK/dgd/data" "$WORK/dgd/lib"
+(cd "$REF/src/gas/species-database" && awk '$1 !~ "#" {print $1}' < species-list.txt | xargs cat defaults.lua) \
+    > "$WORK/dgd/data/species-database.lua"
+cp "$REF/src/gas/species-database/species-list.txt" "$WORK/dgd/data/"
+cp "$REF/src/kinetics/reaction.lua" "$REF/src/kinetics/lex_elems.lua" "$REF/src/kinetics/mechanism.lua" "$WORK/dgd/lib/"
+export DGD=$WORK/dgd
+export DGD_LUA_PATH="$WORK/dgd/lib/?.lua;;"
+export DGD_LUA_CPATH="$WORK/lua/install/lib/?.so;;"
+
+mkdir -p "$OUT"
+prep() {  # name gas-input mechanism-input
+    (cd "$WORK" && "$LUA" "$REF/src/gas/prep_gas.lua" "$2" "$1-gas.lua" > /dev/null \
+        && "$LUA" "$REF/src/kinetics/prep_chem.lua" "$1-gas.lua" "$3" "$1-chem.lua" > /dev/null)
+    # Drop the time-stamp comment so that regenerated files compare equal.
+    grep -v '^-- Auto-generated' "$WORK/$1-gas.lua" > "$OUT/$1-gas.lua"
+    cp "$WORK/$1-chem.lua" "$OUT/$1-chem.lua"
+}
+KIN=$REF/examples/kinetics
+prep park5  "$HERE/inputs/air5-park.inp"                              "$HERE/inputs/park5-arrhenius.lua"
+prep j92    "$KIN/hydrogen-ignition-delay/Jachimowski-1992-species.inp" "$KIN/hydrogen-ignition-delay/Jachimowski-1992.lua"
+prep n2     "$KIN/fixed-volume-reactor-n2/nitrogen-2sp.inp"            "$KIN/fixed-volume-reactor-n2/nitrogen-2sp-2r-Keq.lua"
+prep gupta5 "$KIN/air-chemistry-1T/air-5sp-1T.inp"                     "$KIN/air-chemistry-1T/GuptaEtAl-air-reactions.lua"
+
+# Sample data of the reference's unit tests (known-answer tests).
+cp "$REF/src/kinetics/sample-input/H2-I2-HI.lua" "$OUT/h2i2-gas.lua"
+cp "$REF/src/kinetics/sample-input/H2-I2-inp.lua" "$OUT/h2i2-chem.lua"
+cp "$REF/src/kinetics/sample-input/N2-diss.lua" "$OUT/n2-diss-rate.lua"
+cp "$REF/src/gas/sample-data/O-thermo.lua" "$OUT/O-thermo.lua"
+cp "$REF/src/gas/sample-data/therm-perf-5-species-air.lua" "$OUT/tpg-air5-gas.lua"
+chmod u+w "$OUT"/*.lua
+echo "fixtures written to $OUT"

@@ -1,0 +1,172 @@
+"""Pins the CPU oracle against every known-answer test the reference holds for this path.
+
+Each expected value and tolerance below is the reference's own assertion (file:line in
+the gdtk source tree).  The oracle must reproduce all of them before it is trusted as
+the checker for the CUDA kernels.
+"""
+import math
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import mech, GOLDEN
+
+R_universal = 8.31451
+
+
+def close(a, b, rel):
+    return math.isclose(a, b, rel_tol=rel)
+
+
+def approx_equal_numbers(a, b, tol):
+    # nm/number.d approxEqualNumbers: relative test with the same tolerance as absolute floor
+    return abs(a - b) <= tol * max(abs(a), abs(b)) or abs(a - b) <= tol
+
+
+@pytest.fixture(scope="module")
+def o_thermo(tmp_path_factory):
+    # cea_thermo_curves.d:194-199: a single curve for O with R = 8.31451/0.0159994.
+    from oracle.luatable import read_lua_file, array
+    t = read_lua_file(mech("O-thermo.lua"))['CEA_coeffs']
+    d = tmp_path_factory.mktemp("othermo")
+    body = ["species = {'O', }", "db = {}", "db['O'] = {}", "db['O'].M = 0.0159994", "db['O'].thermoCoeffs = {",
+            "  nsegments = %d," % t['nsegments'],
+            "  T_break_points = {%s}," % ", ".join(repr(x) for x in array(t['T_break_points'])),
+            "  T_blend_ranges = {%s}," % ", ".join(repr(x) for x in array(t['T_blend_ranges']))]
+    for s in range(t['nsegments']):
+        body.append("  segment%d = {%s}," % (s, ", ".join(repr(x) for x in array(t['segment%d' % s]))))
+    body.append("}")
+    path = d / "O-gas.lua"
+    path.write_text("\n".join(body) + "\n")
+    return oracle.Oracle(str(path))
+
+
+def test_cea_curve_oxygen(o_thermo):
+    # cea_thermo_curves.d:201-206
+    cp, _, _ = o_thermo.species_thermo(0, 500.0)
+    assert close(1328.627, cp, 1.0e-6)
+    _, h, _ = o_thermo.species_thermo(0, 3700.0)
+    assert close(20_030_794.683, h, 1.0e-6)
+    _, _, s = o_thermo.species_thermo(0, 10_000.0)
+    assert close(14_772.717, s, 1.0e-3)
+
+
+def test_thermally_perfect_air5():
+    # therm_perf_gas_mix.d:491-504 (and composite_gas.d:281-288)
+    o = oracle.Oracle(mech("tpg-air5-gas.lua"))
+    mf = np.full((1, 5), 0.2)
+    rho, u = o.update_thermo_from_pT([1.0e6], [2000.0], mf)
+    assert approx_equal_numbers(11801825.6, u[0], 1.0e-6)
+    assert approx_equal_numbers(1.2840117, rho[0], 1.0e-6)
+    T, p, st = o.update_thermo_from_rhou([2.0], [14.0e6], mf, [2000.0])
+    assert st[0] == 0
+    assert approx_equal_numbers(3373757.4, p[0], 1.0e-6)
+    assert approx_equal_numbers(4331.944, T[0], 1.0e-6)
+    # updateFromRhoT (therm_perf_gas_mix.d:506-510): p = rho R T and u(T)
+    rho2, u2 = o.update_thermo_from_pT([5841068.3], [10000.0], mf)
+    assert approx_equal_numbers(1.5, rho2[0], 1.0e-6)
+    assert approx_equal_numbers(20340105.9, u2[0], 1.0e-6)
+
+
+def test_arrhenius_rate_constants(tmp_path):
+    # rate_constant.d:604-617.  Test 2 reads sample-input/N2-diss.lua.
+    from oracle.luatable import read_lua_file
+    r = read_lua_file(mech("n2-diss-rate.lua"))['rate']
+    A, n, C = r['A'], r['n'], r['C']
+    chem = tmp_path / "chem.lua"
+    chem.write_text(
+        "species = {[0]='H2', [1]='I2', [2]='HI', }\n"
+        "config = {maxSubcycles=50, maxAttempts=2, tightTempCoupling=false,\n"
+        "  tempLimits={lower=100.0, upper=1.0e5}, odeStep={method='rkf', errTol=1.0e-3}}\n"
+        "reaction = {}\n"
+        "reaction[1] = {type='elementary', frc={model='Arrhenius', A=%r, n=0.0, C=20620.0},\n"
+        "  brc={model='Arrhenius', A=%r, n=%r, C=%r}, reacIdx={0,1}, reacCoeffs={1,1}, prodIdx={2}, prodCoeffs={2}}\n"
+        % (1.94e14 * 1e-6, A, n, C))
+    o = oracle.Oracle(mech("h2i2-gas.lua"), str(chem))
+    kf, _ = o.rate_constants(700.0)
+    assert close(3.10850956e-5, kf[0], 1.0e-2)
+    _, kb = o.rate_constants(4000.0)
+    assert close(0.00159439, kb[0], 1.0e-5)
+
+
+def test_reaction_mechanism_rates():
+    # reaction_mechanism.d:264-283 and reaction.d:538-556
+    o = oracle.Oracle(mech("h2i2-gas.lua"), os.path.join(GOLDEN, "inputs", "h2i2-kat-chem.lua"))
+    q, L, wf, wb = o.split_rates(700.0, np.array([4.54, 4.54, 0.0]))
+    rates = q - L
+    for got, want in zip(rates, [-643.9303, -643.9303, 1287.8606]):
+        assert close(want, got, 1.0e-6)
+    # production(2) = 2 w_f, loss(0) = loss(1) = w_f, production(0) = loss(2) = 0 (w_b = 0)
+    assert close(1287.8606, q[2], 1.0e-6) and close(643.9303, L[0], 1.0e-6) and close(643.9303, L[1], 1.0e-6)
+    assert q[0] == 0.0 and q[1] == 0.0 and L[2] == 0.0
+
+
+@pytest.fixture(scope="module")
+def h2i2():
+    return oracle.Oracle(mech("h2i2-gas.lua"), mech("h2i2-chem.lua"))
+
+
+def test_rkf_order(h2i2):
+    # chemistry_update.d:695-713: error ratio 1.96809 when dt shrinks by 2^(-1/5)
+    analytical = 7.1420197868416215
+    c0 = 4.54
+    y0, _ = h2i2.integrate_fixed('rkf', 700.0, [c0, c0, 0.0], 287.175, 60_000.0)
+    y1, _ = h2i2.integrate_fixed('rkf', 700.0, [c0, c0, 0.0], 287.175 * 2.0 ** (-1.0 / 5.0), 60_000.0)
+    assert close(1.96809, (analytical - y0[2]) / (analytical - y1[2]), 1.0e-4)
+
+
+def test_alpha_qss_order(h2i2):
+    # chemistry_update.d:715-734 (the reference constructs the step with eps1 1e-3, eps2 5e-4,
+    # delta 1e-10, maxIters 10, the defaults this oracle uses for alpha-qss)
+    analytical = 7.1420197868416215
+    c0 = 4.54
+    y0, _ = h2i2.integrate_fixed('alpha-qss', 700.0, [c0, c0, 0.0], 2.0, 60_000.0)
+    y1, _ = h2i2.integrate_fixed('alpha-qss', 700.0, [c0, c0, 0.0], 1.0, 60_000.0)
+    assert close(7.1420197868416215, y1[2], 1.0e-4)
+    assert close(4.001, (analytical - y0[2]) / (analytical - y1[2]), 1.0e-4)
+
+
+def test_full_chemistry_update(h2i2):
+    # chemistry_update.d:736-750: the complete update over 60,000 s from dtSuggest = 200
+    T = 700.0
+    c0 = 4.54
+    p = 2.0 * c0 * R_universal * T
+    M = h2i2.M
+    molef = np.array([0.5, 0.5, 0.0])
+    mix = float(np.dot(molef, M))
+    massf = molef * M / mix
+    rho, u = h2i2.update_thermo_from_pT([p], [T], massf[None, :])
+    out = h2i2.chem_update(rho, u, [T], [p], massf[None, :], [200.0], 60_000.0,
+                           update_thermo=False, retry=False)
+    assert out['status'][0] == 0
+    conc = out['massf'][0] * rho[0] / M
+    assert close(7.14201983840, conc[2], 1.0e-9)
+
+
+def test_fixed_volume_reactor_n2():
+    # examples/kinetics/fixed-volume-reactor-n2/test_fvreactor.py:30-55: N2/N with backward
+    # rates from K_c, 300 us in 1 us updates, each followed by update_thermo_from_rhou.
+    o = oracle.Oracle(mech("n2-gas.lua"), mech("n2-chem.lua"))
+    M = o.M
+    molef = np.array([2 / 3, 1 / 3])
+    massf = molef * M / float(np.dot(molef, M))
+    p, T = 1.0e5, 4000.0
+    rho, u = o.update_thermo_from_pT([p], [T], massf[None, :])
+    state = dict(T=np.array([T]), p=np.array([p]), massf=massf[None, :])
+    t, dt, dt_suggest, t_final = 0.0, 1.0e-6, 1.0e-11, 300.0e-6
+    while t <= t_final:
+        out = o.chem_update(rho, u, state['T'], state['p'], state['massf'], [dt_suggest], dt, retry=False)
+        assert out['status'][0] == 0
+        state = out
+        dt_suggest = out['dt_chem'][0]
+        t = t + dt
+    assert close(t, t_final, 1.0e-6)
+    assert close(state['T'][0], 6177.3, 1.0e-4)
+    assert close(state['p'][0], 145.518e3, 1.0e-4)
+    assert close(state['massf'][0][0], 8.692812671003e-01, 1.0e-4)
+    assert close(state['massf'][0][1], 1.307187328997e-01, 1.0e-4)
+    conc = state['massf'][0] * rho[0] / M
+    assert close(conc[0], 2.178123112237e+00, 1.0e-4)
+    assert close(conc[1], 6.550733441684e-01, 1.0e-4)
