@@ -1,0 +1,107 @@
+"""GB300-native engine for Eilmer's operator-split finite-rate chemistry update.
+
+The compute path is libgdtk_chem.so (CUDA for sm_103a, built from csrc/ by buildlib.py); this
+package only binds it.  `gas` mirrors the reference's Python wrapper gdtk.gas
+(src/lib/gdtk/gas.py) over the libgas-compatible C ABI; `cells` drives the batch entry
+points on device tensors.  There is no CPU implementation behind either: if the library
+is missing, importing `lib()` raises.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libgdtk_chem.so")
+INCLUDE_H = os.path.join(os.path.dirname(HERE), "include", "gdtk_chem.h")
+
+_lib = None
+
+_d = ctypes.POINTER(ctypes.c_double)
+_i = ctypes.POINTER(ctypes.c_int)
+_c = ctypes.c_char_p
+_v = ctypes.c_void_p
+_ull = ctypes.POINTER(ctypes.c_ulonglong)
+
+# name: (restype, argtypes) for every entry point of include/gdtk_chem.h
+SIGNATURES = {
+    "cwrap_gas_init": (ctypes.c_int, []),
+    "gas_model_new": (ctypes.c_int, [_c]),
+    "gas_model_type_str": (ctypes.c_int, [ctypes.c_int, _c, ctypes.c_int]),
+    "gas_model_n_species": (ctypes.c_int, [ctypes.c_int]),
+    "gas_model_n_modes": (ctypes.c_int, [ctypes.c_int]),
+    "gas_model_species_name": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _c, ctypes.c_int]),
+    "gas_model_mol_masses": (ctypes.c_int, [ctypes.c_int, _d]),
+    "gas_state_new": (ctypes.c_int, [ctypes.c_int]),
+    "gas_state_set_scalar_field": (ctypes.c_int, [ctypes.c_int, _c, ctypes.c_double]),
+    "gas_state_get_scalar_field": (ctypes.c_int, [ctypes.c_int, _c, _d]),
+    "gas_state_get_thermo_scalars": (ctypes.c_int, [ctypes.c_int, _d]),
+    "gas_state_set_array_field": (ctypes.c_int, [ctypes.c_int, _c, _d, ctypes.c_int]),
+    "gas_state_get_array_field": (ctypes.c_int, [ctypes.c_int, _c, _d, ctypes.c_int]),
+    "gas_state_copy_values": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
+    "gas_model_gas_state_update_thermo_from_pT": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
+    "gas_model_gas_state_update_thermo_from_rhou": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
+    "gas_model_gas_state_update_thermo_from_rhoT": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
+    "gas_model_gas_state_R": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _d]),
+    "gas_model_gas_state_molecular_mass": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _d]),
+    "gas_model_massf2molef": (ctypes.c_int, [ctypes.c_int, _d, _d]),
+    "gas_model_molef2massf": (ctypes.c_int, [ctypes.c_int, _d, _d]),
+    "gas_model_gas_state_get_molef": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _d]),
+    "gas_model_gas_state_get_conc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _d]),
+    "thermochemical_reactor_new": (ctypes.c_int, [ctypes.c_int, _c, _c]),
+    "thermochemical_reactor_gas_state_update": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_double, _d]),
+    "thermochemical_reactor_eval_source_terms": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                                ctypes.c_int, ctypes.c_int, _d]),
+    "reaction_mechanism_new": (ctypes.c_int, [ctypes.c_int, _c]),
+    "reaction_mechanism_n_reactions": (ctypes.c_int, [ctypes.c_int]),
+    "reaction_mechanism_tickrates": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _d, _d]),
+    "chem_reactor_update_cells": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _v, _v, _v, _v, _v, _v, _v,
+                                                 ctypes.c_double, ctypes.c_double, ctypes.c_int, _v]),
+    "chem_reactor_update_cells_ex": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _v, _v, _v, _v, _v, _v, _v,
+                                                    ctypes.c_double, ctypes.c_double, ctypes.c_int, _v, _v, _v]),
+    "chem_reactor_update_cells_host": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _v, _v, _v, _v, _v, _v, _v,
+                                                      ctypes.c_double, ctypes.c_double, ctypes.c_int]),
+    "chem_reactor_source_terms_cells": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _v, _v, _v, _v, _v, _v]),
+    "gas_model_update_thermo_from_pT_cells": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _v, _v, _v, _v, _v,
+                                                             _v, _v]),
+    "gas_model_update_thermo_from_rhou_cells": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _v, _v, _v, _v, _v,
+                                                               _v, _v]),
+    "chem_reactor_info": (ctypes.c_int, [ctypes.c_int, _i, _i, _i, _i]),
+    "chem_reactor_last_launch": (ctypes.c_int, [ctypes.c_int, _i, _i, _i, _i]),
+    "gdtk_last_error": (ctypes.c_char_p, []),
+    "gdtk_measure_fp64_peak": (ctypes.c_int, [_d]),
+}
+
+
+def build():
+    """Compiles the CUDA library for sm_103a (see buildlib.py)."""
+    from . import buildlib
+    return buildlib.build()
+
+
+def lib():
+    """The loaded libgdtk_chem.so; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libgdtk_chem.so is not built (run gdtk_gb300.build()); "
+                               "this package has no CPU implementation")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def last_error():
+    return lib().gdtk_last_error().decode()
+
+
+class ChemError(RuntimeError):
+    pass
+
+
+def check(rc, what):
+    if rc < 0:
+        raise ChemError("%s failed: %s" % (what, last_error()))
+    return rc

@@ -1,0 +1,116 @@
+"""Batch chemistry updates over device-resident cell arrays (torch tensors on cuda).
+
+Cells are structure-of-arrays, FP64, contiguous: rho, u, T, p, dt_chem of shape (n,) and
+mass fractions of shape (nsp, n) (species-major), as the batch entry points of
+include/gdtk_chem.h expect.  Launches go on torch's current CUDA stream.
+"""
+import ctypes
+
+import numpy as np
+
+from . import lib, check
+from .gas import GasModel, ThermochemicalReactor
+
+UPDATE_THERMO = 1
+RETRY = 2
+
+STATUS_NAMES = {0: "ok", 1: "h_min", 2: "max_attempts", 3: "max_subcycles", 4: "newton_fail",
+                5: "bad_input", 6: "frozen", 7: "cea_range"}
+
+
+def _ptr(t):
+    if t is None:
+        return None
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def _stream():
+    import torch
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _f64(t, shape):
+    import torch
+    if not (t.is_cuda and t.dtype == torch.float64 and t.is_contiguous() and tuple(t.shape) == tuple(shape)):
+        raise ValueError("expected a contiguous cuda float64 tensor of shape %s" % (shape,))
+    return t
+
+
+class ReactorCells:
+    """A gas model + mechanism pair with batch entry points (chem_reactor_update_cells etc.)."""
+
+    def __init__(self, gas_file, chem_file):
+        self.gmodel = GasModel(gas_file)
+        self.reactor = ThermochemicalReactor(self.gmodel, chem_file)
+        nsp, nr, method, tight = (ctypes.c_int() for _ in range(4))
+        check(lib().chem_reactor_info(self.reactor.id, ctypes.byref(nsp), ctypes.byref(nr), ctypes.byref(method),
+                                      ctypes.byref(tight)), "chem_reactor_info")
+        self.nsp, self.nr = nsp.value, nr.value
+        self.method = "rkf" if method.value == 0 else "alpha-qss"
+        self.tight = bool(tight.value)
+        self.species_names = self.gmodel.species_names
+        self.mol_masses = np.array(self.gmodel.mol_masses)
+
+    def thermo_from_pT(self, p, T, massf, status=None):
+        import torch
+        n = p.shape[0]
+        rho = torch.empty_like(p)
+        u = torch.empty_like(p)
+        check(lib().gas_model_update_thermo_from_pT_cells(self.gmodel.id, n, _ptr(_f64(p, (n,))), _ptr(_f64(T, (n,))),
+                                                          _ptr(_f64(massf, (self.nsp, n))), _ptr(rho), _ptr(u),
+                                                          _ptr(status), _stream()), "update_thermo_from_pT_cells")
+        return rho, u
+
+    def thermo_from_rhou(self, rho, u, massf, T, p, status=None):
+        """Updates T (in: guess) and p in place."""
+        n = rho.shape[0]
+        check(lib().gas_model_update_thermo_from_rhou_cells(self.gmodel.id, n, _ptr(_f64(rho, (n,))),
+                                                            _ptr(_f64(u, (n,))), _ptr(_f64(massf, (self.nsp, n))),
+                                                            _ptr(_f64(T, (n,))), _ptr(_f64(p, (n,))), _ptr(status),
+                                                            _stream()), "update_thermo_from_rhou_cells")
+
+    def update(self, rho, u, T, p, massf, dt_chem, t_interval, status=None, T_frozen=0.0,
+               flags=UPDATE_THERMO | RETRY, cell_counters=None, totals=None):
+        """One chemistry increment per cell, in place (chem_reactor_update_cells_ex)."""
+        n = rho.shape[0]
+        for t in (rho, u, T, p, dt_chem):
+            _f64(t, (n,))
+        _f64(massf, (self.nsp, n))
+        check(lib().chem_reactor_update_cells_ex(self.reactor.id, n, _ptr(rho), _ptr(u), _ptr(T), _ptr(p),
+                                                 _ptr(massf), _ptr(dt_chem), _ptr(status), float(t_interval),
+                                                 float(T_frozen), int(flags), _stream(), _ptr(cell_counters),
+                                                 _ptr(totals)), "chem_reactor_update_cells")
+
+    def update_host(self, rho, u, T, p, massf, dt_chem, t_interval, status=None, T_frozen=0.0,
+                    flags=UPDATE_THERMO | RETRY):
+        """Host-array form (numpy, float64, massf (nsp, n)); returns the number of failed cells."""
+        n = rho.shape[0]
+        arrs = [rho, u, T, p, massf, dt_chem]
+        for a in arrs:
+            if a.dtype != np.float64 or not a.flags['C_CONTIGUOUS']:
+                raise ValueError("expected C-contiguous float64 arrays")
+        st = status if status is not None else np.empty(n, np.int32)
+        vp = lambda a: ctypes.c_void_p(a.ctypes.data)
+        return check(lib().chem_reactor_update_cells_host(self.reactor.id, n, vp(rho), vp(u), vp(T), vp(p), vp(massf),
+                                                          vp(dt_chem), vp(st), float(t_interval), float(T_frozen),
+                                                          int(flags)), "chem_reactor_update_cells_host")
+
+    def source_terms(self, rho, T, massf, status=None):
+        import torch
+        n = rho.shape[0]
+        out = torch.empty((self.nsp, n), dtype=torch.float64, device=rho.device)
+        check(lib().chem_reactor_source_terms_cells(self.reactor.id, n, _ptr(_f64(rho, (n,))), _ptr(_f64(T, (n,))),
+                                                    _ptr(_f64(massf, (self.nsp, n))), _ptr(out), _ptr(status),
+                                                    _stream()), "chem_reactor_source_terms_cells")
+        return out
+
+    def last_launch(self):
+        v = [ctypes.c_int() for _ in range(4)]
+        check(lib().chem_reactor_last_launch(self.reactor.id, *[ctypes.byref(x) for x in v]), "last_launch")
+        return dict(grid=v[0].value, block=v[1].value, smem=v[2].value, blocks_per_sm=v[3].value)
+
+
+def measure_fp64_peak():
+    v = ctypes.c_double()
+    check(lib().gdtk_measure_fp64_peak(ctypes.byref(v)), "gdtk_measure_fp64_peak")
+    return v.value

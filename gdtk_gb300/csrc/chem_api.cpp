@@ -1,0 +1,684 @@
+// chem_api.cpp -- the C ABI of include/gdtk_chem.h.
+//
+// Handle tables mirror the reference's global arrays in gas/gas_cwrap.d:35-38 (gas models,
+// gas states, thermochemical reactors, reaction mechanisms).  Every physics evaluation is a
+// kernel launch (chem_kernels.cu); a per-state call is a batch of one cell.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/gdtk_chem.h"
+#include "chem_launch.h"
+#include "chem_types.h"
+#include "mechanism.h"
+
+namespace gdtk {
+namespace {
+
+thread_local std::string g_last_error;
+
+void report(const std::string& msg) {
+    g_last_error = msg;
+    std::fprintf(stderr, "gdtk_chem: %s\n", msg.c_str());
+}
+
+struct Cuda {
+    bool ok = false;
+    int sm_count = 0;
+    std::string why;
+};
+
+Cuda& cuda() {
+    static Cuda c;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        int n = 0;
+        cudaError_t e = cudaGetDeviceCount(&n);
+        if (e != cudaSuccess || n == 0) {
+            c.why = std::string("no CUDA device available: this library evaluates chemistry and thermo on the GPU only (") +
+                    (e != cudaSuccess ? cudaGetErrorString(e) : "0 devices") + ")";
+            return;
+        }
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&c.sm_count, cudaDevAttrMultiProcessorCount, dev);
+        c.ok = true;
+    });
+    return c;
+}
+
+void require_cuda() {
+    if (!cuda().ok) throw std::runtime_error(cuda().why);
+}
+
+void check(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    void ensure(size_t want) {
+        if (want <= n) return;
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+        check(cudaMalloc(&p, want * sizeof(T)), "cudaMalloc");
+        n = want;
+    }
+    ~DevBuf() { if (p) cudaFree(p); }
+};
+
+struct DeviceMech {
+    PackedMech host;
+    int* I = nullptr;
+    double* D = nullptr;
+    void upload(const PackedMech& pm) {
+        require_cuda();
+        host = pm;
+        check(cudaMalloc(&I, pm.I.size() * sizeof(int)), "cudaMalloc");
+        check(cudaMalloc(&D, pm.D.size() * sizeof(double)), "cudaMalloc");
+        check(cudaMemcpy(I, pm.I.data(), pm.I.size() * sizeof(int), cudaMemcpyHostToDevice), "cudaMemcpy");
+        check(cudaMemcpy(D, pm.D.data(), pm.D.size() * sizeof(double), cudaMemcpyHostToDevice), "cudaMemcpy");
+    }
+    ~DeviceMech() {
+        if (I) cudaFree(I);
+        if (D) cudaFree(D);
+    }
+};
+
+// Scratch for per-state (one-cell) calls and for the host-pointer batch form.
+struct Staging {
+    DevBuf<double> d;
+    DevBuf<int> st;
+    cudaStream_t stream = nullptr;
+    cudaStream_t get_stream() {
+        if (!stream) check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        return stream;
+    }
+    ~Staging() { if (stream) cudaStreamDestroy(stream); }
+};
+
+struct GasModelObj {
+    GasModelHost gm;
+    std::unique_ptr<DeviceMech> dev;   // gas-only tables (no reactions), made on first GPU use
+    Staging stage;
+    DeviceMech& device() {
+        if (!dev) {
+            auto d = std::make_unique<DeviceMech>();
+            d->upload(pack(gm, nullptr));
+            dev = std::move(d);
+        }
+        return *dev;
+    }
+};
+
+struct GasStateObj {
+    int gm;
+    double rho = 0, p = 0, T = 0, u = 0, a = 0, mu = 0, k = 0;
+    std::vector<double> massf;
+};
+
+struct ReactorObj {
+    int gm;
+    MechanismHost mh;
+    DeviceMech dev;
+    int scratch = 0;
+    unsigned* counter = nullptr;
+    Staging stage;
+    LaunchInfo last{};
+    ~ReactorObj() { if (counter) cudaFree(counter); }
+};
+
+struct MechObj {
+    int gm;
+    MechanismHost mh;
+    DeviceMech dev;
+    Staging stage;
+};
+
+std::mutex g_mu;
+std::vector<std::unique_ptr<GasModelObj>> g_models;
+std::vector<std::unique_ptr<GasStateObj>> g_states;
+std::vector<std::unique_ptr<ReactorObj>> g_reactors;
+std::vector<std::unique_ptr<MechObj>> g_mechs;
+
+template <typename T>
+T& lookup(std::vector<std::unique_ptr<T>>& v, int i, const char* what) {
+    if (i < 0 || i >= (int)v.size() || !v[i]) throw std::runtime_error(std::string("invalid ") + what + " handle");
+    return *v[i];
+}
+
+GasModelObj& model(int i) { return lookup(g_models, i, "gas model"); }
+GasStateObj& state(int i) { return lookup(g_states, i, "gas state"); }
+ReactorObj& reactor(int i) { return lookup(g_reactors, i, "thermochemical reactor"); }
+MechObj& mechobj(int i) { return lookup(g_mechs, i, "reaction mechanism"); }
+
+template <typename F>
+int guarded(F&& f) {
+    try {
+        return f();
+    } catch (std::exception& e) {
+        report(e.what());
+        return -1;
+    }
+}
+
+// Runs one gas-service mode over `n` cells whose data sit in device buffers.
+void run_service(const DeviceMech& dm, int mode, int clip, int n, double* rho, double* u, double* T, double* p,
+                 const double* massf, double* out1, double* out2, int* status, cudaStream_t s) {
+    GasServiceArgs a{};
+    a.mech_i = dm.I;
+    a.mech_d = dm.D;
+    a.n_mech_i = (int)dm.host.I.size();
+    a.n_mech_d = (int)dm.host.D.size();
+    a.nsp_hint = dm.host.nsp;
+    a.nr_hint = dm.host.nr;
+    a.ncell = n;
+    a.mode = mode;
+    a.clip = clip;
+    a.rho = rho; a.u = u; a.T = T; a.p = p; a.massf = massf; a.out1 = out1; a.out2 = out2; a.status = status;
+    check(launch_gas_service(a, cuda().sm_count, s), "gas service launch");
+}
+
+// One-cell service on a gas state: uploads [rho, u, T, p, massf...], runs, downloads.
+// Returns the cell status.  out1/out2 (host) receive nout1/nout2 values when given.
+int state_service(const DeviceMech& dm, Staging& stg, int mode, int clip, GasStateObj& gs, double* out1, int nout1,
+                  double* out2, int nout2) {
+    require_cuda();
+    const int nsp = (int)gs.massf.size();
+    const size_t nd = 4 + nsp + nout1 + nout2;
+    stg.d.ensure(nd);
+    stg.st.ensure(1);
+    cudaStream_t s = stg.get_stream();
+    std::vector<double> h(nd, 0.0);
+    h[0] = gs.rho; h[1] = gs.u; h[2] = gs.T; h[3] = gs.p;
+    for (int i = 0; i < nsp; ++i) h[4 + i] = gs.massf[i];
+    double* d = stg.d.p;
+    check(cudaMemcpyAsync(d, h.data(), nd * sizeof(double), cudaMemcpyHostToDevice, s), "cudaMemcpyAsync");
+    run_service(dm, mode, clip, 1, d + 0, d + 1, d + 2, d + 3, d + 4, d + 4 + nsp, d + 4 + nsp + nout1, stg.st.p, s);
+    int st = 0;
+    check(cudaMemcpyAsync(h.data(), d, nd * sizeof(double), cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
+    check(cudaMemcpyAsync(&st, stg.st.p, sizeof(int), cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
+    check(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    if (st == 0) {
+        gs.rho = h[0]; gs.u = h[1]; gs.T = h[2]; gs.p = h[3];
+        for (int k = 0; k < nout1; ++k) out1[k] = h[4 + nsp + k];
+        for (int k = 0; k < nout2; ++k) out2[k] = h[4 + nsp + nout1 + k];
+    }
+    return st;
+}
+
+const char* status_text(int st) {
+    switch (st) {
+    case CELL_H_MIN: return "Hit the minimum allowable timestep in chemistry update.";
+    case CELL_MAX_ATTEMPTS: return "Hit maximum number of step attempts within a subcycle for chemistry update.";
+    case CELL_MAX_SUBCYCLES: return "Hit maximum number of subcycles while attempting chemistry update.";
+    case CELL_NEWTON_FAIL: return "update_temperature_from_energy function failed to converge.";
+    case CELL_BAD_INPUT: return "Invalid density.";
+    case CELL_CEA_RANGE: return "Coefficients for CEA curve could not be determined.";
+    default: return "chemistry update failed";
+    }
+}
+
+int launch_update(ReactorObj& r, int ncell, const double* rho, const double* u, double* T, double* p, double* massf,
+                  double* dt_chem, int* status, double t_interval, double T_frozen, int flags, cudaStream_t s,
+                  int* cell_counters, unsigned long long* totals) {
+    require_cuda();
+    if (ncell < 0) throw std::runtime_error("ncell must be >= 0");
+    if (ncell == 0) return 0;
+    if (!rho || !u || !T || !p || !massf || !dt_chem) throw std::runtime_error("null cell array");
+    if (!(t_interval > 0.0)) throw std::runtime_error("t_interval must be > 0");
+    if (!r.counter) check(cudaMalloc(&r.counter, sizeof(unsigned)), "cudaMalloc");
+    check(cudaMemsetAsync(r.counter, 0, sizeof(unsigned), s), "cudaMemsetAsync");
+    ChemUpdateArgs a{};
+    a.mech_i = r.dev.I;
+    a.mech_d = r.dev.D;
+    a.n_mech_i = (int)r.dev.host.I.size();
+    a.n_mech_d = (int)r.dev.host.D.size();
+    a.ncell = ncell;
+    a.rho = rho; a.u = u; a.T = T; a.p = p; a.massf = massf; a.dt_chem = dt_chem; a.status = status;
+    a.t_interval = t_interval;
+    a.T_frozen = T_frozen;
+    a.flags = flags;
+    a.counter = r.counter;
+    a.cell_counters = cell_counters;
+    a.totals = totals;
+    check(launch_chem_update(a, r.mh.method, r.scratch, cuda().sm_count, s, &r.last), "chemistry update launch");
+    return 0;
+}
+
+}  // namespace
+}  // namespace gdtk
+
+using namespace gdtk;
+
+extern "C" {
+
+int cwrap_gas_init(void) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_reactors.clear();
+    g_mechs.clear();
+    g_states.clear();
+    g_models.clear();
+    return 0;
+}
+
+int gas_model_new(const char* file_name) {
+    return guarded([&] {
+        if (!file_name) throw std::runtime_error("null file name");
+        auto m = std::make_unique<GasModelObj>();
+        m->gm = load_gas_model(file_name);
+        std::lock_guard<std::mutex> lk(g_mu);
+        g_models.push_back(std::move(m));
+        return (int)g_models.size() - 1;
+    });
+}
+
+int gas_model_type_str(int gm_i, char* dest_str, int n) {
+    return guarded([&] {
+        const std::string& s = model(gm_i).gm.type_str;
+        if (!dest_str || n <= 0) throw std::runtime_error("bad destination buffer");
+        std::strncpy(dest_str, s.c_str(), (size_t)n);
+        dest_str[n - 1] = '\0';
+        return 0;
+    });
+}
+
+int gas_model_n_species(int gm_i) { return guarded([&] { return model(gm_i).gm.n_species(); }); }
+
+int gas_model_n_modes(int gm_i) { return guarded([&] { (void)model(gm_i); return 0; }); }
+
+int gas_model_species_name(int gm_i, int isp, char* dest_name, int n) {
+    return guarded([&] {
+        auto& gm = model(gm_i).gm;
+        if (isp < 0 || isp >= gm.n_species()) throw std::runtime_error("species index out of range");
+        if (!dest_name || n <= 0) throw std::runtime_error("bad destination buffer");
+        std::strncpy(dest_name, gm.names[isp].c_str(), (size_t)n);
+        dest_name[n - 1] = '\0';
+        return 0;
+    });
+}
+
+int gas_model_mol_masses(int gm_i, double* mm) {
+    return guarded([&] {
+        auto& gm = model(gm_i).gm;
+        for (int i = 0; i < gm.n_species(); ++i) mm[i] = gm.M[i];
+        return 0;
+    });
+}
+
+int gas_state_new(int gm_i) {
+    return guarded([&] {
+        auto& gm = model(gm_i).gm;
+        auto s = std::make_unique<GasStateObj>();
+        s->gm = gm_i;
+        s->massf.assign(gm.n_species(), 0.0);
+        if (gm.n_species() == 1) s->massf[0] = 1.0;
+        std::lock_guard<std::mutex> lk(g_mu);
+        g_states.push_back(std::move(s));
+        return (int)g_states.size() - 1;
+    });
+}
+
+int gas_state_set_scalar_field(int gs_i, const char* field_name, double value) {
+    return guarded([&] {
+        auto& s = state(gs_i);
+        std::string f = field_name ? field_name : "";
+        if (f == "rho") s.rho = value;
+        else if (f == "p") s.p = value;
+        else if (f == "T") s.T = value;
+        else if (f == "u") s.u = value;
+        else throw std::runtime_error("Cannot set field name: " + f);
+        return 0;
+    });
+}
+
+int gas_state_get_scalar_field(int gs_i, const char* field_name, double* value) {
+    return guarded([&] {
+        auto& s = state(gs_i);
+        std::string f = field_name ? field_name : "";
+        if (f == "rho") *value = s.rho;
+        else if (f == "p") *value = s.p;
+        else if (f == "T") *value = s.T;
+        else if (f == "u") *value = s.u;
+        else if (f == "a") *value = s.a;
+        else if (f == "mu") *value = s.mu;
+        else if (f == "k") *value = s.k;
+        else throw std::runtime_error("Cannot get field name: " + f);
+        return 0;
+    });
+}
+
+int gas_state_get_thermo_scalars(int gs_i, double* values) {
+    return guarded([&] {
+        auto& s = state(gs_i);
+        values[0] = s.rho; values[1] = s.p; values[2] = s.T; values[3] = s.u; values[4] = s.a;
+        return 0;
+    });
+}
+
+int gas_state_set_array_field(int gs_i, const char* field_name, double* values, int n) {
+    return guarded([&] {
+        auto& s = state(gs_i);
+        std::string f = field_name ? field_name : "";
+        if (f != "massf") throw std::runtime_error("Cannot set array field name: " + f);
+        if (n != (int)s.massf.size()) throw std::runtime_error("massf length mismatch");
+        for (int i = 0; i < n; ++i) s.massf[i] = values[i];
+        return 0;
+    });
+}
+
+int gas_state_get_array_field(int gs_i, const char* field_name, double* values, int n) {
+    return guarded([&] {
+        auto& s = state(gs_i);
+        std::string f = field_name ? field_name : "";
+        if (f != "massf") throw std::runtime_error("Cannot get array field name: " + f);
+        if (n != (int)s.massf.size()) throw std::runtime_error("massf length mismatch");
+        for (int i = 0; i < n; ++i) values[i] = s.massf[i];
+        return 0;
+    });
+}
+
+int gas_state_copy_values(int gs_to_i, int gs_from_i) {
+    return guarded([&] {
+        auto& to = state(gs_to_i);
+        auto& from = state(gs_from_i);
+        if (to.massf.size() != from.massf.size()) throw std::runtime_error("gas states of different models");
+        int gm = to.gm;
+        to = from;
+        to.gm = gm;
+        return 0;
+    });
+}
+
+static int thermo_update(int gm_i, int gs_i, int mode) {
+    return guarded([&] {
+        auto& m = model(gm_i);
+        auto& s = state(gs_i);
+        if ((int)s.massf.size() != m.gm.n_species()) throw std::runtime_error("gas state does not belong to this model");
+        int st = state_service(m.device(), m.stage, mode, 1, s, nullptr, 0, nullptr, 0);
+        if (st) throw std::runtime_error(status_text(st));
+        return 0;
+    });
+}
+
+int gas_model_gas_state_update_thermo_from_pT(int gm_i, int gs_i) { return thermo_update(gm_i, gs_i, 0); }
+int gas_model_gas_state_update_thermo_from_rhou(int gm_i, int gs_i) { return thermo_update(gm_i, gs_i, 1); }
+int gas_model_gas_state_update_thermo_from_rhoT(int gm_i, int gs_i) { return thermo_update(gm_i, gs_i, 4); }
+
+int gas_model_gas_state_R(int gm_i, int gs_i, double* result) {
+    return guarded([&] {
+        auto& m = model(gm_i).gm;
+        auto& s = state(gs_i);
+        double r = 0.0;   // mass_average(Q, mR), gas_model.d:410-418
+        for (int i = 0; i < m.n_species(); ++i) r += s.massf[i] * (8.31451 / m.M[i]);
+        *result = r;
+        return 0;
+    });
+}
+
+int gas_model_gas_state_molecular_mass(int gm_i, int gs_i, double* result) {
+    return guarded([&] {
+        auto& m = model(gm_i).gm;
+        auto& s = state(gs_i);
+        double sum = 0.0;   // gas_model.d:454-462: 1 / sum(Y_i / M_i)
+        for (int i = 0; i < m.n_species(); ++i) sum += s.massf[i] / m.M[i];
+        *result = 1.0 / sum;
+        return 0;
+    });
+}
+
+int gas_model_massf2molef(int gm_i, double* massf, double* molef) {
+    return guarded([&] {
+        auto& m = model(gm_i).gm;
+        double mix = 0.0;   // gas_model.d:454-472: M_mix = 1/sum(Y/M); X = Y M_mix / M
+        for (int i = 0; i < m.n_species(); ++i) mix += massf[i] / m.M[i];
+        mix = 1.0 / mix;
+        for (int i = 0; i < m.n_species(); ++i) molef[i] = massf[i] * mix / m.M[i];
+        return 0;
+    });
+}
+
+int gas_model_molef2massf(int gm_i, double* molef, double* massf) {
+    return guarded([&] {
+        auto& m = model(gm_i).gm;
+        double mix = 0.0;   // gas_model.d:474-482
+        for (int i = 0; i < m.n_species(); ++i) mix += molef[i] * m.M[i];
+        for (int i = 0; i < m.n_species(); ++i) massf[i] = molef[i] * m.M[i] / mix;
+        return 0;
+    });
+}
+
+int gas_model_gas_state_get_molef(int gm_i, int gs_i, double* molef) {
+    return guarded([&] { return gas_model_massf2molef(gm_i, state(gs_i).massf.data(), molef); });
+}
+
+int gas_model_gas_state_get_conc(int gm_i, int gs_i, double* conc) {
+    return guarded([&] {
+        auto& m = model(gm_i).gm;
+        auto& s = state(gs_i);
+        if (std::isnan(s.rho) || s.rho <= 0.0) throw std::runtime_error("Invalid density.");
+        for (int i = 0; i < m.n_species(); ++i) {   // gas_model.d:237-253
+            double c = s.massf[i] * s.rho / m.M[i];
+            conc[i] = c < 1.0e-30 ? 0.0 : c;
+        }
+        return 0;
+    });
+}
+
+int thermochemical_reactor_new(int gm_i, const char* filename1, const char* filename2) {
+    (void)filename2;   // a second file is used only by multi-temperature reactors
+    return guarded([&] {
+        auto& m = model(gm_i);
+        if (!filename1) throw std::runtime_error("null file name");
+        auto r = std::make_unique<ReactorObj>();
+        r->gm = gm_i;
+        r->mh = load_mechanism(filename1, m.gm, true);
+        PackedMech pm = pack(m.gm, &r->mh);
+        r->scratch = chem_scratch_doubles(pm.nsp, pm.nr, pm.neff, pm.method);
+        r->dev.upload(pm);
+        std::lock_guard<std::mutex> lk(g_mu);
+        g_reactors.push_back(std::move(r));
+        return (int)g_reactors.size() - 1;
+    });
+}
+
+int thermochemical_reactor_gas_state_update(int cr_i, int gs_i, double t_interval, double* dt_suggest) {
+    return guarded([&] {
+        auto& r = reactor(cr_i);
+        auto& s = state(gs_i);
+        const int nsp = (int)s.massf.size();
+        if (nsp != r.dev.host.nsp) throw std::runtime_error("gas state does not match the reactor's gas model");
+        require_cuda();
+        const size_t nd = 5 + nsp;
+        r.stage.d.ensure(nd);
+        r.stage.st.ensure(1);
+        cudaStream_t st = r.stage.get_stream();
+        std::vector<double> h(nd);
+        h[0] = s.rho; h[1] = s.u; h[2] = s.T; h[3] = s.p; h[4] = *dt_suggest;
+        for (int i = 0; i < nsp; ++i) h[5 + i] = s.massf[i];
+        double* d = r.stage.d.p;
+        check(cudaMemcpyAsync(d, h.data(), nd * sizeof(double), cudaMemcpyHostToDevice, st), "cudaMemcpyAsync");
+        // ThermochemicalReactor.opCall alone: no retry and no rhou update (gas_cwrap.d:906-921).
+        launch_update(r, 1, d + 0, d + 1, d + 2, d + 3, d + 5, d + 4, r.stage.st.p, t_interval, -1.0e300, 0, st,
+                      nullptr, nullptr);
+        int status = 0;
+        check(cudaMemcpyAsync(h.data(), d, nd * sizeof(double), cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync");
+        check(cudaMemcpyAsync(&status, r.stage.st.p, sizeof(int), cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync");
+        check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+        if (status != CELL_OK) throw std::runtime_error(status_text(status));
+        s.T = h[2]; s.p = h[3];
+        *dt_suggest = h[4];
+        for (int i = 0; i < nsp; ++i) s.massf[i] = h[5 + i];
+        return 0;
+    });
+}
+
+int thermochemical_reactor_eval_source_terms(int cr_i, int gm_i, int gs_i, int nsp, int nmodes, double* source) {
+    return guarded([&] {
+        auto& r = reactor(cr_i);
+        (void)model(gm_i);
+        auto& s = state(gs_i);
+        if (nsp != r.dev.host.nsp || nmodes != 0) throw std::runtime_error("nsp/nmodes do not match the reactor");
+        int st = state_service(r.dev, r.stage, 2, 1, s, source, nsp, nullptr, 0);
+        if (st) throw std::runtime_error(status_text(st));
+        return 0;
+    });
+}
+
+int reaction_mechanism_new(int gm_i, const char* filename) {
+    return guarded([&] {
+        auto& m = model(gm_i);
+        if (!filename) throw std::runtime_error("null file name");
+        auto r = std::make_unique<MechObj>();
+        r->gm = gm_i;
+        r->mh = load_mechanism(filename, m.gm, false);
+        r->mh.T_lower = 300.0;   // gas_cwrap.d:947: createReactionMechanism(..., 300.0, 30000.0)
+        r->mh.T_upper = 30000.0;
+        r->dev.upload(pack(m.gm, &r->mh));
+        std::lock_guard<std::mutex> lk(g_mu);
+        g_mechs.push_back(std::move(r));
+        return (int)g_mechs.size() - 1;
+    });
+}
+
+int reaction_mechanism_n_reactions(int rm_i) { return guarded([&] { return (int)mechobj(rm_i).mh.reactions.size(); }); }
+
+int reaction_mechanism_tickrates(int rm_i, int gm_i, int gs_i, double* forwardrates, double* backwardrates) {
+    return guarded([&] {
+        auto& r = mechobj(rm_i);
+        (void)model(gm_i);
+        auto& s = state(gs_i);
+        const int nr = (int)r.mh.reactions.size();
+        int st = state_service(r.dev, r.stage, 3, 1, s, forwardrates, nr, backwardrates, nr);
+        if (st) throw std::runtime_error(status_text(st));
+        return 0;
+    });
+}
+
+int chem_reactor_update_cells(int cr_i, int ncell, const double* rho, const double* u, double* T, double* p,
+                              double* massf, double* dt_chem, int* status, double t_interval, double T_frozen,
+                              int flags, void* stream) {
+    return guarded([&] {
+        return launch_update(reactor(cr_i), ncell, rho, u, T, p, massf, dt_chem, status, t_interval, T_frozen, flags,
+                             (cudaStream_t)stream, nullptr, nullptr);
+    });
+}
+
+int chem_reactor_update_cells_ex(int cr_i, int ncell, const double* rho, const double* u, double* T, double* p,
+                                 double* massf, double* dt_chem, int* status, double t_interval, double T_frozen,
+                                 int flags, void* stream, int* cell_counters, unsigned long long* totals) {
+    return guarded([&] {
+        return launch_update(reactor(cr_i), ncell, rho, u, T, p, massf, dt_chem, status, t_interval, T_frozen, flags,
+                             (cudaStream_t)stream, cell_counters, totals);
+    });
+}
+
+int chem_reactor_update_cells_host(int cr_i, int ncell, const double* rho, const double* u, double* T, double* p,
+                                   double* massf, double* dt_chem, int* status, double t_interval, double T_frozen,
+                                   int flags) {
+    return guarded([&] {
+        auto& r = reactor(cr_i);
+        require_cuda();
+        if (ncell <= 0) return 0;
+        const int nsp = r.dev.host.nsp;
+        const size_t n = (size_t)ncell;
+        r.stage.d.ensure(n * (6 + nsp));
+        r.stage.st.ensure(n);
+        cudaStream_t s = r.stage.get_stream();
+        double* d = r.stage.d.p;
+        double *drho = d, *du = d + n, *dT = d + 2 * n, *dp = d + 3 * n, *ddt = d + 4 * n, *dmf = d + 5 * n;
+        const size_t B = n * sizeof(double);
+        check(cudaMemcpyAsync(drho, rho, B, cudaMemcpyHostToDevice, s), "H2D");
+        check(cudaMemcpyAsync(du, u, B, cudaMemcpyHostToDevice, s), "H2D");
+        check(cudaMemcpyAsync(dT, T, B, cudaMemcpyHostToDevice, s), "H2D");
+        check(cudaMemcpyAsync(dp, p, B, cudaMemcpyHostToDevice, s), "H2D");
+        check(cudaMemcpyAsync(ddt, dt_chem, B, cudaMemcpyHostToDevice, s), "H2D");
+        check(cudaMemcpyAsync(dmf, massf, B * nsp, cudaMemcpyHostToDevice, s), "H2D");
+        launch_update(r, ncell, drho, du, dT, dp, dmf, ddt, r.stage.st.p, t_interval, T_frozen, flags, s, nullptr,
+                      nullptr);
+        check(cudaMemcpyAsync(T, dT, B, cudaMemcpyDeviceToHost, s), "D2H");
+        check(cudaMemcpyAsync(p, dp, B, cudaMemcpyDeviceToHost, s), "D2H");
+        check(cudaMemcpyAsync(dt_chem, ddt, B, cudaMemcpyDeviceToHost, s), "D2H");
+        check(cudaMemcpyAsync(massf, dmf, B * nsp, cudaMemcpyDeviceToHost, s), "D2H");
+        std::vector<int> local;
+        int* st_host = status;
+        if (!st_host) { local.resize(n); st_host = local.data(); }
+        check(cudaMemcpyAsync(st_host, r.stage.st.p, n * sizeof(int), cudaMemcpyDeviceToHost, s), "D2H");
+        check(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+        int nfail = 0;
+        for (size_t c = 0; c < n; ++c) nfail += (st_host[c] != CELL_OK && st_host[c] != CELL_FROZEN);
+        return nfail;
+    });
+}
+
+int chem_reactor_source_terms_cells(int cr_i, int ncell, const double* rho, const double* T, const double* massf,
+                                    double* source, int* status, void* stream) {
+    return guarded([&] {
+        auto& r = reactor(cr_i);
+        require_cuda();
+        if (ncell <= 0) return 0;
+        run_service(r.dev, 2, 1, ncell, const_cast<double*>(rho), nullptr, const_cast<double*>(T), nullptr, massf,
+                    source, nullptr, status, (cudaStream_t)stream);
+        return 0;
+    });
+}
+
+int gas_model_update_thermo_from_pT_cells(int gm_i, int ncell, const double* p, const double* T, const double* massf,
+                                          double* rho, double* u, int* status, void* stream) {
+    return guarded([&] {
+        auto& m = model(gm_i);
+        require_cuda();
+        if (ncell <= 0) return 0;
+        run_service(m.device(), 0, 1, ncell, rho, u, const_cast<double*>(T), const_cast<double*>(p), massf, nullptr,
+                    nullptr, status, (cudaStream_t)stream);
+        return 0;
+    });
+}
+
+int gas_model_update_thermo_from_rhou_cells(int gm_i, int ncell, const double* rho, const double* u,
+                                            const double* massf, double* T, double* p, int* status, void* stream) {
+    return guarded([&] {
+        auto& m = model(gm_i);
+        require_cuda();
+        if (ncell <= 0) return 0;
+        run_service(m.device(), 1, 1, ncell, const_cast<double*>(rho), const_cast<double*>(u), T, p, massf, nullptr,
+                    nullptr, status, (cudaStream_t)stream);
+        return 0;
+    });
+}
+
+int chem_reactor_info(int cr_i, int* nsp, int* nr, int* method, int* tight) {
+    return guarded([&] {
+        auto& r = reactor(cr_i);
+        if (nsp) *nsp = r.dev.host.nsp;
+        if (nr) *nr = r.dev.host.nr;
+        if (method) *method = r.mh.method;
+        if (tight) *tight = r.mh.tight ? 1 : 0;
+        return 0;
+    });
+}
+
+int chem_reactor_last_launch(int cr_i, int* grid, int* block, int* smem_bytes, int* blocks_per_sm) {
+    return guarded([&] {
+        auto& r = reactor(cr_i);
+        if (grid) *grid = r.last.grid;
+        if (block) *block = r.last.block;
+        if (smem_bytes) *smem_bytes = r.last.smem;
+        if (blocks_per_sm) *blocks_per_sm = r.last.blocks_per_sm;
+        return 0;
+    });
+}
+
+const char* gdtk_last_error(void) { return g_last_error.c_str(); }
+
+}  // extern "C"

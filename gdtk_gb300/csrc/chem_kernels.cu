@@ -1,0 +1,681 @@
+// chem_kernels.cu -- FP64 chemistry-update kernels for sm_103a (reference-order arithmetic).
+//
+// One thread integrates one cell.  A block stages the packed mechanism (chem_types.h) into
+// shared memory once; each thread's working vectors (concentrations, rate constants, stage
+// values) also live in shared memory, lane-interleaved so that the 32 lanes of a warp touch
+// 32 consecutive 8-byte words (no bank conflicts).  The grid is persistent: threads pull
+// cells from a device work counter, and a thread whose cell finishes takes the next one
+// while its neighbours carry on, so cells of very different step counts share warps without
+// idling them.  Each loop iteration of a thread is one ODE attempt, so all lanes of a warp
+// run the same code (rate constants -> ODE step -> step control) in lock-step.
+//
+// The arithmetic restates the reference in its evaluation order (this file is compiled with
+// --fmad=false so that a*b+c keeps two roundings, as the reference's x86-64 build does):
+//   kinetics/chemistry_update.d        opCall 139-326, RKFStep 404-478, AlphaQssStep 533-655
+//   kinetics/reaction_mechanism.d      eval_rate_constants 49-63, eval_split_rates 82-96,
+//                                      estimateStepSize 161-203, eval_gibbs_free_energies 204-218
+//   kinetics/reaction.d                compute_equilibrium_constant 26-52, eval_rate_constants 94-143,
+//                                      tick rates and production/loss 145-149, 267-311, 393-456
+//   kinetics/rate_constant.d           ArrheniusRateConstant.eval 72-75
+//   gas/thermo/cea_thermo_curves.d     eval_Cp/eval_h/eval_s 55-137, determineCoefficients 149-182
+//   gas/thermo/therm_perf_gas_mix.d    GibbsFreeEnergies 354-364, update_temperature_from_energy 426-468
+//   gas/gas_model.d                    massf2conc 237-253, conc2massf 255-271, rates2source 273-279
+//   lmr/fluidfvcell.d                  thermochemical_increment 883-997 (caller contract)
+#include <cuda_runtime.h>
+
+#include "chem_types.h"
+#include "chem_launch.h"
+#include "cea_thermo.h"
+
+namespace gdtk {
+namespace {
+
+constexpr double R_universal = 8.31451;   // gas/physical_constants.d:13
+constexpr double P_atm = 101.325e3;       // gas/physical_constants.d:16
+constexpr double MIN_MOLES = 1.0e-30;     // gas/gas_model.d:43
+constexpr double MIN_MASS_FRACTION = 1.0e-30;
+constexpr double DT_INCREASE_PERCENT = 10.0;   // chemistry_update.d:23-31
+constexpr double DT_REDUCTION_FACTOR = 10.0;
+constexpr double H_MIN = 1.0e-15;
+constexpr double ALLOWABLE_MASSF_ERROR = 1.0e-3;
+constexpr double ZERO_EPS = 1.0e-50;
+
+// Per-thread vector in shared memory: element k of this thread lives at b[k * s].
+struct Vec {
+    double* b;
+    int s;
+    __device__ __forceinline__ double& operator[](int k) const { return b[k * s]; }
+    __device__ __forceinline__ Vec operator+(int k) const { return Vec{b + k * s, s}; }
+};
+
+// D's pow(double, int) (std.math, binary exponentiation), in double.
+__device__ __forceinline__ double ipow(double x, int n) {
+    if (n < 0) {
+        if (n == -1) return 1.0 / x;
+        unsigned m = (unsigned)(-n);
+        double p = 1.0, v = p / x;
+        while (true) { if (m & 1u) p *= v; m >>= 1; if (!m) break; v *= v; }
+        return p;
+    }
+    if (n == 0) return 1.0;
+    if (n == 1) return x;
+    if (n == 2) return x * x;
+    unsigned m = (unsigned)n;
+    double p = 1.0, v = x;
+    while (true) { if (m & 1u) p *= v; m >>= 1; if (!m) break; v *= v; }
+    return p;
+}
+
+// therm_perf_gas_mix.d:406-413
+__device__ double internal_energy(const MechView& m, Vec mf, double T, double logT, int& err) {
+    double u = 0.0;
+    for (int i = 0; i < m.nsp; ++i) u += mf[i] * (cea_h(m, i, T, logT, err) - m.sp(i)[SP_R] * T);
+    return u;
+}
+
+// therm_perf_gas_mix.d:416-423
+__device__ double cv_mix(const MechView& m, Vec mf, double T, int& err) {
+    double c = 0.0;
+    for (int i = 0; i < m.nsp; ++i) c += mf[i] * (cea_Cp(m, i, T, err) - m.sp(i)[SP_R]);
+    return c;
+}
+
+__device__ double gas_constant(const MechView& m, Vec mf) {   // mass_average(Q, mR), gas_model.d:410-418
+    double r = 0.0;
+    for (int i = 0; i < m.nsp; ++i) r += mf[i] * m.sp(i)[SP_R];
+    return r;
+}
+
+// therm_perf_gas_mix.d:426-468.  Returns T; sets err on failure.  *iters counts Newton iterations.
+__device__ double T_from_u(const MechView& m, Vec mf, double u_tgt, double T_guess, int& err, int& iters) {
+    const double TOL = 1e-10;
+    double T = T_guess;
+    double f = internal_energy(m, mf, T, log(T), err) - u_tgt;
+    double dT = 0.0;
+    for (int iter = 0; iter < 10; ++iter) {
+        ++iters;
+        double cv = cv_mix(m, mf, T, err);
+        dT = -f / cv;
+        T += dT;
+        if (fabs(dT) / T < TOL) return T;
+        f = internal_energy(m, mf, T, log(T), err) - u_tgt;
+    }
+    if (fabs(dT) > 1e-3) err = CELL_NEWTON_FAIL;
+    return T;
+}
+
+// ---------------------------------------------------------------- kinetics
+// reaction_mechanism.d:49-63 with Gibbs energies at P_atm (:204-218, therm_perf_gas_mix.d:354-364),
+// reaction.d:26-52 and 94-143 for a single-temperature gas.  g is scratch of nsp doubles.
+__device__ void rate_constants(const MechView& m, double Tq, Vec kf, Vec kb, Vec g, int& err) {
+    double T = Tq;
+    if (T < m.T_lower()) T = m.T_lower();
+    if (T > m.T_upper()) T = m.T_upper();
+    const double logT = log(T);
+    // logp = log(P_atm/P_atm) = 0 and s - R*0 = s exactly, so the pressure term is omitted.
+    for (int i = 0; i < m.nsp; ++i) {
+        double h = cea_h(m, i, T, logT, err);
+        double s = cea_s(m, i, T, logT, err);
+        g[i] = h - T * s;
+    }
+    for (int ir = 0; ir < m.nr; ++ir) {
+        const int* r = m.rx(ir);
+        const double* d = m.rxd(ir);
+        double Kc = 1.0;
+        if (r[RX_FRC] == RATE_FROM_EQ || r[RX_BRC] == RATE_FROM_EQ) {
+            double dG = 0.0, nuSum = 0.0;
+            for (int k = 0; k < r[RX_NPART]; ++k) {
+                int isp = r[RX_PART + k];
+                int nu = r[RX_PART_NU + k];
+                dG += nu * g[isp] * m.sp(isp)[SP_M];
+                nuSum += nu;
+            }
+            double K_p = exp(-dG / (R_universal * T));
+            Kc = K_p * ipow(P_atm / (R_universal * T), (int)nuSum);
+        }
+        if (r[RX_FRC] == RATE_ARRHENIUS) {
+            double f = d[0] * pow(T, d[1]) * exp(-d[2] / T);
+            kf[ir] = f;
+            kb[ir] = (r[RX_BRC] == RATE_FROM_EQ) ? f / Kc : d[3] * pow(T, d[4]) * exp(-d[5] / T);
+        } else {
+            double b = d[3] * pow(T, d[4]) * exp(-d[5] / T);
+            kb[ir] = b;
+            kf[ir] = b * Kc;
+        }
+    }
+}
+
+// Third-body sums of the distinct efficiency lists (identical lists are summed once; the
+// sum for each list is in the reference's order, reaction.d:450-456).
+__device__ __forceinline__ void collider_terms(const MechView& m, Vec c, Vec meff) {
+    for (int s = 0; s < m.neff; ++s) {
+        const int* ei = m.eff_i(s);
+        const double* ev = m.eff_d(s);
+        double term = 0.0;
+        for (int k = 0; k < ei[0]; ++k) {
+            int isp = ei[1 + k];
+            term += ev[isp] * c[isp];
+        }
+        meff[s] = term;
+    }
+}
+
+// reaction_mechanism.d:82-96: per-reaction tick rates, then q/L accumulation in reaction order.
+__device__ void split_rates(const MechView& m, Vec c, Vec q, Vec L, Vec kf, Vec kb, Vec meff) {
+    collider_terms(m, c, meff);
+    for (int i = 0; i < m.nsp; ++i) { q[i] = 0.0; L[i] = 0.0; }
+    for (int ir = 0; ir < m.nr; ++ir) {
+        const int* r = m.rx(ir);
+        double wf = kf[ir], wb = kb[ir];
+        if (r[RX_COLLIDER]) { double t = meff[r[RX_EFFSET]]; wf = wf * t; wb = wb * t; }
+        for (int k = 0; k < r[RX_NREAC]; ++k) wf *= ipow(c[r[RX_REAC_IDX + k]], r[RX_REAC_COEFF + k]);
+        for (int k = 0; k < r[RX_NPROD]; ++k) wb *= ipow(c[r[RX_PROD_IDX + k]], r[RX_PROD_COEFF + k]);
+        for (int k = 0; k < r[RX_NPART]; ++k) {
+            int isp = r[RX_PART + k];
+            int nu = r[RX_PART_NU + k];
+            if (nu > 0) { q[isp] += nu * wf; L[isp] += nu * wb; }
+            else if (nu < 0) { q[isp] += -nu * wb; L[isp] += -nu * wf; }
+        }
+    }
+}
+
+// Tick rates only (reaction_mechanism.d:65-73).
+__device__ void tick_rates(const MechView& m, Vec c, Vec kf, Vec kb, Vec meff, double* wf_out, double* wb_out,
+                           int stride) {
+    collider_terms(m, c, meff);
+    for (int ir = 0; ir < m.nr; ++ir) {
+        const int* r = m.rx(ir);
+        double wf = kf[ir], wb = kb[ir];
+        if (r[RX_COLLIDER]) { double t = meff[r[RX_EFFSET]]; wf = wf * t; wb = wb * t; }
+        for (int k = 0; k < r[RX_NREAC]; ++k) wf *= ipow(c[r[RX_REAC_IDX + k]], r[RX_REAC_COEFF + k]);
+        for (int k = 0; k < r[RX_NPROD]; ++k) wb *= ipow(c[r[RX_PROD_IDX + k]], r[RX_PROD_COEFF + k]);
+        wf_out[(size_t)ir * stride] = wf;
+        wb_out[(size_t)ir * stride] = wb;
+    }
+}
+
+// Phobos std.algorithm.sum (pairwise) over n doubles of a per-thread vector.
+__device__ double sum_pairwise(Vec d, int n) {
+    double store[8];
+    int idx = 0;
+    int pos = 0;
+    auto collapse = [&](unsigned k) {
+        int lastToKeep = idx - (__ffs((int)(k + 1)) - 1);
+        while (idx > lastToKeep) { store[idx - 1] += store[idx]; --idx; }
+    };
+    for (unsigned k = 0; k < (unsigned)n / 16; ++k) {
+        Vec x = d + pos;
+        double s = (((x[0] + x[1]) + (x[2] + x[3])) + ((x[4] + x[5]) + (x[6] + x[7])))
+                 + (((x[8] + x[9]) + (x[10] + x[11])) + ((x[12] + x[13]) + (x[14] + x[15])));
+        store[idx] = s;
+        pos += 16;
+        collapse(k);
+        ++idx;
+    }
+    unsigned i = 0;
+    for (; pos < n; ++pos) { store[idx] = d[pos]; collapse(i); ++idx; ++i; }
+    double s = store[idx - 1];
+    for (int j = idx - 1; j-- > 0;) s += store[j];
+    return 0.0 + s;
+}
+
+// reaction_mechanism.d:161-203 given the split rates at c.
+__device__ double estimate_from_rates(int nsp, Vec c, Vec q, Vec L) {
+    const double MUCH_LARGER_FACTOR = 10000.0, ZERO_TOL = 1.0e-30, EPS1 = 1.0e-3;
+    double min_dt = 1.0e6, dt;
+    for (int i = 0; i < nsp; ++i) {
+        double ci = c[i], qi = q[i], Li = L[i];
+        if (ci > 0.0 && (fabs(qi - Li) > ZERO_TOL)) {
+            if (qi > MUCH_LARGER_FACTOR * Li) dt = ci / (Li + ZERO_EPS);
+            else dt = fabs(ci / (qi - Li));
+            min_dt = fmin(min_dt, dt);
+        }
+    }
+    double dt_chem = EPS1 * min_dt;
+    dt_chem = fmin(dt_chem, 1.0e-10);
+    dt_chem = fmax(dt_chem, 1.0e-15);
+    return dt_chem;
+}
+
+// ---------------------------------------------------------------- per-thread workspace
+// Offsets (in doubles) into a thread's shared-memory vectors.
+struct Layout {
+    int y0, yout, q, L, kf, kb, meff, ext, total;
+    __device__ __host__ void make(int nsp, int nr, int neff, int method) {
+        y0 = 0; yout = nsp; q = 2 * nsp; L = 3 * nsp; kf = 4 * nsp; kb = kf + nr; meff = kb + nr;
+        ext = meff + (neff > 0 ? neff : 1);
+        total = ext + (method == METHOD_RKF ? 7 * nsp : 4 * nsp);
+    }
+};
+
+// chemistry_update.d:404-478.  ext holds k1..k6 and yTmp.
+__device__ bool rkf_step(const MechView& m, Vec y0, double h, Vec yOut, double& hSuggest, Vec q, Vec L, Vec kf,
+                         Vec kb, Vec meff, Vec ext, int& nrhs) {
+    const double a21 = 1. / 5., a31 = 3. / 40., a32 = 9. / 40., a41 = 3. / 10., a42 = -9. / 10., a43 = 6. / 5.,
+        a51 = -11. / 54., a52 = 5. / 2., a53 = -70. / 27., a54 = 35. / 27., a61 = 1631. / 55296., a62 = 175. / 512.,
+        a63 = 575. / 13824., a64 = 44275. / 110592., a65 = 253. / 4096.;
+    const double b51 = 37. / 378., b53 = 250. / 621., b54 = 125. / 594., b56 = 512. / 1771., b41 = 2825. / 27648.,
+        b43 = 18575. / 48384., b44 = 13525. / 55296., b45 = 277. / 14336., b46 = 1.0 / 4.0;
+    const int n = m.nsp;
+    Vec k1 = ext, k2 = ext + n, k3 = ext + 2 * n, k4 = ext + 3 * n, k5 = ext + 4 * n, k6 = ext + 5 * n,
+        yT = ext + 6 * n;
+    auto rates = [&](Vec c, Vec out) {
+        split_rates(m, c, q, L, kf, kb, meff);
+        ++nrhs;
+        for (int i = 0; i < n; ++i) out[i] = q[i] - L[i];
+    };
+    rates(y0, k1);
+    for (int i = 0; i < n; ++i) yT[i] = y0[i] + h * (a21 * k1[i]);
+    rates(yT, k2);
+    for (int i = 0; i < n; ++i) yT[i] = y0[i] + h * (a31 * k1[i] + a32 * k2[i]);
+    rates(yT, k3);
+    for (int i = 0; i < n; ++i) yT[i] = y0[i] + h * (a41 * k1[i] + a42 * k2[i] + a43 * k3[i]);
+    rates(yT, k4);
+    for (int i = 0; i < n; ++i) yT[i] = y0[i] + h * (a51 * k1[i] + a52 * k2[i] + a53 * k3[i] + a54 * k4[i]);
+    rates(yT, k5);
+    for (int i = 0; i < n; ++i)
+        yT[i] = y0[i] + h * (a61 * k1[i] + a62 * k2[i] + a63 * k3[i] + a64 * k4[i] + a65 * k5[i]);
+    rates(yT, k6);
+    const double atol = m.err_tol(), rtol = m.err_tol();
+    double err = 0.0;
+    for (int i = 0; i < n; ++i) {
+        double yo = y0[i] + h * (b51 * k1[i] + b53 * k3[i] + b54 * k4[i] + b56 * k6[i]);
+        yOut[i] = yo;
+        double ye = yo - (y0[i] + h * (b41 * k1[i] + b43 * k3[i] + b44 * k4[i] + b45 * k5[i] + b46 * k6[i]));
+        double sk = atol + rtol * fmax(fabs(y0[i]), fabs(yo));
+        err += (ye / sk) * (ye / sk);
+    }
+    err = sqrt(err / n);
+    const double maxscale = 10.0, minscale = 0.2, safe = 0.9, alpha = 0.2;
+    double scale;
+    if (err <= 1.0) {
+        if (err == 0.0) scale = maxscale;
+        else {
+            scale = safe * pow(err, -alpha);
+            if (scale < minscale) scale = minscale;
+            if (scale > maxscale) scale = maxscale;
+        }
+        hSuggest = scale * h;
+        return true;
+    }
+    scale = fmax(safe * pow(err, -alpha), minscale);
+    hSuggest = scale * h;
+    return false;
+}
+
+__device__ __forceinline__ double alpha_of(double p, double h) {   // chemistry_update.d:599-604
+    double r = 1.0 / (p * h + ZERO_EPS);
+    return (180.0 * r * r * r + 60.0 * r * r + 11.0 * r + 1.0) / (360.0 * r * r * r + 60.0 * r * r + 12.0 * r + 1.0);
+}
+
+// chemistry_update.d:533-655.  ext holds q0, p0, yp0, yp (yp becomes yc in place).
+__device__ bool aqss_step(const MechView& m, Vec y0, double h, Vec yOut, double& hSuggest, Vec q, Vec L, Vec kf,
+                          Vec kb, Vec meff, Vec ext, int& nrhs) {
+    const int n = m.nsp;
+    const double eps1 = m.eps1(), eps2 = m.eps2(), delta = m.delta();
+    Vec q0 = ext, p0 = ext + n, yp0 = ext + 2 * n, yp = ext + 3 * n;
+    split_rates(m, y0, q, L, kf, kb, meff);
+    ++nrhs;
+    for (int i = 0; i < n; ++i) {
+        double y = y0[i];
+        double qi = q[i];
+        double pi = L[i] / (y + ZERO_EPS);
+        double a = alpha_of(pi, h);
+        double v = y + (h * (qi - pi * y)) / (1.0 + a * h * pi);
+        q0[i] = qi; p0[i] = pi; yp[i] = v; yp0[i] = v;
+    }
+    bool converged = false;
+    for (int corr = 0; corr < m.max_iters(); ++corr) {
+        split_rates(m, yp, q, L, kf, kb, meff);
+        ++nrhs;
+        converged = true;
+        for (int i = 0; i < n; ++i) {
+            double y = y0[i];
+            double pp = L[i] / (yp[i] + ZERO_EPS);
+            double ab = alpha_of(pp, h);
+            double qt = ab * q[i] + (1 - ab) * q0[i];
+            double pb = 0.5 * (p0[i] + pp);
+            double yc = y + (h * (qt - pb * y)) / (1.0 + ab * h * pb);
+            yp[i] = yc;
+            if (!(yc < ZERO_EPS)) {
+                double test = fabs(yc - yp0[i]);
+                if (test >= (eps1 * (yc + delta))) converged = false;
+            }
+        }
+        if (converged) break;
+    }
+    // step_suggest (chemistry_update.d:629-655) with yc = yp, yp = yp0
+    double sigma = 0.0;
+    for (int i = 0; i < n; ++i) {
+        double yc = yp[i];
+        if (yc < ZERO_EPS) continue;
+        double test = fabs(yc - yp0[i]) / (eps2 * (yc + delta));
+        if (test > sigma) sigma = test;
+    }
+    double h_new;
+    if (sigma <= 0.0) h_new = 10.0 * h;
+    else {
+        double x = sigma;
+        x = x - 0.5 * (x * x - sigma) / x;
+        x = x - 0.5 * (x * x - sigma) / x;
+        x = x - 0.5 * (x * x - sigma) / x;
+        h_new = h * ((1.0 / x) + 0.005);
+    }
+    hSuggest = h_new;
+    if (converged)
+        for (int i = 0; i < n; ++i) yOut[i] = yp[i];
+    return converged;
+}
+
+__device__ __forceinline__ unsigned fetch_cell(unsigned* counter) {
+    unsigned mask = __activemask();
+    int lane = threadIdx.x & 31;
+    int leader = __ffs(mask) - 1;
+    unsigned rank = __popc(mask & ((1u << lane) - 1u));
+    unsigned base = 0;
+    if (lane == leader) base = atomicAdd(counter, (unsigned)__popc(mask));
+    base = __shfl_sync(mask, base, leader);
+    return base + rank;
+}
+
+__device__ void stage_mechanism(const int* gi, const double* gd, int ni, int nd, int*& si, double*& sd,
+                                double*& scratch) {
+    extern __shared__ double smem_d[];
+    sd = smem_d;
+    si = reinterpret_cast<int*>(smem_d + nd);
+    for (int k = threadIdx.x; k < nd; k += blockDim.x) sd[k] = gd[k];
+    for (int k = threadIdx.x; k < ni; k += blockDim.x) si[k] = gi[k];
+    scratch = smem_d + nd + (ni + 1) / 2;
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------- the chemistry update
+template <int METHOD>
+__global__ void __launch_bounds__(256) chem_update_kernel(ChemUpdateArgs a) {
+    int* si;
+    double* sd;
+    double* scratch;
+    stage_mechanism(a.mech_i, a.mech_d, a.n_mech_i, a.n_mech_d, si, sd, scratch);
+    MechView m;
+    m.bind(si, sd);
+    Layout lay;
+    lay.make(m.nsp, m.nr, m.neff, METHOD);
+    Vec S{scratch + threadIdx.x, (int)blockDim.x};
+    Vec y0 = S + lay.y0, yout = S + lay.yout, q = S + lay.q, L = S + lay.L, kf = S + lay.kf, kb = S + lay.kb,
+        meff = S + lay.meff, ext = S + lay.ext;
+    const int nsp = m.nsp;
+    const unsigned ncell = (unsigned)a.ncell;
+    const double tI = a.t_interval;
+
+    unsigned c = 0;
+    bool have = false, retried = false, need_kc = false;
+    int phase = 0, cycle = 0, attempt = 0, err = 0;
+    double rho = 0, u = 0, T = 0, T0 = 0, p = 0, p0 = 0, dtS = 0, dtS0 = 0, dtSave = 0, h = 0, t = 0;
+    int n_steps = 0, n_rhs = 0, n_kc = 0, n_newton = 0, n_rej = 0;
+
+    while (true) {
+        if (!have) {
+            c = fetch_cell(a.counter);
+            if (c >= ncell) break;
+            rho = a.rho[c]; u = a.u[c]; T0 = a.T[c]; p0 = a.p[c]; dtS0 = a.dt_chem[c];
+            if (T0 <= a.T_frozen) {
+                if (a.status) a.status[c] = CELL_FROZEN;
+                continue;
+            }
+            if (isnan(rho) || rho <= 0.0) {
+                if (a.status) a.status[c] = CELL_BAD_INPUT;
+                continue;
+            }
+            have = true;
+            retried = false;
+            n_steps = n_rhs = n_kc = n_newton = n_rej = 0;
+            phase = -1;
+        }
+        if (phase == -1) {   // (re)start the update from the stored input state
+            T = T0; p = p0; dtS = dtS0; t = 0.0; err = 0;
+            for (int i = 0; i < nsp; ++i) {
+                double v = a.massf[(size_t)i * ncell + c] * rho / m.sp(i)[SP_M];
+                y0[i] = (v < MIN_MOLES) ? 0.0 : v;
+            }
+            need_kc = true;
+            phase = 0;
+        }
+        if (need_kc) {
+            rate_constants(m, T, kf, kb, L, err);
+            ++n_kc;
+            need_kc = false;
+        }
+        if (phase == 0) {
+            if (dtS > tI) h = tI;
+            else if (dtS <= 0.0) {
+                split_rates(m, y0, q, L, kf, kb, meff);
+                ++n_rhs;
+                h = estimate_from_rates(nsp, y0, q, L);
+            } else h = dtS;
+            cycle = 0;
+            phase = 1;
+        }
+        if (phase == 1) {   // start of a subcycle
+            dtSave = dtS;
+            h = fmin(h, tI - t);
+            attempt = 0;
+            phase = 2;
+        }
+        // ---- one attempt of the ODE step
+        ++n_steps;
+        bool ok = (METHOD == METHOD_RKF) ? rkf_step(m, y0, h, yout, dtS, q, L, kf, kb, meff, ext, n_rhs)
+                                         : aqss_step(m, y0, h, yout, dtS, q, L, kf, kb, meff, ext, n_rhs);
+        if (ok) {   // mass-fraction test on conc2massf(concOut)
+            for (int i = 0; i < nsp; ++i) {
+                double mfv = yout[i] * m.sp(i)[SP_M] / rho;
+                L[i] = (mfv < MIN_MASS_FRACTION) ? 0.0 : mfv;
+            }
+            double tot = sum_pairwise(L, nsp);
+            if (fabs(tot - 1.0) > ALLOWABLE_MASSF_ERROR) ok = false;
+        }
+        int fail = 0;
+        bool done = false;
+        if (ok) {
+            t += h;
+            for (int i = 0; i < nsp; ++i) y0[i] = yout[i];
+            double hMax = h * (1.0 + DT_INCREASE_PERCENT / 100.0);
+            if (dtS > h) h = fmin(dtS, hMax);
+            if (m.tight()) {   // chemistry_update.d:265-269
+                for (int i = 0; i < nsp; ++i) {
+                    double mfv = y0[i] * m.sp(i)[SP_M] / rho;
+                    q[i] = (mfv < MIN_MASS_FRACTION) ? 0.0 : mfv;
+                }
+                T = T_from_u(m, q, u, T, err, n_newton);
+                p = rho * gas_constant(m, q) * T;
+                need_kc = true;
+            }
+            if (err) fail = err;
+            else if (t >= tI) {
+                if (cycle == 0) dtSave = dtS;
+                done = true;
+            } else {
+                ++cycle;
+                if (cycle == m.max_subcycles()) fail = CELL_MAX_SUBCYCLES;
+                else phase = 1;
+            }
+        } else {
+            ++n_rej;
+            h /= DT_REDUCTION_FACTOR;
+            if (err) fail = err;
+            else if (h < H_MIN) fail = CELL_H_MIN;
+            else if (++attempt == m.max_attempts()) fail = CELL_MAX_ATTEMPTS;
+        }
+        if (fail) {
+            bool retryable = fail == CELL_H_MIN || fail == CELL_MAX_ATTEMPTS || fail == CELL_MAX_SUBCYCLES;
+            if ((a.flags & CHEM_FLAG_RETRY) && retryable && !retried) {   // fluidfvcell.d:924-941
+                retried = true;
+                dtS0 = -1.0;
+                phase = -1;
+                continue;
+            }
+            if (a.status) a.status[c] = fail;
+            done = false;
+            have = false;
+        }
+        if (done) {   // chemistry_update.d:290-325, then fluidfvcell.d:956
+            for (int i = 0; i < nsp; ++i) {
+                double mfv = y0[i] * m.sp(i)[SP_M] / rho;
+                q[i] = (mfv < MIN_MASS_FRACTION) ? 0.0 : mfv;
+            }
+            double tot = sum_pairwise(q, nsp);
+            for (int i = 0; i < nsp; ++i) q[i] = q[i] / tot;
+            int st = 0;
+            if (a.flags & CHEM_FLAG_UPDATE_THERMO) {
+                T = T_from_u(m, q, u, T, st, n_newton);
+                p = rho * gas_constant(m, q) * T;
+            }
+            if (st) {
+                if (a.status) a.status[c] = st;
+            } else {
+                for (int i = 0; i < nsp; ++i) a.massf[(size_t)i * ncell + c] = q[i];
+                a.T[c] = T;
+                a.p[c] = p;
+                a.dt_chem[c] = dtSave;
+                if (a.status) a.status[c] = CELL_OK;
+            }
+            have = false;
+        }
+        if (!have) {
+            if (a.cell_counters) {
+                a.cell_counters[0 * (size_t)ncell + c] = n_steps;
+                a.cell_counters[1 * (size_t)ncell + c] = n_rhs;
+                a.cell_counters[2 * (size_t)ncell + c] = n_kc;
+                a.cell_counters[3 * (size_t)ncell + c] = n_newton;
+                a.cell_counters[4 * (size_t)ncell + c] = n_rej;
+            }
+            if (a.totals) {
+                atomicAdd(a.totals + 0, (unsigned long long)n_steps);
+                atomicAdd(a.totals + 1, (unsigned long long)n_rhs);
+                atomicAdd(a.totals + 2, (unsigned long long)n_kc);
+                atomicAdd(a.totals + 3, (unsigned long long)n_newton);
+                atomicAdd(a.totals + 4, (unsigned long long)n_rej);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------- gas-state services
+// mode 0: update_thermo_from_pT  (p, T, massf -> rho, u)          therm_perf_gas_mix.d:57-61
+// mode 1: update_thermo_from_rhou (rho, u, massf, T guess -> T, p) therm_perf_gas_mix.d:63-67
+// mode 2: source terms (rho, T, massf -> source[nsp])              reaction_mechanism.d:98-105
+// mode 3: tick rates (rho, T, massf -> forward[nr], backward[nr])  gas_cwrap.d:968-990
+// mode 4: update_thermo_from_rhoT (rho, T, massf -> p, u)          therm_perf_gas_mix.d:69-73
+__global__ void __launch_bounds__(128) gas_service_kernel(GasServiceArgs a) {
+    int* si;
+    double* sd;
+    double* scratch;
+    stage_mechanism(a.mech_i, a.mech_d, a.n_mech_i, a.n_mech_d, si, sd, scratch);
+    MechView m;
+    m.bind(si, sd);
+    const int nsp = m.nsp, nr = m.nr;
+    Vec S{scratch + threadIdx.x, (int)blockDim.x};
+    Vec mf = S, c = S + nsp, q = S + 2 * nsp, L = S + 3 * nsp, kf = S + 4 * nsp, kb = kf + nr, meff = kb + nr;
+    for (int cell = blockIdx.x * blockDim.x + threadIdx.x; cell < a.ncell; cell += gridDim.x * blockDim.x) {
+        for (int i = 0; i < nsp; ++i) mf[i] = a.massf[(size_t)i * a.ncell + cell];
+        int err = 0;
+        if (a.mode == 0) {
+            double T = a.T[cell], pr = a.p[cell];
+            double rho = pr / (gas_constant(m, mf) * T);
+            double logT = log(T);
+            double uu = 0.0;
+            for (int i = 0; i < nsp; ++i) uu += mf[i] * (cea_h(m, i, T, logT, err) - m.sp(i)[SP_R] * T);
+            a.rho[cell] = rho;
+            a.u[cell] = uu;
+        } else if (a.mode == 4) {
+            double T = a.T[cell], rho = a.rho[cell];
+            double logT = log(T);
+            double uu = 0.0;
+            for (int i = 0; i < nsp; ++i) uu += mf[i] * (cea_h(m, i, T, logT, err) - m.sp(i)[SP_R] * T);
+            a.u[cell] = uu;
+            a.p[cell] = rho * gas_constant(m, mf) * T;
+        } else if (a.mode == 1) {
+            int it = 0;
+            double T = T_from_u(m, mf, a.u[cell], a.T[cell], err, it);
+            if (!err) {
+                a.T[cell] = T;
+                a.p[cell] = a.rho[cell] * gas_constant(m, mf) * T;
+            }
+        } else {
+            double rho = a.rho[cell];
+            if (isnan(rho) || rho <= 0.0) err = CELL_BAD_INPUT;
+            else {
+                for (int i = 0; i < nsp; ++i) {
+                    double v = mf[i] * rho / m.sp(i)[SP_M];
+                    c[i] = (a.clip && v < MIN_MOLES) ? 0.0 : v;
+                }
+                rate_constants(m, a.T[cell], kf, kb, L, err);
+                if (a.mode == 2) {
+                    split_rates(m, c, q, L, kf, kb, meff);
+                    for (int i = 0; i < nsp; ++i)
+                        a.out1[(size_t)i * a.ncell + cell] = (q[i] - L[i]) * m.sp(i)[SP_M];
+                } else {
+                    tick_rates(m, c, kf, kb, meff, a.out1 + cell, a.out2 + cell, a.ncell);
+                }
+            }
+        }
+        if (a.status) a.status[cell] = err;
+    }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- host-side launchers
+int chem_scratch_doubles(int nsp, int nr, int neff, int method) {
+    Layout l;
+    l.make(nsp, nr, neff, method);
+    return l.total;
+}
+
+static size_t mech_smem_bytes(int ni, int nd) { return (size_t)nd * 8 + (size_t)((ni + 1) / 2) * 8; }
+
+cudaError_t launch_chem_update(const ChemUpdateArgs& a, int method, int scratch_doubles, int sm_count,
+                               cudaStream_t stream, LaunchInfo* info) {
+    const size_t mech = mech_smem_bytes(a.n_mech_i, a.n_mech_d);
+    const size_t limit = 227 * 1024;
+    int block = 256;
+    while (block > 32 && mech + (size_t)scratch_doubles * 8 * block > limit) block /= 2;
+    size_t smem = mech + (size_t)scratch_doubles * 8 * block;
+    if (smem > limit) return cudaErrorInvalidConfiguration;
+    const void* fn = method == METHOD_RKF ? (const void*)chem_update_kernel<METHOD_RKF>
+                                          : (const void*)chem_update_kernel<METHOD_ALPHA_QSS>;
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, block, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    long long want = ((long long)a.ncell + block - 1) / block;
+    long long grid = (long long)sm_count * per_sm;
+    if (want < grid) grid = want;
+    if (grid < 1) grid = 1;
+    if (info) { info->grid = (int)grid; info->block = block; info->smem = (int)smem; info->blocks_per_sm = per_sm; }
+    if (method == METHOD_RKF)
+        chem_update_kernel<METHOD_RKF><<<(unsigned)grid, block, smem, stream>>>(a);
+    else
+        chem_update_kernel<METHOD_ALPHA_QSS><<<(unsigned)grid, block, smem, stream>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gas_service(const GasServiceArgs& a, int sm_count, cudaStream_t stream) {
+    const size_t mech = mech_smem_bytes(a.n_mech_i, a.n_mech_d);
+    const int nsp = a.nsp_hint, nr = a.nr_hint;
+    const size_t per_thread = (size_t)(4 * nsp + 2 * nr + 16) * 8;
+    int block = 128;
+    while (block > 32 && mech + per_thread * block > 200 * 1024) block /= 2;
+    size_t smem = mech + per_thread * block;
+    cudaError_t e = cudaFuncSetAttribute((const void*)gas_service_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    long long grid = ((long long)a.ncell + block - 1) / block;
+    if (grid > (long long)sm_count * 8) grid = (long long)sm_count * 8;
+    if (grid < 1) grid = 1;
+    gas_service_kernel<<<(unsigned)grid, block, smem, stream>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace gdtk

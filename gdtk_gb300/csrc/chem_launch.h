@@ -1,0 +1,57 @@
+// chem_launch.h -- kernel argument blocks and launchers (internal to the library).
+#pragma once
+#include <cuda_runtime.h>
+
+namespace gdtk {
+
+enum { CHEM_FLAG_UPDATE_THERMO = 1, CHEM_FLAG_RETRY = 2 };
+
+// All pointers are device pointers.  Mass fractions are species-major: massf[isp * ncell + cell].
+struct ChemUpdateArgs {
+    const int* mech_i;
+    const double* mech_d;
+    int n_mech_i, n_mech_d;
+    int ncell;
+    const double* rho;
+    const double* u;
+    double* T;
+    double* p;
+    double* massf;
+    double* dt_chem;
+    int* status;              // may be null
+    double t_interval;
+    double T_frozen;
+    int flags;
+    unsigned* counter;        // work counter, zero at launch
+    int* cell_counters;       // optional [5][ncell]: steps, rhs, rate-constant evals, Newton iters, rejects
+    unsigned long long* totals;   // optional [5], same quantities summed
+};
+
+struct GasServiceArgs {
+    const int* mech_i;
+    const double* mech_d;
+    int n_mech_i, n_mech_d;
+    int nsp_hint, nr_hint;
+    int ncell;
+    int mode;
+    int clip;
+    double* rho;
+    double* u;
+    double* T;
+    double* p;
+    const double* massf;
+    double* out1;
+    double* out2;
+    int* status;
+};
+
+struct LaunchInfo {
+    int grid, block, smem, blocks_per_sm;
+};
+
+int chem_scratch_doubles(int nsp, int nr, int neff, int method);
+cudaError_t launch_chem_update(const ChemUpdateArgs& a, int method, int scratch_doubles, int sm_count,
+                               cudaStream_t stream, LaunchInfo* info);
+cudaError_t launch_gas_service(const GasServiceArgs& a, int sm_count, cudaStream_t stream);
+
+}  // namespace gdtk

@@ -1,0 +1,88 @@
+// chem_types.h -- packed, device-resident description of a gas model + reaction mechanism.
+//
+// The host (mechanism.cpp) flattens the prep-gas / prep-chem files into two arrays, one of
+// ints and one of doubles, with the layout below.  Kernels copy both into shared memory once
+// per block and read them through MechView.  All offsets depend only on nsp, nr and neff.
+//
+// int array
+//   [0..HI)            header: nsp, nr, neff, method, maxIters, tight, maxSubcycles, maxAttempts
+//   [HI + isp]         nseg of species isp                                 (nsp ints)
+//   [RX + 40*ir + k]   reaction ir: collider, frc_model, brc_model, eff_set, nreac, nprod, npart, -,
+//                      reac_idx[4], reac_coeff[4], prod_idx[4], prod_coeff[4], part[8], part_nu[8]
+//   [EF + (1+nsp)*s]   efficiency set s: n, idx[nsp]
+// double array
+//   [0..HD)            header: T_lower, T_upper, errTol, eps1, eps2, delta, -, -
+//   [SP + 56*isp + k]  species isp: M, R, T_low, T_high, Cp_low, Cp_high, h_low, h_high, s_low, s_high,
+//                      breaks[5], blends[4], -, coeffs[4][9]
+//   [RD + 6*ir]        reaction ir: fA, fn, fC, bA, bn, bC
+//   [ED + nsp*s]       efficiency set s: values[nsp]
+#pragma once
+
+#define GDTK_MAX_SPECIES 32
+#define GDTK_MAX_REACTIONS 128
+#define GDTK_MAX_SEGMENTS 4
+#define GDTK_MAX_EFFSETS 16
+#define GDTK_MAX_TERMS 4
+#define GDTK_MAX_PARTICIPANTS 8
+
+#ifdef __CUDACC__
+#define GDTK_HD __host__ __device__ __forceinline__
+#else
+#define GDTK_HD inline
+#endif
+
+namespace gdtk {
+
+enum { HI = 8, RXI = 40, HD = 8, SPD = 56, RXD = 6 };
+
+// species double-record fields
+enum { SP_M = 0, SP_R, SP_TLOW, SP_THIGH, SP_CPLOW, SP_CPHIGH, SP_HLOW, SP_HHIGH, SP_SLOW, SP_SHIGH,
+       SP_BREAKS = 10, SP_BLENDS = 15, SP_COEFFS = 20 };
+// reaction int-record fields
+enum { RX_COLLIDER = 0, RX_FRC, RX_BRC, RX_EFFSET, RX_NREAC, RX_NPROD, RX_NPART,
+       RX_REAC_IDX = 8, RX_REAC_COEFF = 12, RX_PROD_IDX = 16, RX_PROD_COEFF = 20, RX_PART = 24, RX_PART_NU = 32 };
+enum { RATE_ARRHENIUS = 0, RATE_FROM_EQ = 1 };
+enum { METHOD_RKF = 0, METHOD_ALPHA_QSS = 1 };
+
+GDTK_HD int mech_n_ints(int nsp, int nr, int neff) { return HI + nsp + RXI * nr + (1 + nsp) * neff; }
+GDTK_HD int mech_n_doubles(int nsp, int nr, int neff) { return HD + SPD * nsp + RXD * nr + nsp * neff; }
+
+struct MechView {
+    const int* I;
+    const double* D;
+    int nsp, nr, neff;
+    GDTK_HD void bind(const int* i, const double* d) {
+        I = i; D = d; nsp = i[0]; nr = i[1]; neff = i[2];
+    }
+    GDTK_HD int method() const { return I[3]; }
+    GDTK_HD int max_iters() const { return I[4]; }
+    GDTK_HD bool tight() const { return I[5] != 0; }
+    GDTK_HD int max_subcycles() const { return I[6]; }
+    GDTK_HD int max_attempts() const { return I[7]; }
+    GDTK_HD double T_lower() const { return D[0]; }
+    GDTK_HD double T_upper() const { return D[1]; }
+    GDTK_HD double err_tol() const { return D[2]; }
+    GDTK_HD double eps1() const { return D[3]; }
+    GDTK_HD double eps2() const { return D[4]; }
+    GDTK_HD double delta() const { return D[5]; }
+    GDTK_HD int nseg(int isp) const { return I[HI + isp]; }
+    GDTK_HD const double* sp(int isp) const { return D + HD + SPD * isp; }
+    GDTK_HD const int* rx(int ir) const { return I + HI + nsp + RXI * ir; }
+    GDTK_HD const double* rxd(int ir) const { return D + HD + SPD * nsp + RXD * ir; }
+    GDTK_HD const int* eff_i(int s) const { return I + HI + nsp + RXI * nr + (1 + nsp) * s; }
+    GDTK_HD const double* eff_d(int s) const { return D + HD + SPD * nsp + RXD * nr + nsp * s; }
+};
+
+// Per-cell status codes (shared with include/gdtk_chem.h).
+enum CellStatus {
+    CELL_OK = 0,
+    CELL_H_MIN = 1,          // "Hit the minimum allowable timestep" (chemistry_update.d:233-238)
+    CELL_MAX_ATTEMPTS = 2,   // chemistry_update.d:241-247
+    CELL_MAX_SUBCYCLES = 3,  // chemistry_update.d:281-289
+    CELL_NEWTON_FAIL = 4,    // therm_perf_gas_mix.d:458-466
+    CELL_BAD_INPUT = 5,      // gas_model.d:246-248 (invalid density)
+    CELL_FROZEN = 6,         // T <= T_frozen: skipped (fluidfvcell.d:887)
+    CELL_CEA_RANGE = 7       // cea_thermo_curves.d:178-181
+};
+
+}  // namespace gdtk

@@ -1,0 +1,61 @@
+// mechanism.h -- host-side gas model and reaction mechanism, read from prep-gas / prep-chem files
+// and packed into the device layout of chem_types.h.
+#pragma once
+#include <string>
+#include <vector>
+
+#include "lua_table.h"
+
+namespace gdtk {
+
+struct CeaCurveHost {
+    int nseg = 0;
+    std::vector<double> breaks, blends, coeffs;   // coeffs: nseg * 9
+};
+
+// The thermally-perfect gas model (gas/composite_gas.d:37-120 with physical_model
+// 'thermally-perfect-gas', or the legacy 'ThermallyPerfectGas' file format).
+struct GasModelHost {
+    std::string type_str;
+    std::vector<std::string> names;
+    std::vector<double> M;
+    std::vector<CeaCurveHost> curves;
+    int n_species() const { return (int)names.size(); }
+};
+
+struct RateConstHost {
+    int model = 0;   // RATE_ARRHENIUS or RATE_FROM_EQ
+    double A = 0, n = 0, C = 0;
+};
+
+struct ReactionHost {
+    bool collider = false;
+    RateConstHost frc, brc;
+    std::vector<std::pair<int, int>> reac, prod;
+    std::vector<std::pair<int, double>> eff;   // in Lua traversal order (ascending species index)
+    std::string equation;
+};
+
+struct MechanismHost {
+    std::vector<ReactionHost> reactions;
+    // config table (kinetics/prep_chem.lua:49-91 defaults, chemistry_update.d:75-135 consumer)
+    double T_lower = 300.0, T_upper = 50000.0;
+    int method = 0;
+    double errTol = 1e-3, eps1 = 1e-3, eps2 = 5e-4, delta = 1e-10;
+    int maxIters = 10;
+    bool tight = false;
+    int maxSubcycles = 10000, maxAttempts = 4;
+};
+
+struct PackedMech {
+    std::vector<int> I;
+    std::vector<double> D;
+    int nsp = 0, nr = 0, neff = 0, method = 0;
+};
+
+GasModelHost load_gas_model(const std::string& path);
+// reads `reaction` (and `config` when with_config) of a prep-chem file; checks species order.
+MechanismHost load_mechanism(const std::string& path, const GasModelHost& gm, bool with_config);
+PackedMech pack(const GasModelHost& gm, const MechanismHost* mech);
+
+}  // namespace gdtk

@@ -1,0 +1,61 @@
+"""Seeded synthetic cell states for the reference's chemistry workloads.
+
+No benchmark data set exists for this path; every input is drawn from a numpy PCG64
+generator with a fixed seed, on the host, so the GPU engine and the CPU oracle see the
+same bits.  Densities and energies are then obtained from (p, T, Y) by the gas model
+(update_thermo_from_pT).
+"""
+import numpy as np
+
+AIR5_SPECIES = ['N2', 'O2', 'NO', 'N', 'O']
+H2AIR_RADICALS = ['H', 'O', 'OH', 'HO2', 'H2O2', 'N', 'NO', 'NO2', 'HNO']
+
+
+def air5_cells(n, seed=0):
+    """4096-cell air workload: T ~ U[2000, 8000] K, p = 10^U[3, 5] Pa, Y ~ Dirichlet(1) over
+    (N2, O2, NO, N, O).  Returns T (n,), p (n,), Y (5, n)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    T = rng.uniform(2000.0, 8000.0, n)
+    p = 10.0 ** rng.uniform(3.0, 5.0, n)
+    Y = rng.dirichlet(np.ones(5), n)
+    Y = Y / Y.sum(axis=1, keepdims=True)
+    return T, p, np.ascontiguousarray(Y.T)
+
+
+def h2air_cells(names, mol_masses, n, seed=1, frozen_fraction=0.5, T_cold=(300.0, 600.0), T_hot=(1100.0, 2800.0),
+                p_range=(2.0e4, 5.0e5)):
+    """H2-air workload of uneven stiffness.
+
+    A fraction `frozen_fraction` of the cells is cold (T ~ U[T_cold]), the rest hot
+    (T ~ U[T_hot]); p = 10^U[log10 p_range].  Composition: a blend, weight lambda ~ U[0, 1],
+    of stoichiometric H2-air (X_H2 : X_O2 : X_N2 = 2 : 1 : 3.76) and its complete-combustion
+    products (X_H2O : X_N2 = 2 : 3.76), plus radicals (H, O, OH, HO2, H2O2, N, NO, NO2, HNO)
+    whose total mass fraction is 10^U[-6, -2] split by Dirichlet(0.5); renormalised.
+    Returns T (n,), p (n,), Y (nsp, n).
+    """
+    rng = np.random.Generator(np.random.PCG64(seed))
+    idx = {s: i for i, s in enumerate(names)}
+    M = np.asarray(mol_masses, dtype=np.float64)
+    nsp = len(names)
+    hot = rng.uniform(0.0, 1.0, n) >= frozen_fraction
+    T = np.where(hot, rng.uniform(T_hot[0], T_hot[1], n), rng.uniform(T_cold[0], T_cold[1], n))
+    p = 10.0 ** rng.uniform(np.log10(p_range[0]), np.log10(p_range[1]), n)
+
+    def massf_of(molef):
+        x = np.zeros(nsp)
+        for s, v in molef.items():
+            x[idx[s]] = v
+        y = x * M
+        return y / y.sum()
+
+    unburnt = massf_of({'H2': 2.0, 'O2': 1.0, 'N2': 3.76})
+    burnt = massf_of({'H2O': 2.0, 'N2': 3.76})
+    lam = rng.uniform(0.0, 1.0, n)
+    Y = (1.0 - lam)[:, None] * unburnt[None, :] + lam[:, None] * burnt[None, :]
+    rad_idx = [idx[s] for s in H2AIR_RADICALS if s in idx]
+    share = 10.0 ** rng.uniform(-6.0, -2.0, n)
+    w = rng.dirichlet(np.full(len(rad_idx), 0.5), n)
+    Y *= (1.0 - share)[:, None]
+    Y[:, rad_idx] += share[:, None] * w
+    Y = Y / Y.sum(axis=1, keepdims=True)
+    return T, p, np.ascontiguousarray(Y.T)

@@ -1,0 +1,122 @@
+/* gdtk_chem.h -- C ABI of the GB300 chemistry-update engine (libgdtk_chem.so).
+ *
+ * Two groups of entry points:
+ *
+ * 1. The libgas-compatible subset.  Same names, signatures and 0 / -1 convention as the
+ *    reference's C ABI in src/gas/gas_cwrap.d (gdtk), so that src/lib/gdtk/gas.py (CFFI) or the
+ *    Ruby wrapper can bind this library in place of libgas.so for the chemistry path.  Objects
+ *    are integer handles into library-owned tables; errors are a -1 return plus a message on
+ *    stderr.  Every chemistry and thermo evaluation runs on the GPU; a call that needs one
+ *    fails with -1 when no CUDA device is present.
+ *
+ * 2. Batch entry points over many cells (no counterpart in libgas; they replace the per-cell
+ *    loop of lmr/simcore.d:322-340 -> fluidfvcell.d:883-997 and the legacy GPU path
+ *    eilmer/cuda_gpu_chem.d:155-191).  Arrays are structure-of-arrays; mass fractions are
+ *    species-major, massf[isp * ncell + cell].  The *_cells functions take DEVICE pointers and a
+ *    cudaStream_t (as void*), enqueue work on that stream and return without synchronising;
+ *    the *_cells_host functions take host pointers and return when the results are in them.
+ */
+#ifndef GDTK_CHEM_H
+#define GDTK_CHEM_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Per-cell status codes written by the batch entry points. */
+enum gdtk_cell_status {
+    GDTK_CELL_OK = 0,
+    GDTK_CELL_H_MIN = 1,          /* minimum step size hit (chemistry_update.d:233-238) */
+    GDTK_CELL_MAX_ATTEMPTS = 2,   /* chemistry_update.d:241-247 */
+    GDTK_CELL_MAX_SUBCYCLES = 3,  /* chemistry_update.d:281-289 */
+    GDTK_CELL_NEWTON_FAIL = 4,    /* T from (rho, u) did not converge (therm_perf_gas_mix.d:458-466) */
+    GDTK_CELL_BAD_INPUT = 5,      /* invalid density (gas_model.d:246-248) */
+    GDTK_CELL_FROZEN = 6,         /* T <= T_frozen: left unchanged (fluidfvcell.d:887) */
+    GDTK_CELL_CEA_RANGE = 7       /* no thermo-curve segment for T (cea_thermo_curves.d:178-181) */
+};
+
+/* Flags of chem_reactor_update_cells*. */
+#define GDTK_CHEM_UPDATE_THERMO 1 /* follow the update with update_thermo_from_rhou (fluidfvcell.d:956) */
+#define GDTK_CHEM_RETRY 2         /* retry a failed cell once with dt_chem = -1 (fluidfvcell.d:924-941) */
+
+/* ---- 1. libgas-compatible subset (gas_cwrap.d) ---------------------------------------- */
+int cwrap_gas_init(void);                                                   /* gas_cwrap.d:40-55 */
+int gas_model_new(const char* file_name);                                   /* gas_cwrap.d:69-80 */
+int gas_model_type_str(int gm_i, char* dest_str, int n);                    /* gas_cwrap.d:82-94 */
+int gas_model_n_species(int gm_i);                                          /* gas_cwrap.d:96-105 */
+int gas_model_n_modes(int gm_i);                                            /* gas_cwrap.d:107-116 */
+int gas_model_species_name(int gm_i, int isp, char* dest_name, int n);      /* gas_cwrap.d:134-146 */
+int gas_model_mol_masses(int gm_i, double* mm);                             /* gas_cwrap.d:148-160 */
+int gas_state_new(int gm_i);                                                /* gas_cwrap.d:162-178 */
+int gas_state_set_scalar_field(int gs_i, const char* field_name, double value);   /* gas_cwrap.d:180-210 */
+int gas_state_get_scalar_field(int gs_i, const char* field_name, double* value);  /* gas_cwrap.d:212-252 */
+int gas_state_get_thermo_scalars(int gs_i, double* values);                 /* gas_cwrap.d:254-268 */
+int gas_state_set_array_field(int gs_i, const char* field_name, double* values, int n); /* gas_cwrap.d:270-294 */
+int gas_state_get_array_field(int gs_i, const char* field_name, double* values, int n); /* gas_cwrap.d:296-323 */
+int gas_state_copy_values(int gs_to_i, int gs_from_i);                      /* gas_cwrap.d:412-421 */
+int gas_model_gas_state_update_thermo_from_pT(int gm_i, int gs_i);          /* gas_cwrap.d:469-492 */
+int gas_model_gas_state_update_thermo_from_rhou(int gm_i, int gs_i);        /* gas_cwrap.d:494-517 */
+int gas_model_gas_state_update_thermo_from_rhoT(int gm_i, int gs_i);        /* gas_cwrap.d:519-542 */
+int gas_model_gas_state_R(int gm_i, int gs_i, double* result);              /* gas_cwrap.d:689-698 */
+int gas_model_gas_state_molecular_mass(int gm_i, int gs_i, double* result); /* gas_cwrap.d:755-764 */
+int gas_model_massf2molef(int gm_i, double* massf, double* molef);          /* gas_cwrap.d:826-841 */
+int gas_model_molef2massf(int gm_i, double* molef, double* massf);          /* gas_cwrap.d:843-858 */
+int gas_model_gas_state_get_molef(int gm_i, int gs_i, double* molef);       /* gas_cwrap.d:860-873 */
+int gas_model_gas_state_get_conc(int gm_i, int gs_i, double* conc);         /* gas_cwrap.d:875-888 */
+int thermochemical_reactor_new(int gm_i, const char* filename1, const char* filename2); /* gas_cwrap.d:892-904 */
+int thermochemical_reactor_gas_state_update(int cr_i, int gs_i, double t_interval,
+                                            double* dt_suggest);            /* gas_cwrap.d:906-921 */
+int thermochemical_reactor_eval_source_terms(int cr_i, int gm_i, int gs_i, int nsp, int nmodes,
+                                             double* source);               /* gas_cwrap.d:923-941 */
+int reaction_mechanism_new(int gm_i, const char* filename);                 /* gas_cwrap.d:944-955 */
+int reaction_mechanism_n_reactions(int rm_i);                               /* gas_cwrap.d:957-966 */
+int reaction_mechanism_tickrates(int rm_i, int gm_i, int gs_i, double* forwardrates,
+                                 double* backwardrates);                    /* gas_cwrap.d:968-990 */
+
+/* ---- 2. batch entry points ------------------------------------------------------------- */
+/* One operator-split chemistry increment per cell: ChemistryUpdate.opCall
+ * (chemistry_update.d:139-326) over t_interval with the cell's dt_chem as dtSuggest (in/out,
+ * kinetics/thermochemical_reactor.d:44-50), inside the caller contract of
+ * fluidfvcell.d:883-997 (T_frozen skip, optional retry, optional rhou update).
+ * Inputs rho, u are read; T, p, massf, dt_chem are updated in place for cells whose status
+ * is GDTK_CELL_OK; failed or frozen cells are left unchanged.  status may be NULL.
+ * Device pointers, enqueued on `stream`.  Returns 0 or -1 (bad handle/argument, launch error).
+ * One reactor handle serves one stream at a time (its work counter is shared). */
+int chem_reactor_update_cells(int cr_i, int ncell, const double* rho, const double* u, double* T, double* p,
+                              double* massf, double* dt_chem, int* status, double t_interval,
+                              double T_frozen, int flags, void* stream);
+/* As above, also recording per-cell work counters (cell_counters: int[5][ncell] = ODE step
+ * attempts, RHS evaluations, rate-constant evaluations, Newton iterations, rejected attempts;
+ * may be NULL) and their sums (totals: unsigned long long[5], accumulated; may be NULL). */
+int chem_reactor_update_cells_ex(int cr_i, int ncell, const double* rho, const double* u, double* T, double* p,
+                                 double* massf, double* dt_chem, int* status, double t_interval,
+                                 double T_frozen, int flags, void* stream, int* cell_counters,
+                                 unsigned long long* totals);
+/* Host-pointer form: copies in, updates, copies out, synchronises.  Page-locked host buffers
+ * make the copies run at full link speed.  Returns the number of cells that failed (not
+ * counting frozen ones), or -1 on error. */
+int chem_reactor_update_cells_host(int cr_i, int ncell, const double* rho, const double* u, double* T, double* p,
+                                   double* massf, double* dt_chem, int* status, double t_interval,
+                                   double T_frozen, int flags);
+/* Species source terms (kg/m^3/s) of ReactionMechanism.eval_source_terms
+ * (reaction_mechanism.d:98-105): source[isp * ncell + cell].  Device pointers. */
+int chem_reactor_source_terms_cells(int cr_i, int ncell, const double* rho, const double* T, const double* massf,
+                                    double* source, int* status, void* stream);
+/* Gas-state thermo over many cells (therm_perf_gas_mix.d:57-73).  Device pointers. */
+int gas_model_update_thermo_from_pT_cells(int gm_i, int ncell, const double* p, const double* T,
+                                          const double* massf, double* rho, double* u, int* status, void* stream);
+int gas_model_update_thermo_from_rhou_cells(int gm_i, int ncell, const double* rho, const double* u,
+                                            const double* massf, double* T, double* p, int* status, void* stream);
+/* Reactor description: n species, n reactions, ODE method (0 rkf, 1 alpha-qss), tight coupling. */
+int chem_reactor_info(int cr_i, int* nsp, int* nr, int* method, int* tight);
+/* Launch shape of the last chem_reactor_update_cells* call on this reactor. */
+int chem_reactor_last_launch(int cr_i, int* grid, int* block, int* smem_bytes, int* blocks_per_sm);
+/* Text of the last error reported by this library on the calling thread ("" if none). */
+const char* gdtk_last_error(void);
+/* Measures this GPU's FP64 FMA throughput (TFLOP/s) with a register-resident DFMA loop. */
+int gdtk_measure_fp64_peak(double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GDTK_CHEM_H */

@@ -1,0 +1,285 @@
+"""Parity of the CUDA chemistry path with the CPU oracle, cell by cell, through the C ABI.
+
+Bars (from the engine's specification): every mass fraction within 1e-8 absolute and T, p
+within 1e-7 relative of the oracle, which restates the reference's CPU chemistry update
+and is itself pinned to the reference's known-answer tests (tests/test_oracle_kat.py).
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import mech
+
+pytestmark = pytest.mark.gpu
+
+Y_ABS = 1.0e-8
+TP_REL = 1.0e-7
+
+
+def torch_cuda():
+    import torch
+    assert torch.cuda.is_available(), "GPU tests need a CUDA device"
+    return torch
+
+
+@pytest.fixture(scope="module")
+def park5():
+    from gdtk_gb300.cells import ReactorCells
+    return ReactorCells(mech("park5-gas.lua"), mech("park5-chem.lua")), oracle.Oracle(mech("park5-gas.lua"),
+                                                                                        mech("park5-chem.lua"))
+
+
+@pytest.fixture(scope="module")
+def j92():
+    from gdtk_gb300.cells import ReactorCells
+    return ReactorCells(mech("j92-gas.lua"), mech("j92-chem.lua")), oracle.Oracle(mech("j92-gas.lua"),
+                                                                                    mech("j92-chem.lua"))
+
+
+def to_dev(torch, *arrs):
+    return [torch.tensor(np.ascontiguousarray(a), dtype=torch.float64, device="cuda") for a in arrs]
+
+
+def run_pair(rc, orc, T, p, Y, dt, dt_chem0=-1.0, T_frozen=0.0, flags=3):
+    """Same inputs through the GPU and the oracle; returns (gpu dict, oracle dict, rho, u)."""
+    torch = torch_cuda()
+    n = T.shape[0]
+    dT, dp, dY = to_dev(torch, T, p, Y)
+    rho, u = rc.thermo_from_pT(dp, dT, dY)
+    torch.cuda.synchronize()
+    rho_h, u_h = rho.cpu().numpy(), u.cpu().numpy()
+    dtc = torch.full((n,), dt_chem0, dtype=torch.float64, device="cuda")
+    st = torch.zeros(n, dtype=torch.int32, device="cuda")
+    cnt = torch.zeros((5, n), dtype=torch.int32, device="cuda")
+    rc.update(rho, u, dT, dp, dY, dtc, dt, status=st, T_frozen=T_frozen, flags=flags, cell_counters=cnt)
+    torch.cuda.synchronize()
+    g = dict(T=dT.cpu().numpy(), p=dp.cpu().numpy(), Y=dY.cpu().numpy(), dt_chem=dtc.cpu().numpy(),
+             status=st.cpu().numpy(), counters=cnt.cpu().numpy())
+    o = orc.chem_update(rho_h, u_h, T, p, Y.T, np.full(n, dt_chem0), dt, T_frozen=T_frozen,
+                        update_thermo=bool(flags & 1), retry=bool(flags & 2), counters=True)
+    return g, o, rho_h, u_h
+
+
+def assert_parity(g, o, min_same_path=0.99):
+    assert np.array_equal(g["status"], o["status"]), "per-cell status differs"
+    ok = g["status"] == 0
+    dY = np.abs(g["Y"] - o["massf"].T)[:, ok]
+    relT = np.abs(g["T"] - o["T"])[ok] / np.abs(o["T"][ok])
+    relp = np.abs(g["p"] - o["p"])[ok] / np.abs(o["p"][ok])
+    assert dY.max(initial=0.0) <= Y_ABS, "max |dY| = %g" % dY.max()
+    assert relT.max(initial=0.0) <= TP_REL, "max rel dT = %g" % relT.max()
+    assert relp.max(initial=0.0) <= TP_REL, "max rel dp = %g" % relp.max()
+    # The integrators take the same path (same attempts and right-hand-side evaluations)
+    # on nearly every cell; a differing path comes only from a step-acceptance test that
+    # sits within rounding of its threshold.
+    same = (g["counters"][0] == o["counters"][:, 0]) & (g["counters"][1] == o["counters"][:, 1])
+    assert same.mean() >= min_same_path, "only %.4f of cells took the oracle's path" % same.mean()
+
+
+def test_thermo_pT_and_rhou(park5):
+    from gdtk_gb300.workloads import air5_cells
+    torch = torch_cuda()
+    rc, orc = park5
+    T, p, Y = air5_cells(2048, seed=11)
+    dT, dp, dY = to_dev(torch, T, p, Y)
+    rho, u = rc.thermo_from_pT(dp, dT, dY)
+    rho_o, u_o = orc.update_thermo_from_pT(p, T, Y.T)
+    assert np.allclose(rho.cpu().numpy(), rho_o, rtol=1e-13, atol=0)
+    assert np.allclose(u.cpu().numpy(), u_o, rtol=1e-12, atol=1e-6)
+    # round trip: T from (rho, u) starting 5% off
+    T2 = dT * 1.05
+    p2 = torch.zeros_like(dp)
+    st = torch.zeros(2048, dtype=torch.int32, device="cuda")
+    rc.thermo_from_rhou(rho, u, dY, T2, p2, status=st)
+    torch.cuda.synchronize()
+    assert int(st.abs().sum()) == 0
+    assert np.allclose(T2.cpu().numpy(), T, rtol=1e-9)
+    assert np.allclose(p2.cpu().numpy(), p, rtol=1e-9)
+    To, po, sto = orc.update_thermo_from_rhou(rho.cpu().numpy(), u.cpu().numpy(), Y.T, T * 1.05)
+    assert np.allclose(T2.cpu().numpy(), To, rtol=1e-12)
+
+
+def test_air5_rkf_parity(park5):
+    from gdtk_gb300.workloads import air5_cells
+    rc, orc = park5
+    T, p, Y = air5_cells(1024, seed=0)
+    g, o, _, _ = run_pair(rc, orc, T, p, Y, 1.0e-6)
+    assert (g["status"] == 0).all()
+    assert_parity(g, o)
+
+
+def test_air5_warm_start_parity(park5):
+    from gdtk_gb300.workloads import air5_cells
+    rc, orc = park5
+    T, p, Y = air5_cells(512, seed=5)
+    g, o, _, _ = run_pair(rc, orc, T, p, Y, 1.0e-6, dt_chem0=1.0e-9)
+    assert_parity(g, o)
+
+
+def test_h2air_alpha_qss_tight_parity(j92):
+    from gdtk_gb300.workloads import h2air_cells
+    rc, orc = j92
+    T, p, Y = h2air_cells(rc.species_names, rc.mol_masses, 256, seed=3)
+    g, o, _, _ = run_pair(rc, orc, T, p, Y, 1.0e-6)
+    assert (g["status"] == 0).mean() > 0.95
+    assert_parity(g, o)
+
+
+def test_gupta_given_backward_rates_parity():
+    from gdtk_gb300.cells import ReactorCells
+    rc = ReactorCells(mech("gupta5-gas.lua"), mech("gupta5-chem.lua"))
+    orc = oracle.Oracle(mech("gupta5-gas.lua"), mech("gupta5-chem.lua"))
+    rng = np.random.Generator(np.random.PCG64(7))
+    n = 256
+    T = rng.uniform(3000.0, 9000.0, n)
+    p = 10.0 ** rng.uniform(3.0, 5.0, n)
+    Y = np.ascontiguousarray(rng.dirichlet(np.ones(5), n).T)
+    g, o, _, _ = run_pair(rc, orc, T, p, Y, 1.0e-6)
+    assert_parity(g, o)
+
+
+def test_frozen_and_bad_cells(park5):
+    from gdtk_gb300.workloads import air5_cells
+    torch = torch_cuda()
+    rc, orc = park5
+    T, p, Y = air5_cells(64, seed=2)
+    T[:8] = 250.0            # at or below T_frozen -> untouched
+    g, o, rho, u = run_pair(rc, orc, T, p, Y, 1.0e-6, T_frozen=300.0)
+    assert (g["status"][:8] == oracle.ST_FROZEN).all()
+    assert np.array_equal(g["T"][:8], T[:8]) and np.array_equal(g["Y"][:, :8], Y[:, :8])
+    assert_parity(g, o)
+    # invalid density: status BAD_INPUT, state untouched
+    dT, dp, dY = to_dev(torch, T, p, Y)
+    drho, du = to_dev(torch, rho, u)
+    drho[3] = -1.0
+    drho[4] = float("nan")
+    st = torch.zeros(64, dtype=torch.int32, device="cuda")
+    dtc = torch.full((64,), -1.0, dtype=torch.float64, device="cuda")
+    rc.update(drho, du, dT, dp, dY, dtc, 1.0e-6, status=st, T_frozen=300.0)
+    torch.cuda.synchronize()
+    s = st.cpu().numpy()
+    assert s[3] == oracle.ST_BAD_INPUT and s[4] == oracle.ST_BAD_INPUT
+    assert dT[3].item() == T[3] and dT[4].item() == T[4]
+
+
+def test_failure_restores_state_and_retry(tmp_path):
+    # A mechanism allowed only 3 subcycles cannot finish 1e-6 s from a fresh start: both the
+    # first try and the dt_chem = -1 retry hit maxSubcycles; the cell is left as it was.
+    from gdtk_gb300.cells import ReactorCells
+    from gdtk_gb300.workloads import air5_cells
+    src = open(mech("park5-chem.lua")).read().replace("maxSubcycles = 10000", "maxSubcycles = 3")
+    chem = tmp_path / "park5-short.lua"
+    chem.write_text(src)
+    rc = ReactorCells(mech("park5-gas.lua"), str(chem))
+    orc = oracle.Oracle(mech("park5-gas.lua"), str(chem))
+    T, p, Y = air5_cells(64, seed=9)
+    g, o, _, _ = run_pair(rc, orc, T, p, Y, 1.0e-6)
+    assert (g["status"] == oracle.ST_MAX_SUBCYCLES).all()
+    assert np.array_equal(g["T"], T) and np.array_equal(g["Y"], Y) and np.array_equal(g["p"], p)
+    assert np.array_equal(g["status"], o["status"])
+
+
+def test_empty_batch(park5):
+    torch = torch_cuda()
+    rc, _ = park5
+    z = torch.zeros(0, dtype=torch.float64, device="cuda")
+    rc.update(z, z, z.clone(), z.clone(), torch.zeros((5, 0), dtype=torch.float64, device="cuda"), z.clone(), 1e-6)
+    torch.cuda.synchronize()
+
+
+def test_host_entry_point_matches_device(park5):
+    from gdtk_gb300.workloads import air5_cells
+    torch = torch_cuda()
+    rc, _ = park5
+    T, p, Y = air5_cells(300, seed=4)
+    dT, dp, dY = to_dev(torch, T, p, Y)
+    rho, u = rc.thermo_from_pT(dp, dT, dY)
+    rho_h, u_h = rho.cpu().numpy(), u.cpu().numpy()
+    dtc = torch.full((300,), -1.0, dtype=torch.float64, device="cuda")
+    rc.update(rho, u, dT, dp, dY, dtc, 1e-6)
+    torch.cuda.synchronize()
+    Th, ph, Yh, dth = T.copy(), p.copy(), Y.copy(), np.full(300, -1.0)
+    nfail = rc.update_host(rho_h, u_h, Th, ph, Yh, dth, 1e-6)
+    assert nfail == 0
+    assert np.array_equal(Th, dT.cpu().numpy()) and np.array_equal(Yh, dY.cpu().numpy())
+    assert np.array_equal(dth, dtc.cpu().numpy())
+
+
+def test_source_terms(j92):
+    from gdtk_gb300.workloads import h2air_cells
+    torch = torch_cuda()
+    rc, orc = j92
+    T, p, Y = h2air_cells(rc.species_names, rc.mol_masses, 128, seed=8)
+    dT, dp, dY = to_dev(torch, T, p, Y)
+    rho, _ = rc.thermo_from_pT(dp, dT, dY)
+    src = rc.source_terms(rho, dT, dY).cpu().numpy()
+    rho_h = rho.cpu().numpy()
+    for c in range(0, 128, 7):
+        conc = Y[:, c] * rho_h[c] / orc.M
+        conc[conc < 1e-30] = 0.0
+        q, L, _, _ = orc.split_rates(T[c], conc)
+        want = (q - L) * orc.M
+        scale = np.abs(want).max() + 1e-300
+        assert np.abs(src[:, c] - want).max() <= 1e-12 * scale
+
+
+def test_fixed_volume_reactor_through_gas_api():
+    # examples/kinetics/fixed-volume-reactor-n2/test_fvreactor.py through the mirrored gdtk.gas API
+    from gdtk_gb300.gas import GasModel, PyGasState as GasState, ThermochemicalReactor
+    from math import isclose
+    gm = GasModel(mech("n2-gas.lua"))
+    reactor = ThermochemicalReactor(gm, mech("n2-chem.lua"))
+    gs = GasState(gm)
+    gs.p = 1.0e5
+    gs.T = 4000.0
+    gs.molef = {'N2': 2 / 3, 'N': 1 / 3}
+    gs.update_thermo_from_pT()
+    tFinal = 300.0e-6
+    t = 0.0
+    dt = 1.0e-6
+    dtSuggest = 1.0e-11
+    while t <= tFinal:
+        dtSuggest = reactor.update_state(gs, dt, dtSuggest)
+        t = t + dt
+        gs.update_thermo_from_rhou()
+    assert isclose(t, tFinal, rel_tol=1.0e-6)
+    assert isclose(gs.T, 6177.3, rel_tol=1.0e-4)
+    assert isclose(gs.p, 145.518e3, rel_tol=1.0e-4)
+    assert isclose(gs.massf[0], 8.692812671003e-01, rel_tol=1.0e-4)
+    assert isclose(gs.massf[1], 1.307187328997e-01, rel_tol=1.0e-4)
+    assert isclose(gs.conc[0], 2.178123112237e+00, rel_tol=1.0e-4)
+    assert isclose(gs.conc[1], 6.550733441684e-01, rel_tol=1.0e-4)
+
+
+def test_h2_i2_full_update_kat():
+    # kinetics/chemistry_update.d:736-750 through the per-state C ABI
+    from gdtk_gb300.gas import GasModel, GasState, ThermochemicalReactor
+    from math import isclose
+    gm = GasModel(mech("h2i2-gas.lua"))
+    reactor = ThermochemicalReactor(gm, mech("h2i2-chem.lua"))
+    gs = GasState(gm)
+    gs.T = 700.0
+    gs.p = 2.0 * 4.54 * 8.31451 * 700.0
+    gs.molef = [0.5, 0.5, 0.0]
+    gs.update_thermo_from_pT()
+    reactor.update_state(gs, 60_000.0, 200.0)
+    assert isclose(7.14201983840, gs.conc[2], rel_tol=1.0e-9)
+
+
+def test_tickrates_match_oracle():
+    from gdtk_gb300.gas import GasModel, GasState, ReactionMechanism
+    gm = GasModel(mech("j92-gas.lua"))
+    rm = ReactionMechanism(gm, mech("j92-chem.lua"))
+    orc = oracle.Oracle(mech("j92-gas.lua"), mech("j92-chem.lua"), T_limits=(300.0, 30000.0))
+    gs = GasState(gm)
+    gs.T = 1500.0
+    gs.p = 1.0e5
+    gs.molef = {'H2': 0.25, 'O2': 0.15, 'N2': 0.5, 'H2O': 0.05, 'OH': 0.02, 'H': 0.02, 'O': 0.01}
+    gs.update_thermo_from_pT()
+    f = np.array(rm.forward_tickrates(gs))
+    b = np.array(rm.backward_tickrates(gs))
+    conc = np.array(gs.conc)
+    _, _, wf, wb = orc.split_rates(1500.0, conc)
+    assert np.allclose(f, wf, rtol=1e-13, atol=0) and np.allclose(b, wb, rtol=1e-13, atol=0)
