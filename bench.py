@@ -1,0 +1,315 @@
+"""Throughput benchmark of the operator-split chemistry update (one JSON line on stdout).
+
+Workload (default): 1,048,576 independent cells of 13-species H2-air (Jachimowski 1992,
+33 reactions, alpha-QSS with tight temperature coupling, as its mechanism file says), half
+cold (300-600 K) and half igniting (1100-2800 K), p = 10^U[log10 2e4, log10 5e5] Pa, one
+chemistry update of dt = 1e-6 s per cell from a fresh step size (dt_chem = -1), followed
+by update_thermo_from_rhou, i.e. one thermochemical_increment per cell.  A step is that
+update over all cells; before each step the seeded initial state is restored on the device
+(the restore copy is inside the timed region; it is < 0.1% of a step).  The cell arrays
+(~150 MB) exceed the 129 MB L2, so no separate L2 flush is done.
+
+--impl gdtk (default): the CUDA engine (gdtk_gb300).  `value` = cells/s with inputs resident in
+HBM; `e2e` = the same through the host-pointer C-ABI entry point
+(chem_reactor_update_cells_host) from page-locked host arrays, copies included.
+--impl reference: the reference algorithm on the host CPU cores (oracle/, a C++ restatement of
+the reference's CPU chemistry update, OpenMP over cells), on a bounded sample of the same cells.
+
+Multi-GPU (torchrun): each rank integrates its own replica of the cells (cells are
+independent; there is no data exchange), `value` = all ranks' cells / max time.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+MECH = os.path.join(ROOT, "tests", "golden", "mech")
+METRIC = "cell chem updates/s: plain FP64 vs surrogate+fallback at ≤1e-4 ΔY, 1 GB300"
+
+WORKLOADS = {
+    "h2air-1M": dict(gas="j92-gas.lua", chem="j92-chem.lua", n=1048576, dt=1.0e-6, kind="h2air", seed=1),
+    "air5-4096": dict(gas="park5-gas.lua", chem="park5-chem.lua", n=4096, dt=1.0e-6, kind="air5", seed=0),
+}
+
+
+def make_cells(w, names=None, M=None, n=None):
+    from gdtk_gb300.workloads import air5_cells, h2air_cells
+    n = n or w["n"]
+    if w["kind"] == "air5":
+        return air5_cells(n, seed=w["seed"])
+    return h2air_cells(names, M, n, seed=w["seed"])
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm = [float(r[1]) for r in self.rows if len(r) >= 9 and r[1].replace('.', '', 1).isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) >= 9 and r[2].replace('.', '', 1).isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            if len(r) < 9:
+                continue
+            for k, name in enumerate(names):
+                if r[5 + k].lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def fp64_peak_reference():
+    """The FP64 roofline denominator: measured on this GPU by the library's DFMA probe."""
+    from gdtk_gb300.cells import measure_fp64_peak
+    return max(measure_fp64_peak() for _ in range(3))
+
+
+def cpu_reference_run(w, T, p, Y, rho, u, max_seconds, nthreads=0):
+    """Times the oracle (reference algorithm, C++ restatement) on a bounded sample of cells."""
+    import oracle
+    orc = oracle.Oracle(os.path.join(MECH, w["gas"]), os.path.join(MECH, w["chem"]))
+    n_total = T.shape[0]
+    threads = nthreads if nthreads > 0 else oracle.max_threads()
+
+    def run(idx):
+        t0 = time.perf_counter()
+        out = orc.chem_update(rho[idx], u[idx], T[idx], p[idx], Y[:, idx].T, np.full(len(idx), -1.0), w["dt"],
+                              nthreads=threads)
+        return time.perf_counter() - t0, out
+
+    # probe with a small strided sample, then size the sample to about max_seconds
+    probe = np.arange(0, n_total, max(n_total // 256, 1))[:256]
+    dt_probe, _ = run(probe)
+    per_cell = dt_probe / len(probe)
+    m = int(min(n_total, max(len(probe), max_seconds / max(per_cell, 1e-9))))
+    idx = np.linspace(0, n_total - 1, m).astype(np.int64)
+    secs, out = run(idx)
+    return dict(value=m / secs, cells=m, seconds=secs, threads=threads, out=out, idx=idx)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gdtk", "reference"], default="gdtk")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="h2air-1M")
+    ap.add_argument("--cells", type=int, default=0, help="override the cell count (parity/debug runs)")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    w = dict(WORKLOADS[args.workload])
+    if args.cells:
+        w["n"] = args.cells
+    ws, rank, local = dist_env()
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        from gdtk_gb300.gas import GasModel
+        # gas-state setup (rho, u from p, T) uses the same CPU oracle as the timed run
+        import oracle
+        orc = oracle.Oracle(os.path.join(MECH, w["gas"]))
+        gm_names = orc.names
+        T, p, Y = make_cells(w, gm_names, orc.M)
+        rho, u = orc.update_thermo_from_pT(p, T, Y.T)
+        steps = []
+        for s in range(args.warmup + args.steps):
+            r = cpu_reference_run(w, T, p, Y, rho, u, max_seconds=min(args.cpu_seconds, 20.0))
+            if s >= args.warmup:
+                steps.append(r)
+        v = float(np.mean([r["value"] for r in steps]))
+        line = {
+            "impl": "reference", "metric": METRIC, "value": v, "unit": "cell-updates/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": float(np.mean([r["seconds"] for r in steps]) * 1e3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "cells": w["n"], "dt": w["dt"], "mechanism": w["chem"],
+                       "sample_cells_per_step": steps[0]["cells"]},
+            "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": steps[0]["threads"], "kind": "port",
+                             "sample": "%d of the %d cells (evenly strided) per step, all host threads" %
+                                       (steps[0]["cells"], w["n"])},
+            "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }
+        print(json.dumps(line))
+        return 0
+
+    import torch
+    import gdtk_gb300
+    if not os.path.exists(gdtk_gb300.LIB_PATH):
+        gdtk_gb300.build()
+    gdtk_gb300.lib()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    from gdtk_gb300.cells import ReactorCells, UPDATE_THERMO, RETRY
+    dev = torch.device("cuda", local if ws > 1 else 0)
+    rc = ReactorCells(os.path.join(MECH, w["gas"]), os.path.join(MECH, w["chem"]))
+    n = w["n"]
+    T0, p0, Y0 = make_cells(w, rc.species_names, rc.mol_masses)
+    flags = UPDATE_THERMO | RETRY
+
+    def t64(a):
+        return torch.tensor(np.ascontiguousarray(a), dtype=torch.float64, device=dev)
+
+    sT, sp, sY = t64(T0), t64(p0), t64(Y0)
+    srho, su = rc.thermo_from_pT(sp, sT, sY)
+    sdt = torch.full((n,), -1.0, dtype=torch.float64, device=dev)
+    T, p, Y, dtc = sT.clone(), sp.clone(), sY.clone(), sdt.clone()
+    st = torch.zeros(n, dtype=torch.int32, device=dev)
+    totals = torch.zeros(6, dtype=torch.int64, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def step(tot=None):
+        T.copy_(sT); p.copy_(sp); Y.copy_(sY); dtc.copy_(sdt)
+        rc.update(srho, su, T, p, Y, dtc, w["dt"], status=st, flags=flags, totals=tot)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    peak = fp64_peak_reference()
+
+    if ws > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local if ws > 1 else int(os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] or 0))
+    clocks.start()
+    totals.zero_()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    k0 = torch.cuda.Event(enable_timing=True)
+    k1 = torch.cuda.Event(enable_timing=True)
+    k0.record(stream)
+    for s in range(args.steps):
+        T.copy_(sT); p.copy_(sp); Y.copy_(sY); dtc.copy_(sdt)
+        ev[s][0].record(stream)
+        rc.update(srho, su, T, p, Y, dtc, w["dt"], status=st, flags=flags, totals=totals)
+        ev[s][1].record(stream)
+    k1.record(stream)
+    torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    clk = clocks.stop()
+    total_ms = k0.elapsed_time(k1)
+    launch_ms = [a.elapsed_time(b) for a, b in ev]
+    if ws > 1:
+        t = torch.tensor([total_ms], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = n * ws * args.steps / (total_ms * 1e-3)
+    status = st.cpu().numpy()
+    tot = totals.cpu().numpy().astype(np.float64)
+    flops = rc.algorithmic_flops(tot / args.steps)
+    kernel_ms = float(np.mean(launch_ms))
+    achieved = flops / (kernel_ms * 1e-3) / 1e12
+
+    # ---- end to end through the host-pointer C ABI (page-locked host arrays)
+    e2e = None
+    if not args.no_e2e:
+        pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+        hrho, hu = pin(srho.cpu().numpy()), pin(su.cpu().numpy())
+        hT, hp, hY, hdt = pin(T0), pin(p0), pin(Y0), pin(np.full(n, -1.0))
+        hst = pin(np.zeros(n, np.int32))
+        rc.update_host(hrho, hu, hT.copy(), hp.copy(), hY.copy(), hdt.copy(), w["dt"], status=hst, flags=flags)
+        e2e_steps = max(1, min(args.steps, 3))
+        times = []
+        for _ in range(e2e_steps):
+            hT[:] = T0; hp[:] = p0; hY[:] = Y0; hdt[:] = -1.0
+            t0 = time.perf_counter()
+            rc.update_host(hrho, hu, hT, hp, hY, hdt, w["dt"], status=hst, flags=flags)
+            times.append(time.perf_counter() - t0)
+        nsp = rc.nsp
+        e2e = {"value": n * ws / float(np.mean(times)), "unit": "cell-updates/s",
+               "h2d_bytes_per_step": n * 8 * (5 + nsp), "d2h_bytes_per_step": n * (8 * (3 + nsp) + 4),
+               "steps": e2e_steps}
+
+    # ---- CPU baseline (reference algorithm on the host cores), rank 0 at N=1 only
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        r = cpu_reference_run(w, T0, p0, Y0, srho.cpu().numpy(), su.cpu().numpy(), max_seconds=args.cpu_seconds)
+        cpu = {"value": r["value"], "unit": "cell-updates/s", "cores": r["threads"], "kind": "port",
+               "sample": "%d of the %d cells (evenly strided), %.1f s on %d threads" %
+                         (r["cells"], n, r["seconds"], r["threads"])}
+
+    if rank == 0:
+        traffic = None
+        prof = os.path.join(ROOT, "profiles", "traffic.json")
+        if os.path.exists(prof):
+            with open(prof) as f:
+                tj = json.load(f).get(args.workload)
+            if tj:
+                traffic = tj["bytes_per_cell"] * n
+        ok = int((status == 0).sum())
+        line = {
+            "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "cells_per_gpu": n, "mechanism": w["chem"], "dt": w["dt"],
+                       "method": rc.method, "tight_coupling": rc.tight, "dt_chem_in": -1.0,
+                       "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas x%d" % ws,
+                       "cells_ok": ok, "cells_failed": int(n - ok)},
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "peak_source": "measured: gdtk_measure_fp64_peak DFMA probe on this GPU (no FP64 "
+                                        "entry in MEASURED_PEAKS.json)",
+                         "flops_per_launch": flops, "kernel_ms": kernel_ms,
+                         "work_per_cell": (tot / args.steps / n).tolist()},
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "clocks": clk,
+            "gpu_launches": args.steps,
+        }
+        print(json.dumps(line))
+    if ws > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

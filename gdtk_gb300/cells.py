@@ -104,6 +104,19 @@ class ReactorCells:
                                                     _stream()), "chem_reactor_source_terms_cells")
         return out
 
+    def flop_model(self):
+        """[F_kc, F_rhs, F_step, F_corr, F_newton]: reference-algorithm FP64 operations per unit."""
+        out = (ctypes.c_double * 5)()
+        check(lib().chem_reactor_flop_model(self.reactor.id, out), "chem_reactor_flop_model")
+        return [out[i] for i in range(5)]
+
+    def algorithmic_flops(self, totals, n_cells_counted=None):
+        """FLOPs of a batch from its work counters [steps, rhs, kc, newton, rejects, estimates]."""
+        F = self.flop_model()
+        steps, rhs, kc, newton, _, est = [float(x) for x in totals]
+        corr = max(rhs - steps - est, 0.0) if self.method == "alpha-qss" else 0.0
+        return F[0] * kc + F[1] * rhs + F[2] * steps + F[3] * corr + F[4] * newton
+
     def last_launch(self):
         v = [ctypes.c_int() for _ in range(4)]
         check(lib().chem_reactor_last_launch(self.reactor.id, *[ctypes.byref(x) for x in v]), "last_launch")

@@ -657,6 +657,14 @@ int gas_model_update_thermo_from_rhou_cells(int gm_i, int ncell, const double* r
     });
 }
 
+int chem_reactor_flop_model(int cr_i, double* out) {
+    return guarded([&] {
+        auto& r = reactor(cr_i);
+        flop_model(model(r.gm).gm, r.mh, out);
+        return 0;
+    });
+}
+
 int chem_reactor_info(int cr_i, int* nsp, int* nr, int* method, int* tight) {
     return guarded([&] {
         auto& r = reactor(cr_i);

@@ -411,7 +411,7 @@ __global__ void __launch_bounds__(256) chem_update_kernel(ChemUpdateArgs a) {
     bool have = false, retried = false, need_kc = false;
     int phase = 0, cycle = 0, attempt = 0, err = 0;
     double rho = 0, u = 0, T = 0, T0 = 0, p = 0, p0 = 0, dtS = 0, dtS0 = 0, dtSave = 0, h = 0, t = 0;
-    int n_steps = 0, n_rhs = 0, n_kc = 0, n_newton = 0, n_rej = 0;
+    int n_steps = 0, n_rhs = 0, n_kc = 0, n_newton = 0, n_rej = 0, n_est = 0;
 
     while (true) {
         if (!have) {
@@ -428,7 +428,7 @@ __global__ void __launch_bounds__(256) chem_update_kernel(ChemUpdateArgs a) {
             }
             have = true;
             retried = false;
-            n_steps = n_rhs = n_kc = n_newton = n_rej = 0;
+            n_steps = n_rhs = n_kc = n_newton = n_rej = n_est = 0;
             phase = -1;
         }
         if (phase == -1) {   // (re)start the update from the stored input state
@@ -450,6 +450,7 @@ __global__ void __launch_bounds__(256) chem_update_kernel(ChemUpdateArgs a) {
             else if (dtS <= 0.0) {
                 split_rates(m, y0, q, L, kf, kb, meff);
                 ++n_rhs;
+                ++n_est;
                 h = estimate_from_rates(nsp, y0, q, L);
             } else h = dtS;
             cycle = 0;
@@ -547,6 +548,7 @@ __global__ void __launch_bounds__(256) chem_update_kernel(ChemUpdateArgs a) {
                 a.cell_counters[2 * (size_t)ncell + c] = n_kc;
                 a.cell_counters[3 * (size_t)ncell + c] = n_newton;
                 a.cell_counters[4 * (size_t)ncell + c] = n_rej;
+                a.cell_counters[5 * (size_t)ncell + c] = n_est;
             }
             if (a.totals) {
                 atomicAdd(a.totals + 0, (unsigned long long)n_steps);
@@ -554,6 +556,7 @@ __global__ void __launch_bounds__(256) chem_update_kernel(ChemUpdateArgs a) {
                 atomicAdd(a.totals + 2, (unsigned long long)n_kc);
                 atomicAdd(a.totals + 3, (unsigned long long)n_newton);
                 atomicAdd(a.totals + 4, (unsigned long long)n_rej);
+                atomicAdd(a.totals + 5, (unsigned long long)n_est);
             }
         }
     }
@@ -639,6 +642,8 @@ cudaError_t launch_chem_update(const ChemUpdateArgs& a, int method, int scratch_
     const size_t limit = 227 * 1024;
     int block = 256;
     while (block > 32 && mech + (size_t)scratch_doubles * 8 * block > limit) block /= 2;
+    // Small batches: narrower blocks so that the cells spread over every SM.
+    while (block > 32 && ((long long)a.ncell + block - 1) / block < sm_count) block /= 2;
     size_t smem = mech + (size_t)scratch_doubles * 8 * block;
     if (smem > limit) return cudaErrorInvalidConfiguration;
     const void* fn = method == METHOD_RKF ? (const void*)chem_update_kernel<METHOD_RKF>

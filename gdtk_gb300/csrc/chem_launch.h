@@ -23,8 +23,9 @@ struct ChemUpdateArgs {
     double T_frozen;
     int flags;
     unsigned* counter;        // work counter, zero at launch
-    int* cell_counters;       // optional [5][ncell]: steps, rhs, rate-constant evals, Newton iters, rejects
-    unsigned long long* totals;   // optional [5], same quantities summed
+    int* cell_counters;       // optional [6][ncell]: step attempts, rhs, rate-constant evals, Newton
+                              // iterations, rejected attempts, initial step-size estimates
+    unsigned long long* totals;   // optional [6], same quantities summed
 };
 
 struct GasServiceArgs {

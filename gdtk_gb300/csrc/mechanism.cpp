@@ -257,4 +257,59 @@ PackedMech pack(const GasModelHost& gm, const MechanismHost* mh) {
     return pm;
 }
 
+// Operation counts of the reference expressions, term by term (add/sub/mul/div/sqrt = 1,
+// exp/log = 20, pow = 40; comparisons and copies are free).
+void flop_model(const GasModelHost& gm, const MechanismHost& mh, double out[5]) {
+    const double EXP = 20, LOG = 20, POW = 40;
+    const int nsp = gm.n_species();
+    // eval_rate_constants: log T, log(p/P_atm) and its division; per species eval_h (29),
+    // eval_s with the pressure term (28) and g = h - T s (2) (therm_perf_gas_mix.d:354-364).
+    double kc = 2 * LOG + 1 + 59.0 * nsp;
+    // eval_split_rates: distinct third-body sums (2 per efficiency), then per reaction the
+    // collider products, the concentration powers and four operations per participant.
+    std::vector<std::vector<std::pair<int, double>>> sets;
+    double rhs = 0;
+    for (auto& r : mh.reactions) {
+        std::vector<int> part;
+        for (auto& x : r.reac) part.push_back(x.first);
+        for (auto& x : r.prod) part.push_back(x.first);
+        std::sort(part.begin(), part.end());
+        part.erase(std::unique(part.begin(), part.end()), part.end());
+        // rate constants (rate_constant.d:72-75, reaction.d:26-52, 94-143)
+        const double arr = POW + EXP + 3;
+        if (r.frc.model == RATE_FROM_EQ || r.brc.model == RATE_FROM_EQ)
+            kc += arr + 4.0 * part.size() + (EXP + 2) + 3 + 1 + 1;
+        else
+            kc += 2 * arr;
+        if (r.collider) {
+            if (std::find(sets.begin(), sets.end(), r.eff) == sets.end()) {
+                sets.push_back(r.eff);
+                rhs += 2.0 * r.eff.size();
+            }
+            rhs += 2;
+        }
+        for (auto& x : r.reac) rhs += x.second;
+        for (auto& x : r.prod) rhs += x.second;
+        for (int isp : part) {
+            int nu1 = 0, nu2 = 0;
+            for (auto& x : r.reac) if (x.first == isp) { nu1 = x.second; break; }
+            for (auto& x : r.prod) if (x.first == isp) { nu2 = x.second; break; }
+            if (nu2 != nu1) rhs += 4;
+        }
+    }
+    double step, corr = 0;
+    if (mh.method == METHOD_RKF) {
+        rhs += nsp;                              // rates = q - L
+        step = 62.0 * nsp + 2 + POW + 2 + 3.0 * nsp;   // chemistry_update.d:417-477 + mass test
+    } else {
+        step = 32.0 * nsp + 4.0 * nsp + 18 + 3.0 * nsp;   // predictor, step_suggest, mass test
+        corr = 41.0 * nsp;                       // chemistry_update.d:546-558 per corrector
+    }
+    step += 2;                                   // t += h, hMax
+    // update_temperature_from_energy: per iteration Cv (23 per species), log T and u(T)
+    // (33 per species) and the update/convergence arithmetic.
+    double newton = 56.0 * nsp + LOG + 4;
+    out[0] = kc; out[1] = rhs; out[2] = step; out[3] = corr; out[4] = newton;
+}
+
 }  // namespace gdtk

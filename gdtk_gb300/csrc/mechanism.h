@@ -57,5 +57,7 @@ GasModelHost load_gas_model(const std::string& path);
 // reads `reaction` (and `config` when with_config) of a prep-chem file; checks species order.
 MechanismHost load_mechanism(const std::string& path, const GasModelHost& gm, bool with_config);
 PackedMech pack(const GasModelHost& gm, const MechanismHost* mech);
+// Reference-algorithm FP64 operation counts (see chem_reactor_flop_model in gdtk_chem.h).
+void flop_model(const GasModelHost& gm, const MechanismHost& mh, double out[5]);
 
 }  // namespace gdtk

@@ -85,9 +85,10 @@ int reaction_mechanism_tickrates(int rm_i, int gm_i, int gs_i, double* forwardra
 int chem_reactor_update_cells(int cr_i, int ncell, const double* rho, const double* u, double* T, double* p,
                               double* massf, double* dt_chem, int* status, double t_interval,
                               double T_frozen, int flags, void* stream);
-/* As above, also recording per-cell work counters (cell_counters: int[5][ncell] = ODE step
- * attempts, RHS evaluations, rate-constant evaluations, Newton iterations, rejected attempts;
- * may be NULL) and their sums (totals: unsigned long long[5], accumulated; may be NULL). */
+/* As above, also recording per-cell work counters (cell_counters: int[6][ncell] = ODE step
+ * attempts, RHS evaluations, rate-constant evaluations, Newton iterations, rejected attempts,
+ * initial step-size estimates; may be NULL) and their sums (totals: unsigned long long[6],
+ * accumulated; may be NULL). */
 int chem_reactor_update_cells_ex(int cr_i, int ncell, const double* rho, const double* u, double* T, double* p,
                                  double* massf, double* dt_chem, int* status, double t_interval,
                                  double T_frozen, int flags, void* stream, int* cell_counters,
@@ -107,6 +108,14 @@ int gas_model_update_thermo_from_pT_cells(int gm_i, int ncell, const double* p, 
                                           const double* massf, double* rho, double* u, int* status, void* stream);
 int gas_model_update_thermo_from_rhou_cells(int gm_i, int ncell, const double* rho, const double* u,
                                             const double* massf, double* T, double* p, int* status, void* stream);
+/* Algorithmic FP64 operation counts of the reference algorithm for this mechanism, per unit of
+ * work: out[0] per rate-constant evaluation (Gibbs energies, k_f, K_c, k_b), out[1] per RHS
+ * evaluation (eval_split_rates, plus q - L for rkf), out[2] per ODE step attempt (stage
+ * combinations or alpha-QSS predictor, error/convergence control, mass-fraction test),
+ * out[3] per alpha-QSS corrector iteration beyond its RHS, out[4] per Newton iteration of
+ * T from (rho, u).  add/sub/mul/div/sqrt count 1, exp and log 20, pow 40.  Multiplying by
+ * the work counters of chem_reactor_update_cells_ex gives the FLOPs of a batch. */
+int chem_reactor_flop_model(int cr_i, double* out);
 /* Reactor description: n species, n reactions, ODE method (0 rkf, 1 alpha-qss), tight coupling. */
 int chem_reactor_info(int cr_i, int* nsp, int* nr, int* method, int* tight);
 /* Launch shape of the last chem_reactor_update_cells* call on this reactor. */

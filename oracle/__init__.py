@@ -166,7 +166,7 @@ class Oracle:
 
     def update_thermo_from_pT(self, p, T, massf):
         p = np.ascontiguousarray(p, np.float64); T = np.ascontiguousarray(T, np.float64)
-        mf = np.ascontiguousarray(massf, np.float64).reshape(len(p), self.nsp)
+        mf = np.array(massf, np.float64, order='C').reshape(len(p), self.nsp)
         rho = np.empty_like(p); u = np.empty_like(p)
         rc = lib().oracle_update_thermo_from_pT(self.h, len(p), _dp(p), _dp(T), _dp(mf), _dp(rho), _dp(u))
         if rc:
@@ -175,7 +175,7 @@ class Oracle:
 
     def update_thermo_from_rhou(self, rho, u, massf, T_guess, p=None):
         rho = np.ascontiguousarray(rho, np.float64); u = np.ascontiguousarray(u, np.float64)
-        mf = np.ascontiguousarray(massf, np.float64).reshape(len(rho), self.nsp)
+        mf = np.array(massf, np.float64, order='C').reshape(len(rho), self.nsp)
         T = np.array(T_guess, np.float64, copy=True).reshape(len(rho))
         pp = np.zeros_like(rho) if p is None else np.array(p, np.float64, copy=True)
         st = np.zeros(len(rho), np.int32)
@@ -220,7 +220,7 @@ class Oracle:
         n = len(rho)
         rho = np.ascontiguousarray(rho, np.float64); u = np.ascontiguousarray(u, np.float64)
         T = np.array(T, np.float64, copy=True); p = np.array(p, np.float64, copy=True)
-        mf = np.array(massf, np.float64, copy=True).reshape(n, self.nsp)
+        mf = np.array(massf, np.float64, order='C', copy=True).reshape(n, self.nsp)
         dt = np.array(dt_chem, np.float64, copy=True).reshape(n)
         st = np.zeros(n, np.int32)
         cnt = np.zeros((n, 5), np.int64) if counters else None

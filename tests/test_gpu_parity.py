@@ -52,7 +52,7 @@ def run_pair(rc, orc, T, p, Y, dt, dt_chem0=-1.0, T_frozen=0.0, flags=3):
     rho_h, u_h = rho.cpu().numpy(), u.cpu().numpy()
     dtc = torch.full((n,), dt_chem0, dtype=torch.float64, device="cuda")
     st = torch.zeros(n, dtype=torch.int32, device="cuda")
-    cnt = torch.zeros((5, n), dtype=torch.int32, device="cuda")
+    cnt = torch.zeros((6, n), dtype=torch.int32, device="cuda")
     rc.update(rho, u, dT, dp, dY, dtc, dt, status=st, T_frozen=T_frozen, flags=flags, cell_counters=cnt)
     torch.cuda.synchronize()
     g = dict(T=dT.cpu().numpy(), p=dp.cpu().numpy(), Y=dY.cpu().numpy(), dt_chem=dtc.cpu().numpy(),
