@@ -68,6 +68,11 @@ SIGNATURES = {
     "chem_reactor_info": (ctypes.c_int, [ctypes.c_int, _i, _i, _i, _i]),
     "chem_reactor_last_launch": (ctypes.c_int, [ctypes.c_int, _i, _i, _i, _i]),
     "gdtk_last_error": (ctypes.c_char_p, []),
+    "gdtk_generate_fast_source": (ctypes.c_int, [_c, _c, _c, ctypes.c_int]),
+    "gdtk_exp_host": (ctypes.c_int, [ctypes.c_int, _d, _d]),
+    "gdtk_compile_fast_source_check": (ctypes.c_int, [_c, _c, ctypes.c_int, ctypes.c_int, _c, ctypes.c_int]),
+    "chem_reactor_fast_source": (ctypes.c_int, [ctypes.c_int, _c, ctypes.c_int]),
+    "chem_reactor_jit_log": (ctypes.c_int, [ctypes.c_int, _c, ctypes.c_int]),
     "gdtk_measure_fp64_peak": (ctypes.c_int, [_d]),
 }
 
@@ -92,6 +97,23 @@ def lib():
             f.argtypes = args
         _lib = L
     return _lib
+
+
+def generate_fast_source(gas_file, chem_file):
+    """CUDA source of the mechanism-specialised kernel (no GPU needed)."""
+    L = lib()
+    n = check(L.gdtk_generate_fast_source(gas_file.encode(), chem_file.encode(), None, 0), "generate source")
+    buf = ctypes.create_string_buffer(n)
+    check(L.gdtk_generate_fast_source(gas_file.encode(), chem_file.encode(), buf, n), "generate source")
+    return buf.value.decode()
+
+
+def compile_fast_source_check(gas_file, chem_file, cc=(10, 3)):
+    """NVRTC-compiles the mechanism kernel for sm_<cc> (no GPU needed); returns the ptxas log."""
+    buf = ctypes.create_string_buffer(1 << 16)
+    check(lib().gdtk_compile_fast_source_check(gas_file.encode(), chem_file.encode(), cc[0], cc[1], buf, 1 << 16),
+          "NVRTC compile")
+    return buf.value.decode()
 
 
 def last_error():

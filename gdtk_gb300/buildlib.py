@@ -18,12 +18,35 @@ NVCC = os.environ.get("NVCC", "nvcc")
 
 SOURCES = [
     ("chem_kernels.cu", ["--fmad=false"]),
+    ("codegen.cpp", []),
     ("fp64_probe.cu", []),
     ("chem_api.cpp", []),
     ("mechanism.cpp", []),
     ("lua_table.cpp", []),
 ]
-HEADERS = ["chem_types.h", "chem_launch.h", "cea_thermo.h", "lua_table.h", "mechanism.h"]
+HEADERS = ["chem_types.h", "chem_launch.h", "cea_thermo.h", "lua_table.h", "mechanism.h", "codegen.h", "fast_exp.h",
+           "chem_fast.cuh"]
+# sources compiled at run time by NVRTC, embedded in the library as string literals
+EMBEDDED = [("kFastCuhSource", "chem_fast.cuh"), ("kFastExpSource", "fast_exp.h")]
+
+
+def _write_embedded():
+    path = os.path.join(OUT_DIR, "embedded_sources.cpp")
+    parts = ["// generated by buildlib.py from csrc/: sources compiled at run time by NVRTC",
+             "namespace gdtk {"]
+    for name, fn in EMBEDDED:
+        with open(os.path.join(CSRC, fn)) as f:
+            text = f.read()
+        if ")GDTKSRC\"" in text:
+            raise RuntimeError("embedded source contains the raw-string delimiter")
+        parts.append('extern const char* const %s = R"GDTKSRC(%s)GDTKSRC";' % (name, text))
+    parts.append("}")
+    new = "\n".join(parts) + "\n"
+    old = open(path).read() if os.path.exists(path) else None
+    if old != new:
+        with open(path, "w") as f:
+            f.write(new)
+    return path
 
 
 def _newer(target, deps):
@@ -34,25 +57,37 @@ def _newer(target, deps):
 
 
 def _compile(src, extra):
-    obj = os.path.join(OUT_DIR, src + ".o")
-    deps = [os.path.join(CSRC, src)] + [os.path.join(CSRC, h) for h in HEADERS] + \
+    obj = os.path.join(OUT_DIR, os.path.basename(src) + ".o")
+    srcpath = src if os.path.isabs(src) else os.path.join(CSRC, src)
+    deps = [srcpath] + [os.path.join(CSRC, h) for h in HEADERS] + \
            [os.path.join(HERE, "..", "include", "gdtk_chem.h"), __file__]
     if not _newer(obj, deps):
         return obj
     cmd = [NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
-                           "-I", CSRC, "-c", os.path.join(CSRC, src), "-o", obj] + extra
+                           "-I", CSRC, "-c", srcpath, "-o", obj] + extra
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (src, r.stdout, r.stderr))
     return obj
 
 
+def _which(prog):
+    for d in os.environ.get("PATH", "").split(os.pathsep):
+        c = os.path.join(d, prog)
+        if os.path.isfile(c) and os.access(c, os.X_OK):
+            return os.path.realpath(c)
+    return "/usr/local/cuda/bin/nvcc"
+
+
 def build(verbose=False):
     os.makedirs(OUT_DIR, exist_ok=True)
-    with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        objs = list(ex.map(lambda s: _compile(*s), SOURCES))
+    sources = SOURCES + [(_write_embedded(), [])]
+    with ThreadPoolExecutor(max_workers=len(sources)) as ex:
+        objs = list(ex.map(lambda s: _compile(*s), sources))
     if _newer(LIB, objs):
-        cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
+        cuda_lib = os.path.join(os.path.dirname(os.path.dirname(_which(NVCC))), "lib64")
+        cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart", "-lnvrtc",
+                                                             "-Xlinker", "-rpath," + cuda_lib]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))

@@ -17,6 +17,8 @@
 #include "../../include/gdtk_chem.h"
 #include "chem_launch.h"
 #include "chem_types.h"
+#include "codegen.h"
+#include "fast_exp.h"
 #include "mechanism.h"
 
 namespace gdtk {
@@ -135,6 +137,7 @@ struct ReactorObj {
     unsigned* counter = nullptr;
     Staging stage;
     LaunchInfo last{};
+    std::unique_ptr<FastKernel> fast;   // mechanism-specialised kernel, compiled on first use
     ~ReactorObj() { if (counter) cudaFree(counter); }
 };
 
@@ -239,20 +242,36 @@ int launch_update(ReactorObj& r, int ncell, const double* rho, const double* u, 
     if (!(t_interval > 0.0)) throw std::runtime_error("t_interval must be > 0");
     if (!r.counter) check(cudaMalloc(&r.counter, sizeof(unsigned)), "cudaMalloc");
     check(cudaMemsetAsync(r.counter, 0, sizeof(unsigned), s), "cudaMemsetAsync");
-    ChemUpdateArgs a{};
-    a.mech_i = r.dev.I;
-    a.mech_d = r.dev.D;
-    a.n_mech_i = (int)r.dev.host.I.size();
-    a.n_mech_d = (int)r.dev.host.D.size();
+    if (flags & GDTK_CHEM_REFERENCE_ORDER) {
+        ChemUpdateArgs a{};
+        a.mech_i = r.dev.I;
+        a.mech_d = r.dev.D;
+        a.n_mech_i = (int)r.dev.host.I.size();
+        a.n_mech_d = (int)r.dev.host.D.size();
+        a.ncell = ncell;
+        a.rho = rho; a.u = u; a.T = T; a.p = p; a.massf = massf; a.dt_chem = dt_chem; a.status = status;
+        a.t_interval = t_interval;
+        a.T_frozen = T_frozen;
+        a.flags = flags & (CHEM_FLAG_UPDATE_THERMO | CHEM_FLAG_RETRY);
+        a.counter = r.counter;
+        a.cell_counters = cell_counters;
+        a.totals = totals;
+        check(launch_chem_update(a, r.mh.method, r.scratch, cuda().sm_count, s, &r.last), "chemistry update launch");
+        return 0;
+    }
+    if (!r.fast) r.fast.reset(build_fast_kernel(model(r.gm).gm, r.mh));
+    FastArgs a{};
     a.ncell = ncell;
+    a.flags = flags & (CHEM_FLAG_UPDATE_THERMO | CHEM_FLAG_RETRY);
     a.rho = rho; a.u = u; a.T = T; a.p = p; a.massf = massf; a.dt_chem = dt_chem; a.status = status;
     a.t_interval = t_interval;
     a.T_frozen = T_frozen;
-    a.flags = flags;
     a.counter = r.counter;
     a.cell_counters = cell_counters;
     a.totals = totals;
-    check(launch_chem_update(a, r.mh.method, r.scratch, cuda().sm_count, s, &r.last), "chemistry update launch");
+    check(launch_fast(*r.fast, a, cuda().sm_count, s, &r.last.grid, &r.last.block, &r.last.smem),
+          "chemistry update launch");
+    r.last.blocks_per_sm = r.fast->blocks_per_sm;
     return 0;
 }
 
@@ -509,8 +528,8 @@ int thermochemical_reactor_gas_state_update(int cr_i, int gs_i, double t_interva
         double* d = r.stage.d.p;
         check(cudaMemcpyAsync(d, h.data(), nd * sizeof(double), cudaMemcpyHostToDevice, st), "cudaMemcpyAsync");
         // ThermochemicalReactor.opCall alone: no retry and no rhou update (gas_cwrap.d:906-921).
-        launch_update(r, 1, d + 0, d + 1, d + 2, d + 3, d + 5, d + 4, r.stage.st.p, t_interval, -1.0e300, 0, st,
-                      nullptr, nullptr);
+        launch_update(r, 1, d + 0, d + 1, d + 2, d + 3, d + 5, d + 4, r.stage.st.p, t_interval, -1.0e300,
+                      GDTK_CHEM_REFERENCE_ORDER, st, nullptr, nullptr);
         int status = 0;
         check(cudaMemcpyAsync(h.data(), d, nd * sizeof(double), cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync");
         check(cudaMemcpyAsync(&status, r.stage.st.p, sizeof(int), cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync");
@@ -657,6 +676,30 @@ int gas_model_update_thermo_from_rhou_cells(int gm_i, int ncell, const double* r
     });
 }
 
+int chem_reactor_fast_source(int cr_i, char* dest, int n) {
+    return guarded([&] {
+        auto& r = reactor(cr_i);
+        std::string src = r.fast ? r.fast->source : generate_fast_source(model(r.gm).gm, r.mh, 256, 1);
+        if (dest && n > 0) {
+            std::strncpy(dest, src.c_str(), (size_t)n);
+            dest[n - 1] = '\0';
+        }
+        return (int)src.size() + 1;
+    });
+}
+
+int chem_reactor_jit_log(int cr_i, char* dest, int n) {
+    return guarded([&] {
+        auto& r = reactor(cr_i);
+        std::string log = r.fast ? r.fast->log : std::string();
+        if (dest && n > 0) {
+            std::strncpy(dest, log.c_str(), (size_t)n);
+            dest[n - 1] = '\0';
+        }
+        return (int)log.size() + 1;
+    });
+}
+
 int chem_reactor_flop_model(int cr_i, double* out) {
     return guarded([&] {
         auto& r = reactor(cr_i);
@@ -688,5 +731,38 @@ int chem_reactor_last_launch(int cr_i, int* grid, int* block, int* smem_bytes, i
 }
 
 const char* gdtk_last_error(void) { return g_last_error.c_str(); }
+
+int gdtk_exp_host(int n, const double* x, double* y) {
+    static const double tab[64] = GDTK_EXP2_TABLE_INIT;
+    for (int i = 0; i < n; ++i) y[i] = gdtk_exp(x[i], tab);
+    return 0;
+}
+
+int gdtk_compile_fast_source_check(const char* gas_file, const char* chem_file, int cc_major, int cc_minor,
+                                   char* log, int n) {
+    return guarded([&] {
+        GasModelHost gm = load_gas_model(gas_file);
+        MechanismHost mh = load_mechanism(chem_file, gm, true);
+        std::string l = compile_fast_check(gm, mh, cc_major, cc_minor);
+        if (log && n > 0) {
+            std::strncpy(log, l.c_str(), (size_t)n);
+            log[n - 1] = '\0';
+        }
+        return 0;
+    });
+}
+
+int gdtk_generate_fast_source(const char* gas_file, const char* chem_file, char* dest, int n) {
+    return guarded([&] {
+        GasModelHost gm = load_gas_model(gas_file);
+        MechanismHost mh = load_mechanism(chem_file, gm, true);
+        std::string src = generate_fast_source(gm, mh, 256, 1);
+        if (dest && n > 0) {
+            std::strncpy(dest, src.c_str(), (size_t)n);
+            dest[n - 1] = '\0';
+        }
+        return (int)src.size() + 1;
+    });
+}
 
 }  // extern "C"

@@ -4,7 +4,7 @@
 
 namespace gdtk {
 
-enum { CHEM_FLAG_UPDATE_THERMO = 1, CHEM_FLAG_RETRY = 2 };
+enum { CHEM_FLAG_UPDATE_THERMO = 1, CHEM_FLAG_RETRY = 2, CHEM_FLAG_REFERENCE_ORDER = 4 };
 
 // All pointers are device pointers.  Mass fractions are species-major: massf[isp * ncell + cell].
 struct ChemUpdateArgs {

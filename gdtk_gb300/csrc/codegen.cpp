@@ -1,0 +1,487 @@
+// codegen.cpp -- writes the mechanism as straight-line CUDA, compiles it with NVRTC for the
+// device at hand, and launches it.
+//
+// The generated part is small: compile-time sizes and tolerances, the species constants, and
+// two functions -- gen_kc (rate constants) and gen_rhs (production/loss rates) -- in which
+// every species index, stoichiometric coefficient, third-body efficiency and Arrhenius
+// parameter is a literal.  The integrator around them is chem_fast.cuh.  The reference
+// interprets its reaction objects at run time (kinetics/reaction_mechanism.d:82-96,
+// reaction.d:145-149, 267-311, 394-456); its legacy GPU path generated source in a similar
+// spirit, from prep-chem's compact notation (eilmer/utils/prep-cuda-gpu-chem-kernel.py).
+#include "codegen.h"
+
+#include <cuda.h>
+#include <nvrtc.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <fstream>
+#include <functional>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <sstream>
+#include <stdexcept>
+#include <sys/stat.h>
+#include <unistd.h>
+
+#include "cea_thermo.h"
+#include "chem_types.h"
+#include "fast_exp.h"
+
+namespace gdtk {
+
+extern const char* const kFastCuhSource;
+extern const char* const kFastExpSource;
+
+namespace {
+
+constexpr double R_universal = 8.31451;
+
+std::string lit(double v) {   // exact double literal
+    char buf[64];
+    std::snprintf(buf, sizeof buf, "%a", v);
+    std::string s(buf);
+    if (v == 0.0) return "0.0";
+    return s;
+}
+
+// ---- driver entry points, resolved through the runtime (no link-time libcuda dependency)
+struct Driver {
+    CUresult (*moduleLoadData)(CUmodule*, const void*) = nullptr;
+    CUresult (*moduleUnload)(CUmodule) = nullptr;
+    CUresult (*moduleGetFunction)(CUfunction*, CUmodule, const char*) = nullptr;
+    CUresult (*funcSetAttribute)(CUfunction, CUfunction_attribute, int) = nullptr;
+    CUresult (*launchKernel)(CUfunction, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned,
+                             CUstream, void**, void**) = nullptr;
+    CUresult (*occupancy)(int*, CUfunction, int, size_t) = nullptr;
+    CUresult (*getErrorString)(CUresult, const char**) = nullptr;
+};
+
+template <typename F>
+void resolve(const char* name, F& fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    cudaError_t e = cudaGetDriverEntryPointByVersion(name, &p, 12000, cudaEnableDefault, &q);
+    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !p)
+        throw std::runtime_error(std::string("cannot resolve driver entry point ") + name);
+    fn = reinterpret_cast<F>(p);
+}
+
+Driver& driver() {
+    static Driver d;
+    static std::once_flag once;
+    static std::string failure;
+    std::call_once(once, [] {
+        try {
+            resolve("cuModuleLoadData", d.moduleLoadData);
+            resolve("cuModuleUnload", d.moduleUnload);
+            resolve("cuModuleGetFunction", d.moduleGetFunction);
+            resolve("cuFuncSetAttribute", d.funcSetAttribute);
+            resolve("cuLaunchKernel", d.launchKernel);
+            resolve("cuOccupancyMaxActiveBlocksPerMultiprocessor", d.occupancy);
+            resolve("cuGetErrorString", d.getErrorString);
+        } catch (std::exception& e) {
+            failure = e.what();
+        }
+    });
+    if (!failure.empty()) throw std::runtime_error(failure);
+    return d;
+}
+
+void cu_check(CUresult r, const char* what) {
+    if (r == CUDA_SUCCESS) return;
+    const char* s = "unknown";
+    if (driver().getErrorString) driver().getErrorString(r, &s);
+    throw std::runtime_error(std::string(what) + ": " + s);
+}
+
+// Integer power of a symbol, in the order of D's std.math pow(x, int) (binary exponentiation).
+std::string ipow_expr(const std::string& x, int n) {
+    if (n == 1) return x;
+    if (n == 2) return "(" + x + " * " + x + ")";
+    std::string p, v = x;
+    unsigned m = (unsigned)n;
+    bool have = false;
+    while (true) {
+        if (m & 1u) { p = have ? "(" + p + " * " + v + ")" : v; have = true; }
+        m >>= 1;
+        if (!m) break;
+        v = "(" + v + " * " + v + ")";
+    }
+    return p;
+}
+
+struct Part { int isp; int nu; };
+
+std::vector<Part> participants(const ReactionHost& r) {
+    std::vector<int> sp;
+    for (auto& x : r.reac) sp.push_back(x.first);
+    for (auto& x : r.prod) sp.push_back(x.first);
+    std::sort(sp.begin(), sp.end());
+    sp.erase(std::unique(sp.begin(), sp.end()), sp.end());
+    std::vector<Part> out;
+    for (int isp : sp) {
+        int nu1 = 0, nu2 = 0;
+        for (auto& x : r.reac) if (x.first == isp) { nu1 = x.second; break; }
+        for (auto& x : r.prod) if (x.first == isp) { nu2 = x.second; break; }
+        out.push_back({isp, nu2 - nu1});
+    }
+    return out;
+}
+
+// ln k = ln A + n ln T - C / T as an expression; empty if A == 0.
+std::string log_arrhenius(const RateConstHost& rc) {
+    if (rc.A <= 0.0) return "";
+    std::string e = lit(std::log(rc.A));
+    if (rc.n != 0.0) e = "fma(" + lit(rc.n) + ", lnT, " + e + ")";
+    if (rc.C != 0.0) e = "fma(" + lit(-rc.C) + ", rT, " + e + ")";
+    return e;
+}
+
+// k = A T^n as products when C == 0 and n is a small integer (no exponential needed).
+bool power_arrhenius(const RateConstHost& rc, std::string& out) {
+    if (rc.C != 0.0 || rc.n != std::floor(rc.n) || std::fabs(rc.n) > 4) return false;
+    int n = (int)rc.n;
+    if (n == 0) { out = lit(rc.A); return true; }
+    out = lit(rc.A) + " * " + ipow_expr(n > 0 ? "T" : "rT", n > 0 ? n : -n);
+    return true;
+}
+
+}  // namespace
+
+FastKernel::~FastKernel() {
+    if (module) driver().moduleUnload((CUmodule)module);
+    if (d_thermo) cudaFree(d_thermo);
+    if (d_exp) cudaFree(d_exp);
+}
+
+std::vector<double> fast_thermo_table(const GasModelHost& gm) {
+    const int nsp = gm.n_species();
+    PackedMech pm = pack(gm, nullptr);   // reference-form curve ends (cea_thermo_curves.d:46-53)
+    MechView v;
+    v.bind(pm.I.data(), pm.D.data());
+    std::vector<double> t((size_t)nsp * 120, 0.0);
+    for (int i = 0; i < nsp; ++i) {
+        const CeaCurveHost& c = gm.curves[i];
+        const double* s = v.sp(i);
+        const double R = R_universal / gm.M[i];
+        double* th = t.data() + (size_t)i * 120;
+        th[0] = s[SP_TLOW];
+        th[1] = s[SP_THIGH];
+        th[2] = s[SP_HLOW] / R;
+        th[3] = s[SP_HHIGH] / R;
+        th[4] = s[SP_CPLOW] / R;
+        th[5] = s[SP_CPHIGH] / R;
+        th[6] = s[SP_SLOW] / R;
+        th[7] = s[SP_SHIGH] / R;
+        th[8] = std::log(s[SP_TLOW]);
+        th[9] = std::log(s[SP_THIGH]);
+        th[10] = c.nseg;
+        for (int k = 0; k <= c.nseg; ++k) th[11 + k] = c.breaks[k];
+        for (int k = 0; k < c.nseg - 1; ++k) { th[16 + k] = c.blends[k]; th[20 + k] = 1. / c.blends[k]; }
+        for (int sg = 0; sg < c.nseg; ++sg) {
+            const double* a = c.coeffs.data() + 9 * sg;
+            double* h = th + 24 + 24 * sg;
+            // H/R = -a0/T + a1 lnT + a7 + T (a2 + T (a3/2 + T (a4/3 + T (a5/4 + T a6/5))))
+            h[0] = -a[0]; h[1] = a[1]; h[2] = a[2]; h[3] = a[3] / 2.0; h[4] = a[4] / 3.0; h[5] = a[5] / 4.0;
+            h[6] = a[6] / 5.0; h[7] = a[7];
+            // Cp/R = a0/T^2 + a1/T + a2 + T (a3 + T (a4 + T (a5 + T a6)))
+            for (int k = 0; k < 7; ++k) h[8 + k] = a[k];
+            // G/RT = H/RT - S/R
+            h[15] = -a[0] / 2.0; h[16] = a[1]; h[17] = a[7]; h[18] = a[2]; h[19] = -a[8];
+            h[20] = -a[3] / 2.0; h[21] = -a[4] / 6.0; h[22] = -a[5] / 12.0; h[23] = -a[6] / 20.0;
+        }
+    }
+    return t;
+}
+
+std::string generate_fast_source(const GasModelHost& gm, const MechanismHost& mh, int block, int min_blocks) {
+    const int nsp = gm.n_species();
+    const int nr = (int)mh.reactions.size();
+    std::ostringstream o;
+    o << "// generated: " << nsp << " species, " << nr << " reactions\n";
+    o << "#define GDTK_NSP " << nsp << "\n#define GDTK_NR " << nr << "\n";
+    o << "#define GDTK_METHOD " << mh.method << "\n#define GDTK_TIGHT " << (mh.tight ? 1 : 0) << "\n";
+    o << "#define GDTK_MAX_ITERS " << mh.maxIters << "\n#define GDTK_MAX_SUBCYCLES " << mh.maxSubcycles << "\n";
+    o << "#define GDTK_MAX_ATTEMPTS " << mh.maxAttempts << "\n";
+    o << "#define GDTK_T_LOWER " << lit(mh.T_lower) << "\n#define GDTK_T_UPPER " << lit(mh.T_upper) << "\n";
+    o << "#define GDTK_ERRTOL " << lit(mh.errTol) << "\n#define GDTK_EPS1 " << lit(mh.eps1) << "\n";
+    o << "#define GDTK_EPS2 " << lit(mh.eps2) << "\n#define GDTK_DELTA " << lit(mh.delta) << "\n";
+    o << "#define GDTK_BLOCK " << block << "\n#define GDTK_MIN_BLOCKS " << min_blocks << "\n";
+    o << kFastExpSource << "\n";
+    auto arr = [&](const char* name, std::function<double(int)> f) {
+        o << "__constant__ double " << name << "[" << nsp << "] = {";
+        for (int i = 0; i < nsp; ++i) o << (i ? ", " : "") << lit(f(i));
+        o << "};\n";
+    };
+    arr("GDTK_M", [&](int i) { return gm.M[i]; });
+    arr("GDTK_RM", [&](int i) { return 1.0 / gm.M[i]; });
+    arr("GDTK_R", [&](int i) { return R_universal / gm.M[i]; });
+    o << "namespace gdtk_fast {\nusing gdtk::gdtk_exp;\n";
+
+    // ---- rate constants
+    o << "__device__ __forceinline__ void gen_kc(double T, double lnT, double rT, const double* g, double* K, int ks, "
+         "const double* etab) {\n";
+    o << "  (void)T;\n";
+    for (int ir = 0; ir < nr; ++ir) {
+        const ReactionHost& r = mh.reactions[ir];
+        auto parts = participants(r);
+        if (ir > 0 && ir % 4 == 0) o << "  asm volatile(\"\" ::: \"memory\");\n";
+        std::ostringstream dg;   // sum nu * G/RT
+        int nusum = 0;
+        for (auto& p : parts) {
+            if (p.nu == 0) continue;
+            nusum += p.nu;
+            std::string term = "g[" + std::to_string(p.isp) + "]";
+            if (dg.tellp() == 0) {
+                if (p.nu == 1) dg << term;
+                else dg << lit((double)p.nu) << " * " << term;
+            } else {
+                if (p.nu == 1) dg << " + " << term;
+                else if (p.nu == -1) dg << " - " << term;
+                else dg << " + " << lit((double)p.nu) << " * " << term;
+            }
+        }
+        std::string dgs = dg.tellp() == 0 ? std::string("0.0") : dg.str();
+        // ln K_c = -sum(nu G/RT) + sum(nu) ln(P_atm / R T)   (reaction.d:26-52)
+        std::string lnKc = "(-(" + dgs + ")" +
+                           (nusum ? " + " + lit((double)nusum) + " * (" + lit(std::log(101325.0 / R_universal)) + " - lnT)" : std::string("")) + ")";
+        o << "  { // " << (r.equation.empty() ? std::string("reaction") : r.equation) << "\n";
+        if (r.frc.model == RATE_ARRHENIUS) {
+            std::string pw;
+            if (power_arrhenius(r.frc, pw)) {
+                o << "    const double kf = " << pw << ";\n";
+                if (r.brc.model == RATE_FROM_EQ) o << "    const double kb = kf * gdtk_exp(-" << lnKc << ", etab);\n";
+            } else {
+                std::string l = log_arrhenius(r.frc);
+                if (l.empty()) o << "    const double lkf = -1.0e300; const double kf = 0.0;\n";
+                else o << "    const double lkf = " << l << ";\n    const double kf = gdtk_exp(lkf, etab);\n";
+                if (r.brc.model == RATE_FROM_EQ) o << "    const double kb = gdtk_exp(lkf - " << lnKc << ", etab);\n";
+            }
+            if (r.brc.model == RATE_ARRHENIUS) {
+                std::string pb;
+                if (power_arrhenius(r.brc, pb)) o << "    const double kb = " << pb << ";\n";
+                else {
+                    std::string l = log_arrhenius(r.brc);
+                    o << "    const double kb = " << (l.empty() ? std::string("0.0") : "gdtk_exp(" + l + ", etab)")
+                      << ";\n";
+                }
+            }
+        } else {   // forward from K_c and a given backward rate constant
+            std::string l = log_arrhenius(r.brc);
+            if (l.empty()) o << "    const double kb = 0.0; const double kf = 0.0;\n";
+            else o << "    const double lkb = " << l << ";\n    const double kb = gdtk_exp(lkb, etab);\n"
+                   << "    const double kf = gdtk_exp(lkb + " << lnKc << ", etab);\n";
+        }
+        o << "    K[" << ir << " * ks] = kf;\n    K[" << (nr + ir) << " * ks] = kb;\n  }\n";
+    }
+    o << "}\n";
+
+    // ---- production / loss rates
+    o << "__device__ __forceinline__ void gen_rhs(const double* c, double* q, double* L, const double* K, int ks) {\n";
+    // distinct third-body lists
+    std::vector<std::vector<std::pair<int, double>>> sets;
+    std::vector<int> set_of(nr, -1);
+    for (int ir = 0; ir < nr; ++ir) {
+        const ReactionHost& r = mh.reactions[ir];
+        if (!r.collider) continue;
+        int f = -1;
+        for (size_t s = 0; s < sets.size(); ++s) if (sets[s] == r.eff) { f = (int)s; break; }
+        if (f < 0) { sets.push_back(r.eff); f = (int)sets.size() - 1; }
+        set_of[ir] = f;
+    }
+    for (size_t s = 0; s < sets.size(); ++s) {
+        o << "  double M" << s << " = 0.0;\n";
+        bool first = true;
+        for (auto& e : sets[s]) {
+            std::string cc = "c[" + std::to_string(e.first) + "]";
+            if (first) {
+                o << "  M" << s << " = " << (e.second == 1.0 ? cc : lit(e.second) + " * " + cc) << ";\n";
+                first = false;
+            } else if (e.second == 1.0) {
+                o << "  M" << s << " += " << cc << ";\n";
+            } else {
+                o << "  M" << s << " = fma(" << lit(e.second) << ", " << cc << ", M" << s << ");\n";
+            }
+        }
+    }
+    std::vector<bool> qset(nsp, false), lset(nsp, false);
+    auto acc = [&](std::vector<bool>& set, const char* arr, int isp, int coeff, const char* w) {
+        std::string dst = std::string(arr) + "[" + std::to_string(isp) + "]";
+        std::string val = coeff == 1 ? std::string(w) : lit((double)coeff) + " * " + w;
+        if (!set[isp]) { o << "    " << dst << " = " << val << ";\n"; set[isp] = true; }
+        else if (coeff == 1) o << "    " << dst << " += " << w << ";\n";
+        else o << "    " << dst << " = fma(" << lit((double)coeff) << ", " << w << ", " << dst << ");\n";
+    };
+    for (int ir = 0; ir < nr; ++ir) {
+        const ReactionHost& r = mh.reactions[ir];
+        // A compiler barrier every few reactions stops the scheduler from hoisting every k_f/k_b
+        // load to the top, which would hold 2 NR doubles live and spill registers.
+        if (ir > 0 && ir % 4 == 0) o << "  asm volatile(\"\" ::: \"memory\");\n";
+        o << "  {\n    double wf = K[" << ir << " * ks], wb = K[" << (nr + ir) << " * ks];\n";
+        if (r.collider) o << "    wf *= M" << set_of[ir] << "; wb *= M" << set_of[ir] << ";\n";
+        for (auto& x : r.reac) o << "    wf *= " << ipow_expr("c[" + std::to_string(x.first) + "]", x.second) << ";\n";
+        for (auto& x : r.prod) o << "    wb *= " << ipow_expr("c[" + std::to_string(x.first) + "]", x.second) << ";\n";
+        for (auto& p : participants(r)) {
+            if (p.nu > 0) { acc(qset, "q", p.isp, p.nu, "wf"); acc(lset, "L", p.isp, p.nu, "wb"); }
+            else if (p.nu < 0) { acc(qset, "q", p.isp, -p.nu, "wb"); acc(lset, "L", p.isp, -p.nu, "wf"); }
+        }
+        o << "  }\n";
+    }
+    for (int i = 0; i < nsp; ++i) {
+        if (!qset[i]) o << "  q[" << i << "] = 0.0;\n";
+        if (!lset[i]) o << "  L[" << i << "] = 0.0;\n";
+    }
+    o << "}\n}  // namespace gdtk_fast\n";
+    o << kFastCuhSource;
+    return o.str();
+}
+
+namespace {
+
+std::string cache_dir() {
+    const char* env = std::getenv("GDTK_JIT_CACHE");
+    if (env && *env) return env;
+    const char* home = std::getenv("HOME");
+    return std::string(home && *home ? home : "/tmp") + "/.cache/gdtk_gb300";
+}
+
+std::string compile_cubin(const std::string& src, int major, int minor, std::string& log) {
+    std::string arch = "--gpu-architecture=sm_" + std::to_string(major) + std::to_string(minor) +
+                       (major >= 9 ? "a" : "");
+    const char* opts[] = {arch.c_str(), "--std=c++17", "--fmad=true", "-default-device", "-lineinfo",
+                          "--ptxas-options=-v"};
+    nvrtcProgram prog;
+    if (nvrtcCreateProgram(&prog, src.c_str(), "gdtk_chem_fast.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS)
+        throw std::runtime_error("nvrtcCreateProgram failed");
+    nvrtcResult rc = nvrtcCompileProgram(prog, (int)(sizeof(opts) / sizeof(opts[0])), opts);
+    size_t n = 0;
+    nvrtcGetProgramLogSize(prog, &n);
+    log.assign(n, '\0');
+    if (n) nvrtcGetProgramLog(prog, &log[0]);
+    if (rc != NVRTC_SUCCESS) {
+        nvrtcDestroyProgram(&prog);
+        throw std::runtime_error(std::string("NVRTC compilation of the mechanism kernel failed: ") +
+                                 nvrtcGetErrorString(rc) + "\n" + log);
+    }
+    size_t cn = 0;
+    nvrtcGetCUBINSize(prog, &cn);
+    std::string cubin(cn, '\0');
+    nvrtcGetCUBIN(prog, &cubin[0]);
+    nvrtcDestroyProgram(&prog);
+    return cubin;
+}
+
+std::mutex g_jit_mu;
+std::map<std::string, std::string> g_cubins;   // source hash key -> cubin (this process)
+
+}  // namespace
+
+std::string compile_fast_check(const GasModelHost& gm, const MechanismHost& mh, int major, int minor) {
+    std::string log;
+    std::string src = generate_fast_source(gm, mh, 256, 1);
+    std::string cubin = compile_cubin(src, major, minor, log);
+    return log;
+}
+
+FastKernel* build_fast_kernel(const GasModelHost& gm, const MechanismHost& mh) {
+    int dev = 0, major = 0, minor = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+    cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int nsp = gm.n_species(), nr = (int)mh.reactions.size();
+    const int per_thread = 2 * nr + (mh.method == METHOD_RKF ? 5 : 3) * nsp;
+    const int table = nsp * 120 + 64;
+    // Block size: as many resident threads as shared memory allows, up to 256 per SM.
+    const double budget = 227.0 * 1024 / 8;   // doubles of shared memory per SM
+    int block = 256, min_blocks = 1;
+    while (block > 32 && table + (double)per_thread * block > budget) block -= 32;
+    if (table + (double)per_thread * block > budget) throw std::runtime_error("mechanism too large for shared memory");
+    if (block <= 128 && 2 * (table + (double)per_thread * block) <= budget) min_blocks = 2;
+
+    auto k = std::make_unique<FastKernel>();
+    k->block = block;
+    k->min_blocks = min_blocks;
+    k->per_thread_doubles = per_thread;
+    k->table_doubles = table;
+    k->source = generate_fast_source(gm, mh, block, min_blocks);
+    std::string key = std::to_string(std::hash<std::string>{}(k->source)) + "_sm" + std::to_string(major) +
+                      std::to_string(minor);
+    std::string cubin;
+    {
+        std::lock_guard<std::mutex> lk(g_jit_mu);
+        auto it = g_cubins.find(key);
+        if (it != g_cubins.end()) cubin = it->second;
+    }
+    std::string dir = cache_dir(), path = dir + "/" + key + ".cubin";
+    if (cubin.empty()) {
+        std::ifstream f(path, std::ios::binary);
+        if (f) {
+            std::ostringstream ss;
+            ss << f.rdbuf();
+            cubin = ss.str();
+            k->log = "loaded from " + path;
+        }
+    }
+    if (cubin.empty()) {
+        cubin = compile_cubin(k->source, major, minor, k->log);
+        std::string tmp = path + ".tmp" + std::to_string((long)getpid());
+        ::mkdir((dir.substr(0, dir.rfind('/'))).c_str(), 0755);
+        ::mkdir(dir.c_str(), 0755);
+        std::ofstream f(tmp, std::ios::binary);
+        if (f) {
+            f.write(cubin.data(), (std::streamsize)cubin.size());
+            f.close();
+            std::rename(tmp.c_str(), path.c_str());
+        }
+    }
+    {
+        std::lock_guard<std::mutex> lk(g_jit_mu);
+        g_cubins[key] = cubin;
+    }
+    Driver& d = driver();
+    CUmodule mod;
+    cu_check(d.moduleLoadData(&mod, cubin.data()), "cuModuleLoadData");
+    k->module = mod;
+    CUfunction fn;
+    cu_check(d.moduleGetFunction(&fn, mod, "gdtk_chem_fast"), "cuModuleGetFunction");
+    k->function = fn;
+    const size_t smem_max = (size_t)(table + per_thread * block) * 8;
+    cu_check(d.funcSetAttribute(fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)smem_max),
+             "cuFuncSetAttribute");
+    cu_check(d.occupancy(&k->blocks_per_sm, fn, block, smem_max), "cuOccupancyMaxActiveBlocksPerMultiprocessor");
+    if (k->blocks_per_sm < 1) throw std::runtime_error("fast kernel cannot be resident (registers/shared memory)");
+    std::vector<double> th = fast_thermo_table(gm);
+    static const double etab[64] = GDTK_EXP2_TABLE_INIT;
+    if (cudaMalloc(&k->d_thermo, th.size() * 8) != cudaSuccess || cudaMalloc(&k->d_exp, 64 * 8) != cudaSuccess)
+        throw std::runtime_error("cudaMalloc failed");
+    cudaMemcpy(k->d_thermo, th.data(), th.size() * 8, cudaMemcpyHostToDevice);
+    cudaMemcpy(k->d_exp, etab, 64 * 8, cudaMemcpyHostToDevice);
+    (void)sms;
+    return k.release();
+}
+
+cudaError_t launch_fast(FastKernel& k, FastArgs& a, int sm_count, cudaStream_t stream, int* grid_out, int* block_out,
+                        int* smem_out) {
+    a.thermo = k.d_thermo;
+    a.exp_table = k.d_exp;
+    int block = k.block;
+    while (block > 32 && ((long long)a.ncell + block - 1) / block < sm_count) block -= 32;
+    long long want = ((long long)a.ncell + block - 1) / block;
+    long long grid = (long long)sm_count * k.blocks_per_sm * (k.block / block);
+    if (want < grid) grid = want;
+    if (grid < 1) grid = 1;
+    size_t smem = (size_t)(k.table_doubles + k.per_thread_doubles * block) * 8;
+    void* params[] = {&a};
+    CUresult r = driver().launchKernel((CUfunction)k.function, (unsigned)grid, 1, 1, (unsigned)block, 1, 1,
+                                       (unsigned)smem, (CUstream)stream, params, nullptr);
+    if (grid_out) *grid_out = (int)grid;
+    if (block_out) *block_out = block;
+    if (smem_out) *smem_out = (int)smem;
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorLaunchFailure;
+}
+
+}  // namespace gdtk

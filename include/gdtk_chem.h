@@ -38,6 +38,9 @@ enum gdtk_cell_status {
 /* Flags of chem_reactor_update_cells*. */
 #define GDTK_CHEM_UPDATE_THERMO 1 /* follow the update with update_thermo_from_rhou (fluidfvcell.d:956) */
 #define GDTK_CHEM_RETRY 2         /* retry a failed cell once with dt_chem = -1 (fluidfvcell.d:924-941) */
+#define GDTK_CHEM_REFERENCE_ORDER 4 /* use the kernel that keeps the reference's operation order
+                                       (default: the mechanism-specialised kernel, which rearranges
+                                       the arithmetic to spend fewer FP64 operations) */
 
 /* ---- 1. libgas-compatible subset (gas_cwrap.d) ---------------------------------------- */
 int cwrap_gas_init(void);                                                   /* gas_cwrap.d:40-55 */
@@ -116,6 +119,20 @@ int gas_model_update_thermo_from_rhou_cells(int gm_i, int ncell, const double* r
  * T from (rho, u).  add/sub/mul/div/sqrt count 1, exp and log 20, pow 40.  Multiplying by
  * the work counters of chem_reactor_update_cells_ex gives the FLOPs of a batch. */
 int chem_reactor_flop_model(int cr_i, double* out);
+/* The CUDA source generated for this reactor's mechanism-specialised kernel, and the NVRTC /
+ * ptxas log of its compilation ("" before first use).  Both return the length + 1 and copy
+ * at most n bytes (NUL-terminated) when dest is not NULL.  No counterpart in the reference. */
+int chem_reactor_fast_source(int cr_i, char* dest, int n);
+int chem_reactor_jit_log(int cr_i, char* dest, int n);
+/* The same source for a gas-model file and a mechanism file, without a GPU (for inspection
+ * and offline compilation checks). */
+int gdtk_generate_fast_source(const char* gas_file, const char* chem_file, char* dest, int n);
+/* The kernels' exponential (table-driven, Tang 1989), evaluated on the host for testing. */
+int gdtk_exp_host(int n, const double* x, double* y);
+/* Compiles that source with NVRTC for compute capability cc_major.cc_minor without a GPU and
+ * copies the compiler log (register use) into log; 0 on success, -1 on a compile error. */
+int gdtk_compile_fast_source_check(const char* gas_file, const char* chem_file, int cc_major, int cc_minor,
+                                   char* log, int n);
 /* Reactor description: n species, n reactions, ODE method (0 rkf, 1 alpha-qss), tight coupling. */
 int chem_reactor_info(int cr_i, int* nsp, int* nr, int* method, int* tight);
 /* Launch shape of the last chem_reactor_update_cells* call on this reactor. */

@@ -1,0 +1,97 @@
+"""CPU-only checks of the C ABI library: it loads, exports what include/gdtk_chem.h declares,
+reads the reference's gas/mechanism files like the oracle's independent reader, compiles its
+mechanism kernels with NVRTC, and refuses GPU work loudly when there is no GPU."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import gdtk_gb300
+import oracle
+from conftest import mech, ROOT
+
+HEADER = os.path.join(ROOT, "include", "gdtk_chem.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(\w+)\s*\(", text, flags=re.M)))
+
+
+def test_library_exports_every_declared_symbol():
+    L = gdtk_gb300.lib()
+    names = declared_functions()
+    assert len(names) >= 40
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+    # and the Python binding table covers all of them
+    assert sorted(gdtk_gb300.SIGNATURES) == names
+
+
+@pytest.mark.parametrize("name", ["park5", "j92", "gupta5", "n2", "h2i2"])
+def test_gas_model_reader_matches_oracle_reader(name):
+    from gdtk_gb300.gas import GasModel
+    gm = GasModel(mech(name + "-gas.lua"))
+    names, species = oracle.load_gas(mech(name + "-gas.lua"))
+    assert gm.species_names == names
+    assert np.array_equal(np.array(gm.mol_masses), np.array([s["M"] for s in species]))
+    assert gm.n_modes == 0
+
+
+def test_reader_rejects_wrong_species_order(tmp_path):
+    from gdtk_gb300.gas import GasModel
+    src = open(mech("park5-chem.lua")).read().replace("[0]='N2', [1]='O2'", "[0]='O2', [1]='N2'")
+    bad = tmp_path / "bad.lua"
+    bad.write_text(src)
+    L = gdtk_gb300.lib()
+    gm = GasModel(mech("park5-gas.lua"))
+    assert L.thermochemical_reactor_new(gm.id, str(bad).encode(), b"") == -1
+    assert "Species order" in gdtk_gb300.last_error() or "CUDA" in gdtk_gb300.last_error()
+
+
+def test_unsupported_rate_model_is_refused(tmp_path):
+    src = open(mech("park5-chem.lua")).read().replace("model='Arrhenius', A=7.0", "model='Troe', A=7.0", 1)
+    bad = tmp_path / "troe.lua"
+    bad.write_text(src)
+    L = gdtk_gb300.lib()
+    n = L.gdtk_generate_fast_source(mech("park5-gas.lua").encode(), str(bad).encode(), None, 0)
+    assert n == -1 and "not supported" in gdtk_gb300.last_error()
+
+
+def test_gpu_work_fails_loudly_without_gpu():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from gdtk_gb300.gas import GasModel, GasState
+    gm = GasModel(mech("park5-gas.lua"))
+    gs = GasState(gm)
+    gs.p, gs.T = 1e5, 3000.0
+    gs.massf = [0.2] * 5
+    with pytest.raises(gdtk_gb300.ChemError, match="GPU"):
+        gm.update_thermo_from_pT(gs)
+
+
+def test_table_driven_exp_accuracy():
+    rng = np.random.Generator(np.random.PCG64(3))
+    x = np.concatenate([rng.uniform(-745.0, 709.7, 200000), rng.uniform(-40.0, 40.0, 200000),
+                        np.array([0.0, 1.0, -1.0, 709.78, -745.0, -708.4, 1e-300, -1e-300])])
+    y = np.empty_like(x)
+    gdtk_gb300.lib().gdtk_exp_host(len(x), x.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                   y.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+    ref = np.exp(x.astype(np.longdouble))
+    ok = np.isfinite(y) & (ref > np.finfo(np.float64).tiny)
+    ulp = np.spacing(ref[ok].astype(np.float64))
+    err = np.abs((y[ok].astype(np.longdouble) - ref[ok]) / ulp.astype(np.longdouble))
+    assert float(err.max()) <= 1.5, float(err.max())
+    assert y[-8] == 1.0
+
+
+@pytest.mark.parametrize("name", ["park5", "j92"])
+def test_mechanism_kernel_compiles_for_sm103a(name):
+    log = gdtk_gb300.compile_fast_source_check(mech(name + "-gas.lua"), mech(name + "-chem.lua"))
+    assert "sm_103a" in log
+    m = re.search(r"Used (\d+) registers", log)
+    assert m and int(m.group(1)) <= 255

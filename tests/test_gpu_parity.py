@@ -42,7 +42,10 @@ def to_dev(torch, *arrs):
     return [torch.tensor(np.ascontiguousarray(a), dtype=torch.float64, device="cuda") for a in arrs]
 
 
-def run_pair(rc, orc, T, p, Y, dt, dt_chem0=-1.0, T_frozen=0.0, flags=3):
+KERNELS = {"fast": 0, "reference_order": 4}
+
+
+def run_pair(rc, orc, T, p, Y, dt, dt_chem0=-1.0, T_frozen=0.0, flags=3, kernel="fast"):
     """Same inputs through the GPU and the oracle; returns (gpu dict, oracle dict, rho, u)."""
     torch = torch_cuda()
     n = T.shape[0]
@@ -53,7 +56,8 @@ def run_pair(rc, orc, T, p, Y, dt, dt_chem0=-1.0, T_frozen=0.0, flags=3):
     dtc = torch.full((n,), dt_chem0, dtype=torch.float64, device="cuda")
     st = torch.zeros(n, dtype=torch.int32, device="cuda")
     cnt = torch.zeros((6, n), dtype=torch.int32, device="cuda")
-    rc.update(rho, u, dT, dp, dY, dtc, dt, status=st, T_frozen=T_frozen, flags=flags, cell_counters=cnt)
+    rc.update(rho, u, dT, dp, dY, dtc, dt, status=st, T_frozen=T_frozen, flags=flags | KERNELS[kernel],
+              cell_counters=cnt)
     torch.cuda.synchronize()
     g = dict(T=dT.cpu().numpy(), p=dp.cpu().numpy(), Y=dY.cpu().numpy(), dt_chem=dtc.cpu().numpy(),
              status=st.cpu().numpy(), counters=cnt.cpu().numpy())
@@ -101,33 +105,37 @@ def test_thermo_pT_and_rhou(park5):
     assert np.allclose(T2.cpu().numpy(), To, rtol=1e-12)
 
 
-def test_air5_rkf_parity(park5):
+@pytest.mark.parametrize("kernel", sorted(KERNELS))
+def test_air5_rkf_parity(park5, kernel):
     from gdtk_gb300.workloads import air5_cells
     rc, orc = park5
     T, p, Y = air5_cells(1024, seed=0)
-    g, o, _, _ = run_pair(rc, orc, T, p, Y, 1.0e-6)
+    g, o, _, _ = run_pair(rc, orc, T, p, Y, 1.0e-6, kernel=kernel)
     assert (g["status"] == 0).all()
     assert_parity(g, o)
 
 
-def test_air5_warm_start_parity(park5):
+@pytest.mark.parametrize("kernel", sorted(KERNELS))
+def test_air5_warm_start_parity(park5, kernel):
     from gdtk_gb300.workloads import air5_cells
     rc, orc = park5
     T, p, Y = air5_cells(512, seed=5)
-    g, o, _, _ = run_pair(rc, orc, T, p, Y, 1.0e-6, dt_chem0=1.0e-9)
+    g, o, _, _ = run_pair(rc, orc, T, p, Y, 1.0e-6, dt_chem0=1.0e-9, kernel=kernel)
     assert_parity(g, o)
 
 
-def test_h2air_alpha_qss_tight_parity(j92):
+@pytest.mark.parametrize("kernel", sorted(KERNELS))
+def test_h2air_alpha_qss_tight_parity(j92, kernel):
     from gdtk_gb300.workloads import h2air_cells
     rc, orc = j92
-    T, p, Y = h2air_cells(rc.species_names, rc.mol_masses, 256, seed=3)
-    g, o, _, _ = run_pair(rc, orc, T, p, Y, 1.0e-6)
+    T, p, Y = h2air_cells(rc.species_names, rc.mol_masses, 512, seed=3)
+    g, o, _, _ = run_pair(rc, orc, T, p, Y, 1.0e-6, kernel=kernel)
     assert (g["status"] == 0).mean() > 0.95
     assert_parity(g, o)
 
 
-def test_gupta_given_backward_rates_parity():
+@pytest.mark.parametrize("kernel", sorted(KERNELS))
+def test_gupta_given_backward_rates_parity(kernel):
     from gdtk_gb300.cells import ReactorCells
     rc = ReactorCells(mech("gupta5-gas.lua"), mech("gupta5-chem.lua"))
     orc = oracle.Oracle(mech("gupta5-gas.lua"), mech("gupta5-chem.lua"))
@@ -136,7 +144,7 @@ def test_gupta_given_backward_rates_parity():
     T = rng.uniform(3000.0, 9000.0, n)
     p = 10.0 ** rng.uniform(3.0, 5.0, n)
     Y = np.ascontiguousarray(rng.dirichlet(np.ones(5), n).T)
-    g, o, _, _ = run_pair(rc, orc, T, p, Y, 1.0e-6)
+    g, o, _, _ = run_pair(rc, orc, T, p, Y, 1.0e-6, kernel=kernel)
     assert_parity(g, o)
 
 
@@ -153,18 +161,19 @@ def test_frozen_and_bad_cells(park5):
     # invalid density: status BAD_INPUT, state untouched
     dT, dp, dY = to_dev(torch, T, p, Y)
     drho, du = to_dev(torch, rho, u)
-    drho[3] = -1.0
-    drho[4] = float("nan")
+    drho[10] = -1.0
+    drho[11] = float("nan")
     st = torch.zeros(64, dtype=torch.int32, device="cuda")
     dtc = torch.full((64,), -1.0, dtype=torch.float64, device="cuda")
     rc.update(drho, du, dT, dp, dY, dtc, 1.0e-6, status=st, T_frozen=300.0)
     torch.cuda.synchronize()
     s = st.cpu().numpy()
-    assert s[3] == oracle.ST_BAD_INPUT and s[4] == oracle.ST_BAD_INPUT
-    assert dT[3].item() == T[3] and dT[4].item() == T[4]
+    assert s[10] == oracle.ST_BAD_INPUT and s[11] == oracle.ST_BAD_INPUT
+    assert dT[10].item() == T[10] and dT[11].item() == T[11]
 
 
-def test_failure_restores_state_and_retry(tmp_path):
+@pytest.mark.parametrize("kernel", sorted(KERNELS))
+def test_failure_restores_state_and_retry(tmp_path, kernel):
     # A mechanism allowed only 3 subcycles cannot finish 1e-6 s from a fresh start: both the
     # first try and the dt_chem = -1 retry hit maxSubcycles; the cell is left as it was.
     from gdtk_gb300.cells import ReactorCells
@@ -175,7 +184,7 @@ def test_failure_restores_state_and_retry(tmp_path):
     rc = ReactorCells(mech("park5-gas.lua"), str(chem))
     orc = oracle.Oracle(mech("park5-gas.lua"), str(chem))
     T, p, Y = air5_cells(64, seed=9)
-    g, o, _, _ = run_pair(rc, orc, T, p, Y, 1.0e-6)
+    g, o, _, _ = run_pair(rc, orc, T, p, Y, 1.0e-6, kernel=kernel)
     assert (g["status"] == oracle.ST_MAX_SUBCYCLES).all()
     assert np.array_equal(g["T"], T) and np.array_equal(g["Y"], Y) and np.array_equal(g["p"], p)
     assert np.array_equal(g["status"], o["status"])
