@@ -36,6 +36,13 @@ def _f64(t, shape):
     return t
 
 
+class CellBlockC(ctypes.Structure):
+    """gdtk_cell_block of include/gdtk_chem.h."""
+    _fields_ = [("ncell", ctypes.c_int), ("first", ctypes.c_int), ("t_interval", ctypes.c_double),
+                ("rho", ctypes.c_void_p), ("u", ctypes.c_void_p), ("T", ctypes.c_void_p), ("p", ctypes.c_void_p),
+                ("massf", ctypes.c_void_p), ("dt_chem", ctypes.c_void_p), ("status", ctypes.c_void_p)]
+
+
 class ReactorCells:
     """A gas model + mechanism pair with batch entry points (chem_reactor_update_cells etc.)."""
 
@@ -80,6 +87,30 @@ class ReactorCells:
                                                  _ptr(massf), _ptr(dt_chem), _ptr(status), float(t_interval),
                                                  float(T_frozen), int(flags), _stream(), _ptr(cell_counters),
                                                  _ptr(totals)), "chem_reactor_update_cells")
+
+    def block_table(self, blocks):
+        """ctypes array of gdtk_cell_block for a list of dicts with keys rho, u, T, p, massf,
+        dt_chem, t_interval and optionally status (cuda tensors)."""
+        table = (CellBlockC * len(blocks))()
+        for k, b in enumerate(blocks):
+            n = b["rho"].shape[0]
+            for key in ("rho", "u", "T", "p", "dt_chem"):
+                _f64(b[key], (n,))
+            _f64(b["massf"], (self.nsp, n))
+            st = b.get("status")
+            table[k] = CellBlockC(n, 0, float(b["t_interval"]), b["rho"].data_ptr(), b["u"].data_ptr(),
+                                  b["T"].data_ptr(), b["p"].data_ptr(), b["massf"].data_ptr(), b["dt_chem"].data_ptr(),
+                                  st.data_ptr() if st is not None else None)
+        return table
+
+    def update_blocks(self, blocks, T_frozen=0.0, flags=UPDATE_THERMO | RETRY, cell_counters=None, totals=None,
+                      table=None):
+        """All blocks in one persistent launch (chem_reactor_update_blocks); in place."""
+        if table is None:
+            table = self.block_table(blocks)
+        check(lib().chem_reactor_update_blocks(self.reactor.id, len(table), table, float(T_frozen), int(flags),
+                                               _stream(), _ptr(cell_counters), _ptr(totals)),
+              "chem_reactor_update_blocks")
 
     def update_host(self, rho, u, T, p, massf, dt_chem, t_interval, status=None, T_frozen=0.0,
                     flags=UPDATE_THERMO | RETRY):

@@ -261,14 +261,18 @@ int launch_update(ReactorObj& r, int ncell, const double* rho, const double* u, 
     }
     if (!r.fast) r.fast.reset(build_fast_kernel(model(r.gm).gm, r.mh));
     FastArgs a{};
-    a.ncell = ncell;
+    a.nblocks = 1;
+    a.total = ncell;
     a.flags = flags & (CHEM_FLAG_UPDATE_THERMO | CHEM_FLAG_RETRY);
-    a.rho = rho; a.u = u; a.T = T; a.p = p; a.massf = massf; a.dt_chem = dt_chem; a.status = status;
-    a.t_interval = t_interval;
     a.T_frozen = T_frozen;
     a.counter = r.counter;
     a.cell_counters = cell_counters;
     a.totals = totals;
+    CellBlock& b = a.blocks[0];
+    b.ncell = ncell;
+    b.first = 0;
+    b.t_interval = t_interval;
+    b.rho = rho; b.u = u; b.T = T; b.p = p; b.massf = massf; b.dt_chem = dt_chem; b.status = status;
     check(launch_fast(*r.fast, a, cuda().sm_count, s, &r.last.grid, &r.last.block, &r.last.smem),
           "chemistry update launch");
     r.last.blocks_per_sm = r.fast->blocks_per_sm;
@@ -599,6 +603,53 @@ int chem_reactor_update_cells_ex(int cr_i, int ncell, const double* rho, const d
     return guarded([&] {
         return launch_update(reactor(cr_i), ncell, rho, u, T, p, massf, dt_chem, status, t_interval, T_frozen, flags,
                              (cudaStream_t)stream, cell_counters, totals);
+    });
+}
+
+int chem_reactor_update_blocks(int cr_i, int nblock, const gdtk_cell_block* blocks, double T_frozen, int flags,
+                               void* stream, int* cell_counters, unsigned long long* totals) {
+    return guarded([&] {
+        auto& r = reactor(cr_i);
+        require_cuda();
+        if (nblock < 0 || (nblock > 0 && !blocks)) throw std::runtime_error("bad block table");
+        if (flags & GDTK_CHEM_REFERENCE_ORDER) throw std::runtime_error("the block API uses the fast kernel only");
+        cudaStream_t s = (cudaStream_t)stream;
+        if (!r.fast) r.fast.reset(build_fast_kernel(model(r.gm).gm, r.mh));
+        if (!r.counter) check(cudaMalloc(&r.counter, sizeof(unsigned)), "cudaMalloc");
+        long long done_cells = 0;
+        for (int b0 = 0; b0 < nblock; b0 += FAST_MAX_BLOCKS) {   // one launch per 128 blocks
+            FastArgs a{};
+            a.flags = flags & (CHEM_FLAG_UPDATE_THERMO | CHEM_FLAG_RETRY);
+            a.T_frozen = T_frozen;
+            a.counter = r.counter;
+            a.totals = totals;
+            long long total = 0;
+            for (int k = 0; k < FAST_MAX_BLOCKS && b0 + k < nblock; ++k) {
+                const gdtk_cell_block& in = blocks[b0 + k];
+                if (in.ncell < 0) throw std::runtime_error("negative block size");
+                if (in.ncell > 0 && (!in.rho || !in.u || !in.T || !in.p || !in.massf || !in.dt_chem))
+                    throw std::runtime_error("null cell array in a block");
+                if (in.ncell > 0 && !(in.t_interval > 0.0)) throw std::runtime_error("t_interval must be > 0");
+                CellBlock& b = a.blocks[a.nblocks++];
+                b.ncell = in.ncell;
+                b.first = (int)total;
+                b.t_interval = in.t_interval;
+                b.rho = in.rho; b.u = in.u; b.T = in.T; b.p = in.p; b.massf = in.massf; b.dt_chem = in.dt_chem;
+                b.status = in.status;
+                total += in.ncell;
+            }
+            if (total >= (1LL << 31)) throw std::runtime_error("too many cells in one launch");
+            a.total = (int)total;
+            a.cell_counters = cell_counters ? cell_counters + 0 : nullptr;
+            if (cell_counters && done_cells) throw std::runtime_error("per-cell counters need <= 128 blocks");
+            if (total == 0) continue;
+            check(cudaMemsetAsync(r.counter, 0, sizeof(unsigned), s), "cudaMemsetAsync");
+            check(launch_fast(*r.fast, a, cuda().sm_count, s, &r.last.grid, &r.last.block, &r.last.smem),
+                  "chemistry update launch");
+            r.last.blocks_per_sm = r.fast->blocks_per_sm;
+            done_cells += total;
+        }
+        return 0;
     });
 }
 

@@ -33,24 +33,36 @@ namespace gdtk_fast {
 
 using gdtk::gdtk_exp;
 
-// must match the host's FastArgs (codegen.h)
-struct FastArgs {
-    const double* thermo;
-    const double* exp_table;
+// must match the host's CellBlock / FastArgs (codegen.h)
+struct CellBlock {
     int ncell;
-    int flags;
+    int first;              // global index of the block's first cell
+    double t_interval;
     const double* rho;
     const double* u;
     double* T;
     double* p;
-    double* massf;
+    double* massf;          // [nsp][ncell]
     double* dt_chem;
     int* status;
-    double t_interval;
+};
+
+#define GDTK_MAX_BLOCKS 128
+
+// Passed by value (__grid_constant__): the block table travels in the launch parameters, so a
+// launch needs no device-side table and a captured graph replays it exactly.
+struct FastArgs {
+    const double* thermo;
+    const double* exp_table;
+    int nblocks;
+    int total;
+    int flags;
+    int pad;
     double T_frozen;
     unsigned* counter;
-    int* cell_counters;
+    int* cell_counters;     // [6][total], global cell index
     unsigned long long* totals;
+    CellBlock blocks[GDTK_MAX_BLOCKS];
 };
 
 enum { ST_OK = 0, ST_H_MIN = 1, ST_MAX_ATTEMPTS = 2, ST_MAX_SUBCYCLES = 3, ST_NEWTON = 4, ST_BAD = 5, ST_FROZEN = 6,
@@ -134,47 +146,34 @@ __device__ __forceinline__ double sp_G(const double* TH, int i, double T, double
 }
 
 // T from (rho, u) at fixed composition, therm_perf_gas_mix.d:426-468 (same iteration, same
-// stopping rules).  YR[i * ys] = Y_i R_i.  *iters counts iterations.
-__device__ double T_from_u(const double* TH, const double* YR, int ys, double u_tgt, double T_guess, int& err,
-                           int& iters) {
+// stopping rules).  YR[i * ys] = Y_i R_i.  *iters counts iterations.  Out of line: it is
+// called after accepted steps and at the end of a cell, and one copy of its code serves both.
+__device__ __noinline__ double T_from_u(const double* TH, const double* YR, int ys, double u_tgt, double T_guess,
+                                        int* err, int* iters) {
     const double TOL = 1e-10;
-    double T = T_guess;
-    double dT = 0.0;
-    double lnT = log(T), rT = 1.0 / T;
-    double f = 0.0, cv = 0.0;
-    {
-        double rT2 = rT * rT;
-#pragma unroll
+    double T = T_guess, dT = 0.0;
+    for (int it = 0; it <= 10; ++it) {
+        if (it > 0) {
+            T += dT;
+            if (fabs(dT) / T < TOL) return T;
+            if (it == 10) break;
+        }
+        const double lnT = log(T), rT = 1.0 / T, rT2 = rT * rT;
+        double f = 0.0, cv = 0.0;
+#pragma unroll 1
         for (int i = 0; i < GDTK_NSP; ++i) {
             double H, Cp;
-            sp_H_Cp(TH, i, T, lnT, rT, rT2, H, Cp, err);
+            int e = 0;
+            sp_H_Cp(TH, i, T, lnT, rT, rT2, H, Cp, e);
+            if (e) *err = e;
             const double yr = YR[i * ys];
             f = fma(yr, H - T, f);
             cv = fma(yr, Cp - 1.0, cv);
         }
-        f -= u_tgt;
+        dT = -(f - u_tgt) / cv;
+        ++*iters;
     }
-    for (int iter = 0; iter < 10; ++iter) {
-        ++iters;
-        dT = -f / cv;
-        T += dT;
-        if (fabs(dT) / T < TOL) return T;
-        lnT = log(T);
-        rT = 1.0 / T;
-        double rT2 = rT * rT;
-        f = 0.0;
-        cv = 0.0;
-#pragma unroll
-        for (int i = 0; i < GDTK_NSP; ++i) {
-            double H, Cp;
-            sp_H_Cp(TH, i, T, lnT, rT, rT2, H, Cp, err);
-            const double yr = YR[i * ys];
-            f = fma(yr, H - T, f);
-            cv = fma(yr, Cp - 1.0, cv);
-        }
-        f -= u_tgt;
-    }
-    if (fabs(dT) > 1e-3) err = ST_NEWTON;
+    if (fabs(dT) > 1e-3) *err = ST_NEWTON;
     return T;
 }
 
@@ -207,17 +206,19 @@ __device__ __forceinline__ double sum_pairwise(F d) {
     return s;
 }
 
-// Rate constants at T (clamped to the mechanism's limits, reaction_mechanism.d:49-63).
-__device__ __forceinline__ void rate_constants(const double* TH, double Tq, double* K, int ks, const double* etab,
-                                               int& err) {
+// Rate constants at T (clamped to the mechanism's limits, reaction_mechanism.d:49-63); the
+// species G/RT go through the per-thread scratch vector G.
+__device__ __noinline__ void rate_constants(const double* TH, double Tq, double* K, int ks, const double* etab,
+                                            double* G, int* err) {
     double T = Tq;
     if (T < GDTK_T_LOWER) T = GDTK_T_LOWER;
     if (T > GDTK_T_UPPER) T = GDTK_T_UPPER;
     const double lnT = log(T), rT = 1.0 / T, rT2 = rT * rT, t1 = lnT + 1.0, t2 = 1.0 - lnT;
-    double g[GDTK_NSP];
-#pragma unroll
-    for (int i = 0; i < GDTK_NSP; ++i) g[i] = sp_G(TH, i, T, lnT, rT, rT2, t1, t2, err);
-    gen_kc(T, lnT, rT, g, K, ks, etab);
+    int e = 0;
+#pragma unroll 1
+    for (int i = 0; i < GDTK_NSP; ++i) G[i * ks] = sp_G(TH, i, T, lnT, rT, rT2, t1, t2, e);
+    if (e) *err = e;
+    gen_kc(T, lnT, rT, G, ks, K, ks, etab);
 }
 
 // reaction_mechanism.d:161-203 from the rates at c.
@@ -249,24 +250,37 @@ __device__ __forceinline__ void alpha_nd(double s, double& N, double& D) {
 }
 
 // ---------------------------------------------------------------- the kernel
-extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_chem_fast(FastArgs a) {
+#if GDTK_METHOD == 0
+// Cash-Karp stage coefficients a[s][j] (stage s + 1 from k_1..k_s), chemistry_update.d:409-412
+__constant__ double RKF_A[5][5] = {
+    {1. / 5., 0, 0, 0, 0},
+    {3. / 40., 9. / 40., 0, 0, 0},
+    {3. / 10., -9. / 10., 6. / 5., 0, 0},
+    {-11. / 54., 5. / 2., -70. / 27., 35. / 27., 0},
+    {1631. / 55296., 175. / 512., 575. / 13824., 44275. / 110592., 253. / 4096.}};
+#define GDTK_VEC (6 * GDTK_NSP)
+#else
+#define GDTK_VEC (3 * GDTK_NSP)
+#endif
+
+extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_chem_fast(const __grid_constant__ FastArgs a) {
     extern __shared__ double smem[];
     double* TH = smem;                                   // thermo table, nsp * stride
     double* ETAB = smem + GDTK_NSP * GDTK_TH_STRIDE;     // exp table, 64
+    const CellBlock* BLK = a.blocks;
     double* S = ETAB + 64;                               // per-thread vectors
     for (int k = threadIdx.x; k < GDTK_NSP * GDTK_TH_STRIDE; k += blockDim.x) TH[k] = a.thermo[k];
     for (int k = threadIdx.x; k < 64; k += blockDim.x) ETAB[k] = a.exp_table[k];
     __syncthreads();
     const int ks = blockDim.x;
     double* K = S + threadIdx.x;                         // kf[NR], kb[NR]
-    double* V = K + 2 * GDTK_NR * ks;                    // method vectors
-    const unsigned ncell = (unsigned)a.ncell;
-    const double tI = a.t_interval;
+    double* V = K + 2 * GDTK_NR * ks;                    // method vectors; also G/RT and Y_i R_i scratch
 
-    unsigned c = 0;
+    unsigned g = 0;
+    int b = 0, ci = 0;
     bool have = false, retried = false, need_kc = false;
     int phase = 0, cycle = 0, attempt = 0, err = 0;
-    double rho = 0, rrho = 0, u = 0, T = 0, T0 = 0, p = 0, p0 = 0, dtS = 0, dtS0 = 0, dtSave = 0, h = 0, t = 0;
+    double rho = 0, rrho = 0, u = 0, T = 0, p = 0, dtS = 0, dtS0 = 0, dtSave = 0, h = 0, t = 0, tI = 0;
     double y0[GDTK_NSP];
     int n_steps = 0, n_rhs = 0, n_kc = 0, n_newton = 0, n_rej = 0, n_est = 0;
 
@@ -278,175 +292,164 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
             unsigned base = 0;
             if (lane == leader) base = atomicAdd(a.counter, (unsigned)__popc(mask));
             base = __shfl_sync(mask, base, leader);
-            c = base + __popc(mask & ((1u << lane) - 1u));
-            if (c >= ncell) break;
-            rho = a.rho[c]; u = a.u[c]; T0 = a.T[c]; p0 = a.p[c]; dtS0 = a.dt_chem[c];
-            if (T0 <= a.T_frozen) { if (a.status) a.status[c] = ST_FROZEN; continue; }
-            if (isnan(rho) || rho <= 0.0) { if (a.status) a.status[c] = ST_BAD; continue; }
+            g = base + __popc(mask & ((1u << lane) - 1u));
+            if (g >= (unsigned)a.total) break;
+            int lo = 0, hi = a.nblocks - 1;          // last block with first <= g
+            while (lo < hi) {
+                int mid = (lo + hi + 1) >> 1;
+                if ((unsigned)BLK[mid].first <= g) lo = mid; else hi = mid - 1;
+            }
+            b = lo;
+            ci = (int)(g - (unsigned)BLK[b].first);
+            const CellBlock& B = BLK[b];
+            rho = B.rho[ci]; u = B.u[ci]; tI = B.t_interval; dtS0 = B.dt_chem[ci];
+            if (B.T[ci] <= a.T_frozen) { if (B.status) B.status[ci] = ST_FROZEN; continue; }
+            if (isnan(rho) || rho <= 0.0) { if (B.status) B.status[ci] = ST_BAD; continue; }
             have = true;
             retried = false;
             rrho = 1.0 / rho;
             n_steps = n_rhs = n_kc = n_newton = n_rej = n_est = 0;
             phase = -1;
         }
-        if (phase == -1) {
-            T = T0; p = p0; dtS = dtS0; t = 0.0; err = 0;
+        if (phase == -1) {   // (re)start from the stored input state
+            const CellBlock& B = BLK[b];
+            T = B.T[ci]; p = B.p[ci]; dtS = dtS0; t = 0.0; err = 0;
 #pragma unroll
             for (int i = 0; i < GDTK_NSP; ++i) {
-                double v = a.massf[(size_t)i * ncell + c] * rho * GDTK_RM[i];
+                double v = B.massf[(size_t)i * B.ncell + ci] * rho * GDTK_RM[i];
                 y0[i] = (v < MIN_MOLES) ? 0.0 : v;
             }
             need_kc = true;
             phase = 0;
         }
         if (need_kc) {
-            rate_constants(TH, T, K, ks, ETAB, err);
+            rate_constants(TH, T, K, ks, ETAB, V, &err);
             ++n_kc;
             need_kc = false;
         }
-        // rates at y0: shared by the step-size estimate and the first stage of the step
-        double q[GDTK_NSP], L[GDTK_NSP];
-        gen_rhs(y0, q, L, K, ks);
-        ++n_rhs;
-        if (phase == 0) {
-            if (dtS > tI) h = tI;
-            else if (dtS <= 0.0) {   // the reference evaluates these rates a second time; counted as it does
-                h = estimate_step(y0, q, L);
-                ++n_est;
-                ++n_rhs;
-            }
-            else h = dtS;
-            cycle = 0;
-            phase = 1;
-        }
-        if (phase == 1) {
-            dtSave = dtS;
-            h = fmin(h, tI - t);
-            attempt = 0;
-            phase = 2;
-        }
         ++n_steps;
-        double yn[GDTK_NSP];   // stage input / predictor-corrector, then the step's result
-        bool ok;
+        double yn[GDTK_NSP];   // stage input, then the step's result
+        bool ok = false;
 #if GDTK_METHOD == 0
-        {   // Runge-Kutta-Fehlberg with Cash-Karp coefficients, chemistry_update.d:404-478
-            const double a21 = 1. / 5., a31 = 3. / 40., a32 = 9. / 40., a41 = 3. / 10., a42 = -9. / 10.,
-                a43 = 6. / 5., a51 = -11. / 54., a52 = 5. / 2., a53 = -70. / 27., a54 = 35. / 27.,
-                a61 = 1631. / 55296., a62 = 175. / 512., a63 = 575. / 13824., a64 = 44275. / 110592.,
-                a65 = 253. / 4096.;
-            const double b51 = 37. / 378., b53 = 250. / 621., b54 = 125. / 594., b56 = 512. / 1771.,
-                b41 = 2825. / 27648., b43 = 18575. / 48384., b44 = 13525. / 55296., b45 = 277. / 14336.,
-                b46 = 1.0 / 4.0;
-            double* k1 = V;
-            double* k2 = V + GDTK_NSP * ks;
-            double* k3 = V + 2 * GDTK_NSP * ks;
-            double* k4 = V + 3 * GDTK_NSP * ks;
-            double* k5 = V + 4 * GDTK_NSP * ks;
-            double* yT = yn;
+        // Runge-Kutta-Fehlberg with Cash-Karp coefficients, chemistry_update.d:404-478.
+        // V holds k_1..k_6; all six right-hand sides share one call site.
+        double errn = 0.0;
+#pragma unroll 1
+        for (int s = 0; s < 6; ++s) {
+            double q[GDTK_NSP], L[GDTK_NSP];
+            {
+                double cin[GDTK_NSP];
 #pragma unroll
-            for (int i = 0; i < GDTK_NSP; ++i) {
-                double k = q[i] - L[i];
-                k1[i * ks] = k;
-                yT[i] = fma(h, a21 * k, y0[i]);
+                for (int i = 0; i < GDTK_NSP; ++i) cin[i] = (s == 0) ? y0[i] : yn[i];
+                gen_rhs(cin, q, L, K, ks);
             }
-            gen_rhs(yT, q, L, K, ks);
+            ++n_rhs;
+            if (s == 0) {
+                if (phase == 0) {
+                    if (dtS > tI) h = tI;
+                    else if (dtS <= 0.0) { h = estimate_step(y0, q, L); ++n_est; ++n_rhs; }
+                    else h = dtS;
+                    cycle = 0;
+                    phase = 1;
+                }
+                if (phase == 1) { dtSave = dtS; h = fmin(h, tI - t); attempt = 0; phase = 2; }
+            }
+            double* kv = V + s * GDTK_NSP * ks;
 #pragma unroll
-            for (int i = 0; i < GDTK_NSP; ++i) {
-                double k = q[i] - L[i];
-                k2[i * ks] = k;
-                yT[i] = fma(h, fma(a32, k, a31 * k1[i * ks]), y0[i]);
-            }
-            gen_rhs(yT, q, L, K, ks);
+            for (int i = 0; i < GDTK_NSP; ++i) kv[i * ks] = q[i] - L[i];
+            if (s < 5) {
 #pragma unroll
-            for (int i = 0; i < GDTK_NSP; ++i) {
-                double k = q[i] - L[i];
-                k3[i * ks] = k;
-                yT[i] = fma(h, fma(a43, k, fma(a42, k2[i * ks], a41 * k1[i * ks])), y0[i]);
-            }
-            gen_rhs(yT, q, L, K, ks);
+                for (int i = 0; i < GDTK_NSP; ++i) {
+                    double acc = RKF_A[s][0] * V[i * ks];
+                    for (int j = 1; j <= s; ++j) acc = fma(RKF_A[s][j], V[(j * GDTK_NSP + i) * ks], acc);
+                    yn[i] = fma(h, acc, y0[i]);
+                }
+            } else {
+                const double b51 = 37. / 378., b53 = 250. / 621., b54 = 125. / 594., b56 = 512. / 1771.,
+                    b41 = 2825. / 27648., b43 = 18575. / 48384., b44 = 13525. / 55296., b45 = 277. / 14336.,
+                    b46 = 1.0 / 4.0;
+                double err2 = 0.0;
 #pragma unroll
-            for (int i = 0; i < GDTK_NSP; ++i) {
-                double k = q[i] - L[i];
-                k4[i * ks] = k;
-                yT[i] = fma(h, fma(a54, k, fma(a53, k3[i * ks], fma(a52, k2[i * ks], a51 * k1[i * ks]))), y0[i]);
+                for (int i = 0; i < GDTK_NSP; ++i) {
+                    double K1 = V[i * ks], K3 = V[(2 * GDTK_NSP + i) * ks], K4 = V[(3 * GDTK_NSP + i) * ks],
+                           K5 = V[(4 * GDTK_NSP + i) * ks], K6 = V[(5 * GDTK_NSP + i) * ks];
+                    double o = fma(h, fma(b56, K6, fma(b54, K4, fma(b53, K3, b51 * K1))), y0[i]);
+                    double o4 = fma(h, fma(b46, K6, fma(b45, K5, fma(b44, K4, fma(b43, K3, b41 * K1)))), y0[i]);
+                    double sk = fma(GDTK_ERRTOL, fmax(fabs(y0[i]), fabs(o)), GDTK_ERRTOL);
+                    double e = (o - o4) / sk;
+                    err2 = fma(e, e, err2);
+                    yn[i] = o;
+                }
+                errn = sqrt(err2 * (1.0 / GDTK_NSP));
             }
-            gen_rhs(yT, q, L, K, ks);
-#pragma unroll
-            for (int i = 0; i < GDTK_NSP; ++i) {
-                double k = q[i] - L[i];
-                k5[i * ks] = k;
-                yT[i] = fma(h, fma(a65, k, fma(a64, k4[i * ks], fma(a63, k3[i * ks], fma(a62, k2[i * ks],
-                            a61 * k1[i * ks])))), y0[i]);
-            }
-            gen_rhs(yT, q, L, K, ks);
-            n_rhs += 5;
-            double err2 = 0.0;
-#pragma unroll
-            for (int i = 0; i < GDTK_NSP; ++i) {
-                double K1 = k1[i * ks], K3 = k3[i * ks], K4 = k4[i * ks], K5 = k5[i * ks], K6 = q[i] - L[i];
-                double o = fma(h, fma(b56, K6, fma(b54, K4, fma(b53, K3, b51 * K1))), y0[i]);
-                double o4 = fma(h, fma(b46, K6, fma(b45, K5, fma(b44, K4, fma(b43, K3, b41 * K1)))), y0[i]);
-                yT[i] = o;
-                double sk = fma(GDTK_ERRTOL, fmax(fabs(y0[i]), fabs(o)), GDTK_ERRTOL);
-                double e = (o - o4) / sk;
-                err2 = fma(e, e, err2);
-            }
-            double errn = sqrt(err2 * (1.0 / GDTK_NSP));
+        }
+        {
             double scale;
             if (errn <= 1.0) {
-                if (errn == 0.0) scale = 10.0;
-                else scale = fmin(fmax(0.9 * gdtk_exp(-0.2 * log(errn), ETAB), 0.2), 10.0);
+                scale = (errn == 0.0) ? 10.0 : fmin(fmax(0.9 * gdtk_exp(-0.2 * log(errn), ETAB), 0.2), 10.0);
                 ok = true;
             } else {
                 scale = fmax(0.9 * gdtk_exp(-0.2 * log(errn), ETAB), 0.2);
-                ok = false;
             }
             dtS = scale * h;
         }
 #else
-        {   // alpha-QSS, chemistry_update.d:533-655; V holds q0, p0, yp0
+        // alpha-QSS, chemistry_update.d:533-655.  Iteration 0 is the predictor, 1..maxIters the
+        // correctors; with q0 = q and p0 = p the corrector formula reduces to the predictor's, so
+        // one update (and one right-hand-side call site) serves both.  V holds q0, p0, yp0.
+        {
             double* Q0 = V;
             double* P0 = V + GDTK_NSP * ks;
             double* YP0 = V + 2 * GDTK_NSP * ks;
-            double* yp = yn;
-#pragma unroll
-            for (int i = 0; i < GDTK_NSP; ++i) {
-                double y = y0[i];
-                double pi = L[i] / (y + ZERO_EPS);
-                double x = pi * h;
-                double N, D;
-                alpha_nd(x + ZERO_EPS, N, D);
-                double v = y + (h * (q[i] - pi * y)) * D / fma(N, x, D);
-                Q0[i * ks] = q[i];
-                P0[i * ks] = pi;
-                YP0[i * ks] = v;
-                yp[i] = v;
-            }
             bool conv = false;
-            for (int corr = 0; corr < GDTK_MAX_ITERS; ++corr) {
-                gen_rhs(yp, q, L, K, ks);
+#pragma unroll 1
+            for (int s = 0; s <= GDTK_MAX_ITERS; ++s) {
+                double q[GDTK_NSP], L[GDTK_NSP];
+                {
+                    double cin[GDTK_NSP];
+#pragma unroll
+                    for (int i = 0; i < GDTK_NSP; ++i) cin[i] = (s == 0) ? y0[i] : yn[i];
+                    gen_rhs(cin, q, L, K, ks);
+                }
                 ++n_rhs;
+                if (s == 0) {
+                    if (phase == 0) {
+                        if (dtS > tI) h = tI;
+                        else if (dtS <= 0.0) { h = estimate_step(y0, q, L); ++n_est; ++n_rhs; }
+                        else h = dtS;
+                        cycle = 0;
+                        phase = 1;
+                    }
+                    if (phase == 1) { dtSave = dtS; h = fmin(h, tI - t); attempt = 0; phase = 2; }
+                }
                 conv = true;
 #pragma unroll
                 for (int i = 0; i < GDTK_NSP; ++i) {
-                    double y = y0[i];
-                    double q0 = Q0[i * ks];
-                    double pp = L[i] / (yp[i] + ZERO_EPS);
-                    double x = pp * h;
+                    const double y = y0[i];
+                    const double ci_ = (s == 0) ? y : yn[i];
+                    const double pp = L[i] / (ci_ + ZERO_EPS);
+                    const double x = pp * h;
                     double N, D;
                     alpha_nd(x + ZERO_EPS, N, D);
-                    double pb = 0.5 * (P0[i * ks] + pp);
-                    double num = h * (fma(N, q[i] - q0, D * q0) - D * (pb * y));
-                    double yc = y + num / fma(N, h * pb, D);
-                    yp[i] = yc;
-                    if (!(yc < ZERO_EPS) && fabs(yc - YP0[i * ks]) >= GDTK_EPS1 * (yc + GDTK_DELTA)) conv = false;
+                    const double q0 = (s == 0) ? q[i] : Q0[i * ks];
+                    const double pb = (s == 0) ? pp : 0.5 * (P0[i * ks] + pp);
+                    const double num = h * (fma(N, q[i] - q0, D * q0) - D * (pb * y));
+                    const double v = y + num / fma(N, h * pb, D);
+                    if (s == 0) {
+                        Q0[i * ks] = q[i];
+                        P0[i * ks] = pp;
+                        YP0[i * ks] = v;
+                    } else if (!(v < ZERO_EPS) && fabs(v - YP0[i * ks]) >= GDTK_EPS1 * (v + GDTK_DELTA)) {
+                        conv = false;
+                    }
+                    yn[i] = v;
                 }
-                if (conv) break;
+                if (s > 0 && conv) break;
             }
             double sigma = 0.0;
 #pragma unroll
             for (int i = 0; i < GDTK_NSP; ++i) {
-                double yc = yp[i];
+                double yc = yn[i];
                 if (yc < ZERO_EPS) continue;
                 double test = fabs(yc - YP0[i * ks]) / (GDTK_EPS2 * (yc + GDTK_DELTA));
                 if (test > sigma) sigma = test;
@@ -478,7 +481,7 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
             double hMax = h * 1.1;
             if (dtS > h) h = fmin(dtS, hMax);
 #if GDTK_TIGHT
-            {   // chemistry_update.d:265-269; Y_i R_i go to the method vectors, free until the next step
+            {   // chemistry_update.d:265-269; Y_i R_i go to V, free until the next step
                 double Rm = 0.0;
 #pragma unroll
                 for (int i = 0; i < GDTK_NSP; ++i) {
@@ -488,7 +491,7 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
                     V[i * ks] = yr;
                     Rm += yr;
                 }
-                T = T_from_u(TH, V, ks, u, T, err, n_newton);
+                T = T_from_u(TH, V, ks, u, T, &err, &n_newton);
                 p = rho * Rm * T;
                 need_kc = true;
             }
@@ -511,13 +514,13 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
         }
         if (fail) {
             bool retryable = fail == ST_H_MIN || fail == ST_MAX_ATTEMPTS || fail == ST_MAX_SUBCYCLES;
-            if ((a.flags & F_RETRY) && retryable && !retried) {
+            if ((a.flags & F_RETRY) && retryable && !retried) {   // fluidfvcell.d:924-941
                 retried = true;
                 dtS0 = -1.0;
                 phase = -1;
                 continue;
             }
-            if (a.status) a.status[c] = fail;
+            if (BLK[b].status) BLK[b].status[ci] = fail;
             have = false;
         }
         if (done) {   // chemistry_update.d:290-325, then fluidfvcell.d:956
@@ -535,29 +538,31 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
             }
             int st = 0;
             if (a.flags & F_UPDATE_THERMO) {
-                T = T_from_u(TH, V, ks, u, T, st, n_newton);
+                T = T_from_u(TH, V, ks, u, T, &st, &n_newton);
                 p = rho * Rm * T;
             }
+            const CellBlock& B = BLK[b];
             if (st) {
-                if (a.status) a.status[c] = st;
+                if (B.status) B.status[ci] = st;
             } else {
 #pragma unroll
-                for (int i = 0; i < GDTK_NSP; ++i) a.massf[(size_t)i * ncell + c] = mf_of(i) * rtot;
-                a.T[c] = T;
-                a.p[c] = p;
-                a.dt_chem[c] = dtSave;
-                if (a.status) a.status[c] = ST_OK;
+                for (int i = 0; i < GDTK_NSP; ++i) B.massf[(size_t)i * B.ncell + ci] = mf_of(i) * rtot;
+                B.T[ci] = T;
+                B.p[ci] = p;
+                B.dt_chem[ci] = dtSave;
+                if (B.status) B.status[ci] = ST_OK;
             }
             have = false;
         }
         if (!have) {
             if (a.cell_counters) {
-                a.cell_counters[0 * (size_t)ncell + c] = n_steps;
-                a.cell_counters[1 * (size_t)ncell + c] = n_rhs;
-                a.cell_counters[2 * (size_t)ncell + c] = n_kc;
-                a.cell_counters[3 * (size_t)ncell + c] = n_newton;
-                a.cell_counters[4 * (size_t)ncell + c] = n_rej;
-                a.cell_counters[5 * (size_t)ncell + c] = n_est;
+                const size_t n = (size_t)a.total;
+                a.cell_counters[0 * n + g] = n_steps;
+                a.cell_counters[1 * n + g] = n_rhs;
+                a.cell_counters[2 * n + g] = n_kc;
+                a.cell_counters[3 * n + g] = n_newton;
+                a.cell_counters[4 * n + g] = n_rej;
+                a.cell_counters[5 * n + g] = n_est;
             }
             if (a.totals) {
                 atomicAdd(a.totals + 0, (unsigned long long)n_steps);

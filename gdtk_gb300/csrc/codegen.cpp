@@ -222,8 +222,8 @@ std::string generate_fast_source(const GasModelHost& gm, const MechanismHost& mh
     o << "namespace gdtk_fast {\nusing gdtk::gdtk_exp;\n";
 
     // ---- rate constants
-    o << "__device__ __forceinline__ void gen_kc(double T, double lnT, double rT, const double* g, double* K, int ks, "
-         "const double* etab) {\n";
+    o << "__device__ __forceinline__ void gen_kc(double T, double lnT, double rT, const double* g, int gs, double* K, "
+         "int ks, const double* etab) {\n";
     o << "  (void)T;\n";
     for (int ir = 0; ir < nr; ++ir) {
         const ReactionHost& r = mh.reactions[ir];
@@ -234,7 +234,7 @@ std::string generate_fast_source(const GasModelHost& gm, const MechanismHost& mh
         for (auto& p : parts) {
             if (p.nu == 0) continue;
             nusum += p.nu;
-            std::string term = "g[" + std::to_string(p.isp) + "]";
+            std::string term = "g[" + std::to_string(p.isp) + " * gs]";
             if (dg.tellp() == 0) {
                 if (p.nu == 1) dg << term;
                 else dg << lit((double)p.nu) << " * " << term;
@@ -393,7 +393,7 @@ FastKernel* build_fast_kernel(const GasModelHost& gm, const MechanismHost& mh) {
     cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int nsp = gm.n_species(), nr = (int)mh.reactions.size();
-    const int per_thread = 2 * nr + (mh.method == METHOD_RKF ? 5 : 3) * nsp;
+    const int per_thread = 2 * nr + (mh.method == METHOD_RKF ? 6 : 3) * nsp;
     const int table = nsp * 120 + 64;
     // Block size: as many resident threads as shared memory allows, up to 256 per SM.
     const double budget = 227.0 * 1024 / 8;   // doubles of shared memory per SM
@@ -469,8 +469,8 @@ cudaError_t launch_fast(FastKernel& k, FastArgs& a, int sm_count, cudaStream_t s
     a.thermo = k.d_thermo;
     a.exp_table = k.d_exp;
     int block = k.block;
-    while (block > 32 && ((long long)a.ncell + block - 1) / block < sm_count) block -= 32;
-    long long want = ((long long)a.ncell + block - 1) / block;
+    while (block > 32 && ((long long)a.total + block - 1) / block < sm_count) block -= 32;
+    long long want = ((long long)a.total + block - 1) / block;
     long long grid = (long long)sm_count * k.blocks_per_sm * (k.block / block);
     if (want < grid) grid = want;
     if (grid < 1) grid = 1;

@@ -9,12 +9,13 @@
 
 namespace gdtk {
 
-// Host mirror of gdtk_fast::FastArgs (chem_fast.cuh); the layouts must agree.
-struct FastArgs {
-    const double* thermo;
-    const double* exp_table;
+// Host mirrors of gdtk_fast::CellBlock / FastArgs (chem_fast.cuh); the layouts must agree.
+enum { FAST_MAX_BLOCKS = 128 };
+
+struct CellBlock {
     int ncell;
-    int flags;
+    int first;
+    double t_interval;
     const double* rho;
     const double* u;
     double* T;
@@ -22,11 +23,20 @@ struct FastArgs {
     double* massf;
     double* dt_chem;
     int* status;
-    double t_interval;
+};
+
+struct FastArgs {
+    const double* thermo;
+    const double* exp_table;
+    int nblocks;
+    int total;
+    int flags;
+    int pad;
     double T_frozen;
     unsigned* counter;
     int* cell_counters;
     unsigned long long* totals;
+    CellBlock blocks[FAST_MAX_BLOCKS];
 };
 
 struct FastKernel {

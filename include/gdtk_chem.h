@@ -96,6 +96,27 @@ int chem_reactor_update_cells_ex(int cr_i, int ncell, const double* rho, const d
                                  double* massf, double* dt_chem, int* status, double t_interval,
                                  double T_frozen, int flags, void* stream, int* cell_counters,
                                  unsigned long long* totals);
+/* Cells of many independent blocks, each with its own interval (the multi-block batch of
+ * lmr/simcore.d:322-340, where every block carries its own cell arrays).  The table is a host
+ * array; the pointers in it are device pointers.  Blocks are integrated by one persistent
+ * launch (per 128 blocks) whose work counter walks the cells of all blocks in table order, so
+ * ordering the table by expected cost (most steps first) shortens the tail.  `first` is set
+ * by the library.  The table is passed in the launch parameters: the call can be captured in a
+ * CUDA graph and replayed.  cell_counters, when given, is int[6][total cells] in table order. */
+typedef struct gdtk_cell_block {
+    int ncell;
+    int first;
+    double t_interval;
+    const double* rho;
+    const double* u;
+    double* T;
+    double* p;
+    double* massf;          /* [nsp][ncell] */
+    double* dt_chem;
+    int* status;            /* may be NULL */
+} gdtk_cell_block;
+int chem_reactor_update_blocks(int cr_i, int nblock, const gdtk_cell_block* blocks, double T_frozen, int flags,
+                               void* stream, int* cell_counters, unsigned long long* totals);
 /* Host-pointer form: copies in, updates, copies out, synchronises.  Page-locked host buffers
  * make the copies run at full link speed.  Returns the number of cells that failed (not
  * counting frozen ones), or -1 on error. */

@@ -292,3 +292,29 @@ def test_tickrates_match_oracle():
     conc = np.array(gs.conc)
     _, _, wf, wb = orc.split_rates(1500.0, conc)
     assert np.allclose(f, wf, rtol=1e-13, atol=0) and np.allclose(b, wb, rtol=1e-13, atol=0)
+
+
+def test_block_batch_equals_per_block_updates(j92):
+    # Cells are independent: one launch over uneven blocks with their own intervals gives each
+    # cell exactly the result of updating its block alone.
+    from gdtk_gb300.workloads import h2air_cells
+    torch = torch_cuda()
+    rc, _ = j92
+    sizes, dts = [300, 37, 1200], [1e-7, 1e-5, 1e-6]
+    blocks, solo = [], []
+    for k, (n, dt) in enumerate(zip(sizes, dts)):
+        T, p, Y = h2air_cells(rc.species_names, rc.mol_masses, n, seed=20 + k)
+        dT, dp, dY = to_dev(torch, T, p, Y)
+        rho, u = rc.thermo_from_pT(dp, dT, dY)
+        mk = lambda: dict(rho=rho, u=u, T=dT.clone(), p=dp.clone(), massf=dY.clone(),
+                          dt_chem=torch.full((n,), -1.0, dtype=torch.float64, device="cuda"),
+                          status=torch.zeros(n, dtype=torch.int32, device="cuda"), t_interval=dt)
+        blocks.append(mk())
+        solo.append(mk())
+    rc.update_blocks(blocks)
+    for b in solo:
+        rc.update(b["rho"], b["u"], b["T"], b["p"], b["massf"], b["dt_chem"], b["t_interval"], status=b["status"])
+    torch.cuda.synchronize()
+    for b, s in zip(blocks, solo):
+        for key in ("T", "p", "massf", "dt_chem", "status"):
+            assert torch.equal(b[key], s[key]), key
