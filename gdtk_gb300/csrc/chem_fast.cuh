@@ -237,16 +237,14 @@ __device__ __forceinline__ double estimate_step(const double (&c)[GDTK_NSP], con
     return fmax(dt_chem, 1.0e-15);
 }
 
-// alpha = N/D (chemistry_update.d:599-604) as N(s)/D(s), s = p h + eps.
+// alpha = N/D (chemistry_update.d:599-604) as N(s)/D(s), s = p h + eps, the reference's
+// rational function with numerator and denominator multiplied by s^3.  For s >= 1e50 the ratio
+// is 1 to double precision in either form, so s is capped there, which keeps N and D finite
+// without a branch.
 __device__ __forceinline__ void alpha_nd(double s, double& N, double& D) {
-    if (s < 1.0e50) {
-        N = fma(s, fma(s, 11.0 + s, 60.0), 180.0);
-        D = fma(s, fma(s, 12.0 + s, 60.0), 360.0);
-    } else {
-        double r = 1.0 / s;
-        N = fma(r, fma(r, fma(r, 180.0, 60.0), 11.0), 1.0);
-        D = fma(r, fma(r, fma(r, 360.0, 60.0), 12.0), 1.0);
-    }
+    s = fmin(s, 1.0e50);
+    N = fma(s, fma(s, 11.0 + s, 60.0), 180.0);
+    D = fma(s, fma(s, 12.0 + s, 60.0), 360.0);
 }
 
 // ---------------------------------------------------------------- the kernel
@@ -278,39 +276,55 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
 
     unsigned g = 0;
     int b = 0, ci = 0;
-    bool have = false, retried = false, need_kc = false;
+    bool have = false, alive = true, retried = false, need_kc = false;
     int phase = 0, cycle = 0, attempt = 0, err = 0;
     double rho = 0, rrho = 0, u = 0, T = 0, p = 0, dtS = 0, dtS0 = 0, dtSave = 0, h = 0, t = 0, tI = 0;
     double y0[GDTK_NSP];
     int n_steps = 0, n_rhs = 0, n_kc = 0, n_newton = 0, n_rej = 0, n_est = 0;
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
 
+    // All 32 lanes of a warp stay in this loop until the whole warp is out of work, so that
+    // every iteration can re-converge them (__syncwarp) and lanes that refill with a new cell
+    // run the same iteration as their neighbours instead of splitting the warp.
     while (true) {
-        if (!have) {
-            unsigned mask = __activemask();
-            int lane = threadIdx.x & 31;
-            int leader = __ffs(mask) - 1;
+        const unsigned need = __ballot_sync(FULL, alive && !have);
+        if (need) {   // refill: one atomic per warp for all lanes that need a cell
+            const int leader = __ffs(need) - 1;
             unsigned base = 0;
-            if (lane == leader) base = atomicAdd(a.counter, (unsigned)__popc(mask));
-            base = __shfl_sync(mask, base, leader);
-            g = base + __popc(mask & ((1u << lane) - 1u));
-            if (g >= (unsigned)a.total) break;
-            int lo = 0, hi = a.nblocks - 1;          // last block with first <= g
-            while (lo < hi) {
-                int mid = (lo + hi + 1) >> 1;
-                if ((unsigned)BLK[mid].first <= g) lo = mid; else hi = mid - 1;
+            if (lane == leader) base = atomicAdd(a.counter, (unsigned)__popc(need));
+            base = __shfl_sync(FULL, base, leader);
+            if (alive && !have) {
+                g = base + __popc(need & ((1u << lane) - 1u));
+                if (g >= (unsigned)a.total) {
+                    alive = false;
+                } else {
+                    int lo = 0, hi = a.nblocks - 1;          // last block with first <= g
+                    while (lo < hi) {
+                        int mid = (lo + hi + 1) >> 1;
+                        if ((unsigned)BLK[mid].first <= g) lo = mid; else hi = mid - 1;
+                    }
+                    b = lo;
+                    ci = (int)(g - (unsigned)BLK[b].first);
+                    const CellBlock& B = BLK[b];
+                    rho = B.rho[ci]; u = B.u[ci]; tI = B.t_interval; dtS0 = B.dt_chem[ci];
+                    if (B.T[ci] <= a.T_frozen) {
+                        if (B.status) B.status[ci] = ST_FROZEN;
+                    } else if (isnan(rho) || rho <= 0.0) {
+                        if (B.status) B.status[ci] = ST_BAD;
+                    } else {
+                        have = true;
+                        retried = false;
+                        rrho = 1.0 / rho;
+                        n_steps = n_rhs = n_kc = n_newton = n_rej = n_est = 0;
+                        phase = -1;
+                    }
+                }
             }
-            b = lo;
-            ci = (int)(g - (unsigned)BLK[b].first);
-            const CellBlock& B = BLK[b];
-            rho = B.rho[ci]; u = B.u[ci]; tI = B.t_interval; dtS0 = B.dt_chem[ci];
-            if (B.T[ci] <= a.T_frozen) { if (B.status) B.status[ci] = ST_FROZEN; continue; }
-            if (isnan(rho) || rho <= 0.0) { if (B.status) B.status[ci] = ST_BAD; continue; }
-            have = true;
-            retried = false;
-            rrho = 1.0 / rho;
-            n_steps = n_rhs = n_kc = n_newton = n_rej = n_est = 0;
-            phase = -1;
         }
+        const unsigned hm = __ballot_sync(FULL, have);
+        if (!__any_sync(FULL, alive || have)) break;
+        if (have) {
         if (phase == -1) {   // (re)start from the stored input state
             const CellBlock& B = BLK[b];
             T = B.T[ci]; p = B.p[ci]; dtS = dtS0; t = 0.0; err = 0;
@@ -327,6 +341,7 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
             ++n_kc;
             need_kc = false;
         }
+        __syncwarp(hm);
         ++n_steps;
         double yn[GDTK_NSP];   // stage input, then the step's result
         bool ok = false;
@@ -465,6 +480,7 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
             ok = conv;
         }
 #endif
+        __syncwarp(hm);
         if (ok) {   // mass-fraction test (chemistry_update.d:175-185)
             double tot = sum_pairwise([&](int i) {
                 double v = yn[i] * GDTK_M[i] * rrho;
@@ -518,10 +534,10 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
                 retried = true;
                 dtS0 = -1.0;
                 phase = -1;
-                continue;
+            } else {
+                if (BLK[b].status) BLK[b].status[ci] = fail;
+                have = false;
             }
-            if (BLK[b].status) BLK[b].status[ci] = fail;
-            have = false;
         }
         if (done) {   // chemistry_update.d:290-325, then fluidfvcell.d:956
             auto mf_of = [&](int i) {
@@ -573,6 +589,8 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
                 atomicAdd(a.totals + 5, (unsigned long long)n_est);
             }
         }
+        }   // if (have)
+        __syncwarp(FULL);
     }
 }
 
