@@ -303,7 +303,7 @@ def main():
             "cpu_baseline": cpu,
             "e2e": e2e,
             "clocks": clk,
-            "gpu_launches": args.steps,
+            "gpu_launches": args.steps * 5,
         }
         print(json.dumps(line))
     if ws > 1:

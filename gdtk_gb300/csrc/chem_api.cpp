@@ -138,6 +138,9 @@ struct ReactorObj {
     Staging stage;
     LaunchInfo last{};
     std::unique_ptr<FastKernel> fast;   // mechanism-specialised kernel, compiled on first use
+    DevBuf<float> order_key;            // longest-first scheduling scratch
+    DevBuf<int> order;
+    DevBuf<int> order_hist;
     ~ReactorObj() { if (counter) cudaFree(counter); }
 };
 
@@ -232,6 +235,22 @@ const char* status_text(int st) {
     }
 }
 
+// Fast-kernel launch of an assembled FastArgs, longest-first unless GDTK_CHEM_INDEX_ORDER.
+void run_fast(ReactorObj& r, FastArgs& a, int flags, cudaStream_t s) {
+    if (!(flags & GDTK_CHEM_INDEX_ORDER) && a.total > 1) {
+        r.order_key.ensure((size_t)a.total);
+        r.order.ensure((size_t)a.total);
+        r.order_hist.ensure(256);
+        check(launch_order(*r.fast, a, cuda().sm_count, r.order_key.p, r.order.p, r.order_hist.p, s),
+              "ordering launch");
+        a.order = r.order.p;
+    }
+    check(cudaMemsetAsync(r.counter, 0, sizeof(unsigned), s), "cudaMemsetAsync");
+    check(launch_fast(*r.fast, a, cuda().sm_count, s, &r.last.grid, &r.last.block, &r.last.smem),
+          "chemistry update launch");
+    r.last.blocks_per_sm = r.fast->blocks_per_sm;
+}
+
 int launch_update(ReactorObj& r, int ncell, const double* rho, const double* u, double* T, double* p, double* massf,
                   double* dt_chem, int* status, double t_interval, double T_frozen, int flags, cudaStream_t s,
                   int* cell_counters, unsigned long long* totals) {
@@ -273,8 +292,7 @@ int launch_update(ReactorObj& r, int ncell, const double* rho, const double* u, 
     b.first = 0;
     b.t_interval = t_interval;
     b.rho = rho; b.u = u; b.T = T; b.p = p; b.massf = massf; b.dt_chem = dt_chem; b.status = status;
-    check(launch_fast(*r.fast, a, cuda().sm_count, s, &r.last.grid, &r.last.block, &r.last.smem),
-          "chemistry update launch");
+    run_fast(r, a, flags, s);
     r.last.blocks_per_sm = r.fast->blocks_per_sm;
     return 0;
 }
@@ -643,10 +661,7 @@ int chem_reactor_update_blocks(int cr_i, int nblock, const gdtk_cell_block* bloc
             a.cell_counters = cell_counters ? cell_counters + 0 : nullptr;
             if (cell_counters && done_cells) throw std::runtime_error("per-cell counters need <= 128 blocks");
             if (total == 0) continue;
-            check(cudaMemsetAsync(r.counter, 0, sizeof(unsigned), s), "cudaMemsetAsync");
-            check(launch_fast(*r.fast, a, cuda().sm_count, s, &r.last.grid, &r.last.block, &r.last.smem),
-                  "chemistry update launch");
-            r.last.blocks_per_sm = r.fast->blocks_per_sm;
+            run_fast(r, a, flags, s);
             done_cells += total;
         }
         return 0;

@@ -62,6 +62,7 @@ struct FastArgs {
     unsigned* counter;
     int* cell_counters;     // [6][total], global cell index
     unsigned long long* totals;
+    const int* order;       // visit order of the global cell indices (null: index order)
     CellBlock blocks[GDTK_MAX_BLOCKS];
 };
 
@@ -299,6 +300,7 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
                 if (g >= (unsigned)a.total) {
                     alive = false;
                 } else {
+                    if (a.order) g = (unsigned)a.order[g];
                     int lo = 0, hi = a.nblocks - 1;          // last block with first <= g
                     while (lo < hi) {
                         int mid = (lo + hi + 1) >> 1;
@@ -591,6 +593,54 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
         }
         }   // if (have)
         __syncwarp(FULL);
+    }
+}
+
+// Expected cost of each cell, for longest-first scheduling of the persistent kernel: the
+// number of steps the 10%-per-step growth limit alone imposes (chemistry_update.d:204-219)
+// from the cell's first step size -- dt_chem when the cell carries one, otherwise the
+// estimate of reaction_mechanism.d:161-203 (rate constants + one right-hand side).
+extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_chem_cost(const __grid_constant__ FastArgs a,
+                                                                                     float* key) {
+    extern __shared__ double smem[];
+    double* TH = smem;
+    double* ETAB = smem + GDTK_NSP * GDTK_TH_STRIDE;
+    double* S = ETAB + 64;
+    for (int k = threadIdx.x; k < GDTK_NSP * GDTK_TH_STRIDE; k += blockDim.x) TH[k] = a.thermo[k];
+    for (int k = threadIdx.x; k < 64; k += blockDim.x) ETAB[k] = a.exp_table[k];
+    __syncthreads();
+    const int ks = blockDim.x;
+    double* K = S + threadIdx.x;
+    double* V = K + 2 * GDTK_NR * ks;
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < a.total; g += gridDim.x * blockDim.x) {
+        int lo = 0, hi = a.nblocks - 1;
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (a.blocks[mid].first <= g) lo = mid; else hi = mid - 1;
+        }
+        const CellBlock& B = a.blocks[lo];
+        const int ci = g - B.first;
+        const double rho = B.rho[ci], T = B.T[ci], dtc = B.dt_chem[ci], tI = B.t_interval;
+        float k = 0.0f;
+        if (T > a.T_frozen && rho > 0.0) {
+            double h;
+            if (dtc > 0.0) {
+                h = fmin(dtc, tI);
+            } else {
+                double y[GDTK_NSP], q[GDTK_NSP], L[GDTK_NSP];
+#pragma unroll
+                for (int i = 0; i < GDTK_NSP; ++i) {
+                    double v = B.massf[(size_t)i * B.ncell + ci] * rho * GDTK_RM[i];
+                    y[i] = (v < MIN_MOLES) ? 0.0 : v;
+                }
+                int err = 0;
+                rate_constants(TH, T, K, ks, ETAB, V, &err);
+                gen_rhs(y, q, L, K, ks);
+                h = estimate_step(y, q, L);
+            }
+            k = (float)(log1p(0.1 * tI / h) * 10.492058687799444);   // / ln 1.1
+        }
+        key[g] = k;
     }
 }
 

@@ -625,7 +625,61 @@ __global__ void __launch_bounds__(128) gas_service_kernel(GasServiceArgs a) {
     }
 }
 
+// ---------------------------------------------------------------- longest-first ordering
+// Counting sort of cells into 256 cost buckets (bucket = key/8, descending), the visit order of
+// the persistent chemistry kernel.  Order within a bucket is arbitrary; only scheduling
+// depends on it, never a cell's result.
+constexpr int ORDER_BUCKETS = 256;
+
+__device__ __forceinline__ int order_bucket(float key) {
+    int b = (int)(key * 0.125f);
+    b = b < 0 ? 0 : (b > ORDER_BUCKETS - 1 ? ORDER_BUCKETS - 1 : b);
+    return ORDER_BUCKETS - 1 - b;   // expensive first
+}
+
+__global__ void order_histogram(const float* key, int n, int* hist) {
+    __shared__ int h[ORDER_BUCKETS];
+    for (int k = threadIdx.x; k < ORDER_BUCKETS; k += blockDim.x) h[k] = 0;
+    __syncthreads();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        atomicAdd(&h[order_bucket(key[i])], 1);
+    __syncthreads();
+    for (int k = threadIdx.x; k < ORDER_BUCKETS; k += blockDim.x)
+        if (h[k]) atomicAdd(&hist[k], h[k]);
+}
+
+__global__ void order_scan(int* hist) {   // one block of ORDER_BUCKETS threads: exclusive scan in place
+    __shared__ int v[ORDER_BUCKETS];
+    const int t = threadIdx.x;
+    v[t] = hist[t];
+    __syncthreads();
+    for (int off = 1; off < ORDER_BUCKETS; off <<= 1) {
+        int x = t >= off ? v[t - off] : 0;
+        __syncthreads();
+        v[t] += x;
+        __syncthreads();
+    }
+    hist[t] = v[t] - hist[t];
+}
+
+__global__ void order_scatter(const float* key, int n, int* hist, int* order) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        order[atomicAdd(&hist[order_bucket(key[i])], 1)] = i;
+}
+
 }  // namespace
+
+cudaError_t launch_bucket_order(const float* key, int n, int* order, int* hist, int sm_count, cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(hist, 0, ORDER_BUCKETS * sizeof(int), stream);
+    if (e != cudaSuccess) return e;
+    int grid = (n + 255) / 256;
+    if (grid > sm_count * 4) grid = sm_count * 4;
+    order_histogram<<<grid, 256, 0, stream>>>(key, n, hist);
+    order_scan<<<1, ORDER_BUCKETS, 0, stream>>>(hist);
+    order_scatter<<<grid, 256, 0, stream>>>(key, n, hist, order);
+    return cudaGetLastError();
+}
 
 // ---------------------------------------------------------------- host-side launchers
 int chem_scratch_doubles(int nsp, int nr, int neff, int method) {

@@ -29,6 +29,7 @@
 #include "cea_thermo.h"
 #include "chem_types.h"
 #include "fast_exp.h"
+#include "chem_launch.h"
 
 namespace gdtk {
 
@@ -449,8 +450,13 @@ FastKernel* build_fast_kernel(const GasModelHost& gm, const MechanismHost& mh) {
     CUfunction fn;
     cu_check(d.moduleGetFunction(&fn, mod, "gdtk_chem_fast"), "cuModuleGetFunction");
     k->function = fn;
+    CUfunction cfn;
+    cu_check(d.moduleGetFunction(&cfn, mod, "gdtk_chem_cost"), "cuModuleGetFunction");
+    k->cost_function = cfn;
     const size_t smem_max = (size_t)(table + per_thread * block) * 8;
     cu_check(d.funcSetAttribute(fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)smem_max),
+             "cuFuncSetAttribute");
+    cu_check(d.funcSetAttribute(cfn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)smem_max),
              "cuFuncSetAttribute");
     cu_check(d.occupancy(&k->blocks_per_sm, fn, block, smem_max), "cuOccupancyMaxActiveBlocksPerMultiprocessor");
     if (k->blocks_per_sm < 1) throw std::runtime_error("fast kernel cannot be resident (registers/shared memory)");
@@ -482,6 +488,22 @@ cudaError_t launch_fast(FastKernel& k, FastArgs& a, int sm_count, cudaStream_t s
     if (block_out) *block_out = block;
     if (smem_out) *smem_out = (int)smem;
     return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorLaunchFailure;
+}
+
+cudaError_t launch_order(FastKernel& k, FastArgs& a, int sm_count, float* key, int* order, int* hist,
+                         cudaStream_t stream) {
+    a.thermo = k.d_thermo;
+    a.exp_table = k.d_exp;
+    const int block = k.block;
+    long long grid = ((long long)a.total + block - 1) / block;
+    if (grid > (long long)sm_count * k.blocks_per_sm) grid = (long long)sm_count * k.blocks_per_sm;
+    if (grid < 1) grid = 1;
+    size_t smem = (size_t)(k.table_doubles + k.per_thread_doubles * block) * 8;
+    void* params[] = {&a, &key};
+    CUresult r = driver().launchKernel((CUfunction)k.cost_function, (unsigned)grid, 1, 1, (unsigned)block, 1, 1,
+                                       (unsigned)smem, (CUstream)stream, params, nullptr);
+    if (r != CUDA_SUCCESS) return cudaErrorLaunchFailure;
+    return launch_bucket_order(key, a.total, order, hist, sm_count, stream);
 }
 
 }  // namespace gdtk

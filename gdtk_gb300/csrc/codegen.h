@@ -36,12 +36,14 @@ struct FastArgs {
     unsigned* counter;
     int* cell_counters;
     unsigned long long* totals;
+    const int* order;
     CellBlock blocks[FAST_MAX_BLOCKS];
 };
 
 struct FastKernel {
     void* module = nullptr;     // CUmodule
     void* function = nullptr;   // CUfunction
+    void* cost_function = nullptr;   // CUfunction of the cost pre-pass
     int block = 0;              // threads per block the kernel was compiled for
     int min_blocks = 1;
     int per_thread_doubles = 0;
@@ -66,5 +68,9 @@ FastKernel* build_fast_kernel(const GasModelHost& gm, const MechanismHost& mh);
 // Launches it; `info` receives the launch shape.
 cudaError_t launch_fast(FastKernel& k, FastArgs& a, int sm_count, cudaStream_t stream, int* grid_out, int* block_out,
                         int* smem_out);
+// Longest-first visit order: cost pre-pass into key[total], then a bucket sort into order[total]
+// (hist: 257 ints of scratch).  All on `stream`.
+cudaError_t launch_order(FastKernel& k, FastArgs& a, int sm_count, float* key, int* order, int* hist,
+                         cudaStream_t stream);
 
 }  // namespace gdtk

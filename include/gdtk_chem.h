@@ -38,6 +38,10 @@ enum gdtk_cell_status {
 /* Flags of chem_reactor_update_cells*. */
 #define GDTK_CHEM_UPDATE_THERMO 1 /* follow the update with update_thermo_from_rhou (fluidfvcell.d:956) */
 #define GDTK_CHEM_RETRY 2         /* retry a failed cell once with dt_chem = -1 (fluidfvcell.d:924-941) */
+#define GDTK_CHEM_INDEX_ORDER 8   /* integrate cells in index order (default: a cheap pre-pass ranks
+                                     cells by expected step count and the persistent kernel takes
+                                     the most expensive first, which shortens the tail; results
+                                     do not depend on the order) */
 #define GDTK_CHEM_REFERENCE_ORDER 4 /* use the kernel that keeps the reference's operation order
                                        (default: the mechanism-specialised kernel, which rearranges
                                        the arithmetic to spend fewer FP64 operations) */
