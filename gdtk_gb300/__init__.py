@@ -67,6 +67,7 @@ SIGNATURES = {
     "gas_model_update_thermo_from_rhou_cells": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _v, _v, _v, _v, _v,
                                                                _v, _v]),
     "chem_reactor_flop_model": (ctypes.c_int, [ctypes.c_int, _d]),
+    "chem_reactor_set_lane_stats": (ctypes.c_int, [ctypes.c_int, _v]),
     "chem_reactor_info": (ctypes.c_int, [ctypes.c_int, _i, _i, _i, _i]),
     "chem_reactor_last_launch": (ctypes.c_int, [ctypes.c_int, _i, _i, _i, _i]),
     "gdtk_last_error": (ctypes.c_char_p, []),

@@ -138,6 +138,7 @@ struct ReactorObj {
     Staging stage;
     LaunchInfo last{};
     std::unique_ptr<FastKernel> fast;   // mechanism-specialised kernel, compiled on first use
+    unsigned long long* lane_stats = nullptr;   // when set, the fast kernel counts lane occupancy
     DevBuf<float> order_key;            // longest-first scheduling scratch
     DevBuf<int> order;
     DevBuf<int> order_hist;
@@ -237,6 +238,7 @@ const char* status_text(int st) {
 
 // Fast-kernel launch of an assembled FastArgs, longest-first unless GDTK_CHEM_INDEX_ORDER.
 void run_fast(ReactorObj& r, FastArgs& a, int flags, cudaStream_t s) {
+    a.lane_stats = r.lane_stats;
     if (!(flags & GDTK_CHEM_INDEX_ORDER) && a.total > 1) {
         r.order_key.ensure((size_t)a.total);
         r.order.ensure((size_t)a.total);
@@ -770,6 +772,13 @@ int chem_reactor_flop_model(int cr_i, double* out) {
     return guarded([&] {
         auto& r = reactor(cr_i);
         flop_model(model(r.gm).gm, r.mh, out);
+        return 0;
+    });
+}
+
+int chem_reactor_set_lane_stats(int cr_i, unsigned long long* stats) {
+    return guarded([&] {
+        reactor(cr_i).lane_stats = stats;
         return 0;
     });
 }

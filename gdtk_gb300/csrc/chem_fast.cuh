@@ -63,8 +63,19 @@ struct FastArgs {
     int* cell_counters;     // [6][total], global cell index
     unsigned long long* totals;
     const int* order;       // visit order of the global cell indices (null: index order)
+    unsigned long long* lane_stats;   // optional [2 * 8]: per phase, warp executions and active lanes
     CellBlock blocks[GDTK_MAX_BLOCKS];
 };
+
+// Lane-occupancy instrumentation: for phase k, count warp executions and the lanes active in them.
+__device__ __forceinline__ void lane_stat(unsigned long long* st, int k) {
+    if (!st) return;
+    const unsigned m = __activemask();
+    if ((threadIdx.x & 31) == __ffs(m) - 1) {
+        atomicAdd(st + 2 * k, 1ull);
+        atomicAdd(st + 2 * k + 1, (unsigned long long)__popc(m));
+    }
+}
 
 enum { ST_OK = 0, ST_H_MIN = 1, ST_MAX_ATTEMPTS = 2, ST_MAX_SUBCYCLES = 3, ST_NEWTON = 4, ST_BAD = 5, ST_FROZEN = 6,
        ST_CEA = 7 };
@@ -150,10 +161,11 @@ __device__ __forceinline__ double sp_G(const double* TH, int i, double T, double
 // stopping rules).  YR[i * ys] = Y_i R_i.  *iters counts iterations.  Out of line: it is
 // called after accepted steps and at the end of a cell, and one copy of its code serves both.
 __device__ __noinline__ double T_from_u(const double* TH, const double* YR, int ys, double u_tgt, double T_guess,
-                                        int* err, int* iters) {
+                                        int* err, int* iters, unsigned long long* lst) {
     const double TOL = 1e-10;
     double T = T_guess, dT = 0.0;
     for (int it = 0; it <= 10; ++it) {
+        lane_stat(lst, 4);
         if (it > 0) {
             T += dT;
             if (fabs(dT) / T < TOL) return T;
@@ -325,8 +337,10 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
             }
         }
         const unsigned hm = __ballot_sync(FULL, have);
+        if (need) lane_stat(a.lane_stats, 6);
         if (!__any_sync(FULL, alive || have)) break;
         if (have) {
+        lane_stat(a.lane_stats, 0);
         if (phase == -1) {   // (re)start from the stored input state
             const CellBlock& B = BLK[b];
             T = B.T[ci]; p = B.p[ci]; dtS = dtS0; t = 0.0; err = 0;
@@ -339,6 +353,7 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
             phase = 0;
         }
         if (need_kc) {
+            lane_stat(a.lane_stats, 1);
             rate_constants(TH, T, K, ks, ETAB, V, &err);
             ++n_kc;
             need_kc = false;
@@ -426,6 +441,7 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
                     double cin[GDTK_NSP];
 #pragma unroll
                     for (int i = 0; i < GDTK_NSP; ++i) cin[i] = (s == 0) ? y0[i] : yn[i];
+                    lane_stat(a.lane_stats, 2);
                     gen_rhs(cin, q, L, K, ks);
                 }
                 ++n_rhs;
@@ -483,6 +499,7 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
         }
 #endif
         __syncwarp(hm);
+        lane_stat(a.lane_stats, 3);
         if (ok) {   // mass-fraction test (chemistry_update.d:175-185)
             double tot = sum_pairwise([&](int i) {
                 double v = yn[i] * GDTK_M[i] * rrho;
@@ -509,7 +526,7 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
                     V[i * ks] = yr;
                     Rm += yr;
                 }
-                T = T_from_u(TH, V, ks, u, T, &err, &n_newton);
+                T = T_from_u(TH, V, ks, u, T, &err, &n_newton, a.lane_stats);
                 p = rho * Rm * T;
                 need_kc = true;
             }
@@ -542,6 +559,7 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
             }
         }
         if (done) {   // chemistry_update.d:290-325, then fluidfvcell.d:956
+            lane_stat(a.lane_stats, 5);
             auto mf_of = [&](int i) {
                 double v = y0[i] * GDTK_M[i] * rrho;
                 return (v < 1.0e-30) ? 0.0 : v;
@@ -556,7 +574,7 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
             }
             int st = 0;
             if (a.flags & F_UPDATE_THERMO) {
-                T = T_from_u(TH, V, ks, u, T, &st, &n_newton);
+                T = T_from_u(TH, V, ks, u, T, &st, &n_newton, a.lane_stats);
                 p = rho * Rm * T;
             }
             const CellBlock& B = BLK[b];

@@ -37,6 +37,7 @@ struct FastArgs {
     int* cell_counters;
     unsigned long long* totals;
     const int* order;
+    unsigned long long* lane_stats;
     CellBlock blocks[FAST_MAX_BLOCKS];
 };
 

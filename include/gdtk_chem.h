@@ -158,6 +158,12 @@ int gdtk_exp_host(int n, const double* x, double* y);
  * copies the compiler log (register use) into log; 0 on success, -1 on a compile error. */
 int gdtk_compile_fast_source_check(const char* gas_file, const char* chem_file, int cc_major, int cc_minor,
                                    char* log, int n);
+/* Diagnostics: when stats (device, unsigned long long[16]) is set, later fast-kernel launches
+ * add, for each phase k (0 iteration, 1 rate constants, 2 right-hand side, 3 step control,
+ * 4 Newton iteration, 5 cell completion, 6 refill), the number of warp executions in
+ * stats[2k] and of active lanes in them in stats[2k+1].  NULL turns it off.  No counterpart in
+ * the reference. */
+int chem_reactor_set_lane_stats(int cr_i, unsigned long long* stats);
 /* Reactor description: n species, n reactions, ODE method (0 rkf, 1 alpha-qss), tight coupling. */
 int chem_reactor_info(int cr_i, int* nsp, int* nr, int* method, int* tight);
 /* Launch shape of the last chem_reactor_update_cells* call on this reactor. */
