@@ -57,6 +57,8 @@ SIGNATURES = {
                                                  ctypes.c_double, ctypes.c_double, ctypes.c_int, _v]),
     "chem_reactor_update_cells_ex": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _v, _v, _v, _v, _v, _v, _v,
                                                     ctypes.c_double, ctypes.c_double, ctypes.c_int, _v, _v, _v]),
+    "chem_reactor_update_cells_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _v, _v, _v, _v, _v, _v, _v,
+                                                         ctypes.c_double, ctypes.c_double, ctypes.c_int, _v]),
     "chem_reactor_update_blocks": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _v, ctypes.c_double, ctypes.c_int,
                                                   _v, _v, _v]),
     "chem_reactor_update_cells_host": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _v, _v, _v, _v, _v, _v, _v,

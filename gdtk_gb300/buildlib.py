@@ -20,6 +20,7 @@ SOURCES = [
     ("chem_kernels.cu", ["--fmad=false"]),
     ("codegen.cpp", []),
     ("fp64_probe.cu", []),
+    ("noalloc.cu", []),
     ("chem_api.cpp", []),
     ("mechanism.cpp", []),
     ("lua_table.cpp", []),

@@ -300,6 +300,52 @@ int launch_update(ReactorObj& r, int ncell, const double* rho, const double* u, 
 }
 
 }  // namespace
+
+void report_error(const std::string& msg) { report(msg); }
+
+// The fast-kernel update with caller-provided scratch (the allocation-free entry point of
+// noalloc.cu).  Allocates nothing: the reactor's mechanism kernel must already be loaded (the
+// first chem_reactor_update_cells call on the reactor compiles and loads it).  counter and
+// hist are zeroed here on the stream; key and order are fully overwritten before use.
+int update_cells_with_scratch(int cr_i, int ncell, const double* rho, const double* u, double* T, double* p,
+                              double* massf, double* dt_chem, int* status, double t_interval, double T_frozen,
+                              int flags, void* stream, unsigned* counter, float* key, int* order, int* hist) {
+    return guarded([&] {
+        auto& r = reactor(cr_i);
+        if (!cuda().ok) throw std::runtime_error(cuda().why);
+        if (!r.fast)
+            throw std::runtime_error("chem_reactor_update_cells_noalloc: the reactor's mechanism kernel is not loaded "
+                                     "yet; one chem_reactor_update_cells call on this reactor (which may allocate) "
+                                     "loads it");
+        if (flags & GDTK_CHEM_REFERENCE_ORDER)
+            throw std::runtime_error("chem_reactor_update_cells_noalloc runs the mechanism-specialised kernel only");
+        if (ncell < 0) throw std::runtime_error("ncell must be >= 0");
+        if (ncell == 0) return 0;
+        if (!rho || !u || !T || !p || !massf || !dt_chem) throw std::runtime_error("null cell array");
+        if (!(t_interval > 0.0)) throw std::runtime_error("t_interval must be > 0");
+        cudaStream_t s = (cudaStream_t)stream;
+        FastArgs a{};
+        a.nblocks = 1;
+        a.total = ncell;
+        a.flags = flags & (CHEM_FLAG_UPDATE_THERMO | CHEM_FLAG_RETRY);
+        a.T_frozen = T_frozen;
+        a.counter = counter;
+        CellBlock& b = a.blocks[0];
+        b.ncell = ncell;
+        b.first = 0;
+        b.t_interval = t_interval;
+        b.rho = rho; b.u = u; b.T = T; b.p = p; b.massf = massf; b.dt_chem = dt_chem; b.status = status;
+        if (!(flags & GDTK_CHEM_INDEX_ORDER) && ncell > 1) {
+            check(launch_order(*r.fast, a, cuda().sm_count, key, order, hist, s), "ordering launch");
+            a.order = order;
+        }
+        check(cudaMemsetAsync(counter, 0, sizeof(unsigned), s), "cudaMemsetAsync");
+        int grid = 0, block = 0, smem = 0;
+        check(launch_fast(*r.fast, a, cuda().sm_count, s, &grid, &block, &smem), "chemistry update launch");
+        return 0;
+    });
+}
+
 }  // namespace gdtk
 
 using namespace gdtk;

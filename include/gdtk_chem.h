@@ -121,6 +121,21 @@ typedef struct gdtk_cell_block {
 } gdtk_cell_block;
 int chem_reactor_update_blocks(int cr_i, int nblock, const gdtk_cell_block* blocks, double T_frozen, int flags,
                                void* stream, int* cell_counters, unsigned long long* totals);
+/* Allocation-free form of chem_reactor_update_cells (no counterpart in the reference).  For
+ * callers that cannot allocate device memory where they run the chemistry: inside CUDA graph
+ * capture, under a fixed pre-reserved memory budget, or on a thread that must not take
+ * cudaMalloc's device-wide synchronisation.  Same arguments and results; the per-call scratch
+ * (work counter, ordering keys and visit order) comes from one static device array of about
+ * 8 MiB that every GPU loading this library holds until exit, so ncell is limited to
+ * 1,048,576 (larger batches are rejected with -1 and a message).  It calls no cudaMalloc or
+ * cudaFree.  Its first call on a device looks up that array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.  The reactor's
+ * mechanism kernel must already be loaded: one ordinary chem_reactor_update_cells call on the
+ * reactor does it.  All calls share the array, so calls that overlap on the GPU (different
+ * streams, or concurrent graphs) race on it; serialise them. */
+int chem_reactor_update_cells_noalloc(int cr_i, int ncell, const double* rho, const double* u, double* T, double* p,
+                                      double* massf, double* dt_chem, int* status, double t_interval,
+                                      double T_frozen, int flags, void* stream);
 /* Host-pointer form: copies in, updates, copies out, synchronises.  Page-locked host buffers
  * make the copies run at full link speed.  Returns the number of cells that failed (not
  * counting frozen ones), or -1 on error. */
