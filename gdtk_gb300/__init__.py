@@ -70,6 +70,7 @@ SIGNATURES = {
                                                                _v, _v]),
     "chem_reactor_flop_model": (ctypes.c_int, [ctypes.c_int, _d]),
     "chem_reactor_set_lane_stats": (ctypes.c_int, [ctypes.c_int, _v]),
+    "chem_reactor_configure": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "chem_reactor_info": (ctypes.c_int, [ctypes.c_int, _i, _i, _i, _i]),
     "chem_reactor_last_launch": (ctypes.c_int, [ctypes.c_int, _i, _i, _i, _i]),
     "gdtk_last_error": (ctypes.c_char_p, []),

@@ -138,6 +138,7 @@ struct ReactorObj {
     Staging stage;
     LaunchInfo last{};
     std::unique_ptr<FastKernel> fast;   // mechanism-specialised kernel, compiled on first use
+    int req_block = 0, req_min_blocks = 0;   // launch shape chosen by chem_reactor_configure
     unsigned long long* lane_stats = nullptr;   // when set, the fast kernel counts lane occupancy
     DevBuf<float> order_key;            // longest-first scheduling scratch
     DevBuf<int> order;
@@ -280,7 +281,7 @@ int launch_update(ReactorObj& r, int ncell, const double* rho, const double* u, 
         check(launch_chem_update(a, r.mh.method, r.scratch, cuda().sm_count, s, &r.last), "chemistry update launch");
         return 0;
     }
-    if (!r.fast) r.fast.reset(build_fast_kernel(model(r.gm).gm, r.mh));
+    if (!r.fast) r.fast.reset(build_fast_kernel(model(r.gm).gm, r.mh, r.req_block, r.req_min_blocks));
     FastArgs a{};
     a.nblocks = 1;
     a.total = ncell;
@@ -680,7 +681,7 @@ int chem_reactor_update_blocks(int cr_i, int nblock, const gdtk_cell_block* bloc
         if (nblock < 0 || (nblock > 0 && !blocks)) throw std::runtime_error("bad block table");
         if (flags & GDTK_CHEM_REFERENCE_ORDER) throw std::runtime_error("the block API uses the fast kernel only");
         cudaStream_t s = (cudaStream_t)stream;
-        if (!r.fast) r.fast.reset(build_fast_kernel(model(r.gm).gm, r.mh));
+        if (!r.fast) r.fast.reset(build_fast_kernel(model(r.gm).gm, r.mh, r.req_block, r.req_min_blocks));
         if (!r.counter) check(cudaMalloc(&r.counter, sizeof(unsigned)), "cudaMalloc");
         long long done_cells = 0;
         for (int b0 = 0; b0 < nblock; b0 += FAST_MAX_BLOCKS) {   // one launch per 128 blocks
@@ -818,6 +819,18 @@ int chem_reactor_flop_model(int cr_i, double* out) {
     return guarded([&] {
         auto& r = reactor(cr_i);
         flop_model(model(r.gm).gm, r.mh, out);
+        return 0;
+    });
+}
+
+int chem_reactor_configure(int cr_i, int block, int min_blocks) {
+    return guarded([&] {
+        auto& r = reactor(cr_i);
+        require_cuda();
+        std::unique_ptr<FastKernel> k(build_fast_kernel(model(r.gm).gm, r.mh, block, min_blocks));
+        r.req_block = block;
+        r.req_min_blocks = min_blocks;
+        r.fast = std::move(k);
         return 0;
     });
 }

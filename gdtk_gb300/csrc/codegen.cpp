@@ -387,7 +387,7 @@ std::string compile_fast_check(const GasModelHost& gm, const MechanismHost& mh, 
     return log;
 }
 
-FastKernel* build_fast_kernel(const GasModelHost& gm, const MechanismHost& mh) {
+FastKernel* build_fast_kernel(const GasModelHost& gm, const MechanismHost& mh, int req_block, int req_min_blocks) {
     int dev = 0, major = 0, minor = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
@@ -402,6 +402,14 @@ FastKernel* build_fast_kernel(const GasModelHost& gm, const MechanismHost& mh) {
     while (block > 32 && table + (double)per_thread * block > budget) block -= 32;
     if (table + (double)per_thread * block > budget) throw std::runtime_error("mechanism too large for shared memory");
     if (block <= 128 && 2 * (table + (double)per_thread * block) <= budget) min_blocks = 2;
+    if (req_block > 0) {   // an explicit launch shape (autotuning)
+        if (req_block % 32 || req_block > 1024) throw std::runtime_error("block size must be a multiple of 32, <= 1024");
+        int mb = req_min_blocks > 0 ? req_min_blocks : 1;
+        if (mb * (table + (double)per_thread * req_block) > budget)
+            throw std::runtime_error("requested block shape does not fit in shared memory");
+        block = req_block;
+        min_blocks = mb;
+    }
 
     auto k = std::make_unique<FastKernel>();
     k->block = block;

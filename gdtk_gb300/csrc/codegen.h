@@ -65,7 +65,8 @@ std::string generate_fast_source(const GasModelHost& gm, const MechanismHost& mh
 // (no GPU needed); returns the NVRTC/ptxas log, throws on a compilation error.
 std::string compile_fast_check(const GasModelHost& gm, const MechanismHost& mh, int major, int minor);
 // Compiles (or fetches from the in-process / on-disk cache) and loads the fast kernel.
-FastKernel* build_fast_kernel(const GasModelHost& gm, const MechanismHost& mh);
+// block/min_blocks <= 0: chosen from the shared-memory budget.
+FastKernel* build_fast_kernel(const GasModelHost& gm, const MechanismHost& mh, int block = 0, int min_blocks = 0);
 // Launches it; `info` receives the launch shape.
 cudaError_t launch_fast(FastKernel& k, FastArgs& a, int sm_count, cudaStream_t stream, int* grid_out, int* block_out,
                         int* smem_out);

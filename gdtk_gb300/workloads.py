@@ -59,3 +59,27 @@ def h2air_cells(names, mol_masses, n, seed=1, frozen_fraction=0.5, T_cold=(300.0
     Y[:, rad_idx] += share[:, None] * w
     Y = Y / Y.sum(axis=1, keepdims=True)
     return T, p, np.ascontiguousarray(Y.T)
+
+
+def h2air_blocks(names, mol_masses, nblocks=64, seed=2, n_min=2048, n_max=524288, dts=(1.0e-7, 1.0e-6, 1.0e-5)):
+    """Uneven multi-block H2-air workload.
+
+    Block sizes are log-uniform in [n_min, n_max]; each block draws its own update interval from
+    `dts`, its own cold fraction, and its own sub-ranges of the cold (300-600 K) and hot
+    (1100-2800 K) temperatures and of the pressure (2e4-5e5 Pa), and then its cells as in
+    h2air_cells.  Returns a list of dicts with T, p, Y (nsp, n) and dt.
+    """
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sizes = np.round(10.0 ** rng.uniform(np.log10(n_min), np.log10(n_max), nblocks)).astype(np.int64)
+    out = []
+    for b in range(nblocks):
+        dt = float(rng.choice(dts))
+        cold = np.sort(rng.uniform(300.0, 600.0, 2))
+        hot = np.sort(rng.uniform(1100.0, 2800.0, 2))
+        lp = np.sort(rng.uniform(np.log10(2.0e4), np.log10(5.0e5), 2))
+        frac = float(rng.uniform(0.0, 1.0))
+        T, p, Y = h2air_cells(names, mol_masses, int(sizes[b]), seed=seed * 1000 + b, frozen_fraction=frac,
+                              T_cold=(cold[0], cold[1] + 1e-9), T_hot=(hot[0], hot[1] + 1e-9),
+                              p_range=(10.0 ** lp[0], 10.0 ** lp[1] * (1 + 1e-12)))
+        out.append(dict(T=T, p=p, Y=Y, dt=dt))
+    return out

@@ -173,6 +173,11 @@ int gdtk_exp_host(int n, const double* x, double* y);
  * copies the compiler log (register use) into log; 0 on success, -1 on a compile error. */
 int gdtk_compile_fast_source_check(const char* gas_file, const char* chem_file, int cc_major, int cc_minor,
                                    char* log, int n);
+/* Launch shape of the reactor's mechanism-specialised kernel: threads per block (a multiple of
+ * 32) and resident blocks per SM it is compiled for (its register/shared-memory split).  0, 0
+ * restores the default (largest block the shared-memory budget allows).  Compiles and loads the
+ * variant now; later updates use it.  Used by the autotuner (gdtk_gb300/autotune.py). */
+int chem_reactor_configure(int cr_i, int block, int min_blocks);
 /* Diagnostics: when stats (device, unsigned long long[16]) is set, later fast-kernel launches
  * add, for each phase k (0 iteration, 1 rate constants, 2 right-hand side, 3 step control,
  * 4 Newton iteration, 5 cell completion, 6 refill), the number of warp executions in

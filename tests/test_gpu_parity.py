@@ -318,3 +318,62 @@ def test_block_batch_equals_per_block_updates(j92):
     for b, s in zip(blocks, solo):
         for key in ("T", "p", "massf", "dt_chem", "status"):
             assert torch.equal(b[key], s[key]), key
+
+
+def test_block_batch_graph_replay_matches_direct_calls(j92):
+    # One split step captured once as a CUDA graph and replayed twice (dt_chem carried) gives the
+    # same cells as two direct calls.
+    from gdtk_gb300.workloads import h2air_cells
+    torch = torch_cuda()
+    rc, _ = j92
+    def make():
+        out = []
+        for k, (n, dt) in enumerate(zip([200, 50], [1e-6, 1e-5])):
+            T, p, Y = h2air_cells(rc.species_names, rc.mol_masses, n, seed=60 + k)
+            dT, dp, dY = to_dev(torch, T, p, Y)
+            rho, u = rc.thermo_from_pT(dp, dT, dY)
+            out.append(dict(rho=rho, u=u, T=dT, p=dp, massf=dY,
+                            dt_chem=torch.full((n,), -1.0, dtype=torch.float64, device="cuda"),
+                            status=torch.zeros(n, dtype=torch.int32, device="cuda"), t_interval=dt))
+        return out
+    direct, graphed = make(), make()
+    rc.update_blocks(direct)
+    rc.update_blocks(direct)
+    warm = make()
+    rc.update_blocks(warm)            # sizes the scratch before capture
+    torch.cuda.synchronize()
+    table = rc.block_table(graphed)
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(s):
+        with torch.cuda.graph(g, stream=s):
+            rc.update_blocks(graphed, table=table)
+        g.replay()
+        g.replay()
+    torch.cuda.synchronize()
+    for a, b in zip(direct, graphed):
+        for key in ("T", "p", "massf", "dt_chem", "status"):
+            assert torch.equal(a[key], b[key]), key
+
+
+def test_autotuner_picks_a_fitting_shape(j92, tmp_path, monkeypatch):
+    from gdtk_gb300 import autotune
+    from gdtk_gb300.workloads import h2air_cells
+    torch = torch_cuda()
+    monkeypatch.setenv("GDTK_JIT_CACHE", str(tmp_path))
+    monkeypatch.setattr(autotune, "SHAPES", [(256, 1), (128, 1)])
+    rc, orc = j92
+    T, p, Y = h2air_cells(rc.species_names, rc.mol_masses, 2048, seed=70)
+    dT, dp, dY = to_dev(torch, T, p, Y)
+    rho, u = rc.thermo_from_pT(dp, dT, dY)
+    sample = dict(rho=rho, u=u, T=dT, p=dp, massf=dY, dt_chem=torch.full((2048,), -1.0, dtype=torch.float64,
+                                                                         device="cuda"))
+    choice, oflag, results = autotune.tune(rc, sample, 1e-6, tag="test")
+    assert len(results) == 4 and (choice["block"], choice["min_blocks"]) in [(256, 1), (128, 1)]
+    assert os.path.exists(os.path.join(str(tmp_path), "tune.json"))
+    again, _, _ = autotune.tune(rc, sample, 1e-6, tag="test")     # from the cache
+    assert again["block"] == choice["block"]
+    # results still match the oracle under the tuned shape
+    g, o, _, _ = run_pair(rc, orc, T[:256], p[:256], np.ascontiguousarray(Y[:, :256]), 1.0e-6)
+    assert_parity(g, o)
+    autotune.check_shape(rc, 0, 0)   # back to the default shape for later tests
