@@ -40,6 +40,10 @@ WORKLOADS = {
     # 20 split steps with dt_chem carried, each split step one CUDA-graph replay of one launch
     "h2air-blocks64": dict(gas="j92-gas.lua", chem="j92-chem.lua", n=0, dt=0.0, kind="blocks", seed=2,
                            nblocks=64, split_steps=20),
+    # in-loop drop-in: a 2048 x 1024 mixing-layer block, 100 split steps of 5e-7 s through the
+    # thermochemical_increment contract (T_frozen = 300 K, dt_chem carried, retry, rhou update)
+    "h2air-mixing-layer": dict(gas="j92-gas.lua", chem="j92-chem.lua", n=2048 * 1024, dt=5.0e-7, kind="layer",
+                               seed=4, nx=2048, ny=1024, split_steps=100, T_frozen=300.0),
 }
 
 
@@ -146,12 +150,12 @@ def run_blocks(args, w):
     dev = torch.device("cuda", 0)
     t64 = lambda a: torch.tensor(np.ascontiguousarray(a), dtype=torch.float64, device=dev)
     # launch-shape autotuning on a sample of the same mixture (cached per mechanism and device)
-    sT, sp, sY = h2air_cells(rc.species_names, rc.mol_masses, 65536, seed=77)
+    sT, sp, sY = h2air_cells(rc.species_names, rc.mol_masses, 262144, seed=77)
     dT, dp, dY = t64(sT), t64(sp), t64(sY)
     srho, su = rc.thermo_from_pT(dp, dT, dY)
-    sample = dict(rho=srho, u=su, T=dT, p=dp, massf=dY, dt_chem=torch.full((65536,), -1.0, dtype=torch.float64,
+    sample = dict(rho=srho, u=su, T=dT, p=dp, massf=dY, dt_chem=torch.full((262144,), -1.0, dtype=torch.float64,
                                                                          device=dev))
-    choice, oflag, _ = autotune.tune(rc, sample, 1.0e-6, tag="h2air-65536")
+    choice, oflag, _ = autotune.tune(rc, sample, 1.0e-6, tag="h2air-262144")
     flags = UPDATE_THERMO | RETRY | oflag
     spec = h2air_blocks(rc.species_names, rc.mol_masses, nblocks=w["nblocks"], seed=w["seed"])
     blocks, init = [], []
@@ -199,6 +203,11 @@ def run_blocks(args, w):
     flops = rc.algorithmic_flops(tot)
     peak = fp64_peak_reference()
     failed = int(sum(int(((b["status"] != 0) & (b["status"] != 6)).sum()) for b in blocks))
+    by_status = {}
+    for b in blocks:
+        v, c = np.unique(b["status"].cpu().numpy(), return_counts=True)
+        for vv, cc in zip(v, c):
+            by_status[int(vv)] = by_status.get(int(vv), 0) + int(cc)
     # CPU baseline: the oracle over the same 20 split steps on a strided sample of every block
     import oracle
     orc = oracle.Oracle(os.path.join(MECH, w["gas"]), os.path.join(MECH, w["chem"]))
@@ -223,6 +232,7 @@ def run_blocks(args, w):
         "config": {"workload": "h2air-blocks64", "blocks": len(blocks), "cells": ncell,
                    "dt_per_block": [b["t_interval"] for b in blocks], "graph": "one CUDA-graph replay per split step",
                    "launch_shape": {k: choice[k] for k in ("block", "min_blocks", "order")}, "cells_failed": failed,
+                   "cells_by_status_last_step": by_status,
                    "l2": "inputs larger than L2 (no flush)"},
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                        "per_step": [round(float(x), 3) for x in lat]},
@@ -231,6 +241,91 @@ def run_blocks(args, w):
                      "work_per_cell_update": (tot / (ncell * nsteps)).tolist()},
         "cpu_baseline": {"value": cpu_cells / cpu_secs, "unit": "cell-updates/s", "cores": oracle.max_threads(),
                          "kind": "port", "sample": "32 strided cells of each block over the 20 split steps"},
+        "e2e": None, "clocks": clk, "gpu_launches": nsteps * 5,
+    }
+
+
+def run_layer(args, w):
+    """In-loop drop-in on a mixing-layer block: split steps as graph replays, final fields
+    compared with the CPU reference algorithm on sampled columns (returns the JSON line)."""
+    import torch
+    import oracle
+    from gdtk_gb300.cells import ReactorCells, UPDATE_THERMO, RETRY
+    from gdtk_gb300.workloads import h2air_mixing_layer
+    rc = ReactorCells(os.path.join(MECH, w["gas"]), os.path.join(MECH, w["chem"]))
+    dev = torch.device("cuda", 0)
+    nx, ny = w["nx"], w["ny"]
+    if args.cells:
+        nx = max(1, args.cells // ny)
+    n = nx * ny
+    T0, p0, Y0 = h2air_mixing_layer(rc.species_names, rc.mol_masses, nx=nx, ny=ny, seed=w["seed"])
+    t64 = lambda a: torch.tensor(np.ascontiguousarray(a), dtype=torch.float64, device=dev)
+    T, p, Y = t64(T0), t64(p0), t64(Y0)
+    rho, u = rc.thermo_from_pT(p, T, Y)
+    dtc = torch.full((n,), -1.0, dtype=torch.float64, device=dev)
+    st = torch.zeros(n, dtype=torch.int32, device=dev)
+    totals = torch.zeros(6, dtype=torch.int64, device=dev)
+    flags = UPDATE_THERMO | RETRY
+    init = (T.clone(), p.clone(), Y.clone(), dtc.clone())
+    rc.update(rho, u, T, p, Y, dtc, w["dt"], status=st, T_frozen=w["T_frozen"], flags=flags)   # warm-up
+    torch.cuda.synchronize()
+    stream = torch.cuda.Stream()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(stream):
+        with torch.cuda.graph(graph, stream=stream):
+            rc.update(rho, u, T, p, Y, dtc, w["dt"], status=st, T_frozen=w["T_frozen"], flags=flags, totals=totals)
+    for a, b in zip((T, p, Y, dtc), init):
+        a.copy_(b)
+    totals.zero_()
+    torch.cuda.synchronize()
+    nsteps = w["split_steps"]
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nsteps)]
+    clocks = ClockSampler(int(os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] or 0))
+    clocks.start()
+    with torch.cuda.stream(stream):
+        for k in range(nsteps):
+            ev[k][0].record(stream)
+            graph.replay()
+            ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    lat = np.array([a.elapsed_time(b) for a, b in ev])
+    total_ms = float(lat.sum())
+    tot = totals.cpu().numpy().astype(np.float64)
+    flops = rc.algorithmic_flops(tot)
+    peak = fp64_peak_reference()
+    # the reference algorithm on the CPU over the same 100 split steps, on sampled columns
+    orc = oracle.Oracle(os.path.join(MECH, w["gas"]), os.path.join(MECH, w["chem"]))
+    cols = np.linspace(0, nx - 1, min(4, nx)).astype(np.int64)
+    idx = np.concatenate([c + nx * np.arange(ny) for c in cols])
+    cT, cp, cY, cdt = T0[idx].copy(), p0[idx].copy(), Y0[:, idx].T.copy(), np.full(len(idx), -1.0)
+    crho, cu = rho.cpu().numpy()[idx], u.cpu().numpy()[idx]
+    t0 = time.perf_counter()
+    for _ in range(nsteps):
+        o = orc.chem_update(crho, cu, cT, cp, cY, cdt, w["dt"], T_frozen=w["T_frozen"])
+        cT, cp, cY, cdt = o["T"], o["p"], o["massf"], o["dt_chem"]
+    cpu_secs = time.perf_counter() - t0
+    gT, gY = T.cpu().numpy()[idx], Y.cpu().numpy()[:, idx].T
+    dY = float(np.abs(gY - cY).max())
+    relT = float((np.abs(gT - cT) / cT).max())
+    status = st.cpu().numpy()
+    return {
+        "metric": METRIC, "value": n * nsteps / (total_ms * 1e-3), "unit": "cell-updates/s", "n_gpus": 1,
+        "steps": nsteps, "warmup": 1, "ms_per_step": total_ms / nsteps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "h2air-mixing-layer", "nx": nx, "ny": ny, "cells": n, "dt": w["dt"],
+                   "T_frozen": w["T_frozen"], "graph": "one CUDA-graph replay per split step",
+                   "cells_frozen_last_step": int((status == 6).sum()),
+                   "cells_failed_last_step": int(((status != 0) & (status != 6)).sum())},
+        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                       "first": float(lat[0]), "last": float(lat[-1])},
+        "accuracy_vs_cpu_reference": {"columns": cols.tolist(), "cells": int(len(idx)), "max_abs_dY": dY,
+                                      "max_rel_dT": relT},
+        "roofline": {"bound": "fp64", "achieved": flops / (total_ms * 1e-3) / 1e12, "peak": peak,
+                     "unit": "TFLOP/s", "frac": flops / (total_ms * 1e-3) / 1e12 / peak, "traffic": None},
+        "cpu_baseline": {"value": len(idx) * nsteps / cpu_secs, "unit": "cell-updates/s",
+                         "cores": oracle.max_threads(), "kind": "port",
+                         "sample": "%d full columns (%d cells) over the %d split steps" % (len(cols), len(idx), nsteps)},
         "e2e": None, "clocks": clk, "gpu_launches": nsteps * 5,
     }
 
@@ -251,6 +346,15 @@ def main():
     if args.cells:
         w["n"] = args.cells
     ws, rank, local = dist_env()
+
+    if w["kind"] == "layer":
+        if args.impl == "reference" or rank != 0:
+            if args.impl == "reference" and rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable": "the mixing-layer mode reports its CPU "
+                                  "baseline inside the gdtk line"}))
+            return 0
+        print(json.dumps(run_layer(args, w)))
+        return 0
 
     if w["kind"] == "blocks":
         if args.impl == "reference" or rank != 0:

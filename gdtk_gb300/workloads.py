@@ -83,3 +83,34 @@ def h2air_blocks(names, mol_masses, nblocks=64, seed=2, n_min=2048, n_max=524288
                               p_range=(10.0 ** lp[0], 10.0 ** lp[1] * (1 + 1e-12)))
         out.append(dict(T=T, p=p, Y=Y, dt=dt))
     return out
+
+
+def h2air_mixing_layer(names, mol_masses, nx=2048, ny=1024, seed=4, thickness=16.0, T_fuel=300.0, T_ox=1500.0,
+                       p=1.0e5, radical_share=0.10):
+    """A 2-D structured block (nx x ny cells, cell index i + nx*j) holding a tanh mixing layer
+    across j: fuel stream (pure H2 at T_fuel) on one side, oxidiser stream (air at T_ox) on the
+    other, mixture fraction f = (1 + tanh((j - ny/2) / thickness)) / 2.  The oxidiser carries a
+    seeded radical share (O, OH, H, HO2, NO, N) of up to `radical_share` of its mass per cell.
+    T and Y blend linearly in f.  Returns T (n,), p (n,), Y (nsp, n)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    idx = {s: i for i, s in enumerate(names)}
+    M = np.asarray(mol_masses, dtype=np.float64)
+    nsp = len(names)
+    n = nx * ny
+    j = np.repeat(np.arange(ny), nx)
+    f = 0.5 * (1.0 + np.tanh((j - ny / 2.0) / thickness))
+    fuel = np.zeros(nsp)
+    fuel[idx['H2']] = 1.0
+    air = np.zeros(nsp)
+    air[idx['O2']] = 1.0 * M[idx['O2']]
+    air[idx['N2']] = 3.76 * M[idx['N2']]
+    air /= air.sum()
+    rad = [idx[s] for s in ('O', 'OH', 'H', 'HO2', 'NO', 'N') if s in idx]
+    share = rng.uniform(0.0, radical_share, n)
+    w = rng.dirichlet(np.full(len(rad), 0.5), n)
+    ox = np.repeat(air[None, :], n, axis=0) * (1.0 - share)[:, None]
+    ox[:, rad] += share[:, None] * w
+    Y = f[:, None] * fuel[None, :] + (1.0 - f)[:, None] * ox
+    Y /= Y.sum(axis=1, keepdims=True)
+    T = f * T_fuel + (1.0 - f) * T_ox
+    return T, np.full(n, p), np.ascontiguousarray(Y.T)

@@ -377,3 +377,28 @@ def test_autotuner_picks_a_fitting_shape(j92, tmp_path, monkeypatch):
     g, o, _, _ = run_pair(rc, orc, T[:256], p[:256], np.ascontiguousarray(Y[:, :256]), 1.0e-6)
     assert_parity(g, o)
     autotune.check_shape(rc, 0, 0)   # back to the default shape for later tests
+
+
+def test_mixing_layer_split_steps_track_the_oracle(j92):
+    # In-loop use: 10 split steps of 5e-7 s with dt_chem carried and T_frozen = 300 K on a
+    # small mixing-layer block; every step's output feeds the next, on the GPU and in the oracle.
+    from gdtk_gb300.workloads import h2air_mixing_layer
+    torch = torch_cuda()
+    rc, orc = j92
+    T, p, Y = h2air_mixing_layer(rc.species_names, rc.mol_masses, nx=4, ny=128, seed=9, thickness=4.0)
+    n = T.shape[0]
+    dT, dp, dY = to_dev(torch, T, p, Y)
+    rho, u = rc.thermo_from_pT(dp, dT, dY)
+    dtc = torch.full((n,), -1.0, dtype=torch.float64, device="cuda")
+    st = torch.zeros(n, dtype=torch.int32, device="cuda")
+    rho_h, u_h = rho.cpu().numpy(), u.cpu().numpy()
+    cT, cp, cY, cdt = T.copy(), p.copy(), Y.T.copy(), np.full(n, -1.0)
+    for _ in range(10):
+        rc.update(rho, u, dT, dp, dY, dtc, 5.0e-7, status=st, T_frozen=300.0)
+        o = orc.chem_update(rho_h, u_h, cT, cp, cY, cdt, 5.0e-7, T_frozen=300.0)
+        cT, cp, cY, cdt = o["T"], o["p"], o["massf"], o["dt_chem"]
+    torch.cuda.synchronize()
+    assert np.array_equal(st.cpu().numpy(), o["status"])
+    assert np.abs(dY.cpu().numpy() - cY.T).max() <= Y_ABS
+    assert (np.abs(dT.cpu().numpy() - cT) / cT).max() <= TP_REL
+    assert (o["status"] == 6).any() and (o["status"] == 0).any()
