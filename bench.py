@@ -308,6 +308,18 @@ def run_layer(args, w):
     gT, gY = T.cpu().numpy()[idx], Y.cpu().numpy()[:, idx].T
     dY = float(np.abs(gY - cY).max())
     relT = float((np.abs(gT - cT) / cT).max())
+    # both against a tight (Radau, rtol 1e-10) integration of the coupled ODE over the same
+    # interval, on cells through the mixing zone of the first sampled column
+    from oracle.tight import integrate_cell
+    zone = np.arange(ny // 2 - 30, ny // 2 + 30, 6)
+    tg = {"gpu_dY": 0.0, "gpu_dT": 0.0, "cpu_dY": 0.0, "cpu_dT": 0.0, "cells": int(len(zone))}
+    for j in zone:
+        mf, Tt = integrate_cell(orc, crho[j], cu[j], T0[idx][j], Y0[:, idx][:, j], nsteps * w["dt"], rtol=1e-10,
+                                tight=True)
+        tg["gpu_dY"] = max(tg["gpu_dY"], float(np.abs(gY[j] - mf).max()))
+        tg["gpu_dT"] = max(tg["gpu_dT"], float(abs(gT[j] - Tt) / Tt))
+        tg["cpu_dY"] = max(tg["cpu_dY"], float(np.abs(cY[j] - mf).max()))
+        tg["cpu_dT"] = max(tg["cpu_dT"], float(abs(cT[j] - Tt) / Tt))
     status = st.cpu().numpy()
     return {
         "metric": METRIC, "value": n * nsteps / (total_ms * 1e-3), "unit": "cell-updates/s", "n_gpus": 1,
@@ -321,6 +333,7 @@ def run_layer(args, w):
                        "first": float(lat[0]), "last": float(lat[-1])},
         "accuracy_vs_cpu_reference": {"columns": cols.tolist(), "cells": int(len(idx)), "max_abs_dY": dY,
                                       "max_rel_dT": relT},
+        "accuracy_vs_tight_integration": tg,
         "roofline": {"bound": "fp64", "achieved": flops / (total_ms * 1e-3) / 1e12, "peak": peak,
                      "unit": "TFLOP/s", "frac": flops / (total_ms * 1e-3) / 1e12 / peak, "traffic": None},
         "cpu_baseline": {"value": len(idx) * nsteps / cpu_secs, "unit": "cell-updates/s",
