@@ -21,7 +21,7 @@ _c = ctypes.c_char_p
 _v = ctypes.c_void_p
 _ull = ctypes.POINTER(ctypes.c_ulonglong)
 
-# name: (restype, argtypes) for every entry point of include/gdtk_chem.h
+# name: (restype, argtypes) for every entry point of include/gdtk_chem.h and include/gdtk_surrogate.h
 SIGNATURES = {
     "cwrap_gas_init": (ctypes.c_int, []),
     "gas_model_new": (ctypes.c_int, [_c]),
@@ -80,6 +80,30 @@ SIGNATURES = {
     "chem_reactor_fast_source": (ctypes.c_int, [ctypes.c_int, _c, ctypes.c_int]),
     "chem_reactor_jit_log": (ctypes.c_int, [ctypes.c_int, _c, ctypes.c_int]),
     "gdtk_measure_fp64_peak": (ctypes.c_int, [_d]),
+    # include/gdtk_surrogate.h
+    "chem_surrogate_new": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_ulonglong]),
+    "chem_surrogate_free": (ctypes.c_int, [ctypes.c_int]),
+    "chem_surrogate_dims": (ctypes.c_int, [ctypes.c_int, _i]),
+    "chem_surrogate_get_params": (ctypes.c_int, [ctypes.c_int, _v]),
+    "chem_surrogate_set_params": (ctypes.c_int, [ctypes.c_int, _v]),
+    "chem_surrogate_get_normalisation": (ctypes.c_int, [ctypes.c_int, _v, _v, _v, _v, _v, _v]),
+    "chem_surrogate_set_normalisation": (ctypes.c_int, [ctypes.c_int, _v, _v, _v, _v, _v, _v]),
+    "chem_surrogate_fit_normalisation": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _v, _v, _v, _v]),
+    "chem_surrogate_set_loss_weights": (ctypes.c_int, [ctypes.c_int, _v]),
+    "chem_surrogate_make_samples": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _v, _v, _v, ctypes.c_double, _v, _v,
+                                                   _v, _v, _v, _v, _v]),
+    "chem_surrogate_train_step": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _v, _v, _v, ctypes.c_float,
+                                                 ctypes.c_float, _v, _v]),
+    "chem_surrogate_gradients": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _v, _v, _v, _v, _v, _v]),
+    "chem_surrogate_predict": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _v, _v, _v]),
+    "chem_surrogate_set_gate": (ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                               ctypes.c_double]),
+    "chem_surrogate_update_cells": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _v, _v, _v, _v, _v, _v, _v,
+                                                   ctypes.c_double, ctypes.c_double, ctypes.c_int, _v, _v, _v,
+                                                   ctypes.c_int, _v]),
+    "gdtk_mlp_gemm": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _v, ctypes.c_int, ctypes.c_int, _v,
+                                     ctypes.c_int, ctypes.c_int, _v, ctypes.c_int, _v, _v, _v, ctypes.c_int,
+                                     ctypes.c_int, _v]),
 }
 
 

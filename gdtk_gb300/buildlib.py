@@ -21,12 +21,15 @@ SOURCES = [
     ("codegen.cpp", []),
     ("fp64_probe.cu", []),
     ("noalloc.cu", []),
+    ("mlp_kernels.cu", []),
+    ("surrogate_kernels.cu", []),
+    ("surrogate.cpp", []),
     ("chem_api.cpp", []),
     ("mechanism.cpp", []),
     ("lua_table.cpp", []),
 ]
 HEADERS = ["chem_types.h", "chem_launch.h", "cea_thermo.h", "lua_table.h", "mechanism.h", "codegen.h", "fast_exp.h",
-           "chem_fast.cuh"]
+           "chem_fast.cuh", "mix_thermo.cuh", "api_internal.h", "mlp_launch.h", "surrogate_launch.h"]
 # sources compiled at run time by NVRTC, embedded in the library as string literals
 EMBEDDED = [("kFastCuhSource", "chem_fast.cuh"), ("kFastExpSource", "fast_exp.h")]
 
@@ -61,7 +64,7 @@ def _compile(src, extra):
     obj = os.path.join(OUT_DIR, os.path.basename(src) + ".o")
     srcpath = src if os.path.isabs(src) else os.path.join(CSRC, src)
     deps = [srcpath] + [os.path.join(CSRC, h) for h in HEADERS] + \
-           [os.path.join(HERE, "..", "include", "gdtk_chem.h"), __file__]
+           [os.path.join(HERE, "..", "include", h) for h in ("gdtk_chem.h", "gdtk_surrogate.h")] + [__file__]
     if not _newer(obj, deps):
         return obj
     cmd = [NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2",

@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "../../include/gdtk_chem.h"
+#include "api_internal.h"
 #include "chem_launch.h"
 #include "chem_types.h"
 #include "codegen.h"
@@ -303,6 +304,24 @@ int launch_update(ReactorObj& r, int ncell, const double* rho, const double* u, 
 }  // namespace
 
 void report_error(const std::string& msg) { report(msg); }
+
+ReactorInternals reactor_internals(int cr_i) {
+    auto& r = reactor(cr_i);
+    require_cuda();
+    ReactorInternals v;
+    v.nsp = r.dev.host.nsp;
+    v.mech_i = r.dev.I;
+    v.mech_d = r.dev.D;
+    v.gm = &model(r.gm).gm;
+    v.sm_count = cuda().sm_count;
+    return v;
+}
+
+void reactor_update(int cr_i, int ncell, const double* rho, const double* u, double* T, double* p, double* massf,
+                    double* dt_chem, int* status, double t_interval, double T_frozen, int flags, cudaStream_t s) {
+    launch_update(reactor(cr_i), ncell, rho, u, T, p, massf, dt_chem, status, t_interval, T_frozen, flags, s, nullptr,
+                  nullptr);
+}
 
 // The fast-kernel update with caller-provided scratch (the allocation-free entry point of
 // noalloc.cu).  Allocates nothing: the reactor's mechanism kernel must already be loaded (the

@@ -26,6 +26,7 @@
 #include "chem_types.h"
 #include "chem_launch.h"
 #include "cea_thermo.h"
+#include "mix_thermo.cuh"
 
 namespace gdtk {
 namespace {
@@ -39,14 +40,6 @@ constexpr double DT_REDUCTION_FACTOR = 10.0;
 constexpr double H_MIN = 1.0e-15;
 constexpr double ALLOWABLE_MASSF_ERROR = 1.0e-3;
 constexpr double ZERO_EPS = 1.0e-50;
-
-// Per-thread vector in shared memory: element k of this thread lives at b[k * s].
-struct Vec {
-    double* b;
-    int s;
-    __device__ __forceinline__ double& operator[](int k) const { return b[k * s]; }
-    __device__ __forceinline__ Vec operator+(int k) const { return Vec{b + k * s, s}; }
-};
 
 // D's pow(double, int) (std.math, binary exponentiation), in double.
 __device__ __forceinline__ double ipow(double x, int n) {
@@ -64,44 +57,6 @@ __device__ __forceinline__ double ipow(double x, int n) {
     double p = 1.0, v = x;
     while (true) { if (m & 1u) p *= v; m >>= 1; if (!m) break; v *= v; }
     return p;
-}
-
-// therm_perf_gas_mix.d:406-413
-__device__ double internal_energy(const MechView& m, Vec mf, double T, double logT, int& err) {
-    double u = 0.0;
-    for (int i = 0; i < m.nsp; ++i) u += mf[i] * (cea_h(m, i, T, logT, err) - m.sp(i)[SP_R] * T);
-    return u;
-}
-
-// therm_perf_gas_mix.d:416-423
-__device__ double cv_mix(const MechView& m, Vec mf, double T, int& err) {
-    double c = 0.0;
-    for (int i = 0; i < m.nsp; ++i) c += mf[i] * (cea_Cp(m, i, T, err) - m.sp(i)[SP_R]);
-    return c;
-}
-
-__device__ double gas_constant(const MechView& m, Vec mf) {   // mass_average(Q, mR), gas_model.d:410-418
-    double r = 0.0;
-    for (int i = 0; i < m.nsp; ++i) r += mf[i] * m.sp(i)[SP_R];
-    return r;
-}
-
-// therm_perf_gas_mix.d:426-468.  Returns T; sets err on failure.  *iters counts Newton iterations.
-__device__ double T_from_u(const MechView& m, Vec mf, double u_tgt, double T_guess, int& err, int& iters) {
-    const double TOL = 1e-10;
-    double T = T_guess;
-    double f = internal_energy(m, mf, T, log(T), err) - u_tgt;
-    double dT = 0.0;
-    for (int iter = 0; iter < 10; ++iter) {
-        ++iters;
-        double cv = cv_mix(m, mf, T, err);
-        dT = -f / cv;
-        T += dT;
-        if (fabs(dT) / T < TOL) return T;
-        f = internal_energy(m, mf, T, log(T), err) - u_tgt;
-    }
-    if (fabs(dT) > 1e-3) err = CELL_NEWTON_FAIL;
-    return T;
 }
 
 // ---------------------------------------------------------------- kinetics

@@ -1,6 +1,8 @@
 // mechanism.cpp -- reading gas-model and mechanism files, and packing them for the device.
 #include "mechanism.h"
 
+#include <map>
+
 #include <algorithm>
 #include <cmath>
 #include <stdexcept>
@@ -66,6 +68,15 @@ GasModelHost load_gas_model(const std::string& path) {
         const LuaValue& e = db.get(name);
         if (e.is_nil()) throw std::runtime_error("no database entry for species " + name);
         gm.M.push_back(e.get("M").number());
+        std::map<std::string, int> comp;   // atomicConstituents = { H=2, O=1 } (prep-gas species record)
+        const LuaValue& ac = e.get("atomicConstituents");
+        if (ac.kind == LuaValue::TABLE)
+            for (auto& kv : *ac.tab)
+                if (kv.second.kind == LuaValue::NUMBER) comp[kv.first] = (int)kv.second.number();
+        for (auto& kv : comp)
+            if (std::find(gm.elements.begin(), gm.elements.end(), kv.first) == gm.elements.end())
+                gm.elements.push_back(kv.first);
+        gm.composition.push_back(comp);
         const LuaValue& th = e.get("thermoCoeffs");
         CeaCurveHost c;
         c.nseg = (int)th.get("nsegments").number();

@@ -1,6 +1,7 @@
 // mechanism.h -- host-side gas model and reaction mechanism, read from prep-gas / prep-chem files
 // and packed into the device layout of chem_types.h.
 #pragma once
+#include <map>
 #include <string>
 #include <vector>
 
@@ -20,6 +21,8 @@ struct GasModelHost {
     std::vector<std::string> names;
     std::vector<double> M;
     std::vector<CeaCurveHost> curves;
+    std::vector<std::string> elements;                    // in order of first appearance
+    std::vector<std::map<std::string, int>> composition;  // per species: element -> atoms
     int n_species() const { return (int)names.size(); }
 };
 

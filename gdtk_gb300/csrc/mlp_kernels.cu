@@ -1,0 +1,335 @@
+// mlp_kernels.cu -- BF16 tensor-core kernels of the chemistry surrogate, a multilayer perceptron
+// that predicts a cell's mass-fraction and temperature increments over an update interval.
+// There is no counterpart in the reference; the network, its training and its use are this
+// engine's own.
+//
+//   gemm:  D = alpha * op(A) * op(B) (+ bias) (+ beta * D), BF16 operands, FP32 accumulation,
+//          mma.sync.m16n8k16 on 64x64x32 block tiles staged through shared memory with 16-byte
+//          loads; epilogues: GELU (keeping the pre-activation), GELU backward; split-K with a
+//          fixed-order reduction for the weight gradients (K = batch).
+//   column sums (bias gradients), weighted squared-error gradient, AdamW, row gather, casts.
+//
+// The network's GEMMs are small (K, N <= 256): a training step over 8192 samples is about
+// 10 GFLOP, and inference over a million cells about 0.4 TFLOP, far below the FP64 cost of
+// the integrations it replaces.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "mlp_launch.h"
+
+namespace gdtk {
+namespace {
+
+constexpr int BM = 64, BN = 64, BK = 32;
+constexpr int LDS = BK + 8;   // smem row stride in bf16 (80 bytes: conflict-free fragment loads)
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// GELU, tanh form: 0.5 x (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3))), and its derivative.
+__device__ __forceinline__ float gelu_f(float x) {
+    const float c = 0.7978845608028654f;
+    return 0.5f * x * (1.0f + tanhf(c * (x + 0.044715f * x * x * x)));
+}
+__device__ __forceinline__ float gelu_grad(float x) {
+    const float c = 0.7978845608028654f;
+    const float x2 = x * x;
+    const float t = tanhf(c * (x + 0.044715f * x2 * x));
+    return 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * c * (1.0f + 3.0f * 0.044715f * x2);
+}
+
+// Stage a 64 x 32 tile of op(X) into S[64][LDS] (rows = the M or N index, columns = k).
+// row_major: X[r][k] at X[r * ld + k] (16-byte chunks along k); else X[k][r] at X[k * ld + r]
+// (chunks along r, transposed into shared memory).  Out-of-range rows and k read as zero.
+__device__ __forceinline__ void stage_tile(__nv_bfloat16 (*S)[LDS], const __nv_bfloat16* X, int ld, bool row_major,
+                                           int r0, int rows, int k0, int kend, int tid) {
+    const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
+    if (row_major) {
+#pragma unroll
+        for (int it = 0; it < 2; ++it) {
+            const int idx = tid + it * 128;     // 256 chunks: 64 rows x 4 chunks of 8
+            const int rr = idx >> 2, kc = (idx & 3) * 8;
+            const int r = r0 + rr, k = k0 + kc;
+            uint4 v = zero;
+            if (r < rows && k < kend) v = *reinterpret_cast<const uint4*>(X + (size_t)r * ld + k);
+            *reinterpret_cast<uint4*>(&S[rr][kc]) = v;
+        }
+    } else {
+#pragma unroll
+        for (int it = 0; it < 2; ++it) {
+            const int idx = tid + it * 128;     // 256 chunks: 32 k-rows x 8 chunks of 8
+            const int kk = idx >> 3, rc = (idx & 7) * 8;
+            const int k = k0 + kk, r = r0 + rc;
+            uint4 v = zero;
+            if (k < kend && r < rows) v = *reinterpret_cast<const uint4*>(X + (size_t)k * ld + r);
+            const __nv_bfloat16* e = reinterpret_cast<const __nv_bfloat16*>(&v);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) S[rc + j][kk] = e[j];
+        }
+    }
+}
+
+// 128 threads = 4 warps in 2 x 2; each warp computes a 32 x 32 sub-tile (2 m16 x 4 n8 mma tiles).
+__global__ void __launch_bounds__(128) gemm_bf16_kernel(const GemmArgs g) {
+    __shared__ __align__(16) __nv_bfloat16 As[BM][LDS];
+    __shared__ __align__(16) __nv_bfloat16 Bs[BN][LDS];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
+    const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+    const int gid = lane >> 2, tig = lane & 3;
+    // this block's K range (split-K over blockIdx.z, in BK multiples)
+    const int kper = ((g.K + g.splits - 1) / g.splits + BK - 1) / BK * BK;
+    const int kbeg = blockIdx.z * kper;
+    const int kend = min(g.K, kbeg + kper);
+    float acc[2][4][4];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int r = 0; r < 4; ++r) acc[i][j][r] = 0.f;
+
+    for (int k0 = kbeg; k0 < kend; k0 += BK) {
+        stage_tile(As, g.A, g.lda, !g.trans_a, m0, g.M, k0, kend, tid);
+        stage_tile(Bs, g.B, g.ldb, g.trans_b != 0, n0, g.N, k0, kend, tid);
+        __syncthreads();
+#pragma unroll
+        for (int ks = 0; ks < BK; ks += 16) {
+            uint32_t a[2][4], b[4][2];
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                const int r = wm + i * 16 + gid;
+                a[i][0] = *reinterpret_cast<const uint32_t*>(&As[r][ks + 2 * tig]);
+                a[i][1] = *reinterpret_cast<const uint32_t*>(&As[r + 8][ks + 2 * tig]);
+                a[i][2] = *reinterpret_cast<const uint32_t*>(&As[r][ks + 2 * tig + 8]);
+                a[i][3] = *reinterpret_cast<const uint32_t*>(&As[r + 8][ks + 2 * tig + 8]);
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int c = wn + j * 8 + gid;
+                b[j][0] = *reinterpret_cast<const uint32_t*>(&Bs[c][ks + 2 * tig]);
+                b[j][1] = *reinterpret_cast<const uint32_t*>(&Bs[c][ks + 2 * tig + 8]);
+            }
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) mma_bf16(acc[i][j], a[i], b[j]);
+        }
+        __syncthreads();
+    }
+
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const int m = m0 + wm + i * 16 + gid + (r >= 2 ? 8 : 0);
+                const int n = n0 + wn + j * 8 + 2 * tig + (r & 1);
+                if (m >= g.M || n >= g.N) continue;
+                if (g.splits > 1) {   // raw partial; the reduction applies alpha and beta
+                    g.work[((size_t)blockIdx.z * g.M + m) * g.N + n] = acc[i][j][r];
+                    continue;
+                }
+                const size_t o = (size_t)m * g.ldd + n;
+                float v = g.alpha * acc[i][j][r];
+                if (g.bias) v += g.bias[n];
+                if (g.beta != 0.f) v += g.beta * g.D[o];
+                if (g.act == ACT_GELU) {
+                    if (g.pre) g.pre[o] = v;
+                    v = gelu_f(v);
+                } else if (g.act == ACT_GELU_BWD) {
+                    v *= gelu_grad(g.pre_in[o]);
+                }
+                if (g.D) g.D[o] = v;
+                if (g.Dh) g.Dh[o] = __float2bfloat16(v);
+            }
+}
+
+// D[m][n] = alpha * sum_z work[z][m][n] (+ beta * D), z ascending.
+__global__ void splitk_reduce_kernel(int M, int N, int splits, const float* work, float alpha, float beta, float* D,
+                                     int ldd) {
+    const size_t MN = (size_t)M * N;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < MN; i += (size_t)gridDim.x * blockDim.x) {
+        float s = 0.f;
+        for (int z = 0; z < splits; ++z) s += work[z * MN + i];
+        const size_t o = (i / N) * ldd + i % N;
+        float v = alpha * s;
+        if (beta != 0.f) v += beta * D[o];
+        D[o] = v;
+    }
+}
+
+// Column sums of x[M][N]: block b sums rows [b*CH, (b+1)*CH) into partial[b][n]; then a single
+// pass adds the partials in ascending b (fixed order).
+constexpr int COLSUM_ROWS = 256;
+
+__global__ void column_partial_kernel(int M, int N, const float* x, float* partial) {
+    const int r0 = blockIdx.x * COLSUM_ROWS, r1 = min(M, r0 + COLSUM_ROWS);
+    for (int n = threadIdx.x; n < N; n += blockDim.x) {
+        float s = 0.f;
+        for (int r = r0; r < r1; ++r) s += x[(size_t)r * N + n];
+        partial[(size_t)blockIdx.x * N + n] = s;
+    }
+}
+
+__global__ void column_final_kernel(int chunks, int N, const float* partial, float* out) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= N) return;
+    float s = 0.f;
+    for (int b = 0; b < chunks; ++b) s += partial[(size_t)b * N + n];
+    out[n] = s;
+}
+
+// Weighted squared error over M rows: loss_sum += sum_n w[n] (pred - y)^2 and
+// grad = 2 w[n] (pred - y) / M (fp32 and bf16 copies).
+__global__ void mse_grad_kernel(int M, int N, const float* pred, const float* y, const float* w, float* grad,
+                                __nv_bfloat16* gradh, float* loss_sum) {
+    float local = 0.f;
+    const size_t total = (size_t)M * N;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const int n = (int)(i % N);
+        const float wt = w ? w[n] : 1.f;
+        const float d = pred[i] - y[i];
+        const float gv = 2.f * wt * d / (float)M;
+        if (grad) grad[i] = gv;
+        if (gradh) gradh[i] = __float2bfloat16(gv);
+        local += wt * d * d;
+    }
+    if (loss_sum) {
+        for (int off = 16; off > 0; off >>= 1) local += __shfl_down_sync(0xffffffffu, local, off);
+        if ((threadIdx.x & 31) == 0) atomicAdd(loss_sum, local);
+    }
+}
+
+// AdamW (decoupled weight decay) on fp32 master weights; refreshes the bf16 copy.
+__global__ void adamw_kernel(int count, float* w, const float* g, float* m, float* v, __nv_bfloat16* wh, float lr,
+                             float beta1, float beta2, float eps, float wd, float bc1, float bc2) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const float gi = g[i];
+        const float mi = beta1 * m[i] + (1.f - beta1) * gi;
+        const float vi = beta2 * v[i] + (1.f - beta2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        float wi = w[i] * (1.f - lr * wd);
+        wi -= lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+        w[i] = wi;
+        if (wh) wh[i] = __float2bfloat16(wi);
+    }
+}
+
+__global__ void cast_bf16_kernel(int count, const float* x, __nv_bfloat16* y) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x)
+        y[i] = __float2bfloat16(x[i]);
+}
+
+// Row idx[r] of X and Y, standardised: Xh[r][c] = bf16((X - xs) / xd), Yg[r][c] = (Y - ys) / yd.
+__global__ void gather_rows_kernel(int n, const int* idx, const float* X, int ldx, const float* xs, const float* xd,
+                                   __nv_bfloat16* Xh, const float* Y, int ldy, const float* ys, const float* yd,
+                                   float* Yg) {
+    const int w = ldx + ldy;
+    const size_t total = (size_t)n * w;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const int r = (int)(i / w), c = (int)(i % w);
+        const size_t src = idx ? (size_t)idx[r] : (size_t)r;
+        if (c < ldx) {
+            Xh[(size_t)r * ldx + c] = __float2bfloat16((X[src * ldx + c] - xs[c]) / xd[c]);
+        } else if (Y) {
+            const int k = c - ldx;
+            Yg[(size_t)r * ldy + k] = (Y[src * ldy + k] - ys[k]) / yd[k];
+        }
+    }
+}
+
+__global__ void affine_columns_kernel(int n, int w, const float* shift, const float* scale, float* x) {
+    const size_t total = (size_t)n * w;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const int k = (int)(i % w);
+        x[i] = x[i] * scale[k] + shift[k];
+    }
+}
+
+int grid_for(size_t count) {
+    size_t g = (count + 255) / 256;
+    return (int)(g > 8192 ? 8192 : (g < 1 ? 1 : g));
+}
+
+bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+
+}  // namespace
+
+cudaError_t launch_gemm_bf16(const GemmArgs& g, cudaStream_t s) {
+    if (g.M <= 0 || g.N <= 0 || g.K <= 0) return cudaSuccess;
+    // 16-byte chunks along the contiguous dimension of each operand
+    const int a_inner = g.trans_a ? g.M : g.K, b_inner = g.trans_b ? g.K : g.N;
+    if (g.K % 8 || a_inner % 8 || b_inner % 8 || g.lda % 8 || g.ldb % 8 || !aligned16(g.A) || !aligned16(g.B))
+        return cudaErrorInvalidValue;
+    if (g.splits < 1 || (g.splits > 1 && (!g.work || g.bias || g.act != ACT_NONE || !g.D)))
+        return cudaErrorInvalidValue;
+    if ((g.act == ACT_GELU_BWD && !g.pre_in) || (g.beta != 0.f && !g.D))
+        return cudaErrorInvalidValue;
+    dim3 grid((g.N + BN - 1) / BN, (g.M + BM - 1) / BM, g.splits);
+    if (grid.y > 65535u || grid.z > 65535u) return cudaErrorInvalidConfiguration;
+    gemm_bf16_kernel<<<grid, 128, 0, s>>>(g);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || g.splits == 1) return e;
+    splitk_reduce_kernel<<<grid_for((size_t)g.M * g.N), 256, 0, s>>>(g.M, g.N, g.splits, g.work, g.alpha, g.beta, g.D,
+                                                                      g.ldd);
+    return cudaGetLastError();
+}
+
+int column_sum_partials(int M) { return (M + COLSUM_ROWS - 1) / COLSUM_ROWS; }
+
+cudaError_t launch_column_sum(int M, int N, const float* x, float* partial, float* out, cudaStream_t s) {
+    if (M <= 0 || N <= 0) return cudaSuccess;
+    const int chunks = column_sum_partials(M);
+    column_partial_kernel<<<chunks, N < 256 ? ((N + 31) / 32) * 32 : 256, 0, s>>>(M, N, x, partial);
+    column_final_kernel<<<(N + 127) / 128, 128, 0, s>>>(chunks, N, partial, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mse_grad(int M, int N, const float* pred, const float* y, const float* w, float* grad,
+                            __nv_bfloat16* gradh, float* loss_sum, cudaStream_t s) {
+    if (M <= 0 || N <= 0) return cudaSuccess;
+    mse_grad_kernel<<<grid_for((size_t)M * N), 256, 0, s>>>(M, N, pred, y, w, grad, gradh, loss_sum);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adamw(int count, float* w, const float* g, float* m, float* v, __nv_bfloat16* wh, float lr,
+                         float beta1, float beta2, float eps, float wd, int step, cudaStream_t s) {
+    if (count <= 0) return cudaSuccess;
+    const float bc1 = 1.f - powf(beta1, (float)step), bc2 = 1.f - powf(beta2, (float)step);
+    adamw_kernel<<<grid_for((size_t)count), 256, 0, s>>>(count, w, g, m, v, wh, lr, beta1, beta2, eps, wd, bc1, bc2);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cast_bf16(int count, const float* x, __nv_bfloat16* y, cudaStream_t s) {
+    if (count <= 0) return cudaSuccess;
+    cast_bf16_kernel<<<grid_for((size_t)count), 256, 0, s>>>(count, x, y);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather_rows(int n, const int* idx, const float* X, int ldx, const float* xs, const float* xd,
+                               __nv_bfloat16* Xh, const float* Y, int ldy, const float* ys, const float* yd, float* Yg,
+                               cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    const int w = ldx + (Y ? ldy : 0);
+    gather_rows_kernel<<<grid_for((size_t)n * w), 256, 0, s>>>(n, idx, X, ldx, xs, xd, Xh, Y, Y ? ldy : 0, ys, yd,
+                                                               Yg);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_affine_columns(int n, int w, const float* shift, const float* scale, float* x, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    affine_columns_kernel<<<grid_for((size_t)n * w), 256, 0, s>>>(n, w, shift, scale, x);
+    return cudaGetLastError();
+}
+
+}  // namespace gdtk

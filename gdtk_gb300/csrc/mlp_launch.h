@@ -1,0 +1,55 @@
+// mlp_launch.h -- host launchers of the surrogate network's BF16 tensor-core kernels (mlp_kernels.cu).
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+namespace gdtk {
+
+enum { ACT_NONE = 0, ACT_GELU = 1, ACT_GELU_BWD = 2 };
+
+// D[M][N] = alpha * op(A)[M][K] * op(B)[K][N] (+ bias[n]) (+ beta * D), epilogue act:
+//   ACT_GELU:     pre <- value (when pre is set), value <- gelu(value)
+//   ACT_GELU_BWD: value <- value * gelu'(pre_in)
+// op(A) = A[M][lda] row-major (trans_a = 0) or A stored as [K][lda] (trans_a = 1); likewise
+// op(B) = B[K][ldb] (trans_b = 0) or B stored as [N][ldb] (trans_b = 1).
+// Requirements (checked by the launcher): K % 8 == 0, the feature dimension of every operand a
+// multiple of 8 (16-byte vector loads), 16-byte aligned base pointers and leading dimensions.
+// splits > 1 partitions K over blockIdx.z; partial tiles go to work[splits][M][N] and a second
+// kernel sums them in a fixed order (deterministic), applying alpha/beta (no bias or act).
+struct GemmArgs {
+    int M = 0, N = 0, K = 0;
+    const __nv_bfloat16* A = nullptr;
+    int lda = 0, trans_a = 0;
+    const __nv_bfloat16* B = nullptr;
+    int ldb = 0, trans_b = 0;
+    float alpha = 1.f, beta = 0.f;
+    const float* bias = nullptr;
+    int act = ACT_NONE;
+    const float* pre_in = nullptr;   // ACT_GELU_BWD
+    float* pre = nullptr;            // ACT_GELU: pre-activation out
+    float* D = nullptr;              // fp32 out (may be null)
+    __nv_bfloat16* Dh = nullptr;     // bf16 out (may be null)
+    int ldd = 0;
+    int splits = 1;
+    float* work = nullptr;
+};
+
+cudaError_t launch_gemm_bf16(const GemmArgs& g, cudaStream_t s);
+cudaError_t launch_column_sum(int M, int N, const float* x, float* partial, float* out, cudaStream_t s);
+cudaError_t launch_mse_grad(int M, int N, const float* pred, const float* y, const float* w, float* grad,
+                            __nv_bfloat16* gradh, float* loss_sum, cudaStream_t s);
+cudaError_t launch_adamw(int count, float* w, const float* g, float* m, float* v, __nv_bfloat16* wh, float lr,
+                         float beta1, float beta2, float eps, float wd, int step, cudaStream_t s);
+cudaError_t launch_cast_bf16(int count, const float* x, __nv_bfloat16* y, cudaStream_t s);
+// rows idx[i] (or i when idx is null) of X (fp32 [.][ldx]) -> Xh[i] = bf16((X - xs) / xd), and
+// of Y (may be null) -> Yg[i] = (Y - ys) / yd (fp32, width ldy)
+cudaError_t launch_gather_rows(int n, const int* idx, const float* X, int ldx, const float* xs, const float* xd,
+                               __nv_bfloat16* Xh, const float* Y, int ldy, const float* ys, const float* yd, float* Yg,
+                               cudaStream_t s);
+
+// x[i][k] = x[i][k] * scale[k] + shift[k] over n rows of width w
+cudaError_t launch_affine_columns(int n, int w, const float* shift, const float* scale, float* x, cudaStream_t s);
+
+int column_sum_partials(int M);   // row chunks used by launch_column_sum (partial holds chunks * N floats)
+
+}  // namespace gdtk

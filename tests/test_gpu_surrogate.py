@@ -1,0 +1,260 @@
+"""GPU tests of the chemistry surrogate (include/gdtk_surrogate.h): the BF16 tensor-core GEMM
+against an FP64 product of the same BF16 values, the training gradient against the CPU oracle
+(oracle/mlp.py), training on samples of the FP64 update, the FP64 gate against its CPU
+restatement (oracle/surrogate_gate.py), the fallback cells against the plain update, the
+held-out monitor, and what the trained network gains over the update without it."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import oracle
+from oracle import mlp
+from oracle import surrogate_gate as sgate
+from conftest import mech
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+@pytest.fixture(scope="module")
+def rc():
+    from gdtk_gb300.cells import ReactorCells
+    return ReactorCells(mech("j92-gas.lua"), mech("j92-chem.lua"))
+
+
+@pytest.fixture(scope="module")
+def samples(rc):
+    """262,144 samples of the FP64 update of seeded H2-air cells (dt log-uniform in [0.5, 2] us)."""
+    from gdtk_gb300.surrogate import ChemSurrogate, generate_samples
+    sg = ChemSurrogate(rc, width=256, depth=4, seed=1)
+    X, Y, valid, _ = generate_samples(rc, sg, 262144, seed=11)
+    rows = torch.nonzero(valid).flatten().to(torch.int32)
+    return X, Y, rows
+
+
+@pytest.fixture(scope="module")
+def trained(rc, samples):
+    from gdtk_gb300.surrogate import ChemSurrogate
+    X, Y, rows = samples
+    n = rows.shape[0]
+    g = torch.Generator(device="cuda")
+    g.manual_seed(0)
+    perm = rows[torch.randperm(n, generator=g, device="cuda")]
+    hold = perm[: n // 20].contiguous()
+    train = perm[n // 20:].contiguous()
+    sg = ChemSurrogate(rc, width=256, depth=4, seed=2)
+    sg.fit_normalisation(X, Y, train)
+    before = sg.heldout_error(X, Y, hold)
+    hist = sg.train(X, Y, train, epochs=12, batch=4096, lr=2e-3)
+    after = sg.heldout_error(X, Y, hold)
+    return sg, hist, before, after
+
+
+@pytest.mark.parametrize("ta,tb", [(0, 1), (0, 0), (1, 0)])
+@pytest.mark.parametrize("M,N,K,act,bias,splits", [(200, 256, 16, 1, True, 1), (1000, 256, 256, 1, True, 1),
+                                                   (256, 16, 4104, 0, False, 4), (512, 24, 272, 0, True, 1)])
+def test_gemm_matches_fp64_product_of_bf16_values(ta, tb, M, N, K, act, bias, splits):
+    from gdtk_gb300 import lib, check
+    g = torch.Generator(device="cuda")
+    g.manual_seed(M * 7 + N * 3 + K)
+    A = torch.randn((M, K), generator=g, device="cuda").to(torch.bfloat16)
+    B = torch.randn((K, N), generator=g, device="cuda").to(torch.bfloat16)
+    b = torch.randn(N, generator=g, device="cuda") if bias else None
+    As = A.t().contiguous() if ta else A.contiguous()
+    Bs = B.t().contiguous() if tb else B.contiguous()
+    lda = M if ta else K
+    ldb = K if tb else N
+    D = torch.empty((M, N), device="cuda")
+    Dh = torch.empty((M, N), device="cuda", dtype=torch.bfloat16)
+    pre = torch.empty((M, N), device="cuda") if act else None
+    check(lib().gdtk_mlp_gemm(M, N, K, _ptr(As), lda, ta, _ptr(Bs), ldb, tb, _ptr(b), act, _ptr(pre), _ptr(D),
+                              _ptr(Dh), N, splits, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)),
+          "gdtk_mlp_gemm")
+    torch.cuda.synchronize()
+    ref = A.double() @ B.double()
+    if bias:
+        ref = ref + b.double()
+    scale = (A.double().abs() @ B.double().abs()).clamp_min(1e-30)
+    if act:
+        assert ((pre.double() - ref).abs() / scale).max().item() < 1e-6
+        z = ref
+        ref = 0.5 * z * (1.0 + torch.tanh(0.7978845608028654 * (z + 0.044715 * z ** 3)))
+        err = ((D.double() - ref).abs() / (scale + 1.0)).max().item()
+        assert err < 2e-6
+    else:
+        assert ((D.double() - ref).abs() / scale).max().item() < 1e-6
+    assert ((Dh.double() - D.double()).abs() <= D.double().abs() * 2 ** -8 + 1e-30).all()
+
+
+def test_training_gradient_matches_cpu_oracle(rc, samples):
+    from gdtk_gb300.surrogate import ChemSurrogate
+    X, Y, rows = samples
+    sg = ChemSurrogate(rc, width=256, depth=4, seed=3)
+    sg.fit_normalisation(X, Y, rows)
+    batch = rows[:1024].contiguous()
+    grad, loss = sg.gradients(X, Y, batch)
+    grad = grad.cpu().numpy().astype(np.float64)
+    nrm = sg.get_normalisation()
+    xb = X[batch.long()].cpu().numpy()
+    yb = Y[batch.long()].cpu().numpy()
+    Xs = ((xb - nrm["x_shift"]) / nrm["x_scale"]).astype(np.float32)
+    Ys = ((yb - nrm["y_shift"]) / nrm["y_scale"]).astype(np.float32).astype(np.float64)
+    w = np.zeros(sg.nout_pad)
+    w[:sg.nout] = 1.0
+    layers = [(W.astype(np.float64), b.astype(np.float64)) for W, b in sg.unpack(sg.get_params())]
+    L_bf, g_bf = mlp.loss_and_grads(layers, Xs, Ys, w, bf=True)
+    L_64, g_64 = mlp.loss_and_grads(layers, Xs.astype(np.float64), Ys, w, bf=False)
+    assert loss / 1024 == pytest.approx(L_bf, rel=2e-3)
+    assert loss / 1024 == pytest.approx(L_64, rel=2e-2)
+    for (dW, db), (oW, ob), (fW, fb) in zip(sg.unpack(grad), g_bf, g_64):
+        for got, ref, ref64 in ((dW, oW, fW), (db, ob, fb)):
+            rel = np.linalg.norm(got - ref) / np.linalg.norm(ref)
+            assert rel < 1e-2, rel
+            rel64 = np.linalg.norm(got - ref64) / np.linalg.norm(ref64)
+            assert rel64 < 8e-2, rel64
+
+
+def test_training_reduces_heldout_error(trained):
+    sg, hist, before, after = trained
+    assert hist[-1] < 0.05 * hist[0]
+    assert np.median(after[0]) < 0.1 * np.median(before[0])
+    assert np.median(after[0]) < 1e-3
+    assert np.median(after[1]) < 1e-3
+
+
+def _fresh_cells(rc, n, seed):
+    from gdtk_gb300.workloads import h2air_cells
+    T, p, Y = h2air_cells(rc.species_names, rc.mol_masses, n, seed=seed)
+    d = dict(T=torch.tensor(T, device="cuda"), p=torch.tensor(p, device="cuda"),
+             massf=torch.tensor(np.ascontiguousarray(Y), device="cuda"))
+    d["rho"], d["u"] = rc.thermo_from_pT(d["p"], d["T"], d["massf"])
+    d["dt_chem"] = torch.full((n,), -1.0, dtype=torch.float64, device="cuda")
+    d["status"] = torch.zeros(n, dtype=torch.int32, device="cuda")
+    return d
+
+
+def _clone(d):
+    return {k: v.clone() for k, v in d.items()}
+
+
+def test_gate_matches_cpu_restatement(rc, trained):
+    sg, *_ = trained
+    sg.set_gate(elem_tol=1e-4, neg_tol=1e-5, T_tol=5e-3)
+    n = 4096
+    d = _fresh_cells(rc, n, seed=21)
+    d0 = _clone(d)
+    # the raw predictions the gate sees (features rounded as in training)
+    X, _, _ = sg.make_samples(d0["T"], d0["p"], d0["massf"], 1e-6, d0["T"], d0["massf"], None)
+    pred = sg.predict(X).double().cpu().numpy()
+    gate = torch.empty(n, dtype=torch.int32, device="cuda")
+    res = sg.update(d["rho"], d["u"], d["T"], d["p"], d["massf"], d["dt_chem"], 1e-6, status=d["status"], gate=gate)
+    codes = gate.cpu().numpy()
+    assert sum(res["gate"].values()) == n
+    orc = oracle.Oracle(mech("j92-gas.lua"))
+    els, E, EM = sgate.element_matrix(mech("j92-gas.lua"))
+    nrm = sg.get_normalisation()
+    c0 = {k: v.cpu().numpy() for k, v in d0.items()}
+    nsp = rc.nsp
+    ref, Y1, T1, p1 = sgate.gate(orc, E, EM, c0["rho"], c0["u"], c0["T"], c0["p"], c0["massf"].T,
+                                 pred[:, :nsp], pred[:, nsp], nrm["x_min"], nrm["x_max"], 1e-6, 0.0,
+                                 elem_tol=1e-4, neg_tol=1e-5, T_tol=5e-3)
+    agree = (codes == ref).mean()
+    assert agree > 0.995, (agree, np.bincount(codes, minlength=9), np.bincount(ref, minlength=9))
+    both = (codes == sgate.ACCEPTED) & (ref == sgate.ACCEPTED)
+    assert both.sum() > 0.2 * n
+    Yg = d["massf"].cpu().numpy().T
+    assert np.abs(Yg[both] - Y1[both]).max() < 1e-8
+    assert (np.abs(d["T"].cpu().numpy()[both] - T1[both]) / T1[both]).max() < 1e-7
+    # accepted cells conserve every element to rounding and hold no negative mass fraction
+    dE = (E @ (Yg[both] - c0["massf"].T[both]).T) * EM[:, None]
+    assert np.abs(dE).max() < 1e-12
+    assert Yg[both].min() >= 0.0
+
+
+def test_fallback_cells_equal_the_plain_update(rc, trained):
+    sg, *_ = trained
+    sg.set_gate(elem_tol=1e-5, neg_tol=1e-6, T_tol=1e-3)
+    n = 8192
+    d = _fresh_cells(rc, n, seed=22)
+    d["T"][:16] = 250.0                       # frozen cells
+    d0 = _clone(d)
+    gate = torch.empty(n, dtype=torch.int32, device="cuda")
+    res = sg.update(d["rho"], d["u"], d["T"], d["p"], d["massf"], d["dt_chem"], 1e-6, status=d["status"], gate=gate,
+                    T_frozen=300.0)
+    rc.update(d0["rho"], d0["u"], d0["T"], d0["p"], d0["massf"], d0["dt_chem"], 1e-6, status=d0["status"],
+              T_frozen=300.0)
+    codes = gate.cpu().numpy()
+    assert res["gate"]["frozen"] == 16 and (codes[:16] == sgate.FROZEN).all()
+    fb = (codes != sgate.ACCEPTED) & (codes != sgate.FROZEN) & (codes != sgate.BAD_INPUT)
+    assert fb.sum() == res["fallback"] > 0
+    fbt = torch.tensor(fb, device="cuda")
+    for k in ("T", "p", "dt_chem", "status"):
+        assert torch.equal(d[k][fbt], d0[k][fbt]), k
+    assert torch.equal(d["massf"][:, fbt], d0["massf"][:, fbt])
+    assert torch.equal(d["status"][:16], d0["status"][:16])      # frozen flagged as the plain update does
+    assert torch.equal(d["T"][:16], d0["T"][:16])
+
+
+def test_monitor_reports_the_error_against_the_fp64_update(rc, trained):
+    sg, *_ = trained
+    sg.set_gate(elem_tol=1e-4, neg_tol=1e-5, T_tol=5e-3)
+    n = 4096
+    d = _fresh_cells(rc, n, seed=23)
+    d0 = _clone(d)
+    gate = torch.empty(n, dtype=torch.int32, device="cuda")
+    res = sg.update(d["rho"], d["u"], d["T"], d["p"], d["massf"], d["dt_chem"], 1e-6, status=d["status"], gate=gate,
+                    monitor_stride=1)
+    rc.update(d0["rho"], d0["u"], d0["T"], d0["p"], d0["massf"], d0["dt_chem"], 1e-6, status=d0["status"])
+    acc = (gate == 0) & (d0["status"] == 0)
+    eY = (d["massf"][:, acc] - d0["massf"][:, acc]).abs().amax(dim=0)
+    eT = (d["T"][acc] - d0["T"][acc]).abs() / d0["T"][acc]
+    m = res["monitor"]
+    assert m["cells"] == int(acc.sum())
+    assert m["max_dY"] == pytest.approx(eY.max().item(), rel=1e-12)
+    assert m["max_rel_dT"] == pytest.approx(eT.max().item(), rel=1e-12)
+    assert m["mean_max_dY"] == pytest.approx(eY.mean().item(), rel=1e-9)
+
+
+def test_trained_network_gains_over_the_update_without_it(rc, trained):
+    """At one gate setting: the trained network takes over cells that carry a large share of
+    the FP64 work, within an error bound checked against the FP64 update, while the same network
+    untrained is rejected almost everywhere."""
+    from gdtk_gb300.surrogate import ChemSurrogate
+    sg, *_ = trained
+    n = 16384
+    base = _fresh_cells(rc, n, seed=24)
+    ref = _clone(base)
+    tot_plain = torch.zeros(6, dtype=torch.int64, device="cuda")
+    rc.update(ref["rho"], ref["u"], ref["T"], ref["p"], ref["massf"], ref["dt_chem"], 1e-6, status=ref["status"],
+              totals=tot_plain)
+    results = {}
+    for name, net in (("trained", sg), ("untrained", ChemSurrogate(rc, width=256, depth=4, seed=9))):
+        if name == "untrained":
+            net.load_state_dict(dict(sg.state_dict(), params=net.get_params()))
+        net.set_gate(elem_tol=2e-5, neg_tol=1e-6, T_tol=1e-3, max_dY=2e-3)
+        d = _clone(base)
+        gate = torch.empty(n, dtype=torch.int32, device="cuda")
+        net.update(d["rho"], d["u"], d["T"], d["p"], d["massf"], d["dt_chem"], 1e-6, status=d["status"], gate=gate)
+        acc = (gate == 0) & (ref["status"] == 0)
+        rej = (gate != 0)
+        # FP64 work left to the fallback: the plain update of the rejected cells alone
+        sub = {k: (v[:, rej] if k == "massf" else v[rej]).contiguous() for k, v in base.items()}
+        tot = torch.zeros(6, dtype=torch.int64, device="cuda")
+        rc.update(sub["rho"], sub["u"], sub["T"], sub["p"], sub["massf"], sub["dt_chem"], 1e-6, status=sub["status"],
+                  totals=tot)
+        err = (d["massf"][:, acc] - ref["massf"][:, acc]).abs().amax(dim=0)
+        errT = ((d["T"][acc] - ref["T"][acc]).abs() / ref["T"][acc])
+        results[name] = dict(accepted=float(acc.float().mean()), work=float(tot[1]) / float(tot_plain[1]),
+                             max_dY=float(err.max()) if acc.any() else 0.0,
+                             max_dT=float(errT.max()) if acc.any() else 0.0)
+    t, u = results["trained"], results["untrained"]
+    assert t["accepted"] > 0.3, results
+    assert t["work"] < 0.85, results               # FP64 right-hand sides left to the fallback
+    assert t["max_dY"] < 5e-3 and t["max_dT"] < 5e-3, results
+    assert u["accepted"] < 0.5 * t["accepted"], results
