@@ -44,6 +44,11 @@ WORKLOADS = {
     # thermochemical_increment contract (T_frozen = 300 K, dt_chem carried, retry, rhou update)
     "h2air-mixing-layer": dict(gas="j92-gas.lua", chem="j92-chem.lua", n=2048 * 1024, dt=5.0e-7, kind="layer",
                                seed=4, nx=2048, ny=1024, split_steps=100, T_frozen=300.0),
+    # learned surrogate: 4x256 GELU MLP trained on 16,777,216 samples of the FP64 update (cells of the
+    # h2air-1M distribution, dt log-uniform in [0.5, 2] us, 5% held out); inference + gate + FP64
+    # fallback on 4,194,304 fresh cells at dt = 1e-6 s, against the plain FP64 update of the same cells
+    "h2air-surrogate": dict(gas="j92-gas.lua", chem="j92-chem.lua", n=4194304, dt=1.0e-6, kind="surrogate",
+                            seed=3, train_samples=16777216, epochs=30, batch=8192),
 }
 
 
@@ -343,6 +348,162 @@ def run_layer(args, w):
     }
 
 
+def run_surrogate(args, w):
+    """Surrogate + FP64 fallback against the plain FP64 update on fresh cells (returns the JSON line)."""
+    import torch
+    import oracle
+    from gdtk_gb300.cells import ReactorCells, UPDATE_THERMO, RETRY
+    from gdtk_gb300.surrogate import ChemSurrogate, generate_samples
+    from gdtk_gb300.workloads import h2air_cells
+    rc = ReactorCells(os.path.join(MECH, w["gas"]), os.path.join(MECH, w["chem"]))
+    dev = torch.device("cuda", 0)
+    n = args.cells or w["n"]
+    n_train = w["train_samples"] if not args.cells else max(65536, 4 * args.cells)
+    sync = torch.cuda.synchronize
+    # ---- training samples from the FP64 update, 5% held out
+    sg = ChemSurrogate(rc, width=256, depth=4, seed=0)
+    t0 = time.perf_counter()
+    X, Yt, valid, t_gen = generate_samples(rc, sg, n_train, seed=7)
+    rows = torch.nonzero(valid).flatten().to(torch.int32)
+    g = torch.Generator(device=dev)
+    g.manual_seed(0)
+    perm = rows[torch.randperm(rows.shape[0], generator=g, device=dev)]
+    hold = perm[: rows.shape[0] // 20].contiguous()
+    train = perm[rows.shape[0] // 20:].contiguous()
+    sg.fit_normalisation(X, Yt, train)
+    sync()
+    t1 = time.perf_counter()
+    hist = sg.train(X, Yt, train, epochs=w["epochs"], batch=w["batch"], lr=2e-3)
+    sync()
+    t_train = time.perf_counter() - t1
+    eY, eT = sg.heldout_error(X, Yt, hold)
+    steps_per_epoch = train.shape[0] // w["batch"]
+    train_flop = 3 * 2 * sum(a * b for a, b in zip(sg.layer_dims()[:-1], sg.layer_dims()[1:])) * \
+        steps_per_epoch * w["batch"] * w["epochs"]
+    del X, Yt, valid, rows, perm, hold, train
+    torch.cuda.empty_cache()
+
+    # ---- fresh cells
+    T0, p0, Y0 = h2air_cells(rc.species_names, rc.mol_masses, n, seed=w["seed"] * 1000 + 17)
+    t64 = lambda a: torch.tensor(np.ascontiguousarray(a), dtype=torch.float64, device=dev)
+    sT, sp, sY = t64(T0), t64(p0), t64(Y0)
+    srho, su = rc.thermo_from_pT(sp, sT, sY)
+    sdt = torch.full((n,), -1.0, dtype=torch.float64, device=dev)
+    T, p, Y, dtc = sT.clone(), sp.clone(), sY.clone(), sdt.clone()
+    st = torch.zeros(n, dtype=torch.int32, device=dev)
+    flags = UPDATE_THERMO | RETRY
+
+    def restore():
+        T.copy_(sT); p.copy_(sp); Y.copy_(sY); dtc.copy_(sdt)
+        sync()
+
+    # plain FP64 update of the same cells (the baseline and the error reference)
+    peak = fp64_peak_reference()
+    totals = torch.zeros(6, dtype=torch.int64, device=dev)
+    plain_s = []
+    for k in range(1 + args.steps):
+        restore()
+        totals.zero_()
+        t1 = time.perf_counter()
+        rc.update(srho, su, T, p, Y, dtc, w["dt"], status=st, flags=flags, totals=totals)
+        sync()
+        if k:
+            plain_s.append(time.perf_counter() - t1)
+    plain_T, plain_Y, plain_st = T.clone(), Y.clone(), st.clone()
+    plain_flops = rc.algorithmic_flops(totals.cpu().numpy().astype(np.float64))
+    plain_time = float(np.mean(plain_s))
+
+    # surrogate + fallback at a sweep of gate settings; the first is the default (reported value)
+    settings = [("strict", dict(elem_tol=1e-4, neg_tol=1e-5, T_tol=1e-3, max_dY=5e-4)),
+                ("max_dY 2e-3", dict(elem_tol=1e-4, neg_tol=1e-5, T_tol=1e-3, max_dY=2e-3)),
+                ("no magnitude cap", dict(elem_tol=1e-4, neg_tol=1e-5, T_tol=1e-3, max_dY=0.0))]
+    gate = torch.empty(n, dtype=torch.int32, device=dev)
+    sweep = []
+    clocks = ClockSampler(int(os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] or 0))
+    for si, (name, gs) in enumerate(settings):
+        sg.set_gate(**gs)
+        reps = (1 + args.steps) if si == 0 else 1
+        times = []
+        if si == 0:
+            clocks.start()
+        for k in range(reps):
+            restore()
+            t1 = time.perf_counter()
+            res = sg.update(srho, su, T, p, Y, dtc, w["dt"], status=st, flags=flags, gate=gate,
+                            monitor_stride=1024)
+            sync()
+            times.append(time.perf_counter() - t1)
+        if si == 0:
+            clk = clocks.stop()
+            first_T, first_Y, first_gate = T.clone(), Y.clone(), gate.clone()
+        secs = float(np.mean(times[1:] if reps > 1 else times))
+        acc = (gate == 0) & (plain_st == 0)
+        e = (Y[:, acc] - plain_Y[:, acc]).abs().amax(dim=0).double()
+        et = ((T[acc] - plain_T[acc]).abs() / plain_T[acc]).double()
+        q = lambda v, x: float(torch.quantile(v[:min(v.shape[0], 1 << 24)], x)) if v.numel() else 0.0
+        sweep.append({"gate": name, **gs, "seconds": secs, "cell_updates_per_s": n / secs,
+                      "speedup_vs_plain": plain_time / secs, "accepted_fraction": float(acc.float().mean()),
+                      "rejected_fraction": res["fallback"] / n, "gate_counts": res["gate"],
+                      "fallback_failed": res["fallback_failed"],
+                      "error_vs_fp64": {"cells": int(acc.sum()), "max_dY": float(e.max()) if e.numel() else 0.0,
+                                        "p999_dY": q(e, 0.999), "p99_dY": q(e, 0.99), "median_dY": q(e, 0.5),
+                                        "max_rel_dT": float(et.max()) if et.numel() else 0.0,
+                                        "p999_rel_dT": q(et, 0.999)},
+                      "monitor": res["monitor"]})
+    # surrogate results of the default gate against the CPU reference algorithm on a strided sample
+    acc0 = ((first_gate == 0) & (plain_st == 0)).cpu().numpy()
+    idx = np.flatnonzero(acc0)
+    idx = idx[np.linspace(0, len(idx) - 1, min(len(idx), 2000)).astype(np.int64)] if len(idx) else idx
+    orc = oracle.Oracle(os.path.join(MECH, w["gas"]), os.path.join(MECH, w["chem"]))
+    cpu_err = None
+    if len(idx):
+        o = orc.chem_update(srho.cpu().numpy()[idx], su.cpu().numpy()[idx], T0[idx], p0[idx], Y0[:, idx].T,
+                            np.full(len(idx), -1.0), w["dt"])
+        okc = o["status"] == 0
+        sY_ = first_Y.cpu().numpy()[:, idx].T
+        sT_ = first_T.cpu().numpy()[idx]
+        pY_ = plain_Y.cpu().numpy()[:, idx].T
+        cpu_err = {"cells": int(okc.sum()),
+                   "surrogate_max_dY": float(np.abs(sY_[okc] - o["massf"][okc]).max()),
+                   "surrogate_max_rel_dT": float((np.abs(sT_[okc] - o["T"][okc]) / o["T"][okc]).max()),
+                   "plain_gpu_max_dY": float(np.abs(pY_[okc] - o["massf"][okc]).max())}
+    cpu = None
+    if not args.no_cpu_baseline:
+        r = cpu_reference_run(w, T0, p0, Y0, srho.cpu().numpy(), su.cpu().numpy(), max_seconds=args.cpu_seconds)
+        cpu = {"value": r["value"], "unit": "cell-updates/s", "cores": r["threads"], "kind": "port",
+               "sample": "%d of the %d cells (evenly strided), %.1f s on %d threads" %
+                         (r["cells"], n, r["seconds"], r["threads"])}
+    d = sweep[0]
+    achieved = plain_flops / plain_time / 1e12
+    return {
+        "metric": METRIC, "value": d["cell_updates_per_s"], "unit": "cell-updates/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": 1, "ms_per_step": d["seconds"] * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64+bf16", "data": "synthetic",
+        "config": {"workload": "h2air-surrogate", "cells": n, "dt": w["dt"], "dt_chem_in": -1.0,
+                   "network": "MLP 16-256x4-14 GELU, BF16 weights/activations, FP32 accumulation",
+                   "train_samples": int(n_train), "heldout_fraction": 0.05, "epochs": w["epochs"],
+                   "batch": w["batch"], "l2": "inputs larger than L2 (no flush)"},
+        "plain_fp64": {"cell_updates_per_s": n / plain_time, "seconds": plain_time,
+                       "roofline_frac": achieved / peak},
+        "surrogate_speedup_vs_plain": d["speedup_vs_plain"],
+        "sweep": sweep,
+        "accuracy_vs_cpu_reference": cpu_err,
+        "training": {"sample_generation_s": t_gen, "train_s": t_train, "samples_per_s":
+                     steps_per_epoch * w["batch"] * w["epochs"] / t_train, "tflops": train_flop / t_train / 1e12,
+                     "loss_first_epoch": hist[0], "loss_last_epoch": hist[-1]},
+        "heldout": {"rows": int(len(eY)), "median_max_dY": float(np.median(eY)),
+                    "p99_max_dY": float(np.percentile(eY, 99)), "max_dY": float(eY.max()),
+                    "median_rel_dT": float(np.median(eT)), "p99_rel_dT": float(np.percentile(eT, 99))},
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "kernel": "plain FP64 update of the same cells (the fallback's kernel)"},
+        "cpu_baseline": cpu, "e2e": None, "clocks": clk,
+        # per 1M-cell chunk: features, 5 GEMMs, gate; fallback: gather, cost + 3 ordering kernels,
+        # chemistry, scatter; monitor: repack, cost + 3 ordering kernels, chemistry, compare
+        "gpu_launches": ((n + (1 << 20) - 1) >> 20) * 7 + 7 + 7,
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -367,6 +528,15 @@ def main():
                                   "baseline inside the gdtk line"}))
             return 0
         print(json.dumps(run_layer(args, w)))
+        return 0
+
+    if w["kind"] == "surrogate":
+        if args.impl == "reference" or rank != 0:
+            if args.impl == "reference" and rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable": "the surrogate mode reports its CPU "
+                                  "baseline inside the gdtk line"}))
+            return 0
+        print(json.dumps(run_surrogate(args, w)))
         return 0
 
     if w["kind"] == "blocks":

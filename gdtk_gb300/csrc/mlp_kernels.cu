@@ -271,7 +271,7 @@ cudaError_t launch_gemm_bf16(const GemmArgs& g, cudaStream_t s) {
     const int a_inner = g.trans_a ? g.M : g.K, b_inner = g.trans_b ? g.K : g.N;
     if (g.K % 8 || a_inner % 8 || b_inner % 8 || g.lda % 8 || g.ldb % 8 || !aligned16(g.A) || !aligned16(g.B))
         return cudaErrorInvalidValue;
-    if (g.splits < 1 || (g.splits > 1 && (!g.work || g.bias || g.act != ACT_NONE || !g.D)))
+    if (g.splits < 1 || (g.splits > 1 && (!g.work || g.bias || g.act != ACT_NONE || !g.D || g.Dh)))
         return cudaErrorInvalidValue;
     if ((g.act == ACT_GELU_BWD && !g.pre_in) || (g.beta != 0.f && !g.D))
         return cudaErrorInvalidValue;

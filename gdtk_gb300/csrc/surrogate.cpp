@@ -74,7 +74,7 @@ struct Surrogate {
     std::vector<double> xmin, xmax;
     Buf<float> d_xs, d_xd, d_ys, d_yd, d_lw;
     Buf<double> d_xmin, d_xmax, d_elem, d_elemM;
-    double elem_tol = 2e-5, neg_tol = 1e-6, T_tol = 2e-3, max_dY = 0.0;
+    double elem_tol = 1e-4, neg_tol = 1e-5, T_tol = 1e-3, max_dY = 5e-4;
     // training buffers
     int tb = 0;
     Buf<__nv_bfloat16> t_xh, t_act, t_g16a, t_g16b, t_dout16;

@@ -95,7 +95,7 @@ class ChemSurrogate:
         assert w.shape == (self.nout,)
         check(lib().chem_surrogate_set_loss_weights(self.id, _vp(w)), "chem_surrogate_set_loss_weights")
 
-    def set_gate(self, elem_tol=2e-5, neg_tol=1e-6, T_tol=2e-3, max_dY=0.0):
+    def set_gate(self, elem_tol=1e-4, neg_tol=1e-5, T_tol=1e-3, max_dY=5e-4):
         check(lib().chem_surrogate_set_gate(self.id, float(elem_tol), float(neg_tol), float(T_tol), float(max_dY)),
               "chem_surrogate_set_gate")
 
@@ -203,14 +203,15 @@ class ChemSurrogate:
 
 
 def generate_samples(rc, sg, n, seed=0, dt_range=(0.5e-6, 2.0e-6), block=65536, blocks_per_launch=16,
-                     cells=None, log=None):
+                     cells=None, log=None, cost=None):
     """n training samples (rounded up to whole blocks) from the FP64 update of seeded cells.
 
     Cells come from `cells(n, seed)` -> (T, p, Y (nsp, n)) (default: the H2-air workload of
     uneven stiffness, gdtk_gb300.workloads.h2air_cells); each block of `block` cells gets its
     own dt, log-uniform in dt_range, and is advanced from a fresh step size (dt_chem = -1) by
     the plain update, blocks_per_launch blocks per persistent launch.  Returns (X, Y, valid,
-    seconds spent in the FP64 update)."""
+    seconds spent in the FP64 update).  `cost` (int32 cuda tensor of the rounded-up size), when
+    given, receives each sample's right-hand-side evaluations in the FP64 update."""
     import torch
     from .workloads import h2air_cells
     if cells is None:
@@ -235,11 +236,16 @@ def generate_samples(rc, sg, n, seed=0, dt_range=(0.5e-6, 2.0e-6), block=65536, 
             d["status"] = torch.zeros(block, dtype=torch.int32, device=dev)
             d["t_interval"] = dt
             group.append((b, d, d0))
+        counters = None
+        if cost is not None:
+            counters = torch.empty((6, len(group) * block), dtype=torch.int32, device=dev)
         torch.cuda.synchronize()
         t0 = time.time()
-        rc.update_blocks([g[1] for g in group])
+        rc.update_blocks([g[1] for g in group], cell_counters=counters)
         torch.cuda.synchronize()
         t_update += time.time() - t0
+        if cost is not None:
+            cost[g0 * block:g0 * block + len(group) * block] = counters[1]
         for b, d, d0 in group:
             sl = slice(b * block, (b + 1) * block)
             sg.make_samples(d0["T"], d0["p"], d0["massf"], d["t_interval"], d["T"], d["massf"], d["status"],

@@ -85,7 +85,7 @@ int chem_surrogate_gradients(int sg, int batch, const float* X, const float* Y, 
                              float* loss_sum, void* stream);
 /* Raw predicted increments out[n][nout_pad] of raw features X[n][nin_pad]. */
 int chem_surrogate_predict(int sg, int n, const float* X, float* out, void* stream);
-/* Gate tolerances (defaults 2e-5, 1e-6, 2e-3, 0). */
+/* Gate tolerances (defaults 1e-4, 1e-5, 1e-3, 5e-4). */
 int chem_surrogate_set_gate(int sg, double elem_tol, double neg_tol, double T_tol, double max_dY);
 /* The surrogate update with FP64 fallback.  Arguments as chem_reactor_update_cells; gate (may be
  * NULL) receives each cell's GDTK_GATE_* code; counts (host, may be NULL) receives
