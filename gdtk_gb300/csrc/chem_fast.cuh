@@ -160,10 +160,48 @@ __device__ __forceinline__ double sp_G(const double* TH, int i, double T, double
 // T from (rho, u) at fixed composition, therm_perf_gas_mix.d:426-468 (same iteration, same
 // stopping rules).  YR[i * ys] = Y_i R_i.  *iters counts iterations.  Out of line: it is
 // called after accepted steps and at the end of a cell, and one copy of its code serves both.
-__device__ __noinline__ double T_from_u(const double* TH, const double* YR, int ys, double u_tgt, double T_guess,
-                                        int* err, int* iters, unsigned long long* lst) {
+//
+// Where every species takes the same curve segment (GDTK_MIX_TLO <= T <= GDTK_MIX_THI, checked by
+// the generator), the mixture's H/R is the same polynomial with coefficients sum_i Y_i R_i c_i,
+// and its Cp/R the derivative of that polynomial: the 8 mixture coefficients are formed once per
+// segment and solve (in the caller's scratch S, stride ys), and each iteration then costs one
+// polynomial instead of one per species.  The sums are reassociated, so f and cv differ from the
+// per-species sums in the last bits only.
+#if GDTK_MIX_THERMO
+__device__ __forceinline__ void mix_coeffs(const double* TH, const double* YR, int ys, int seg, double* m) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        double acc = 0.0;
+#pragma unroll 1
+        for (int i = 0; i < GDTK_NSP; ++i)
+            acc = fma(YR[i * ys], TH[i * GDTK_TH_STRIDE + GDTK_TH_SEG0 + 24 * seg + k], acc);
+        m[k * ys] = acc;
+    }
+}
+// H/R and Cp/R = d(H/R)/dT of the mixture polynomial m (H/R = -a0/T + a1 lnT + a7 + a2 T + a3/2 T^2 + ...)
+__device__ __forceinline__ void mix_H_Cp(const double* m, int ys, double T, double lnT, double rT, double rT2,
+                                         double& H, double& Cp) {
+    const double h0 = m[0], h1 = m[ys], h2 = m[2 * ys], h3 = m[3 * ys], h4 = m[4 * ys], h5 = m[5 * ys],
+                 h6 = m[6 * ys], h7 = m[7 * ys];
+    H = fma(T, fma(T, fma(T, fma(T, fma(T, h6, h5), h4), h3), h2), fma(h0, rT, fma(h1, lnT, h7)));
+    Cp = fma(T, fma(T, fma(T, fma(T, 5.0 * h6, 4.0 * h5), 3.0 * h4), 2.0 * h3), fma(-h0, rT2, fma(h1, rT, h2)));
+}
+#endif
+
+__device__ __noinline__ double T_from_u(const double* TH, const double* YR, int ys, double* S, double u_tgt,
+                                        double T_guess, int* err, int* iters, unsigned long long* lst) {
     const double TOL = 1e-10;
     double T = T_guess, dT = 0.0;
+#if GDTK_MIX_THERMO
+    double* ma = S;
+    double* mb = S + 8 * ys;
+    int seg_a = -1, seg_b = -1;
+    double ysum = 0.0;
+#pragma unroll 1
+    for (int i = 0; i < GDTK_NSP; ++i) ysum += YR[i * ys];
+#else
+    (void)S;
+#endif
     for (int it = 0; it <= 10; ++it) {
         lane_stat(lst, 4);
         if (it > 0) {
@@ -173,15 +211,35 @@ __device__ __noinline__ double T_from_u(const double* TH, const double* YR, int 
         }
         const double lnT = log(T), rT = 1.0 / T, rT2 = rT * rT;
         double f = 0.0, cv = 0.0;
+#if GDTK_MIX_THERMO
+        int sa = 0, sb = 0;
+        double wb = 0.0;
+        if (T >= GDTK_MIX_TLO && T <= GDTK_MIX_THI && seg_of(TH, T, sa, sb, wb)) {
+            if (sa != seg_a) { mix_coeffs(TH, YR, ys, sa, ma); seg_a = sa; }
+            double H, C;
+            mix_H_Cp(ma, ys, T, lnT, rT, rT2, H, C);
+            if (wb != 0.0) {
+                if (sb != seg_b) { mix_coeffs(TH, YR, ys, sb, mb); seg_b = sb; }
+                double Hb, Cb;
+                mix_H_Cp(mb, ys, T, lnT, rT, rT2, Hb, Cb);
+                H = fma(wb, Hb - H, H);
+                C = fma(wb, Cb - C, C);
+            }
+            f = fma(-ysum, T, H);
+            cv = C - ysum;
+        } else
+#endif
+        {
 #pragma unroll 1
-        for (int i = 0; i < GDTK_NSP; ++i) {
-            double H, Cp;
-            int e = 0;
-            sp_H_Cp(TH, i, T, lnT, rT, rT2, H, Cp, e);
-            if (e) *err = e;
-            const double yr = YR[i * ys];
-            f = fma(yr, H - T, f);
-            cv = fma(yr, Cp - 1.0, cv);
+            for (int i = 0; i < GDTK_NSP; ++i) {
+                double H, Cp;
+                int e = 0;
+                sp_H_Cp(TH, i, T, lnT, rT, rT2, H, Cp, e);
+                if (e) *err = e;
+                const double yr = YR[i * ys];
+                f = fma(yr, H - T, f);
+                cv = fma(yr, Cp - 1.0, cv);
+            }
         }
         dT = -(f - u_tgt) / cv;
         ++*iters;
@@ -269,10 +327,9 @@ __constant__ double RKF_A[5][5] = {
     {3. / 10., -9. / 10., 6. / 5., 0, 0},
     {-11. / 54., 5. / 2., -70. / 27., 35. / 27., 0},
     {1631. / 55296., 175. / 512., 575. / 13824., 44275. / 110592., 253. / 4096.}};
-#define GDTK_VEC (6 * GDTK_NSP)
-#else
-#define GDTK_VEC (3 * GDTK_NSP)
 #endif
+// GDTK_VEC (per-thread method vector, doubles) comes from the generator: the method's stage
+// storage, at least nsp + 16 when T(rho, u) uses mixture coefficients
 
 extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_chem_fast(const __grid_constant__ FastArgs a) {
     extern __shared__ double smem[];
@@ -526,7 +583,7 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
                     V[i * ks] = yr;
                     Rm += yr;
                 }
-                T = T_from_u(TH, V, ks, u, T, &err, &n_newton, a.lane_stats);
+                T = T_from_u(TH, V, ks, V + GDTK_NSP * ks, u, T, &err, &n_newton, a.lane_stats);
                 p = rho * Rm * T;
                 need_kc = true;
             }
@@ -574,7 +631,7 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
             }
             int st = 0;
             if (a.flags & F_UPDATE_THERMO) {
-                T = T_from_u(TH, V, ks, u, T, &st, &n_newton, a.lane_stats);
+                T = T_from_u(TH, V, ks, V + GDTK_NSP * ks, u, T, &st, &n_newton, a.lane_stats);
                 p = rho * Rm * T;
             }
             const CellBlock& B = BLK[b];

@@ -198,6 +198,40 @@ std::vector<double> fast_thermo_table(const GasModelHost& gm) {
     return t;
 }
 
+// The temperature range where every species takes the same curve segment and blend of
+// cea_thermo_curves.d:150-182 (so that the mixture's H/R is one polynomial there): species curves
+// with at least two segments and equal first three breaks and first blend range.
+bool mix_thermo_range(const GasModelHost& gm, double& tlo, double& thi) {
+    const int nsp = gm.n_species();
+    if (nsp == 0) return false;
+    PackedMech pm = pack(gm, nullptr);
+    MechView v;
+    v.bind(pm.I.data(), pm.D.data());
+    const CeaCurveHost& c0 = gm.curves[0];
+    tlo = -1e300;
+    thi = 1e300;
+    for (int i = 0; i < nsp; ++i) {
+        const CeaCurveHost& c = gm.curves[i];
+        if (c.nseg < 2 || c0.nseg < 2 || c.breaks[0] != c0.breaks[0] || c.breaks[1] != c0.breaks[1] ||
+            c.breaks[2] != c0.breaks[2] || c.blends[0] != c0.blends[0])
+            return false;
+        tlo = std::max(tlo, v.sp(i)[SP_TLOW]);
+        thi = std::min(thi, v.sp(i)[SP_THIGH]);
+        if (c.nseg > 2) thi = std::min(thi, c.breaks[2] - 0.5 * c.blends[1]);
+    }
+    return thi > tlo;
+}
+
+// Per-thread method vector (doubles): the ODE method's stage storage, and room for the
+// species' Y_i R_i plus two sets of 8 mixture coefficients during T(rho, u).
+int fast_vec_doubles(const GasModelHost& gm, const MechanismHost& mh) {
+    const int nsp = gm.n_species();
+    int vec = (mh.method == METHOD_RKF ? 6 : 3) * nsp;
+    double tlo, thi;
+    if (mix_thermo_range(gm, tlo, thi)) vec = std::max(vec, nsp + 16);
+    return vec;
+}
+
 std::string generate_fast_source(const GasModelHost& gm, const MechanismHost& mh, int block, int min_blocks) {
     const int nsp = gm.n_species();
     const int nr = (int)mh.reactions.size();
@@ -211,6 +245,13 @@ std::string generate_fast_source(const GasModelHost& gm, const MechanismHost& mh
     o << "#define GDTK_ERRTOL " << lit(mh.errTol) << "\n#define GDTK_EPS1 " << lit(mh.eps1) << "\n";
     o << "#define GDTK_EPS2 " << lit(mh.eps2) << "\n#define GDTK_DELTA " << lit(mh.delta) << "\n";
     o << "#define GDTK_BLOCK " << block << "\n#define GDTK_MIN_BLOCKS " << min_blocks << "\n";
+    {
+        double tlo = 0.0, thi = 0.0;
+        const bool mix = mix_thermo_range(gm, tlo, thi);
+        o << "#define GDTK_MIX_THERMO " << (mix ? 1 : 0) << "\n";
+        if (mix) o << "#define GDTK_MIX_TLO " << lit(tlo) << "\n#define GDTK_MIX_THI " << lit(thi) << "\n";
+        o << "#define GDTK_VEC " << fast_vec_doubles(gm, mh) << "\n";
+    }
     o << kFastExpSource << "\n";
     auto arr = [&](const char* name, std::function<double(int)> f) {
         o << "__constant__ double " << name << "[" << nsp << "] = {";
@@ -394,7 +435,7 @@ FastKernel* build_fast_kernel(const GasModelHost& gm, const MechanismHost& mh, i
     cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int nsp = gm.n_species(), nr = (int)mh.reactions.size();
-    const int per_thread = 2 * nr + (mh.method == METHOD_RKF ? 6 : 3) * nsp;
+    const int per_thread = 2 * nr + fast_vec_doubles(gm, mh);
     const int table = nsp * 120 + 64;
     // Block size: as many resident threads as shared memory allows, up to 256 per SM.
     const double budget = 227.0 * 1024 / 8;   // doubles of shared memory per SM

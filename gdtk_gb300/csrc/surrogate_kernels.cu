@@ -229,17 +229,50 @@ __global__ void __launch_bounds__(128) gate_kernel(const GateArgs a) {
                 }
             }
             if (code == GATE_ACCEPTED) {
-                double sum = 0.0, most_neg = 0.0;
+                double most_neg = 0.0;
+                bool clipped = false;
                 for (int s = 0; s < nsp; ++s) {
                     double y = Y0[s] + dY[s];
                     most_neg = fmin(most_neg, y);
-                    y = fmax(y, 0.0);
+                    if (y < 0.0) { y = 0.0; clipped = true; }
                     Y1[s] = y;
-                    sum += y;
                 }
-                if (most_neg < -a.neg_tol || !(sum > 0.0)) code = GATE_NEGATIVE;
-                else
-                    for (int s = 0; s < nsp; ++s) Y1[s] /= sum;
+                if (most_neg < -a.neg_tol) code = GATE_NEGATIVE;
+                if (code == GATE_ACCEPTED && clipped && a.ne > 0) {
+                    // restore the element balance that clipping broke, moving only species present
+                    // (weights Y1, so clipped species stay at zero)
+                    double w[GDTK_MAX_SPECIES];
+                    for (int s = 0; s < nsp; ++s) w[s] = Y1[s] + 1e-300;
+                    for (int e = 0; e < a.ne; ++e) {
+                        double v = 0.0;
+                        for (int s = 0; s < nsp; ++s) v += a.elem[e * nsp + s] * (Y1[s] - Y0[s]);
+                        r[e] = v;
+                    }
+                    double G[SURR_MAX_ELEMENTS][SURR_MAX_ELEMENTS];
+                    for (int e = 0; e < a.ne; ++e)
+                        for (int f = 0; f <= e; ++f) {
+                            double v = 0.0;
+                            for (int s = 0; s < nsp; ++s) v += a.elem[e * nsp + s] * w[s] * a.elem[f * nsp + s];
+                            G[e][f] = v;
+                            G[f][e] = v;
+                        }
+                    if (!spd_solve(G, r, a.ne)) {
+                        code = GATE_ELEMENTS;
+                    } else {
+                        for (int s = 0; s < nsp; ++s) {
+                            double corr = 0.0;
+                            for (int e = 0; e < a.ne; ++e) corr += a.elem[e * nsp + s] * r[e];
+                            Y1[s] = fmax(Y1[s] - w[s] * corr, 0.0);
+                        }
+                    }
+                }
+                if (code == GATE_ACCEPTED) {
+                    double sum = 0.0;
+                    for (int s = 0; s < nsp; ++s) sum += Y1[s];
+                    if (!(sum > 0.0)) code = GATE_NEGATIVE;
+                    else
+                        for (int s = 0; s < nsp; ++s) Y1[s] /= sum;
+                }
             }
             if (code == GATE_ACCEPTED) {
                 int err = 0, its = 0;

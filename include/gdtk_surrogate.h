@@ -16,8 +16,9 @@
  *   domain          every raw input lies within the training samples' [min, max];
  *   elements        the predicted increment changes no element's mass fraction by more than
  *                   elem_tol, and is then projected onto exact element conservation;
- *   non-negativity  no mass fraction falls below -neg_tol (small negatives are clipped to 0 and
- *                   the mass fractions renormalised);
+ *   non-negativity  no mass fraction falls below -neg_tol (small negatives are clipped to 0, the
+ *                   element balance is restored by a second projection that moves only the
+ *                   species present, and the mass fractions are renormalised);
  *   energy          T from (rho, u, Y_new) by the reference's Newton iteration
  *                   (therm_perf_gas_mix.d:426-468) converges and agrees with T + the predicted
  *                   dT within T_tol (relative);

@@ -74,7 +74,13 @@ def gate(orc, E, EM, rho, u, T, p, Y, dY, dT, x_min, x_max, dt, T_frozen, elem_t
         if y.min() < -neg_tol:
             codes[c] = NEGATIVE
             continue
-        y = np.maximum(y, 0.0)
+        if y.min() < 0.0:
+            # clip, then restore the element balance moving only the species present
+            y = np.maximum(y, 0.0)
+            w2 = y + 1e-300
+            G2 = (E * w2[None, :]) @ E.T
+            lam2 = np.linalg.solve(G2, E @ (y - Y[c]))
+            y = np.maximum(y - w2 * (E.T @ lam2), 0.0)
         y = y / y.sum()
         guess = T[c] + dT[c]
         if not guess > 0:
