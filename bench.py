@@ -373,13 +373,14 @@ def run_surrogate(args, w):
     sg.fit_normalisation(X, Yt, train)
     sync()
     t1 = time.perf_counter()
-    hist = sg.train(X, Yt, train, epochs=w["epochs"], batch=w["batch"], lr=2e-3)
+    epochs = args.epochs or w["epochs"]
+    hist = sg.train(X, Yt, train, epochs=epochs, batch=w["batch"], lr=2e-3)
     sync()
     t_train = time.perf_counter() - t1
     eY, eT = sg.heldout_error(X, Yt, hold)
     steps_per_epoch = train.shape[0] // w["batch"]
     train_flop = 3 * 2 * sum(a * b for a, b in zip(sg.layer_dims()[:-1], sg.layer_dims()[1:])) * \
-        steps_per_epoch * w["batch"] * w["epochs"]
+        steps_per_epoch * w["batch"] * epochs
     del X, Yt, valid, rows, perm, hold, train
     torch.cuda.empty_cache()
 
@@ -481,7 +482,7 @@ def run_surrogate(args, w):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64+bf16", "data": "synthetic",
         "config": {"workload": "h2air-surrogate", "cells": n, "dt": w["dt"], "dt_chem_in": -1.0,
                    "network": "MLP 16-256x4-14 GELU, BF16 weights/activations, FP32 accumulation",
-                   "train_samples": int(n_train), "heldout_fraction": 0.05, "epochs": w["epochs"],
+                   "train_samples": int(n_train), "heldout_fraction": 0.05, "epochs": epochs,
                    "batch": w["batch"], "l2": "inputs larger than L2 (no flush)"},
         "plain_fp64": {"cell_updates_per_s": n / plain_time, "seconds": plain_time,
                        "roofline_frac": achieved / peak},
@@ -489,7 +490,7 @@ def run_surrogate(args, w):
         "sweep": sweep,
         "accuracy_vs_cpu_reference": cpu_err,
         "training": {"sample_generation_s": t_gen, "train_s": t_train, "samples_per_s":
-                     steps_per_epoch * w["batch"] * w["epochs"] / t_train, "tflops": train_flop / t_train / 1e12,
+                     steps_per_epoch * w["batch"] * epochs / t_train, "tflops": train_flop / t_train / 1e12,
                      "loss_first_epoch": hist[0], "loss_last_epoch": hist[-1]},
         "heldout": {"rows": int(len(eY)), "median_max_dY": float(np.median(eY)),
                     "p99_max_dY": float(np.percentile(eY, 99)), "max_dY": float(eY.max()),
@@ -512,6 +513,7 @@ def main():
     ap.add_argument("--impl", choices=["gdtk", "reference"], default="gdtk")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="h2air-1M")
     ap.add_argument("--cells", type=int, default=0, help="override the cell count (parity/debug runs)")
+    ap.add_argument("--epochs", type=int, default=0, help="surrogate mode: override the training epochs")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
