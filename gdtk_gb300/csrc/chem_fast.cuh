@@ -279,6 +279,8 @@ __device__ __forceinline__ double sum_pairwise(F d) {
 
 // Rate constants at T (clamped to the mechanism's limits, reaction_mechanism.d:49-63); the
 // species G/RT go through the per-thread scratch vector G.
+// G: scratch of GDTK_NSP slots (stride ks); the third-body concentrations of the pressure-dependent
+// rate constants (gen_falloff_M) are read from the GDTK_NFALLOFF slots after it.
 __device__ __noinline__ void rate_constants(const double* TH, double Tq, double* K, int ks, const double* etab,
                                             double* G, int* err) {
     double T = Tq;
@@ -289,7 +291,7 @@ __device__ __noinline__ void rate_constants(const double* TH, double Tq, double*
 #pragma unroll 1
     for (int i = 0; i < GDTK_NSP; ++i) G[i * ks] = sp_G(TH, i, T, lnT, rT, rT2, t1, t2, e);
     if (e) *err = e;
-    gen_kc(T, lnT, rT, G, ks, K, ks, etab);
+    gen_kc(T, lnT, rT, G, ks, K, ks, etab, G + GDTK_NSP * ks, ks);
 }
 
 // reaction_mechanism.d:161-203 from the rates at c.
@@ -411,6 +413,7 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
         }
         if (need_kc) {
             lane_stat(a.lane_stats, 1);
+            if (GDTK_NFALLOFF) gen_falloff_M(y0, V + GDTK_NSP * ks, ks);
             rate_constants(TH, T, K, ks, ETAB, V, &err);
             ++n_kc;
             need_kc = false;
@@ -709,6 +712,7 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
                     y[i] = (v < MIN_MOLES) ? 0.0 : v;
                 }
                 int err = 0;
+                if (GDTK_NFALLOFF) gen_falloff_M(y, V + GDTK_NSP * ks, ks);
                 rate_constants(TH, T, K, ks, ETAB, V, &err);
                 gen_rhs(y, q, L, K, ks);
                 h = estimate_step(y, q, L);

@@ -60,9 +60,58 @@ __device__ __forceinline__ double ipow(double x, int n) {
 }
 
 // ---------------------------------------------------------------- kinetics
+__device__ __forceinline__ double arrhenius(double A, double n, double C, double T) {   // rate_constant.d:72-75
+    return A * pow(T, n) * exp(-C / T);
+}
+
+// Forward rate constant of a pressure-dependent reaction: the third-body concentration of its
+// efficiency list from the gas state's mass fractions (rate_constant.d:114-121), then
+// Lindemann-Hinshelwood (155-160), Troe (258-287) or Yungster-Rabinowitz (338-350).
+__device__ double pressure_dependent_kf(const MechView& m, const int* r, const double* d, double T, Vec mf,
+                                        double rho) {
+    const int* ei = m.eff_i(r[RX_EFFSET]);
+    const double* ev = m.eff_d(r[RX_EFFSET]);
+    double M = 0.0;
+    for (int k = 0; k < ei[0]; ++k) {
+        const int isp = ei[1 + k];
+        M += ev[isp] * (mf[isp] * rho / m.sp(isp)[SP_M]);
+    }
+    const double kInf = arrhenius(d[0], d[1], d[2], T);
+    const double k0 = arrhenius(d[RD_K0A], d[RD_K0N], d[RD_K0C], T);
+    if (r[RX_FRC] == RATE_LH) return k0 * kInf * M / (k0 * M + kInf);
+    const double essentially_zero = 1.0e-30;
+    if (r[RX_FRC] == RATE_TROE) {
+        const double p_r = k0 * M / kInf;
+        const double log_p_r = log10(fmax(p_r, essentially_zero));
+        const int fl = (int)d[RD_TFLAGS];
+        double Fcent = d[RD_FCENT];
+        if (!(fl & TROE_FCENT)) {
+            Fcent = (1.0 - d[RD_TA]) * exp(-T / d[RD_T3]);
+            if (fl & TROE_T1) Fcent += d[RD_TA] * exp(-T / d[RD_T1]);
+            if (fl & TROE_T2) Fcent += exp(-d[RD_T2] / T);
+        }
+        const double log_F_cent = log10(fmax(Fcent, essentially_zero));
+        const double c = -0.4 - 0.67 * log_F_cent;
+        const double n = 0.75 - 1.27 * log_F_cent;
+        const double dd = 0.14;
+        const double numer = log_p_r + c;
+        const double denom = n - dd * numer;
+        const double frac = numer / denom;
+        const double log_F = log_F_cent / (1.0 + frac * frac);
+        const double F = pow(10.0, log_F);
+        return F * k0 * kInf * M / (k0 * M + kInf);
+    }
+    const double p_r = k0 * M / kInf;   // Yungster-Rabinowitz
+    const double log_p_r = log(p_r);
+    const double Fc = d[RD_TA] * exp(-d[RD_T1] / T) + (1.0 - d[RD_TA]) * exp(-d[RD_T2] / T);
+    const double xt = 1.0 / (1.0 + log_p_r * log_p_r);
+    return kInf * (p_r / (1.0 + p_r)) * Fc * xt;
+}
+
 // reaction_mechanism.d:49-63 with Gibbs energies at P_atm (:204-218, therm_perf_gas_mix.d:354-364),
-// reaction.d:26-52 and 94-143 for a single-temperature gas.  g is scratch of nsp doubles.
-__device__ void rate_constants(const MechView& m, double Tq, Vec kf, Vec kb, Vec g, int& err) {
+// reaction.d:26-52 and 94-143 for a single-temperature gas.  g is scratch of nsp doubles; mf and
+// rho are the gas state's mass fractions and density (third bodies of pressure-dependent rates).
+__device__ void rate_constants(const MechView& m, double Tq, Vec kf, Vec kb, Vec g, Vec mf, double rho, int& err) {
     double T = Tq;
     if (T < m.T_lower()) T = m.T_lower();
     if (T > m.T_upper()) T = m.T_upper();
@@ -88,8 +137,9 @@ __device__ void rate_constants(const MechView& m, double Tq, Vec kf, Vec kb, Vec
             double K_p = exp(-dG / (R_universal * T));
             Kc = K_p * ipow(P_atm / (R_universal * T), (int)nuSum);
         }
-        if (r[RX_FRC] == RATE_ARRHENIUS) {
-            double f = d[0] * pow(T, d[1]) * exp(-d[2] / T);
+        if (r[RX_FRC] != RATE_FROM_EQ) {
+            double f = (r[RX_FRC] == RATE_ARRHENIUS) ? d[0] * pow(T, d[1]) * exp(-d[2] / T)
+                                                     : pressure_dependent_kf(m, r, d, T, mf, rho);
             kf[ir] = f;
             kb[ir] = (r[RX_BRC] == RATE_FROM_EQ) ? f / Kc : d[3] * pow(T, d[4]) * exp(-d[5] / T);
         } else {
@@ -363,7 +413,7 @@ __global__ void __launch_bounds__(256) chem_update_kernel(ChemUpdateArgs a) {
     const double tI = a.t_interval;
 
     unsigned c = 0;
-    bool have = false, retried = false, need_kc = false;
+    bool have = false, retried = false, need_kc = false, kc_from_input = false;
     int phase = 0, cycle = 0, attempt = 0, err = 0;
     double rho = 0, u = 0, T = 0, T0 = 0, p = 0, p0 = 0, dtS = 0, dtS0 = 0, dtSave = 0, h = 0, t = 0;
     int n_steps = 0, n_rhs = 0, n_kc = 0, n_newton = 0, n_rej = 0, n_est = 0;
@@ -393,10 +443,13 @@ __global__ void __launch_bounds__(256) chem_update_kernel(ChemUpdateArgs a) {
                 y0[i] = (v < MIN_MOLES) ? 0.0 : v;
             }
             need_kc = true;
+            kc_from_input = true;
             phase = 0;
         }
         if (need_kc) {
-            rate_constants(m, T, kf, kb, L, err);
+            // Q.massf at this point: the input mass fractions, or conc2massf of the last step (in q)
+            rate_constants(m, T, kf, kb, L, kc_from_input ? Vec{a.massf + c, (int)ncell} : q, rho, err);
+            kc_from_input = false;
             ++n_kc;
             need_kc = false;
         }
@@ -566,7 +619,7 @@ __global__ void __launch_bounds__(128) gas_service_kernel(GasServiceArgs a) {
                     double v = mf[i] * rho / m.sp(i)[SP_M];
                     c[i] = (a.clip && v < MIN_MOLES) ? 0.0 : v;
                 }
-                rate_constants(m, a.T[cell], kf, kb, L, err);
+                rate_constants(m, a.T[cell], kf, kb, L, mf, rho, err);
                 if (a.mode == 2) {
                     split_rates(m, c, q, L, kf, kb, meff);
                     for (int i = 0; i < nsp; ++i)

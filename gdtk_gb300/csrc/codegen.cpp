@@ -150,6 +150,55 @@ bool power_arrhenius(const RateConstHost& rc, std::string& out) {
     return true;
 }
 
+// k = A T^n exp(-C/T) as an expression (products, one exponential, or 0).
+std::string arrhenius_expr(double A, double n, double C) {
+    RateConstHost rc;
+    rc.A = A; rc.n = n; rc.C = C;
+    std::string e;
+    if (power_arrhenius(rc, e)) return e;
+    e = log_arrhenius(rc);
+    return e.empty() ? std::string("0.0") : "gdtk_exp(" + e + ", etab)";
+}
+
+// Forward rate constant of a pressure-dependent reaction (rate_constant.d:155-160, 258-287,
+// 338-350) as statements ending in `kf`, from the third-body concentration `Mc`.  log10 and
+// pow(10, x) are written as ln x / ln 10 and exp(x ln 10).
+std::string pressure_dependent_code(const RateConstHost& f) {
+    std::ostringstream o;
+    o << "    const double kinf = " << arrhenius_expr(f.A, f.n, f.C) << ";\n";
+    o << "    const double k0 = " << arrhenius_expr(f.A0, f.n0, f.C0) << ";\n";
+    o << "    const double klh = k0 * kinf * Mc / fma(k0, Mc, kinf);\n";
+    if (f.model == RATE_LH) {
+        o << "    const double kf = klh;\n";
+    } else if (f.model == RATE_TROE) {
+        const double INV_LN10 = 1.0 / std::log(10.0);
+        o << "    const double pr = k0 * Mc / kinf;\n";
+        o << "    const double lpr = log(fmax(pr, 1.0e-30)) * " << lit(INV_LN10) << ";\n";
+        if (f.troe_flags & TROE_FCENT) {
+            const double lfc = std::log10(std::max(f.Fcent, 1.0e-30));
+            o << "    const double lfc = " << lit(lfc) << ", cc = " << lit(-0.4 - 0.67 * lfc)
+              << ", nn = " << lit(0.75 - 1.27 * lfc) << ";\n";
+        } else {
+            o << "    double fcent = " << lit(1.0 - f.a) << " * gdtk_exp(" << lit(-1.0 / f.T3) << " * T, etab);\n";
+            if (f.troe_flags & TROE_T1)
+                o << "    fcent = fma(" << lit(f.a) << ", gdtk_exp(" << lit(-1.0 / f.T1) << " * T, etab), fcent);\n";
+            if (f.troe_flags & TROE_T2) o << "    fcent += gdtk_exp(" << lit(-f.T2) << " * rT, etab);\n";
+            o << "    const double lfc = log(fmax(fcent, 1.0e-30)) * " << lit(INV_LN10) << ";\n";
+            o << "    const double cc = fma(-0.67, lfc, -0.4), nn = fma(-1.27, lfc, 0.75);\n";
+        }
+        o << "    const double numer = lpr + cc;\n";
+        o << "    const double frac = numer / fma(-0.14, numer, nn);\n";
+        o << "    const double kf = gdtk_exp(lfc / fma(frac, frac, 1.0) * " << lit(std::log(10.0)) << ", etab) * klh;\n";
+    } else {   // Yungster-Rabinowitz: a, b, c in a, T1, T2
+        o << "    const double pr = k0 * Mc / kinf;\n";
+        o << "    const double lpr = log(pr);\n";
+        o << "    const double fc = fma(" << lit(f.a) << ", gdtk_exp(" << lit(-f.T1) << " * rT, etab), " << lit(1.0 - f.a)
+          << " * gdtk_exp(" << lit(-f.T2) << " * rT, etab));\n";
+        o << "    const double kf = kinf * (pr / (1.0 + pr)) * fc / fma(lpr, lpr, 1.0);\n";
+    }
+    return o.str();
+}
+
 }  // namespace
 
 FastKernel::~FastKernel() {
@@ -229,7 +278,9 @@ int fast_vec_doubles(const GasModelHost& gm, const MechanismHost& mh) {
     int vec = (mh.method == METHOD_RKF ? 6 : 3) * nsp;
     double tlo, thi;
     if (mix_thermo_range(gm, tlo, thi)) vec = std::max(vec, nsp + 16);
-    return vec;
+    int nfall = 0;   // third-body concentrations of pressure-dependent rates, beside G/RT
+    for (auto& r : mh.reactions) nfall += r.frc.pressure_dependent() ? 1 : 0;
+    return std::max(vec, nsp + nfall);
 }
 
 std::string generate_fast_source(const GasModelHost& gm, const MechanismHost& mh, int block, int min_blocks) {
@@ -263,10 +314,26 @@ std::string generate_fast_source(const GasModelHost& gm, const MechanismHost& mh
     arr("GDTK_R", [&](int i) { return R_universal / gm.M[i]; });
     o << "namespace gdtk_fast {\nusing gdtk::gdtk_exp;\n";
 
+    // ---- third-body concentrations of the pressure-dependent rate constants (rate_constant.d:114-121),
+    // from the concentrations at which the rate constants are evaluated
+    int nfall = 0;
+    o << "__device__ __forceinline__ void gen_falloff_M(const double (&c)[GDTK_NSP], double* Mv, int ms) {\n";
+    o << "  (void)c; (void)Mv; (void)ms;\n";
+    for (int ir = 0; ir < nr; ++ir) {
+        const ReactionHost& r = mh.reactions[ir];
+        if (!r.frc.pressure_dependent()) continue;
+        o << "  Mv[" << nfall << " * ms] = 0.0";
+        for (auto& e : r.eff) o << " + " << lit(e.second) << " * c[" << e.first << "]";
+        o << ";\n";
+        ++nfall;
+    }
+    o << "}\n#define GDTK_NFALLOFF " << nfall << "\n";
+
     // ---- rate constants
     o << "__device__ __forceinline__ void gen_kc(double T, double lnT, double rT, const double* g, int gs, double* K, "
-         "int ks, const double* etab) {\n";
-    o << "  (void)T;\n";
+         "int ks, const double* etab, const double* Mv, int ms) {\n";
+    o << "  (void)T; (void)Mv; (void)ms;\n";
+    int ifall = 0;
     for (int ir = 0; ir < nr; ++ir) {
         const ReactionHost& r = mh.reactions[ir];
         auto parts = participants(r);
@@ -291,7 +358,11 @@ std::string generate_fast_source(const GasModelHost& gm, const MechanismHost& mh
         std::string lnKc = "(-(" + dgs + ")" +
                            (nusum ? " + " + lit((double)nusum) + " * (" + lit(std::log(101325.0 / R_universal)) + " - lnT)" : std::string("")) + ")";
         o << "  { // " << (r.equation.empty() ? std::string("reaction") : r.equation) << "\n";
-        if (r.frc.model == RATE_ARRHENIUS) {
+        if (r.frc.pressure_dependent()) {   // backward from K_c (checked when the mechanism is read)
+            o << "    const double Mc = Mv[" << ifall++ << " * ms];\n";
+            o << pressure_dependent_code(r.frc);
+            o << "    const double kb = kf * gdtk_exp(-" << lnKc << ", etab);\n";
+        } else if (r.frc.model == RATE_ARRHENIUS) {
             std::string pw;
             if (power_arrhenius(r.frc, pw)) {
                 o << "    const double kf = " << pw << ";\n";

@@ -21,22 +21,49 @@ std::vector<std::string> species_list(const LuaValue& v) {
     return out;
 }
 
+void arrhenius_params(const LuaValue& t, double& A, double& n, double& C) {   // rate_constant.d:60-66
+    A = t.get("A").number();
+    n = t.get("n").number();
+    C = t.get("C").number();
+    if (t.has("rctIndex") && t.get("rctIndex").number() != -1)
+        throw std::runtime_error("rate constants on a temperature other than T need a multi-temperature gas");
+}
+
+// createRateConstant, kinetics/rate_constant.d:570-597, for a single-temperature gas.
 RateConstHost rate_const(const LuaValue& t) {
     RateConstHost r;
     const std::string& model = t.get("model").string();
     if (model == "Arrhenius") {
         r.model = RATE_ARRHENIUS;
-        r.A = t.get("A").number();
-        r.n = t.get("n").number();
-        r.C = t.get("C").number();
-        if (t.has("rctIndex") && t.get("rctIndex").number() != -1)
-            throw std::runtime_error("rate constants on a temperature other than T need a multi-temperature gas");
+        arrhenius_params(t, r.A, r.n, r.C);
     } else if (model == "fromEqConst") {
         r.model = RATE_FROM_EQ;
+    } else if (model == "Lindemann-Hinshelwood" || model == "Troe" || model == "Yungster-Rabinowitz") {
+        arrhenius_params(t.get("kInf"), r.A, r.n, r.C);
+        arrhenius_params(t.get("k0"), r.A0, r.n0, r.C0);
+        if (model == "Lindemann-Hinshelwood") {
+            r.model = RATE_LH;
+        } else if (model == "Troe") {   // rate_constant.d:190-229
+            r.model = RATE_TROE;
+            if (t.has("F_cent")) {
+                r.troe_flags = TROE_FCENT;
+                r.Fcent = t.get("F_cent").number();
+            } else {
+                r.a = t.get("a").number();
+                r.T3 = t.get("T3").number();
+                if (t.get("T1").kind == LuaValue::NUMBER) { r.troe_flags |= TROE_T1; r.T1 = t.get("T1").number(); }
+                if (t.get("T2").kind == LuaValue::NUMBER) { r.troe_flags |= TROE_T2; r.T2 = t.get("T2").number(); }
+            }
+        } else {   // rate_constant.d:321-333
+            r.model = RATE_YR;
+            r.a = t.get("a").number();
+            r.T1 = t.get("b").number();
+            r.T2 = t.get("c").number();
+        }
     } else {
-        // kinetics/rate_constant.d:570-597 also knows Arrhenius2, Lindemann-Hinshelwood, Troe,
-        // Yungster-Rabinowitz, Park, Marrone-Treanor and MMT; this engine implements the
-        // Arrhenius/third-body path only.
+        // kinetics/rate_constant.d:570-597 also knows Arrhenius2, Park, Marrone-Treanor and MMT
+        // (multi-temperature or alternative forms); this engine implements the single-temperature
+        // Arrhenius, third-body and pressure-dependent path.
         throw std::runtime_error("rate-constant model '" + model + "' is not supported by this engine");
     }
     return r;
@@ -145,6 +172,9 @@ MechanismHost load_mechanism(const std::string& path, const GasModelHost& gm, bo
         rh.brc = rate_const(r.get("brc"));
         if (rh.frc.model == RATE_FROM_EQ && rh.brc.model == RATE_FROM_EQ)
             throw std::runtime_error("a reaction needs at least one Arrhenius rate constant");
+        if (rh.brc.pressure_dependent() || (rh.frc.pressure_dependent() && rh.brc.model != RATE_FROM_EQ))
+            throw std::runtime_error("pressure-dependent rate constants are supported as the forward rate with a "
+                                     "backward rate from K_c");
         std::vector<int> ri = r.get("reacIdx").ints(), rc = r.get("reacCoeffs").ints();
         std::vector<int> pi = r.get("prodIdx").ints(), pc = r.get("prodCoeffs").ints();
         if (ri.size() != rc.size() || pi.size() != pc.size())
@@ -182,7 +212,7 @@ PackedMech pack(const GasModelHost& gm, const MechanismHost* mh) {
     std::vector<int> set_of(nr, -1);
     for (int ir = 0; ir < nr; ++ir) {
         const ReactionHost& r = mh->reactions[ir];
-        if (!r.collider) continue;
+        if (!r.collider && !r.frc.pressure_dependent()) continue;   // third bodies of the reaction or its rate
         int found = -1;
         for (size_t s = 0; s < sets.size(); ++s)
             if (sets[s] == r.eff) { found = (int)s; break; }
@@ -255,6 +285,9 @@ PackedMech pack(const GasModelHost& gm, const MechanismHost* mh) {
         }
         rd[0] = r.frc.A; rd[1] = r.frc.n; rd[2] = r.frc.C;
         rd[3] = r.brc.A; rd[4] = r.brc.n; rd[5] = r.brc.C;
+        rd[RD_K0A] = r.frc.A0; rd[RD_K0N] = r.frc.n0; rd[RD_K0C] = r.frc.C0;
+        rd[RD_FCENT] = r.frc.Fcent; rd[RD_TA] = r.frc.a; rd[RD_T1] = r.frc.T1; rd[RD_T2] = r.frc.T2;
+        rd[RD_T3] = r.frc.T3; rd[RD_TFLAGS] = r.frc.troe_flags;
     }
     for (int s = 0; s < neff; ++s) {
         int* ei = I + HI + nsp + RXI * nr + (1 + nsp) * s;
@@ -288,10 +321,24 @@ void flop_model(const GasModelHost& gm, const MechanismHost& mh, double out[5]) 
         part.erase(std::unique(part.begin(), part.end()), part.end());
         // rate constants (rate_constant.d:72-75, reaction.d:26-52, 94-143)
         const double arr = POW + EXP + 3;
+        // pressure-dependent forward rates (rate_constant.d:114-121, 155-160, 258-287, 338-350): two
+        // Arrhenius terms, the third-body sum (4 per efficiency) and the blending
+        double fwd = arr;
+        const double tb = 2 * arr + 4.0 * r.eff.size() + 5;
+        if (r.frc.model == RATE_LH) {
+            fwd = tb;
+        } else if (r.frc.model == RATE_TROE) {
+            double fc = 0;
+            if (!(r.frc.troe_flags & TROE_FCENT))
+                fc = (EXP + 4) + ((r.frc.troe_flags & TROE_T1) ? EXP + 3 : 0) + ((r.frc.troe_flags & TROE_T2) ? EXP + 2 : 0);
+            fwd = tb + 2 + LOG + fc + LOG + 4 + 7 + POW + 1;
+        } else if (r.frc.model == RATE_YR) {
+            fwd = tb + 2 + LOG + 2 * EXP + 7 + 3 + 4;
+        }
         if (r.frc.model == RATE_FROM_EQ || r.brc.model == RATE_FROM_EQ)
-            kc += arr + 4.0 * part.size() + (EXP + 2) + 3 + 1 + 1;
+            kc += (r.frc.model == RATE_FROM_EQ ? arr : fwd) + 4.0 * part.size() + (EXP + 2) + 3 + 1 + 1;
         else
-            kc += 2 * arr;
+            kc += fwd + arr;
         if (r.collider) {
             if (std::find(sets.begin(), sets.end(), r.eff) == sets.end()) {
                 sets.push_back(r.eff);

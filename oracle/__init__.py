@@ -49,7 +49,9 @@ def lib():
                                         ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         L.oracle_n_reactions.argtypes = [ctypes.c_void_p]
         L.oracle_species_thermo.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, _d, _d, _d]
-        L.oracle_rate_constants.argtypes = [ctypes.c_void_p, ctypes.c_double, _d, _d]
+        L.oracle_rate_constants.argtypes = [ctypes.c_void_p, ctypes.c_double, _d, _d, _d]
+        L.oracle_set_pressure_dependent.argtypes = [ctypes.c_void_p, ctypes.c_int] + [ctypes.c_double] * 8 + \
+            [ctypes.c_int]
         L.oracle_split_rates.argtypes = [ctypes.c_void_p, ctypes.c_double, _d, _d, _d, _d, _d]
         L.oracle_estimate_step.restype = ctypes.c_double
         L.oracle_estimate_step.argtypes = [ctypes.c_void_p, ctypes.c_double, _d]
@@ -126,20 +128,43 @@ class Oracle:
         self.config = None
         if chem_file is not None:
             reactions, cfg = load_mechanism(chem_file, self.names)
+            pd_models = {'Lindemann-Hinshelwood': 2, 'Troe': 3, 'Yungster-Rabinowitz': 4}
             for r in reactions:
                 def rcm(d):
                     if d['model'] == 'Arrhenius':
                         return 0, float(d['A']), float(d['n']), float(d['C'])
                     if d['model'] == 'fromEqConst':
                         return 1, 0.0, 0.0, 0.0
+                    if d['model'] in pd_models:   # k_inf here, k_0 and the blending below
+                        k = d['kInf']
+                        return pd_models[d['model']], float(k['A']), float(k['n']), float(k['C'])
                     raise ValueError("rate-constant model %s is outside this path" % d['model'])
                 fm, fA, fn, fC = rcm(r['frc'])
                 bm, bA, bn, bC = rcm(r['brc'])
                 ri = np.array([i for i, _ in r['reac']], np.int32); rcf = np.array([k for _, k in r['reac']], np.int32)
                 pi = np.array([i for i, _ in r['prod']], np.int32); pcf = np.array([k for _, k in r['prod']], np.int32)
                 ei = np.array([i for i, _ in r['eff']], np.int32); ev = np.array([v for _, v in r['eff']], np.float64)
-                L.oracle_add_reaction(self.h, int(r['collider']), fm, fA, fn, fC, bm, bA, bn, bC,
-                                      len(ri), _ip(ri), _ip(rcf), len(pi), _ip(pi), _ip(pcf), len(ei), _ip(ei), _dp(ev))
+                ir = L.oracle_add_reaction(self.h, int(r['collider']), fm, fA, fn, fC, bm, bA, bn, bC,
+                                           len(ri), _ip(ri), _ip(rcf), len(pi), _ip(pi), _ip(pcf), len(ei), _ip(ei),
+                                           _dp(ev))
+                if fm >= 2:   # rate_constant.d:135-145, 181-229, 310-333
+                    d = r['frc']
+                    k0 = d['k0']
+                    flags = 0
+                    Fc = a = T1 = T2 = T3 = 0.0
+                    if fm == 3:
+                        if d.get('F_cent') is not None:
+                            flags, Fc = 1, float(d['F_cent'])
+                        else:
+                            a, T3 = float(d['a']), float(d['T3'])
+                            if d.get('T1') is not None:
+                                flags |= 2; T1 = float(d['T1'])
+                            if d.get('T2') is not None:
+                                flags |= 4; T2 = float(d['T2'])
+                    elif fm == 4:
+                        a, T1, T2 = float(d['a']), float(d['b']), float(d['c'])
+                    L.oracle_set_pressure_dependent(self.h, ir, float(k0['A']), float(k0['n']), float(k0['C']), Fc, a,
+                                                    T1, T2, T3, flags)
             ode = cfg['odeStep']
             lim = cfg['tempLimits']
             T_lo, T_hi = (lim['lower'], lim['upper']) if T_limits is None else T_limits
@@ -183,9 +208,11 @@ class Oracle:
         return T, pp, st
 
     # --- kinetics -----------------------------------------------------------------------
-    def rate_constants(self, T):
+    def rate_constants(self, T, conc=None):
+        """k_f, k_b at T; conc (mol/m^3) gives the third bodies of pressure-dependent rates."""
         kf = np.empty(self.nr); kb = np.empty(self.nr)
-        rc = lib().oracle_rate_constants(self.h, T, _dp(kf), _dp(kb))
+        c = None if conc is None else _dp(np.ascontiguousarray(conc, np.float64))
+        rc = lib().oracle_rate_constants(self.h, T, c, _dp(kf), _dp(kb))
         if rc:
             raise ValueError("rate constants failed (%d)" % rc)
         return kf, kb

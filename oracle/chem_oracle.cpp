@@ -19,6 +19,9 @@
 //                                        update_density 386-390, internal_energy 406-413,
 //                                        constant_volume_specific_heat 416-423,
 //                                        update_temperature_from_energy 426-468
+//   src/kinetics/rate_constant.d        Arrhenius 72-75, third-body concentration 114-121,
+//                                        Lindemann-Hinshelwood 155-160, Troe 258-287,
+//                                        Yungster-Rabinowitz 338-350
 //   src/gas/gas_model.d                  massf2conc 237-253, conc2massf 255-271, mass_average 410-418
 //   src/gas/physical_constants.d         R_universal, P_atm 13-16
 //   src/lmr/fluidfvcell.d                thermochemical_increment 883-997 (caller contract:
@@ -126,7 +129,14 @@ struct CEACurve {
     }
 };
 
-struct RateConst { int model = 0; double A = 0, n = 0, C = 0; };  // model 0 Arrhenius, 1 fromEqConst
+// model 0 Arrhenius, 1 fromEqConst, and the pressure-dependent 2 Lindemann-Hinshelwood, 3 Troe,
+// 4 Yungster-Rabinowitz (A, n, C are then k_inf; yr a, b, c are held in a, T1, T2)
+struct RateConst {
+    int model = 0;
+    double A = 0, n = 0, C = 0;
+    double A0 = 0, n0 = 0, C0 = 0, Fcent = 0, a = 0, T1 = 0, T2 = 0, T3 = 0;
+    int flags = 0;   // Troe: 1 F_cent given, 2 T1 given, 4 T2 given
+};
 
 // D's pow(double, int): binary exponentiation (std.math.exponential), here in double.
 inline double ipow(double x, int n) {
@@ -144,6 +154,41 @@ inline double ipow(double x, int n) {
 
 // rate_constant.d:72-75
 inline double arrhenius(const RateConst& rc, double T) { return rc.A * std::pow(T, rc.n) * std::exp(-rc.C / T); }
+inline double arrhenius0(const RateConst& rc, double T) { return rc.A0 * std::pow(T, rc.n0) * std::exp(-rc.C0 / T); }
+
+// Pressure-dependent rate constants with third-body concentration M (rate_constant.d:114-121 forms
+// M = sum eff * massf * rho / M_i): Lindemann-Hinshelwood 155-160, Troe 258-287, Yungster-Rabinowitz 338-350.
+inline double pressure_dependent(const RateConst& rc, double T, double M) {
+    double kInf = arrhenius(rc, T);
+    double k0 = arrhenius0(rc, T);
+    if (rc.model == 2) return k0 * kInf * M / (k0 * M + kInf);
+    const double essentially_zero = 1.0e-30;
+    if (rc.model == 3) {
+        double p_r = k0 * M / kInf;
+        double log_p_r = std::log10(std::fmax(p_r, essentially_zero));
+        double Fcent = rc.Fcent;
+        if (!(rc.flags & 1)) {
+            Fcent = (1.0 - rc.a) * std::exp(-T / rc.T3);
+            if (rc.flags & 2) Fcent += rc.a * std::exp(-T / rc.T1);
+            if (rc.flags & 4) Fcent += std::exp(-rc.T2 / T);
+        }
+        double log_F_cent = std::log10(std::fmax(Fcent, essentially_zero));
+        double c = -0.4 - 0.67 * log_F_cent;
+        double n = 0.75 - 1.27 * log_F_cent;
+        double d = 0.14;
+        double numer = log_p_r + c;
+        double denom = n - d * numer;
+        double frac = numer / denom;
+        double log_F = log_F_cent / (1.0 + frac * frac);
+        double F = std::pow(10.0, log_F);
+        return F * k0 * kInf * M / (k0 * M + kInf);
+    }
+    double p_r = k0 * M / kInf;
+    double log_p_r = std::log(p_r);
+    double Fc = rc.a * std::exp(-rc.T1 / T) + (1.0 - rc.a) * std::exp(-rc.T2 / T);
+    double xt = 1.0 / (1.0 + log_p_r * log_p_r);
+    return kInf * (p_r / (1.0 + p_r)) * Fc * xt;
+}
 
 struct Reaction {
     bool collider = false;
@@ -227,8 +272,9 @@ struct Work {
         double pw = (nsi == std::floor(nsi) && std::fabs(nsi) < 32768.0) ? ipow(base, (int)nsi) : std::pow(base, nsi);
         return K_p * pw;
     }
-    // reaction_mechanism.d:49-63 and reaction.d:94-143 (single-temperature gas: n_modes == 0)
-    void rate_constants(double Tq) {
+    // reaction_mechanism.d:49-63 and reaction.d:94-143 (single-temperature gas: n_modes == 0).
+    // tbc[i] = Q.massf[i] * Q.rho / M_i, the third-body terms of pressure-dependent rates.
+    void rate_constants(double Tq, const double* tbc) {
         cnt.kc++;
         double T = Tq;
         if (T < m.T_lower) T = m.T_lower;
@@ -236,8 +282,14 @@ struct Work {
         gibbs(T);
         for (size_t ir = 0; ir < m.reactions.size(); ++ir) {
             const Reaction& r = m.reactions[ir];
-            if (r.frc.model == 0) {
-                kf[ir] = arrhenius(r.frc, T);
+            if (r.frc.model == 0 || r.frc.model >= 2) {
+                if (r.frc.model == 0) {
+                    kf[ir] = arrhenius(r.frc, T);
+                } else {
+                    double M = 0.0;
+                    for (auto& e : r.eff) M += e.second * tbc[e.first];
+                    kf[ir] = pressure_dependent(r.frc, T, M);
+                }
                 if (r.brc.model == 1) kb[ir] = kf[ir] / Kc(r, T);
                 else kb[ir] = arrhenius(r.brc, T);
             } else {
@@ -416,6 +468,11 @@ struct Work {
     }
 
     // gas_model.d:237-253
+    double tb[64];
+    const double* third_body_terms(const Cell& Q) {   // rate_constant.d:117-119
+        for (int i = 0; i < m.nsp; ++i) tb[i] = Q.massf[i] * Q.rho / m.M[i];
+        return tb;
+    }
     void massf2conc(const Cell& Q, double* c) const {
         if (std::isnan(Q.rho) || Q.rho <= 0.0) throw Failure{ST_BAD_INPUT};
         for (int i = 0; i < m.nsp; ++i) {
@@ -486,7 +543,7 @@ struct Work {
         double conc0[64], concOut[64];
         try {
             massf2conc(Q, conc0);
-            rate_constants(Q.T);
+            rate_constants(Q.T, third_body_terms(Q));
             double t = 0.0, h, dtSave = dtSuggest;
             if (dtSuggest > tInterval) h = tInterval;
             else if (dtSuggest <= 0.0) h = estimate_step(conc0);
@@ -520,7 +577,7 @@ struct Work {
                 if (m.tight) {
                     conc2massf(conc0, Q);
                     update_from_rhou(Q);
-                    rate_constants(Q.T);
+                    rate_constants(Q.T, third_body_terms(Q));
                 }
                 if (t >= tInterval) {
                     if (cycle == 0) dtSave = dtSuggest;
@@ -582,7 +639,8 @@ int oracle_set_species(void* h, int isp, double M, int nseg, const double* break
     return 0;
 }
 
-// One reaction (reaction.d:478-535).  frc_model/brc_model: 0 Arrhenius, 1 fromEqConst.
+// One reaction (reaction.d:478-535).  frc_model/brc_model: 0 Arrhenius, 1 fromEqConst; frc_model
+// 2-4 pressure-dependent (see RateConst; completed by oracle_set_pressure_dependent).
 int oracle_add_reaction(void* h, int collider, int frc_model, double fA, double fn, double fC,
                         int brc_model, double bA, double bn, double bC,
                         int nreac, const int* reac_idx, const int* reac_coeff,
@@ -591,8 +649,8 @@ int oracle_add_reaction(void* h, int collider, int frc_model, double fA, double 
     Model* m = (Model*)h;
     Reaction r;
     r.collider = collider != 0;
-    r.frc = {frc_model, fA, fn, fC};
-    r.brc = {brc_model, bA, bn, bC};
+    r.frc.model = frc_model; r.frc.A = fA; r.frc.n = fn; r.frc.C = fC;
+    r.brc.model = brc_model; r.brc.A = bA; r.brc.n = bn; r.brc.C = bC;
     std::vector<int> part;
     for (int i = 0; i < nreac; ++i) { r.reactants.push_back({reac_idx[i], reac_coeff[i]}); part.push_back(reac_idx[i]); }
     for (int i = 0; i < nprod; ++i) { r.products.push_back({prod_idx[i], prod_coeff[i]}); part.push_back(prod_idx[i]); }
@@ -609,6 +667,18 @@ int oracle_add_reaction(void* h, int collider, int frc_model, double fA, double 
     for (int i = 0; i < neff; ++i) r.eff.push_back({eff_idx[i], eff_val[i]});
     m->reactions.push_back(r);
     return (int)m->reactions.size() - 1;
+}
+
+// k_0 and the Troe / Yungster-Rabinowitz parameters of reaction ir's forward rate constant
+// (its model and k_inf were given to oracle_add_reaction).
+int oracle_set_pressure_dependent(void* h, int ir, double A0, double n0, double C0, double Fcent, double a, double T1,
+                                  double T2, double T3, int flags) {
+    Model* m = (Model*)h;
+    if (ir < 0 || ir >= (int)m->reactions.size()) return -1;
+    RateConst& rc = m->reactions[ir].frc;
+    rc.A0 = A0; rc.n0 = n0; rc.C0 = C0; rc.Fcent = Fcent; rc.a = a; rc.T1 = T1; rc.T2 = T2; rc.T3 = T3;
+    rc.flags = flags;
+    return 0;
 }
 
 int oracle_set_config(void* h, double T_lower, double T_upper, int method, double errTol, double eps1, double eps2,
@@ -634,10 +704,11 @@ int oracle_species_thermo(void* h, int isp, double T, double* Cp, double* hh, do
 }
 
 // kf, kb at T (clamped to the mechanism's limits), as ReactionMechanism.eval_rate_constants.
-int oracle_rate_constants(void* h, double T, double* kf, double* kb) {
+// conc (may be NULL without pressure-dependent reactions) gives their third-body concentrations.
+int oracle_rate_constants(void* h, double T, const double* conc, double* kf, double* kb) {
     Model* m = (Model*)h;
     Work w(*m);
-    try { w.rate_constants(T); } catch (Failure& f) { return f.code; }
+    try { w.rate_constants(T, conc); } catch (Failure& f) { return f.code; }
     for (size_t i = 0; i < m->reactions.size(); ++i) { kf[i] = w.kf[i]; kb[i] = w.kb[i]; }
     return 0;
 }
@@ -646,7 +717,7 @@ int oracle_rate_constants(void* h, double T, double* kf, double* kb) {
 int oracle_split_rates(void* h, double T, const double* conc, double* q, double* L, double* wf, double* wb) {
     Model* m = (Model*)h;
     Work w(*m);
-    try { w.rate_constants(T); } catch (Failure& f) { return f.code; }
+    try { w.rate_constants(T, conc); } catch (Failure& f) { return f.code; }
     w.split_rates(conc, q, L);
     if (wf) for (size_t i = 0; i < m->reactions.size(); ++i) wf[i] = w.wf[i];
     if (wb) for (size_t i = 0; i < m->reactions.size(); ++i) wb[i] = w.wb[i];
@@ -656,7 +727,7 @@ int oracle_split_rates(void* h, double T, const double* conc, double* q, double*
 double oracle_estimate_step(void* h, double T, const double* conc) {
     Model* m = (Model*)h;
     Work w(*m);
-    w.rate_constants(T);
+    w.rate_constants(T, conc);
     return w.estimate_step(conc);
 }
 
@@ -666,7 +737,7 @@ int oracle_ode_step(void* h, int method, double T, const double* y0, double dt, 
     Model* m = (Model*)h;
     Model mm = *m; mm.method = method;
     Work w(mm);
-    w.rate_constants(T);
+    w.rate_constants(T, y0);
     return w.ode_step(y0, dt, yOut, *hSuggest) ? 1 : 0;
 }
 
@@ -676,7 +747,7 @@ int oracle_integrate_fixed(void* h, int method, double T, double* y, double dt, 
     Model* m = (Model*)h;
     Model mm = *m; mm.method = method;
     Work w(mm);
-    w.rate_constants(T);
+    w.rate_constants(T, y);
     double t = 0.0, dummy, y1[64];
     int count = 0;
     while ((tMax - t) > 1.0e-9) {

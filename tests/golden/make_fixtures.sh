@@ -27,14 +27,19 @@ mkdir -p "$WORK/dgd/data" "$WORK/dgd/lib"
     > "$WORK/dgd/data/species-database.lua"
 cp "$REF/src/gas/species-database/species-list.txt" "$WORK/dgd/data/"
 cp "$REF/src/kinetics/reaction.lua" "$REF/src/kinetics/lex_elems.lua" "$REF/src/kinetics/mechanism.lua" "$WORK/dgd/lib/"
+# The species check of reaction.lua (checkEquationSpecies) indexes every parsed participant, but the
+# '(+ M)' marker of a pressure-dependent reaction parses to a plain string, so prep_chem stops with
+# "Species nil ... not found".  In the scratch copy only, such entries are treated as the collider M.
+sed -i 's/local sp = p\[2\]$/local sp = type(p) == "table" and p[2] or "M"/' "$WORK/dgd/lib/reaction.lua"
 export DGD=$WORK/dgd
 export DGD_LUA_PATH="$WORK/dgd/lib/?.lua;;"
 export DGD_LUA_CPATH="$WORK/lua/install/lib/?.so;;"
 
 mkdir -p "$OUT"
 prep() {  # name gas-input mechanism-input
-    (cd "$WORK" && "$LUA" "$REF/src/gas/prep_gas.lua" "$2" "$1-gas.lua" > /dev/null \
-        && "$LUA" "$REF/src/kinetics/prep_chem.lua" "$1-gas.lua" "$3" "$1-chem.lua" > /dev/null)
+    (cd "$WORK" && "$LUA" "$REF/src/gas/prep_gas.lua" "$2" "$1-gas.lua" > "$WORK/$1-prep.log" 2>&1 \
+        && "$LUA" "$REF/src/kinetics/prep_chem.lua" "$1-gas.lua" "$3" "$1-chem.lua" >> "$WORK/$1-prep.log" 2>&1) \
+        || { cat "$WORK/$1-prep.log"; exit 1; }
     # Drop the time-stamp comment so that regenerated files compare equal.
     grep -v '^-- Auto-generated' "$WORK/$1-gas.lua" > "$OUT/$1-gas.lua"
     cp "$WORK/$1-chem.lua" "$OUT/$1-chem.lua"
@@ -44,6 +49,9 @@ prep park5  "$HERE/inputs/air5-park.inp"                              "$HERE/inp
 prep j92    "$KIN/hydrogen-ignition-delay/Jachimowski-1992-species.inp" "$KIN/hydrogen-ignition-delay/Jachimowski-1992.lua"
 prep n2     "$KIN/fixed-volume-reactor-n2/nitrogen-2sp.inp"            "$KIN/fixed-volume-reactor-n2/nitrogen-2sp-2r-Keq.lua"
 prep gupta5 "$KIN/air-chemistry-1T/air-5sp-1T.inp"                     "$KIN/air-chemistry-1T/GuptaEtAl-air-reactions.lua"
+# pressure-dependent (Troe) reactions: F_cent given (Stanford-2011), and a, T3, T1, T2 (DRM19 methane)
+prep stanford "$KIN/hydrogen-ignition-delay/Stanford-2011-species.inp"  "$KIN/hydrogen-ignition-delay/Stanford-2011.lua"
+prep drm19  "$KIN/methane-combustion-w-drm19/drm19-prep-gas.inp"       "$KIN/methane-combustion-w-drm19/drm19-prep-chem.inp"
 
 # Sample data of the reference's unit tests (known-answer tests).
 cp "$REF/src/kinetics/sample-input/H2-I2-HI.lua" "$OUT/h2i2-gas.lua"
@@ -51,5 +59,9 @@ cp "$REF/src/kinetics/sample-input/H2-I2-inp.lua" "$OUT/h2i2-chem.lua"
 cp "$REF/src/kinetics/sample-input/N2-diss.lua" "$OUT/n2-diss-rate.lua"
 cp "$REF/src/gas/sample-data/O-thermo.lua" "$OUT/O-thermo.lua"
 cp "$REF/src/gas/sample-data/therm-perf-5-species-air.lua" "$OUT/tpg-air5-gas.lua"
+# The DRM19 example's comparison data (Eilmer3's fixed-volume reactor, CH4:O2:N2 = 1:2:7.52 at 2000 K
+# and 1 atm, 2000 steps of 2e-7 s): time and temperature columns.
+grep -v '^[A-Za-z#]' "$KIN/methane-combustion-w-drm19/eilmer3-result-for-comparison.data" | awk '{print $1, $4}' \
+    > "$HERE/drm19-fvr-eilmer3-T.txt"
 chmod u+w "$OUT"/*.lua
 echo "fixtures written to $OUT"

@@ -32,7 +32,7 @@ def test_library_exports_every_declared_symbol():
     assert sorted(gdtk_gb300.SIGNATURES) == names
 
 
-@pytest.mark.parametrize("name", ["park5", "j92", "gupta5", "n2", "h2i2"])
+@pytest.mark.parametrize("name", ["park5", "j92", "gupta5", "n2", "h2i2", "stanford", "drm19"])
 def test_gas_model_reader_matches_oracle_reader(name):
     from gdtk_gb300.gas import GasModel
     gm = GasModel(mech(name + "-gas.lua"))
@@ -54,8 +54,8 @@ def test_reader_rejects_wrong_species_order(tmp_path):
 
 
 def test_unsupported_rate_model_is_refused(tmp_path):
-    src = open(mech("park5-chem.lua")).read().replace("model='Arrhenius', A=7.0", "model='Troe', A=7.0", 1)
-    bad = tmp_path / "troe.lua"
+    src = open(mech("park5-chem.lua")).read().replace("model='Arrhenius', A=7.0", "model='Park', A=7.0", 1)
+    bad = tmp_path / "park.lua"
     bad.write_text(src)
     L = gdtk_gb300.lib()
     n = L.gdtk_generate_fast_source(mech("park5-gas.lua").encode(), str(bad).encode(), None, 0)
@@ -90,7 +90,7 @@ def test_table_driven_exp_accuracy():
     assert y[-8] == 1.0
 
 
-@pytest.mark.parametrize("name", ["park5", "j92"])
+@pytest.mark.parametrize("name", ["park5", "j92", "stanford", "drm19"])
 def test_mechanism_kernel_compiles_for_sm103a(name):
     log = gdtk_gb300.compile_fast_source_check(mech(name + "-gas.lua"), mech(name + "-chem.lua"))
     assert "sm_103a" in log

@@ -402,3 +402,78 @@ def test_mixing_layer_split_steps_track_the_oracle(j92):
     assert np.abs(dY.cpu().numpy() - cY.T).max() <= Y_ABS
     assert (np.abs(dT.cpu().numpy() - cT) / cT).max() <= TP_REL
     assert (o["status"] == 0).any()
+
+
+def _premixed_cells(names, M, n, seed, majors, T_range=(1100.0, 2500.0), logp=(4.0, 6.0)):
+    """Seeded cells: the premixed `majors` (mole ratios) with a 10^U[-6, -2] share of the other
+    species (Dirichlet(0.5)), T ~ U[T_range], p = 10^U[logp]."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    x = np.zeros(len(names))
+    for s, v in majors.items():
+        x[names.index(s)] = v
+    y0 = x * M / (x * M).sum()
+    minor = [i for i, s in enumerate(names) if s not in majors]
+    Y = np.repeat(y0[None, :], n, axis=0)
+    share = 10.0 ** rng.uniform(-6.0, -2.0, n)
+    Y *= (1.0 - share)[:, None]
+    Y[:, minor] += share[:, None] * rng.dirichlet(np.full(len(minor), 0.5), n)
+    T = rng.uniform(T_range[0], T_range[1], n)
+    p = 10.0 ** rng.uniform(logp[0], logp[1], n)
+    return T, p, np.ascontiguousarray(Y.T)
+
+
+FALLOFF = {"stanford": {'H2': 2.0, 'O2': 1.0, 'N2': 3.76},          # Troe with F_cent given
+           "drm19": {'CH4': 1.0, 'O2': 2.0, 'N2': 7.52}}            # Troe with a, T3, T1, T2 (tight coupling)
+
+
+@pytest.mark.parametrize("kernel", sorted(KERNELS))
+@pytest.mark.parametrize("name", sorted(FALLOFF))
+def test_pressure_dependent_rates_parity(name, kernel):
+    """Troe falloff reactions (third-body concentration from the cell's own composition)."""
+    from gdtk_gb300.cells import ReactorCells
+    rc = ReactorCells(mech(name + "-gas.lua"), mech(name + "-chem.lua"))
+    orc = oracle.Oracle(mech(name + "-gas.lua"), mech(name + "-chem.lua"))
+    T, p, Y = _premixed_cells(rc.species_names, rc.mol_masses, 384, seed=31, majors=FALLOFF[name])
+    g, o, _, _ = run_pair(rc, orc, T, p, Y, 1.0e-6, kernel=kernel)
+    assert (g["status"] == 0).mean() > 0.95
+    assert_parity(g, o)
+
+
+def test_pressure_dependent_tickrates_match_oracle():
+    from gdtk_gb300.gas import GasModel, GasState, ReactionMechanism
+    gm = GasModel(mech("drm19-gas.lua"))
+    rm = ReactionMechanism(gm, mech("drm19-chem.lua"))
+    orc = oracle.Oracle(mech("drm19-gas.lua"), mech("drm19-chem.lua"))
+    gs = GasState(gm)
+    gs.T = 1800.0
+    gs.p = 3.0e5
+    gs.molef = {'CH4': 0.08, 'O2': 0.17, 'N2': 0.62, 'H2O': 0.05, 'CO': 0.03, 'CH3': 0.02, 'H': 0.02, 'OH': 0.01}
+    gs.update_thermo_from_pT()
+    f = np.array(rm.forward_tickrates(gs))
+    b = np.array(rm.backward_tickrates(gs))
+    conc = np.array(gs.conc)
+    _, _, wf, wb = orc.split_rates(1800.0, conc)
+    assert np.allclose(f, wf, rtol=1e-12, atol=0) and np.allclose(b, wb, rtol=1e-12, atol=0)
+
+
+def test_troe_fixed_volume_reactor_on_the_gpu_against_eilmer3():
+    """The DRM19 reactor of tests/test_oracle_kat.py, 1,999 chained updates through the GPU's
+    mechanism-specialised kernel: same bounds against the Eilmer3 history as the oracle's."""
+    import test_oracle_kat as kat
+    from gdtk_gb300.cells import ReactorCells
+    torch = torch_cuda()
+    rc = ReactorCells(mech("drm19-gas.lua"), mech("drm19-chem.lua"))
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+
+    def update(rho, u, T, p, Y, dtc, dt):
+        drho, du, dT, dp, ddt = to_dev(torch, rho, u, T, p, dtc)
+        dY = torch.tensor(np.ascontiguousarray(Y[:, None]), dtype=torch.float64, device="cuda")
+        rc.update(drho, du, dT, dp, dY, ddt, dt, status=st)
+        assert int(st.item()) == 0
+        return dT.cpu().numpy(), dp.cpu().numpy(), dY.cpu().numpy()[:, 0], ddt.cpu().numpy()
+
+    Ts = kat.drm19_fixed_volume_reactor(update)
+    rel, t_ign, t_ign_ref = kat.compare_with_eilmer3(Ts)
+    assert abs(t_ign - t_ign_ref) <= 0.01 * t_ign_ref
+    assert rel.max() < 0.03
+    assert rel[-1] < 2e-3
