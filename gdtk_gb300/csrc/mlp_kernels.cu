@@ -4,9 +4,10 @@
 // engine's own.
 //
 //   gemm:  D = alpha * op(A) * op(B) (+ bias) (+ beta * D), BF16 operands, FP32 accumulation,
-//          mma.sync.m16n8k16 on 64x64x32 block tiles staged through shared memory with 16-byte
-//          loads; epilogues: GELU (keeping the pre-activation), GELU backward; split-K with a
-//          fixed-order reduction for the weight gradients (K = batch).
+//          mma.sync.m16n8k16 on 128x64x32 block tiles fed by a 3-stage cp.async pipeline, fragments
+//          by ldmatrix (.trans for row-contiguous operands); epilogues: GELU (keeping the
+//          pre-activation), GELU backward; split-K with a fixed-order reduction for the weight
+//          gradients (K = batch).
 //   column sums (bias gradients), weighted squared-error gradient, AdamW, row gather, casts.
 //
 // The network's GEMMs are small (K, N <= 256): a training step over 8192 samples is about
@@ -22,8 +23,8 @@
 namespace gdtk {
 namespace {
 
-constexpr int BM = 64, BN = 64, BK = 32;
-constexpr int LDS = BK + 8;   // smem row stride in bf16 (80 bytes: conflict-free fragment loads)
+constexpr int BM = 128, BN = 64, BK = 32, STAGES = 3, THREADS = 256;
+constexpr int PADH = 8;   // bf16 padding per shared-memory row: rows of 80 or 272 bytes, conflict-free ldmatrix
 
 __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
     asm volatile(
@@ -31,6 +32,25 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], 
         "{%0,%1,%2,%3};\n"
         : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// 16-byte global -> shared copy; src_bytes = 0 fills the destination with zeros (out-of-range chunks)
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, int src_bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(smem_addr(dst)), "l"(src), "r"(src_bytes));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
+__device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const void* p) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]) : "r"(smem_addr(p)));
+}
+__device__ __forceinline__ void ldsm_x4_t(uint32_t (&r)[4], const void* p) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]) : "r"(smem_addr(p)));
 }
 
 // GELU, tanh form: 0.5 x (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3))), and its derivative.
@@ -45,49 +65,54 @@ __device__ __forceinline__ float gelu_grad(float x) {
     return 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * c * (1.0f + 3.0f * 0.044715f * x2);
 }
 
-// Stage a 64 x 32 tile of op(X) into S[64][LDS] (rows = the M or N index, columns = k).
-// row_major: X[r][k] at X[r * ld + k] (16-byte chunks along k); else X[k][r] at X[k * ld + r]
-// (chunks along r, transposed into shared memory).  Out-of-range rows and k read as zero.
-__device__ __forceinline__ void stage_tile(__nv_bfloat16 (*S)[LDS], const __nv_bfloat16* X, int ld, bool row_major,
-                                           int r0, int rows, int k0, int kend, int tid) {
-    const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
-    if (row_major) {
+// One pipeline stage of an operand tile: ROWS (M or N) x BK (k).  K-contiguous operands are kept
+// [ROWS][BK + PADH]; row-contiguous ones [BK][ROWS + PADH] and read back with ldmatrix.trans.
+template <int ROWS, bool KCONTIG>
+struct Tile {
+    static constexpr int ELEMS = KCONTIG ? ROWS * (BK + PADH) : BK * (ROWS + PADH);
+};
+
+// Issue the cp.async copies of one operand tile: rows [r0, r0 + ROWS) of op(X), k in [k0, k0 + BK)
+// clipped to kend.  Chunks of 8 bf16 along the contiguous dimension; out-of-range chunks read zeros.
+template <int ROWS, bool KCONTIG>
+__device__ __forceinline__ void load_tile(__nv_bfloat16* S, const __nv_bfloat16* X, int ld, int r0, int rows, int k0,
+                                          int kend, int tid) {
+    constexpr int CHUNKS = ROWS * BK / 8;
 #pragma unroll
-        for (int it = 0; it < 2; ++it) {
-            const int idx = tid + it * 128;     // 256 chunks: 64 rows x 4 chunks of 8
-            const int rr = idx >> 2, kc = (idx & 3) * 8;
+    for (int it = 0; it < (CHUNKS + THREADS - 1) / THREADS; ++it) {
+        const int idx = tid + it * THREADS;
+        if (idx >= CHUNKS) break;
+        if (KCONTIG) {   // X[r][k]
+            const int rr = idx / (BK / 8), kc = (idx % (BK / 8)) * 8;
             const int r = r0 + rr, k = k0 + kc;
-            uint4 v = zero;
-            if (r < rows && k < kend) v = *reinterpret_cast<const uint4*>(X + (size_t)r * ld + k);
-            *reinterpret_cast<uint4*>(&S[rr][kc]) = v;
-        }
-    } else {
-#pragma unroll
-        for (int it = 0; it < 2; ++it) {
-            const int idx = tid + it * 128;     // 256 chunks: 32 k-rows x 8 chunks of 8
-            const int kk = idx >> 3, rc = (idx & 7) * 8;
+            const bool in = r < rows && k < kend;
+            cp_async16(S + rr * (BK + PADH) + kc, in ? X + (size_t)r * ld + k : X, in ? 16 : 0);
+        } else {         // X[k][r]
+            const int kk = idx / (ROWS / 8), rc = (idx % (ROWS / 8)) * 8;
             const int k = k0 + kk, r = r0 + rc;
-            uint4 v = zero;
-            if (k < kend && r < rows) v = *reinterpret_cast<const uint4*>(X + (size_t)k * ld + r);
-            const __nv_bfloat16* e = reinterpret_cast<const __nv_bfloat16*>(&v);
-#pragma unroll
-            for (int j = 0; j < 8; ++j) S[rc + j][kk] = e[j];
+            const bool in = k < kend && r < rows;
+            cp_async16(S + kk * (ROWS + PADH) + rc, in ? X + (size_t)k * ld + r : X, in ? 16 : 0);
         }
     }
 }
 
-// 128 threads = 4 warps in 2 x 2; each warp computes a 32 x 32 sub-tile (2 m16 x 4 n8 mma tiles).
-__global__ void __launch_bounds__(128) gemm_bf16_kernel(const GemmArgs g) {
-    __shared__ __align__(16) __nv_bfloat16 As[BM][LDS];
-    __shared__ __align__(16) __nv_bfloat16 Bs[BN][LDS];
+// 256 threads = 8 warps in 4 (M) x 2 (N); each warp computes 32 x 32 (2 m16 x 4 n8 mma tiles).
+// A 3-stage cp.async pipeline feeds shared memory; fragments are loaded with ldmatrix (.trans for
+// row-contiguous operands).
+template <bool AK, bool BKC>
+__global__ void __launch_bounds__(THREADS) gemm_bf16_kernel(const GemmArgs g) {
+    __shared__ __align__(128) __nv_bfloat16 As[STAGES][Tile<BM, AK>::ELEMS];
+    __shared__ __align__(128) __nv_bfloat16 Bs[STAGES][Tile<BN, BKC>::ELEMS];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
     const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
     const int gid = lane >> 2, tig = lane & 3;
+    const int q = lane >> 3, r8 = lane & 7;
     // this block's K range (split-K over blockIdx.z, in BK multiples)
     const int kper = ((g.K + g.splits - 1) / g.splits + BK - 1) / BK * BK;
     const int kbeg = blockIdx.z * kper;
     const int kend = min(g.K, kbeg + kper);
+    const int nk = kend > kbeg ? (kend - kbeg + BK - 1) / BK : 0;
     float acc[2][4][4];
 #pragma unroll
     for (int i = 0; i < 2; ++i)
@@ -96,34 +121,49 @@ __global__ void __launch_bounds__(128) gemm_bf16_kernel(const GemmArgs g) {
 #pragma unroll
             for (int r = 0; r < 4; ++r) acc[i][j][r] = 0.f;
 
-    for (int k0 = kbeg; k0 < kend; k0 += BK) {
-        stage_tile(As, g.A, g.lda, !g.trans_a, m0, g.M, k0, kend, tid);
-        stage_tile(Bs, g.B, g.ldb, g.trans_b != 0, n0, g.N, k0, kend, tid);
+#pragma unroll
+    for (int st = 0; st < STAGES - 1; ++st) {
+        if (st < nk) {
+            load_tile<BM, AK>(As[st], g.A, g.lda, m0, g.M, kbeg + st * BK, kend, tid);
+            load_tile<BN, BKC>(Bs[st], g.B, g.ldb, n0, g.N, kbeg + st * BK, kend, tid);
+        }
+        cp_async_commit();
+    }
+    for (int kt = 0; kt < nk; ++kt) {
+        cp_async_wait<STAGES - 2>();
         __syncthreads();
+        const __nv_bfloat16* A_ = As[kt % STAGES];
+        const __nv_bfloat16* B_ = Bs[kt % STAGES];
 #pragma unroll
         for (int ks = 0; ks < BK; ks += 16) {
             uint32_t a[2][4], b[4][2];
 #pragma unroll
             for (int i = 0; i < 2; ++i) {
-                const int r = wm + i * 16 + gid;
-                a[i][0] = *reinterpret_cast<const uint32_t*>(&As[r][ks + 2 * tig]);
-                a[i][1] = *reinterpret_cast<const uint32_t*>(&As[r + 8][ks + 2 * tig]);
-                a[i][2] = *reinterpret_cast<const uint32_t*>(&As[r][ks + 2 * tig + 8]);
-                a[i][3] = *reinterpret_cast<const uint32_t*>(&As[r + 8][ks + 2 * tig + 8]);
+                const int mb = wm + i * 16;
+                if (AK) ldsm_x4(a[i], A_ + (mb + (lane & 15)) * (BK + PADH) + ks + ((lane >> 4) << 3));
+                else ldsm_x4_t(a[i], A_ + (ks + r8 + ((q >> 1) << 3)) * (BM + PADH) + mb + ((q & 1) << 3));
             }
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const int c = wn + j * 8 + gid;
-                b[j][0] = *reinterpret_cast<const uint32_t*>(&Bs[c][ks + 2 * tig]);
-                b[j][1] = *reinterpret_cast<const uint32_t*>(&Bs[c][ks + 2 * tig + 8]);
+            for (int j = 0; j < 4; j += 2) {
+                const int nb = wn + j * 8;
+                uint32_t t[4];
+                if (BKC) ldsm_x4(t, B_ + (nb + r8 + ((q >> 1) << 3)) * (BK + PADH) + ks + ((q & 1) << 3));
+                else ldsm_x4_t(t, B_ + (ks + r8 + ((q & 1) << 3)) * (BN + PADH) + nb + ((q >> 1) << 3));
+                b[j][0] = t[0]; b[j][1] = t[1]; b[j + 1][0] = t[2]; b[j + 1][1] = t[3];
             }
 #pragma unroll
             for (int i = 0; i < 2; ++i)
 #pragma unroll
                 for (int j = 0; j < 4; ++j) mma_bf16(acc[i][j], a[i], b[j]);
         }
-        __syncthreads();
+        const int nxt = kt + STAGES - 1;
+        if (nxt < nk) {
+            load_tile<BM, AK>(As[nxt % STAGES], g.A, g.lda, m0, g.M, kbeg + nxt * BK, kend, tid);
+            load_tile<BN, BKC>(Bs[nxt % STAGES], g.B, g.ldb, n0, g.N, kbeg + nxt * BK, kend, tid);
+        }
+        cp_async_commit();
     }
+    cp_async_wait<0>();
 
 #pragma unroll
     for (int i = 0; i < 2; ++i)
@@ -277,7 +317,11 @@ cudaError_t launch_gemm_bf16(const GemmArgs& g, cudaStream_t s) {
         return cudaErrorInvalidValue;
     dim3 grid((g.N + BN - 1) / BN, (g.M + BM - 1) / BM, g.splits);
     if (grid.y > 65535u || grid.z > 65535u) return cudaErrorInvalidConfiguration;
-    gemm_bf16_kernel<<<grid, 128, 0, s>>>(g);
+    const bool ak = !g.trans_a, bk = g.trans_b != 0;   // K-contiguous operands
+    if (ak && bk) gemm_bf16_kernel<true, true><<<grid, THREADS, 0, s>>>(g);
+    else if (ak) gemm_bf16_kernel<true, false><<<grid, THREADS, 0, s>>>(g);
+    else if (bk) gemm_bf16_kernel<false, true><<<grid, THREADS, 0, s>>>(g);
+    else gemm_bf16_kernel<false, false><<<grid, THREADS, 0, s>>>(g);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || g.splits == 1) return e;
     splitk_reduce_kernel<<<grid_for((size_t)g.M * g.N), 256, 0, s>>>(g.M, g.N, g.splits, g.work, g.alpha, g.beta, g.D,
