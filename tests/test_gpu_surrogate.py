@@ -261,3 +261,68 @@ def test_trained_network_gains_over_the_update_without_it(rc, trained):
     assert t["work"] < 0.9, results                # FP64 right-hand sides left to the fallback
     assert t["max_dY"] < 5e-3 and t["max_dT"] < 2e-2, results
     assert u["accepted"] < 0.1 * t["accepted"], results
+
+
+def test_surrogate_on_another_mechanism():
+    """The surrogate is mechanism-generic: 5-species air (elements N, O; RKF) trained briefly,
+    then updated with the fallback; accepted cells conserve N and O, rejected ones equal the
+    plain update."""
+    from gdtk_gb300.cells import ReactorCells
+    from gdtk_gb300.surrogate import ChemSurrogate, generate_samples
+    from gdtk_gb300.workloads import air5_cells
+    rc = ReactorCells(mech("park5-gas.lua"), mech("park5-chem.lua"))
+    sg = ChemSurrogate(rc, width=64, depth=2, seed=5)
+    assert (sg.nin, sg.nin_pad, sg.nout, sg.nout_pad, sg.n_elements) == (8, 8, 6, 8, 2)
+    X, Y, valid, _ = generate_samples(rc, sg, 131072, seed=3, block=32768, blocks_per_launch=4,
+                                      cells=lambda m, s: air5_cells(m, seed=s))
+    rows = torch.nonzero(valid).flatten().to(torch.int32)
+    sg.fit_normalisation(X, Y, rows)
+    hist = sg.train(X, Y, rows, epochs=4, batch=4096)
+    assert hist[-1] < hist[0]
+    sg.set_gate(elem_tol=1e-3, neg_tol=1e-4, T_tol=1e-2, max_dY=0.0)
+    T, p, Yc = air5_cells(4096, seed=99)
+    d = {"T": torch.tensor(T, device="cuda"), "p": torch.tensor(p, device="cuda"),
+         "massf": torch.tensor(np.ascontiguousarray(Yc), device="cuda")}
+    d["rho"], d["u"] = rc.thermo_from_pT(d["p"], d["T"], d["massf"])
+    d["dt_chem"] = torch.full((4096,), -1.0, dtype=torch.float64, device="cuda")
+    d["status"] = torch.zeros(4096, dtype=torch.int32, device="cuda")
+    d0 = _clone(d)
+    gate = torch.empty(4096, dtype=torch.int32, device="cuda")
+    res = sg.update(d["rho"], d["u"], d["T"], d["p"], d["massf"], d["dt_chem"], 1e-6, status=d["status"], gate=gate)
+    assert sum(res["gate"].values()) == 4096
+    rc.update(d0["rho"], d0["u"], d0["T"], d0["p"], d0["massf"], d0["dt_chem"], 1e-6, status=d0["status"])
+    codes = gate.cpu().numpy()
+    rej = torch.tensor(codes != 0, device="cuda")
+    assert torch.equal(d["massf"][:, rej], d0["massf"][:, rej]) and torch.equal(d["T"][rej], d0["T"][rej])
+    acc = codes == 0
+    if acc.any():
+        els, E, EM = sgate.element_matrix(mech("park5-gas.lua"))
+        dE = (E @ (d["massf"].cpu().numpy()[:, acc] - Yc[:, acc])) * EM[:, None]
+        assert np.abs(dE).max() < 1e-12
+
+
+def test_largest_batch_indexing():
+    """2^24 + 13 cells (a ragged size) in one call: a strided sample of cells, including the last,
+    matches the oracle."""
+    from gdtk_gb300.cells import ReactorCells
+    from gdtk_gb300.workloads import air5_cells
+    rc = ReactorCells(mech("park5-gas.lua"), mech("park5-chem.lua"))
+    orc = oracle.Oracle(mech("park5-gas.lua"), mech("park5-chem.lua"))
+    n = (1 << 24) + 13
+    T, p, Y = air5_cells(n, seed=12)
+    d = {"T": torch.tensor(T, device="cuda"), "p": torch.tensor(p, device="cuda"),
+         "massf": torch.tensor(np.ascontiguousarray(Y), device="cuda")}
+    d["rho"], d["u"] = rc.thermo_from_pT(d["p"], d["T"], d["massf"])
+    d["dt_chem"] = torch.full((n,), -1.0, dtype=torch.float64, device="cuda")
+    d["status"] = torch.zeros(n, dtype=torch.int32, device="cuda")
+    rho, u = d["rho"].cpu().numpy(), d["u"].cpu().numpy()
+    rc.update(d["rho"], d["u"], d["T"], d["p"], d["massf"], d["dt_chem"], 1e-6, status=d["status"])
+    idx = np.concatenate([np.arange(0, n, n // 2000), [n - 1]])
+    o = orc.chem_update(rho[idx], u[idx], T[idx], p[idx], Y[:, idx].T, np.full(len(idx), -1.0), 1e-6)
+    g_st = d["status"].cpu().numpy()[idx]
+    assert np.array_equal(g_st, o["status"])
+    ok = g_st == 0
+    gY = d["massf"].cpu().numpy()[:, idx].T
+    assert np.abs(gY[ok] - o["massf"][ok]).max() <= 1e-8
+    gT = d["T"].cpu().numpy()[idx]
+    assert (np.abs(gT[ok] - o["T"][ok]) / o["T"][ok]).max() <= 1e-7
