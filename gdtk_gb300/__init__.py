@@ -101,6 +101,16 @@ SIGNATURES = {
     "chem_surrogate_update_cells": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _v, _v, _v, _v, _v, _v, _v,
                                                    ctypes.c_double, ctypes.c_double, ctypes.c_int, _v, _v, _v,
                                                    ctypes.c_int, _v]),
+    "chem_surrogate_error_model_new": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_ulonglong]),
+    "chem_surrogate_error_dims": (ctypes.c_int, [ctypes.c_int, _i]),
+    "chem_surrogate_error_get_params": (ctypes.c_int, [ctypes.c_int, _v]),
+    "chem_surrogate_error_set_params": (ctypes.c_int, [ctypes.c_int, _v]),
+    "chem_surrogate_error_train_step": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _v, _v, _v, ctypes.c_float,
+                                                       ctypes.c_float, ctypes.c_float, _v, _v]),
+    "chem_surrogate_error_gradients": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _v, _v, _v, ctypes.c_float, _v, _v,
+                                                      _v]),
+    "chem_surrogate_predict_error": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _v, _v, _v]),
+    "chem_surrogate_set_error_gate": (ctypes.c_int, [ctypes.c_int, ctypes.c_double]),
     "gdtk_mlp_gemm": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _v, ctypes.c_int, ctypes.c_int, _v,
                                      ctypes.c_int, ctypes.c_int, _v, ctypes.c_int, _v, _v, _v, ctypes.c_int,
                                      ctypes.c_int, _v]),

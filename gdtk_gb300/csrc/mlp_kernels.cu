@@ -296,6 +296,57 @@ __global__ void affine_columns_kernel(int n, int w, const float* shift, const fl
     }
 }
 
+// feat[r] = [xh[r][0..nin), bf16(out[r][0..nout))]: the error network's input
+__global__ void error_features_kernel(int B, const __nv_bfloat16* xh, int nin, const float* out, int nout,
+                                      __nv_bfloat16* feat) {
+    const int w = nin + nout;
+    const size_t total = (size_t)B * w;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const size_t r = i / w;
+        const int c = (int)(i % w);
+        feat[i] = c < nin ? xh[r * nin + c] : __float2bfloat16(out[r * nout + (c - nin)]);
+    }
+}
+
+// tgt[r][0] = log10(max_s |(out[r][s] - y[r][s]) y_scale[s]| + 1e-12) over the nsp mass-fraction
+// outputs (the raw-unit error of the standardised prediction out against the target y); other
+// columns of the w-wide row are zero.
+__global__ void error_targets_kernel(int B, const float* out, const float* y, int ld, const float* y_scale, int nsp,
+                                     float* tgt, int w) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < B; r += gridDim.x * blockDim.x) {
+        float e = 0.f;
+        for (int k = 0; k < nsp; ++k) e = fmaxf(e, fabsf((out[(size_t)r * ld + k] - y[(size_t)r * ld + k]) * y_scale[k]));
+        tgt[(size_t)r * w] = log10f(e + 1e-12f);
+        for (int c = 1; c < w; ++c) tgt[(size_t)r * w + c] = 0.f;
+    }
+}
+
+// Pinball (quantile) loss of column 0 of pred[B][w] against tgt: loss_sum += max(tau r, (tau - 1) r),
+// r = tgt - pred; grad = d(mean loss)/d pred = (r > 0 ? -tau : 1 - tau) / B (other columns 0).
+__global__ void pinball_grad_kernel(int B, int w, const float* pred, const float* tgt, float tau, float* grad,
+                                    __nv_bfloat16* gradh, float* loss_sum) {
+    float local = 0.f;
+    const size_t total = (size_t)B * w;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        float gv = 0.f;
+        if (i % w == 0) {
+            const float r = tgt[i] - pred[i];
+            local += r > 0.f ? tau * r : (tau - 1.f) * r;
+            gv = (r > 0.f ? -tau : 1.f - tau) / (float)B;
+        }
+        grad[i] = gv;
+        gradh[i] = __float2bfloat16(gv);
+    }
+    if (loss_sum) {
+        for (int off = 16; off > 0; off >>= 1) local += __shfl_down_sync(0xffffffffu, local, off);
+        if ((threadIdx.x & 31) == 0) atomicAdd(loss_sum, local);
+    }
+}
+
+__global__ void copy_column_kernel(int n, const float* x, int ld, int col, float* out) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) out[r] = x[(size_t)r * ld + col];
+}
+
 int grid_for(size_t count) {
     size_t g = (count + 255) / 256;
     return (int)(g > 8192 ? 8192 : (g < 1 ? 1 : g));
@@ -373,6 +424,33 @@ cudaError_t launch_gather_rows(int n, const int* idx, const float* X, int ldx, c
 cudaError_t launch_affine_columns(int n, int w, const float* shift, const float* scale, float* x, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
     affine_columns_kernel<<<grid_for((size_t)n * w), 256, 0, s>>>(n, w, shift, scale, x);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_error_features(int B, const __nv_bfloat16* xh, int nin, const float* out, int nout,
+                                  __nv_bfloat16* feat, cudaStream_t s) {
+    if (B <= 0) return cudaSuccess;
+    error_features_kernel<<<grid_for((size_t)B * (nin + nout)), 256, 0, s>>>(B, xh, nin, out, nout, feat);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_error_targets(int B, const float* out, const float* y, int ld, const float* y_scale, int nsp,
+                                 float* tgt, int w, cudaStream_t s) {
+    if (B <= 0) return cudaSuccess;
+    error_targets_kernel<<<grid_for((size_t)B), 256, 0, s>>>(B, out, y, ld, y_scale, nsp, tgt, w);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pinball_grad(int B, int w, const float* pred, const float* tgt, float tau, float* grad,
+                                __nv_bfloat16* gradh, float* loss_sum, cudaStream_t s) {
+    if (B <= 0) return cudaSuccess;
+    pinball_grad_kernel<<<grid_for((size_t)B * w), 256, 0, s>>>(B, w, pred, tgt, tau, grad, gradh, loss_sum);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_copy_column(int n, const float* x, int ld, int col, float* out, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    copy_column_kernel<<<grid_for((size_t)n), 256, 0, s>>>(n, x, ld, col, out);
     return cudaGetLastError();
 }
 

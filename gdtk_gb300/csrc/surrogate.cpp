@@ -60,46 +60,77 @@ double atomic_mass(const std::string& e) {
 
 int pad8(int n) { return (n + 7) / 8 * 8; }
 
-struct Surrogate {
-    int cr = -1;
-    int nsp = 0, nin = 0, nin_pad = 0, nout = 0, nout_pad = 0, width = 0, depth = 0, ne = 0;
-    std::vector<int> dims;                 // d_0 = nin_pad, d_1..d_depth = width, d_{depth+1} = nout_pad
+void gemm(int M, int N, int K, const __nv_bfloat16* A, int lda, int ta, const __nv_bfloat16* B, int ldb, int tb,
+          const float* bias, int act, const float* pre_in, float* pre, float* D, __nv_bfloat16* Dh, int ldd,
+          cudaStream_t s, int splits = 1, float* work = nullptr) {
+    GemmArgs g;
+    g.M = M; g.N = N; g.K = K;
+    g.A = A; g.lda = lda; g.trans_a = ta;
+    g.B = B; g.ldb = ldb; g.trans_b = tb;
+    g.bias = bias; g.act = act; g.pre_in = pre_in; g.pre = pre;
+    g.D = D; g.Dh = Dh; g.ldd = ldd;
+    g.splits = splits; g.work = work;
+    ck(launch_gemm_bf16(g, s), "surrogate GEMM");
+}
+
+// A multilayer perceptron: nin_pad -> depth x width (GELU) -> nout_pad, BF16 weights and
+// activations, FP32 master parameters and AdamW moments.  Parameters are one flat array:
+// W_0 .. W_depth (row-major [fan_out][fan_in]), then b_0 .. b_depth.
+struct Mlp {
+    int nin = 0, nout = 0, nin_pad = 0, nout_pad = 0, width = 0, depth = 0;
+    std::vector<int> dims;   // d_0 = nin_pad, d_1..d_depth = width, d_{depth+1} = nout_pad
     std::vector<size_t> w_off, b_off;
     size_t n_params = 0, n_weights = 0;
     Buf<float> params, grad, adam_m, adam_v;
     Buf<__nv_bfloat16> params_h;
     int step = 0;
-    // standardisation and domain (host copies + device)
-    std::vector<float> xs, xd, ys, yd, lw;
-    std::vector<double> xmin, xmax;
-    Buf<float> d_xs, d_xd, d_ys, d_yd, d_lw;
-    Buf<double> d_xmin, d_xmax, d_elem, d_elemM;
-    double elem_tol = 1e-4, neg_tol = 1e-5, T_tol = 1e-3, max_dY = 5e-4;
-    // training buffers
-    int tb = 0;
-    Buf<__nv_bfloat16> t_xh, t_act, t_g16a, t_g16b, t_dout16;
-    Buf<float> t_y, t_pre, t_out, t_dout, t_dpre, t_work, t_colpart;
-    // inference buffers
-    int ib = 0;
-    Buf<__nv_bfloat16> i_xh, i_a0, i_a1;
-    Buf<float> i_out;
-    Buf<int> gate, reject, counters, fails, mon_idx, cstatus, mstatus;
-    Buf<unsigned long long> code_counts, mon_res;
-    Buf<double> compact, mon_state, mon_compact, mon_sum;
-    Buf<double> stats_partial, stats_out;
+    int tb = 0;   // training buffers, for batches up to tb rows
+    Buf<__nv_bfloat16> t_act, t_g16a, t_g16b, t_dout16;
+    Buf<float> t_pre, t_out, t_dout, t_dpre, t_work, t_colpart;
+    int ib = 0;   // inference buffers, for chunks up to ib rows
+    Buf<__nv_bfloat16> i_a0, i_a1;
+
+    // initial parameters: U(-1/sqrt(fan_in), 1/sqrt(fan_in)) over the real (unpadded) fan-in;
+    // padded input columns and output rows start at zero
+    void init(int nin_, int nout_, int width_, int depth_, unsigned long long seed) {
+        nin = nin_; nout = nout_; nin_pad = pad8(nin_); nout_pad = pad8(nout_); width = width_; depth = depth_;
+        dims.assign(1, nin_pad);
+        for (int l = 0; l < depth; ++l) dims.push_back(width);
+        dims.push_back(nout_pad);
+        size_t off = 0;
+        for (int l = 0; l <= depth; ++l) {
+            w_off.push_back(off);
+            off += (size_t)dims[l] * dims[l + 1];
+        }
+        n_weights = off;
+        for (int l = 0; l <= depth; ++l) {
+            b_off.push_back(off);
+            off += dims[l + 1];
+        }
+        n_params = off;
+        std::vector<float> h(n_params, 0.f);
+        std::mt19937_64 rng(seed);
+        for (int l = 0; l <= depth; ++l) {
+            const int fin = l == 0 ? nin : dims[l];
+            const int fout = l == depth ? nout : dims[l + 1];
+            const float bound = 1.f / std::sqrt((float)fin);
+            std::uniform_real_distribution<float> U(-bound, bound);
+            for (int o = 0; o < fout; ++o)
+                for (int k = 0; k < fin; ++k) h[w_off[l] + (size_t)o * dims[l] + k] = U(rng);
+            for (int o = 0; o < fout; ++o) h[b_off[l] + o] = U(rng);
+        }
+        params.ensure(n_params);
+        grad.ensure(n_params);
+        adam_m.ensure(n_params);
+        adam_v.ensure(n_params);
+        params_h.ensure(n_params);
+        ck(cudaMemcpy(params.p, h.data(), n_params * 4, cudaMemcpyHostToDevice), "H2D");
+        reset_adam();
+        refresh_bf16(nullptr);
+    }
 
     __nv_bfloat16* W16(int l) { return params_h.p + w_off[l]; }
     float* bias(int l) { return params.p + b_off[l]; }
-
-    void upload_norm() {
-        ck(cudaMemcpy(d_xs.ensure(nin_pad), xs.data(), nin_pad * 4, cudaMemcpyHostToDevice), "H2D");
-        ck(cudaMemcpy(d_xd.ensure(nin_pad), xd.data(), nin_pad * 4, cudaMemcpyHostToDevice), "H2D");
-        ck(cudaMemcpy(d_ys.ensure(nout_pad), ys.data(), nout_pad * 4, cudaMemcpyHostToDevice), "H2D");
-        ck(cudaMemcpy(d_yd.ensure(nout_pad), yd.data(), nout_pad * 4, cudaMemcpyHostToDevice), "H2D");
-        ck(cudaMemcpy(d_lw.ensure(nout_pad), lw.data(), nout_pad * 4, cudaMemcpyHostToDevice), "H2D");
-        ck(cudaMemcpy(d_xmin.ensure(nin_pad), xmin.data(), nin_pad * 8, cudaMemcpyHostToDevice), "H2D");
-        ck(cudaMemcpy(d_xmax.ensure(nin_pad), xmax.data(), nin_pad * 8, cudaMemcpyHostToDevice), "H2D");
-    }
 
     void reset_adam() {
         ck(cudaMemset(adam_m.p, 0, n_params * 4), "cudaMemset");
@@ -109,25 +140,10 @@ struct Surrogate {
 
     void refresh_bf16(cudaStream_t s) { ck(launch_cast_bf16((int)n_params, params.p, params_h.p, s), "cast"); }
 
-    void gemm(int M, int N, int K, const __nv_bfloat16* A, int lda, int ta, const __nv_bfloat16* B, int ldb, int tb_,
-              const float* bias_, int act, const float* pre_in, float* pre, float* D, __nv_bfloat16* Dh, int ldd,
-              cudaStream_t s, int splits = 1, float* work = nullptr) {
-        GemmArgs g;
-        g.M = M; g.N = N; g.K = K;
-        g.A = A; g.lda = lda; g.trans_a = ta;
-        g.B = B; g.ldb = ldb; g.trans_b = tb_;
-        g.bias = bias_; g.act = act; g.pre_in = pre_in; g.pre = pre;
-        g.D = D; g.Dh = Dh; g.ldd = ldd;
-        g.splits = splits; g.work = work;
-        ck(launch_gemm_bf16(g, s), "surrogate GEMM");
-    }
-
     void ensure_train(int B) {
         if (B <= tb) return;
         tb = B;
         const size_t W = width;
-        t_xh.ensure((size_t)B * nin_pad);
-        t_y.ensure((size_t)B * nout_pad);
         t_act.ensure((size_t)depth * B * W);
         t_pre.ensure((size_t)depth * B * W);
         t_out.ensure((size_t)B * nout_pad);
@@ -140,9 +156,18 @@ struct Surrogate {
         t_colpart.ensure((size_t)column_sum_partials(B) * std::max<size_t>(W, nout_pad));
     }
 
-    // forward over B rows of standardised bf16 inputs xh; training keeps every layer's
-    // pre-activation and activation.  Returns the fp32 standardised output.
+    void ensure_infer(int chunk) {
+        if (chunk <= ib) return;
+        ib = chunk;
+        i_a0.ensure((size_t)chunk * width);
+        i_a1.ensure((size_t)chunk * width);
+    }
+
+    // forward over B rows of bf16 inputs xh; training (into t_out) keeps every layer's
+    // pre-activation and activation.  The fp32 output goes to out.
     void forward(int B, const __nv_bfloat16* xh, bool train, float* out, cudaStream_t s) {
+        if (train) ensure_train(B);
+        else ensure_infer(B);
         const __nv_bfloat16* in = xh;
         for (int l = 0; l < depth; ++l) {
             __nv_bfloat16* act;
@@ -161,27 +186,22 @@ struct Surrogate {
              nullptr, nullptr, out, nullptr, dims[depth + 1], s);
     }
 
-    int splits_for(int M, int N, int K, int sm) const {
-        const int tiles = ((M + 63) / 64) * ((N + 63) / 64);
+    static int splits_for(int M, int N, int K, int sm) {
+        const int tiles = ((M + 127) / 128) * ((N + 63) / 64);
         int sp = (2 * sm + tiles - 1) / tiles;
         sp = std::min(sp, std::max(1, K / 256));
         return std::max(1, std::min(sp, 32));
     }
 
-    // loss, gradient into `grad` (device, n_params)
-    void loss_and_grad(int B, const float* X, const float* Y, const int* rows, float* loss_sum, cudaStream_t s,
-                       int sm) {
-        ensure_train(B);
-        ck(launch_gather_rows(B, rows, X, nin_pad, d_xs.p, d_xd.p, t_xh.p, Y, nout_pad, d_ys.p, d_yd.p, t_y.p, s),
-           "gather rows");
-        forward(B, t_xh.p, true, t_out.p, s);
-        ck(launch_mse_grad(B, nout_pad, t_out.p, t_y.p, d_lw.p, t_dout.p, t_dout16.p, loss_sum, s), "loss");
+    // gradient into `grad` from the output gradient in t_dout (fp32) / t_dout16 (bf16), after a
+    // training forward over the same B rows of inputs xh
+    void backward(int B, const __nv_bfloat16* xh, cudaStream_t s, int sm) {
         const float* g32 = t_dout.p;
         const __nv_bfloat16* g16 = t_dout16.p;
         __nv_bfloat16* nxt = t_g16a.p;
         for (int l = depth; l >= 0; --l) {
             const int din = dims[l], dout = dims[l + 1];
-            const __nv_bfloat16* in16 = l == 0 ? t_xh.p : t_act.p + (size_t)(l - 1) * B * width;
+            const __nv_bfloat16* in16 = l == 0 ? xh : t_act.p + (size_t)(l - 1) * B * width;
             ck(launch_column_sum(B, dout, g32, t_colpart.p, grad.p + b_off[l], s), "bias gradient");
             const int sp = splits_for(dout, din, B, sm);
             gemm(dout, din, B, g16, dout, 1, in16, din, 0, nullptr, ACT_NONE, nullptr, nullptr, grad.p + w_off[l],
@@ -196,12 +216,95 @@ struct Surrogate {
         }
     }
 
+    // AdamW (beta 0.9, 0.999, eps 1e-8); weight decay on the weights, not the biases
+    void adam(float lr, float wd, cudaStream_t s) {
+        ++step;
+        ck(launch_adamw((int)n_weights, params.p, grad.p, adam_m.p, adam_v.p, params_h.p, lr, 0.9f, 0.999f, 1e-8f, wd,
+                        step, s),
+           "adamw");
+        const size_t nb = n_params - n_weights;
+        ck(launch_adamw((int)nb, params.p + n_weights, grad.p + n_weights, adam_m.p + n_weights,
+                        adam_v.p + n_weights, params_h.p + n_weights, lr, 0.9f, 0.999f, 1e-8f, 0.f, step, s),
+           "adamw");
+    }
+};
+
+struct Surrogate {
+    int cr = -1;
+    int nsp = 0, nin = 0, nin_pad = 0, nout = 0, nout_pad = 0, ne = 0;
+    Mlp net;                    // state -> increment
+    std::unique_ptr<Mlp> err;   // (standardised state, standardised increment) -> log10 of the increment's error
+    double err_log10_tol = 0.0;
+    bool err_gate = false;
+    // standardisation and domain (host copies + device)
+    std::vector<float> xs, xd, ys, yd, lw;
+    std::vector<double> xmin, xmax;
+    Buf<float> d_xs, d_xd, d_ys, d_yd, d_lw;
+    Buf<double> d_xmin, d_xmax, d_elem, d_elemM;
+    double elem_tol = 1e-4, neg_tol = 1e-5, T_tol = 1e-3, max_dY = 5e-4;
+    // training inputs of the current batch (standardised)
+    Buf<__nv_bfloat16> t_xh, e_xh;
+    Buf<float> t_y, e_main, e_tgt;
+    // inference buffers
+    int ib = 0;
+    Buf<__nv_bfloat16> i_xh, i_exh;
+    Buf<float> i_out, i_err;
+    Buf<int> gate, reject, counters, fails, mon_idx, cstatus, mstatus;
+    Buf<unsigned long long> code_counts, mon_res;
+    Buf<double> compact, mon_state, mon_compact, mon_sum;
+    Buf<double> stats_partial, stats_out;
+
+    void upload_norm() {
+        ck(cudaMemcpy(d_xs.ensure(nin_pad), xs.data(), nin_pad * 4, cudaMemcpyHostToDevice), "H2D");
+        ck(cudaMemcpy(d_xd.ensure(nin_pad), xd.data(), nin_pad * 4, cudaMemcpyHostToDevice), "H2D");
+        ck(cudaMemcpy(d_ys.ensure(nout_pad), ys.data(), nout_pad * 4, cudaMemcpyHostToDevice), "H2D");
+        ck(cudaMemcpy(d_yd.ensure(nout_pad), yd.data(), nout_pad * 4, cudaMemcpyHostToDevice), "H2D");
+        ck(cudaMemcpy(d_lw.ensure(nout_pad), lw.data(), nout_pad * 4, cudaMemcpyHostToDevice), "H2D");
+        ck(cudaMemcpy(d_xmin.ensure(nin_pad), xmin.data(), nin_pad * 8, cudaMemcpyHostToDevice), "H2D");
+        ck(cudaMemcpy(d_xmax.ensure(nin_pad), xmax.data(), nin_pad * 8, cudaMemcpyHostToDevice), "H2D");
+    }
+
+    // rows of raw X, Y -> standardised t_xh (bf16) and t_y
+    void gather(int B, const float* X, const float* Y, const int* rows, cudaStream_t s) {
+        t_xh.ensure((size_t)B * nin_pad);
+        t_y.ensure((size_t)B * nout_pad);
+        ck(launch_gather_rows(B, rows, X, nin_pad, d_xs.p, d_xd.p, t_xh.p, Y, nout_pad, d_ys.p, d_yd.p, t_y.p, s),
+           "gather rows");
+    }
+
+    // the increment network's weighted squared error and its gradient (net.grad)
+    void loss_and_grad(int B, const float* X, const float* Y, const int* rows, float* loss_sum, cudaStream_t s,
+                       int sm) {
+        gather(B, X, Y, rows, s);
+        net.forward(B, t_xh.p, true, net.t_out.p, s);
+        ck(launch_mse_grad(B, nout_pad, net.t_out.p, t_y.p, d_lw.p, net.t_dout.p, net.t_dout16.p, loss_sum, s), "loss");
+        net.backward(B, t_xh.p, s, sm);
+    }
+
+    // The error network's pinball loss at quantile tau and its gradient (err->grad): inputs are
+    // the increment network's standardised input and output, the target is log10 of the largest
+    // |dY| error of that output on the sample.
+    void error_loss_and_grad(int B, const float* X, const float* Y, const int* rows, float tau, float* loss_sum,
+                             cudaStream_t s, int sm) {
+        gather(B, X, Y, rows, s);
+        e_main.ensure((size_t)B * nout_pad);
+        net.forward(B, t_xh.p, false, e_main.p, s);
+        const int nin_e = err->nin_pad;
+        e_xh.ensure((size_t)B * nin_e);
+        e_tgt.ensure((size_t)B * err->nout_pad);
+        ck(launch_error_features(B, t_xh.p, nin_pad, e_main.p, nout_pad, e_xh.p, s), "error features");
+        ck(launch_error_targets(B, e_main.p, t_y.p, nout_pad, d_yd.p, nsp, e_tgt.p, err->nout_pad, s), "error targets");
+        err->forward(B, e_xh.p, true, err->t_out.p, s);
+        ck(launch_pinball_grad(B, err->nout_pad, err->t_out.p, e_tgt.p, tau, err->t_dout.p, err->t_dout16.p, loss_sum,
+                               s),
+           "pinball loss");
+        err->backward(B, e_xh.p, s, sm);
+    }
+
     void ensure_infer(int chunk) {
         if (chunk <= ib) return;
         ib = chunk;
         i_xh.ensure((size_t)chunk * nin_pad);
-        i_a0.ensure((size_t)chunk * width);
-        i_a1.ensure((size_t)chunk * width);
         i_out.ensure((size_t)chunk * nout_pad);
     }
 
@@ -214,17 +317,19 @@ struct Surrogate {
             ck(launch_gather_rows(m, nullptr, X + (size_t)first * nin_pad, nin_pad, d_xs.p, d_xd.p, i_xh.p, nullptr,
                                   0, nullptr, nullptr, nullptr, s),
                "features");
-            forward(m, i_xh.p, false, out + (size_t)first * nout_pad, s);
+            net.forward(m, i_xh.p, false, out + (size_t)first * nout_pad, s);
         }
-        destandardise(n, out, s);   // raw increments, in place
+        ck(launch_affine_columns(n, nout_pad, d_ys.p, d_yd.p, out, s), "destandardise");   // raw increments
     }
 
-    void destandardise(int n, float* out, cudaStream_t s);
+    // the error network's predicted log10 error of each chunk row (i_err, stride err->nout_pad)
+    void predict_error_chunk(int m, cudaStream_t s) {
+        i_exh.ensure((size_t)ib * err->nin_pad);
+        i_err.ensure((size_t)ib * err->nout_pad);
+        ck(launch_error_features(m, i_xh.p, nin_pad, i_out.p, nout_pad, i_exh.p, s), "error features");
+        err->forward(m, i_exh.p, false, i_err.p, s);
+    }
 };
-
-void Surrogate::destandardise(int n, float* out, cudaStream_t s) {
-    ck(launch_affine_columns(n, nout_pad, d_ys.p, d_yd.p, out, s), "destandardise");
-}
 
 std::mutex g_smu;
 std::vector<std::unique_ptr<Surrogate>> g_surr;
@@ -264,43 +369,7 @@ int chem_surrogate_new(int cr_i, int width, int depth, unsigned long long seed) 
         S->nout = ri.nsp + 1;
         S->nin_pad = pad8(S->nin);
         S->nout_pad = pad8(S->nout);
-        S->width = width;
-        S->depth = depth;
-        S->dims.push_back(S->nin_pad);
-        for (int l = 0; l < depth; ++l) S->dims.push_back(width);
-        S->dims.push_back(S->nout_pad);
-        size_t off = 0;
-        for (int l = 0; l <= depth; ++l) {
-            S->w_off.push_back(off);
-            off += (size_t)S->dims[l] * S->dims[l + 1];
-        }
-        S->n_weights = off;
-        for (int l = 0; l <= depth; ++l) {
-            S->b_off.push_back(off);
-            off += S->dims[l + 1];
-        }
-        S->n_params = off;
-        // initial parameters: U(-1/sqrt(fan_in), 1/sqrt(fan_in)) over the real (unpadded) fan-in;
-        // padded input columns and output rows start at zero
-        std::vector<float> h(S->n_params, 0.f);
-        std::mt19937_64 rng(seed);
-        for (int l = 0; l <= depth; ++l) {
-            const int fin = l == 0 ? S->nin : S->dims[l];
-            const int fout = l == depth ? S->nout : S->dims[l + 1];
-            const float bound = 1.f / std::sqrt((float)fin);
-            std::uniform_real_distribution<float> U(-bound, bound);
-            for (int o = 0; o < fout; ++o)
-                for (int k = 0; k < fin; ++k) h[S->w_off[l] + (size_t)o * S->dims[l] + k] = U(rng);
-            for (int o = 0; o < fout; ++o) h[S->b_off[l] + o] = U(rng);
-        }
-        S->params.ensure(S->n_params);
-        S->grad.ensure(S->n_params);
-        S->adam_m.ensure(S->n_params);
-        S->adam_v.ensure(S->n_params);
-        S->params_h.ensure(S->n_params);
-        ck(cudaMemcpy(S->params.p, h.data(), S->n_params * 4, cudaMemcpyHostToDevice), "H2D");
-        S->reset_adam();
-        S->refresh_bf16(nullptr);
+        S->net.init(S->nin, S->nout, width, depth, seed);
         // identity standardisation, unbounded domain, unit loss weights until fitted
         S->xs.assign(S->nin_pad, 0.f);
         S->xd.assign(S->nin_pad, 1.f);
@@ -350,7 +419,7 @@ int chem_surrogate_free(int sg) {
 int chem_surrogate_dims(int sg, int* dims) {
     return guard([&] {
         auto& S = surr(sg);
-        int v[8] = {S.nin, S.nin_pad, S.nout, S.nout_pad, S.width, S.depth, (int)S.n_params, S.ne};
+        int v[8] = {S.nin, S.nin_pad, S.nout, S.nout_pad, S.net.width, S.net.depth, (int)S.net.n_params, S.ne};
         std::memcpy(dims, v, sizeof v);
         return 0;
     });
@@ -359,7 +428,7 @@ int chem_surrogate_dims(int sg, int* dims) {
 int chem_surrogate_get_params(int sg, float* params) {
     return guard([&] {
         auto& S = surr(sg);
-        ck(cudaMemcpy(params, S.params.p, S.n_params * 4, cudaMemcpyDeviceToHost), "D2H");
+        ck(cudaMemcpy(params, S.net.params.p, S.net.n_params * 4, cudaMemcpyDeviceToHost), "D2H");
         return 0;
     });
 }
@@ -367,9 +436,9 @@ int chem_surrogate_get_params(int sg, float* params) {
 int chem_surrogate_set_params(int sg, const float* params) {
     return guard([&] {
         auto& S = surr(sg);
-        ck(cudaMemcpy(S.params.p, params, S.n_params * 4, cudaMemcpyHostToDevice), "H2D");
-        S.reset_adam();
-        S.refresh_bf16(nullptr);
+        ck(cudaMemcpy(S.net.params.p, params, S.net.n_params * 4, cudaMemcpyHostToDevice), "H2D");
+        S.net.reset_adam();
+        S.net.refresh_bf16(nullptr);
         ck(cudaDeviceSynchronize(), "set params");
         return 0;
     });
@@ -478,14 +547,7 @@ int chem_surrogate_train_step(int sg, int batch, const float* X, const float* Y,
         cudaStream_t s = (cudaStream_t)stream;
         ReactorInternals ri = reactor_internals(S.cr);
         S.loss_and_grad(batch, X, Y, rows, loss_sum, s, ri.sm_count);
-        ++S.step;
-        ck(launch_adamw((int)S.n_weights, S.params.p, S.grad.p, S.adam_m.p, S.adam_v.p, S.params_h.p, lr, 0.9f, 0.999f,
-                        1e-8f, weight_decay, S.step, s),
-           "adamw");
-        const size_t nb = S.n_params - S.n_weights;
-        ck(launch_adamw((int)nb, S.params.p + S.n_weights, S.grad.p + S.n_weights, S.adam_m.p + S.n_weights,
-                        S.adam_v.p + S.n_weights, S.params_h.p + S.n_weights, lr, 0.9f, 0.999f, 1e-8f, 0.f, S.step, s),
-           "adamw");
+        S.net.adam(lr, weight_decay, s);
         return 0;
     });
 }
@@ -498,7 +560,7 @@ int chem_surrogate_gradients(int sg, int batch, const float* X, const float* Y, 
         cudaStream_t s = (cudaStream_t)stream;
         ReactorInternals ri = reactor_internals(S.cr);
         S.loss_and_grad(batch, X, Y, rows, loss_sum, s, ri.sm_count);
-        ck(cudaMemcpyAsync(grad, S.grad.p, S.n_params * 4, cudaMemcpyDeviceToDevice, s), "D2D");
+        ck(cudaMemcpyAsync(grad, S.net.grad.p, S.net.n_params * 4, cudaMemcpyDeviceToDevice, s), "D2D");
         return 0;
     });
 }
@@ -561,7 +623,9 @@ int chem_surrogate_update_cells(int sg, int ncell, const double* rho, const doub
             fa.x_shift = S.d_xs.p; fa.x_scale = S.d_xd.p; fa.x_min = S.d_xmin.p; fa.x_max = S.d_xmax.p;
             fa.Xh = S.i_xh.p; fa.gate = gate_p;
             ck(launch_features(fa, s), "surrogate features");
-            S.forward(m, S.i_xh.p, false, S.i_out.p, s);
+            S.net.forward(m, S.i_xh.p, false, S.i_out.p, s);
+            const bool use_err = S.err && S.err_gate;
+            if (use_err) S.predict_error_chunk(m, s);
             GateArgs ga{};
             ga.n = m; ga.first = first; ga.ncell = ncell; ga.nsp = nsp; ga.nout_pad = S.nout_pad; ga.ne = S.ne;
             ga.update_thermo = (flags & GDTK_CHEM_UPDATE_THERMO) ? 1 : 0;
@@ -573,6 +637,9 @@ int chem_surrogate_update_cells(int sg, int ncell, const double* rho, const doub
             ga.reject = rej; ga.counters = cnt; ga.code_counts = cc;
             ga.monitor_stride = cap ? monitor_stride : 0; ga.monitor_cap = cap;
             ga.mon_idx = S.mon_idx.p; ga.mon_state = S.mon_state.p; ga.dt_chem = dt_chem;
+            ga.pred_err = use_err ? S.i_err.p : nullptr;
+            ga.pred_err_ld = use_err ? S.err->nout_pad : 0;
+            ga.err_log10_tol = S.err_log10_tol;
             ck(launch_gate(ga, s), "surrogate gate");
         }
         int hc[2] = {0, 0};
@@ -629,6 +696,110 @@ int chem_surrogate_update_cells(int sg, int ncell, const double* rho, const doub
             counts[GATE_COUNT] = n_rej;
             counts[GATE_COUNT + 1] = n_fail;
         }
+        return 0;
+    });
+}
+
+int chem_surrogate_error_model_new(int sg, int width, int depth, unsigned long long seed) {
+    return guard([&] {
+        auto& S = surr(sg);
+        if (width < 8 || width % 8 || width > 4096) throw std::runtime_error("width must be a multiple of 8 in 8..4096");
+        if (depth < 1 || depth > 16) throw std::runtime_error("depth must be in 1..16");
+        auto e = std::make_unique<Mlp>();
+        e->init(S.nin_pad + S.nout_pad, 1, width, depth, seed);
+        ck(cudaDeviceSynchronize(), "error model init");
+        S.err = std::move(e);
+        return 0;
+    });
+}
+
+int chem_surrogate_error_dims(int sg, int* dims) {
+    return guard([&] {
+        auto& S = surr(sg);
+        if (!S.err) throw std::runtime_error("the surrogate has no error model");
+        int v[5] = {S.err->nin, S.err->nout_pad, S.err->width, S.err->depth, (int)S.err->n_params};
+        std::memcpy(dims, v, sizeof v);
+        return 0;
+    });
+}
+
+int chem_surrogate_error_get_params(int sg, float* params) {
+    return guard([&] {
+        auto& S = surr(sg);
+        if (!S.err) throw std::runtime_error("the surrogate has no error model");
+        ck(cudaMemcpy(params, S.err->params.p, S.err->n_params * 4, cudaMemcpyDeviceToHost), "D2H");
+        return 0;
+    });
+}
+
+int chem_surrogate_error_set_params(int sg, const float* params) {
+    return guard([&] {
+        auto& S = surr(sg);
+        if (!S.err) throw std::runtime_error("the surrogate has no error model");
+        ck(cudaMemcpy(S.err->params.p, params, S.err->n_params * 4, cudaMemcpyHostToDevice), "H2D");
+        S.err->reset_adam();
+        S.err->refresh_bf16(nullptr);
+        ck(cudaDeviceSynchronize(), "set params");
+        return 0;
+    });
+}
+
+int chem_surrogate_error_train_step(int sg, int batch, const float* X, const float* Y, const int* rows, float lr,
+                                    float weight_decay, float quantile, float* loss_sum, void* stream) {
+    return guard([&] {
+        auto& S = surr(sg);
+        if (!S.err) throw std::runtime_error("the surrogate has no error model");
+        if (batch <= 0) throw std::runtime_error("batch must be > 0");
+        if (!(quantile > 0.f && quantile < 1.f)) throw std::runtime_error("quantile must be in (0, 1)");
+        cudaStream_t s = (cudaStream_t)stream;
+        ReactorInternals ri = reactor_internals(S.cr);
+        S.error_loss_and_grad(batch, X, Y, rows, quantile, loss_sum, s, ri.sm_count);
+        S.err->adam(lr, weight_decay, s);
+        return 0;
+    });
+}
+
+int chem_surrogate_error_gradients(int sg, int batch, const float* X, const float* Y, const int* rows, float quantile,
+                                   float* grad, float* loss_sum, void* stream) {
+    return guard([&] {
+        auto& S = surr(sg);
+        if (!S.err) throw std::runtime_error("the surrogate has no error model");
+        if (batch <= 0) throw std::runtime_error("batch must be > 0");
+        cudaStream_t s = (cudaStream_t)stream;
+        ReactorInternals ri = reactor_internals(S.cr);
+        S.error_loss_and_grad(batch, X, Y, rows, quantile, loss_sum, s, ri.sm_count);
+        ck(cudaMemcpyAsync(grad, S.err->grad.p, S.err->n_params * 4, cudaMemcpyDeviceToDevice, s), "D2D");
+        return 0;
+    });
+}
+
+int chem_surrogate_predict_error(int sg, int n, const float* X, float* out, void* stream) {
+    return guard([&] {
+        auto& S = surr(sg);
+        if (!S.err) throw std::runtime_error("the surrogate has no error model");
+        if (n <= 0) return 0;
+        cudaStream_t s = (cudaStream_t)stream;
+        const int chunk = std::min(n, 1 << 20);
+        S.ensure_infer(chunk);
+        for (int first = 0; first < n; first += chunk) {
+            const int m = std::min(chunk, n - first);
+            ck(launch_gather_rows(m, nullptr, X + (size_t)first * S.nin_pad, S.nin_pad, S.d_xs.p, S.d_xd.p, S.i_xh.p,
+                                  nullptr, 0, nullptr, nullptr, nullptr, s),
+               "features");
+            S.net.forward(m, S.i_xh.p, false, S.i_out.p, s);
+            S.predict_error_chunk(m, s);
+            ck(launch_copy_column(m, S.i_err.p, S.err->nout_pad, 0, out + first, s), "copy");
+        }
+        return 0;
+    });
+}
+
+int chem_surrogate_set_error_gate(int sg, double tol) {
+    return guard([&] {
+        auto& S = surr(sg);
+        if (tol > 0.0 && !S.err) throw std::runtime_error("the surrogate has no error model");
+        S.err_gate = tol > 0.0;
+        S.err_log10_tol = tol > 0.0 ? std::log10(tol) : 0.0;
         return 0;
     });
 }

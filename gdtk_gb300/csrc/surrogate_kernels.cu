@@ -195,6 +195,8 @@ __global__ void __launch_bounds__(128) gate_kernel(const GateArgs a) {
             }
             const double dT = (double)o[nsp] * (double)a.y_scale[nsp] + (double)a.y_shift[nsp];
             if (a.max_dY > 0.0 && maxd > a.max_dY) code = GATE_MAGNITUDE;
+            if (code == GATE_ACCEPTED && a.pred_err && !((double)a.pred_err[(size_t)i * a.pred_err_ld] <= a.err_log10_tol))
+                code = GATE_PREDICTED_ERROR;
             // element balance of the predicted increment (mol of element per kg of mixture)
             double r[SURR_MAX_ELEMENTS];
             double worst = 0.0;

@@ -17,7 +17,8 @@ enum GateCode {
     GATE_ENERGY = 6,
     GATE_NEWTON = 7,
     GATE_MAGNITUDE = 8,
-    GATE_COUNT = 9
+    GATE_PREDICTED_ERROR = 9,
+    GATE_COUNT = 10
 };
 
 // Raw features of a cell: ln T, ln p, Y[0..nsp), ln dt, zero padding to nin_pad.
@@ -70,6 +71,9 @@ struct GateArgs {
     int* mon_idx;            // [monitor_cap]
     double* mon_state;       // [(5 + nsp) * monitor_cap]: rho, u, T, p, dt_chem, Y (original)
     const double* dt_chem;
+    const float* pred_err;   // [n][pred_err_ld] error network output (log10 |dY| error) or null
+    int pred_err_ld;
+    double err_log10_tol;
 };
 cudaError_t launch_gate(const GateArgs& a, cudaStream_t s);
 

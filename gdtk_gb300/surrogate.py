@@ -17,7 +17,8 @@ import numpy as np
 from . import lib, check
 from .cells import ReactorCells, UPDATE_THERMO, RETRY, _ptr, _stream, _f64
 
-GATE_NAMES = ["accepted", "frozen", "bad_input", "domain", "elements", "negative", "energy", "newton", "magnitude"]
+GATE_NAMES = ["accepted", "frozen", "bad_input", "domain", "elements", "negative", "energy", "newton", "magnitude",
+              "predicted_error"]
 
 
 def _vp(a):
@@ -181,6 +182,76 @@ class ChemSurrogate:
         T = torch.exp(Xr[:, T_col].double())
         eT = (pr[:, self.nout - 1].double() - Yr[:, self.nout - 1].double()).abs() / (T + Yr[:, self.nout - 1].double())
         return eY.cpu().numpy(), eT.cpu().numpy()
+
+    # ---------------------------------------------------------------- error model
+    def add_error_model(self, width=128, depth=2, seed=0):
+        """Attach the error network (include/gdtk_surrogate.h): an estimate of log10 of the largest
+        |dY| error of this network's prediction, from its standardised input and output."""
+        check(lib().chem_surrogate_error_model_new(self.id, int(width), int(depth), ctypes.c_ulonglong(seed)),
+              "chem_surrogate_error_model_new")
+        d = (ctypes.c_int * 5)()
+        check(lib().chem_surrogate_error_dims(self.id, d), "chem_surrogate_error_dims")
+        self.err_nin, self.err_nout_pad, self.err_width, self.err_depth, self.err_n_params = list(d)
+
+    def error_layer_dims(self):
+        return [self.err_nin] + [self.err_width] * self.err_depth + [self.err_nout_pad]
+
+    def get_error_params(self):
+        out = np.empty(self.err_n_params, np.float32)
+        check(lib().chem_surrogate_error_get_params(self.id, _vp(out)), "chem_surrogate_error_get_params")
+        return out
+
+    def set_error_params(self, params):
+        params = np.ascontiguousarray(params, np.float32)
+        check(lib().chem_surrogate_error_set_params(self.id, _vp(params)), "chem_surrogate_error_set_params")
+
+    def error_gradients(self, X, Y, rows, quantile=0.9):
+        import torch
+        g = torch.empty(self.err_n_params, dtype=torch.float32, device=X.device)
+        loss = torch.zeros(1, dtype=torch.float32, device=X.device)
+        check(lib().chem_surrogate_error_gradients(self.id, int(rows.shape[0]), _ptr(X), _ptr(Y), _ptr(rows),
+                                                   ctypes.c_float(quantile), _ptr(g), _ptr(loss), _stream()),
+              "chem_surrogate_error_gradients")
+        return g, float(loss.item())
+
+    def train_error_model(self, X, Y, rows, epochs=8, batch=8192, lr=2e-3, lr_min=1e-5, quantile=0.9, seed=1,
+                          log=None):
+        """AdamW on the error network's pinball loss, cosine schedule; returns the mean loss per epoch."""
+        import torch
+        n = int(rows.shape[0])
+        steps_per_epoch = max(1, n // batch)
+        total = epochs * steps_per_epoch
+        gen = torch.Generator(device=rows.device)
+        gen.manual_seed(seed)
+        loss = torch.zeros(1, dtype=torch.float32, device=rows.device)
+        hist, step = [], 0
+        for ep in range(epochs):
+            perm = rows[torch.randperm(n, generator=gen, device=rows.device)]
+            loss.zero_()
+            for i in range(steps_per_epoch):
+                q = step / max(1, total - 1)
+                cur = lr_min + 0.5 * (lr - lr_min) * (1.0 + math.cos(math.pi * q))
+                check(lib().chem_surrogate_error_train_step(self.id, batch, _ptr(X), _ptr(Y),
+                                                            _ptr(perm[i * batch:(i + 1) * batch]), ctypes.c_float(cur),
+                                                            ctypes.c_float(0.0), ctypes.c_float(quantile), _ptr(loss),
+                                                            _stream()), "chem_surrogate_error_train_step")
+                step += 1
+            hist.append(float(loss.item()) / (steps_per_epoch * batch))
+            if log:
+                log("error model epoch %d loss %.4e" % (ep, hist[-1]))
+        return hist
+
+    def predict_error(self, X):
+        """The error network's estimate, log10 of the largest |dY| error, per row of raw X."""
+        import torch
+        out = torch.empty(X.shape[0], dtype=torch.float32, device=X.device)
+        check(lib().chem_surrogate_predict_error(self.id, int(X.shape[0]), _ptr(X), _ptr(out), _stream()),
+              "chem_surrogate_predict_error")
+        return out
+
+    def set_error_gate(self, tol):
+        """Reject cells whose estimated |dY| error exceeds tol (<= 0: off)."""
+        check(lib().chem_surrogate_set_error_gate(self.id, float(tol)), "chem_surrogate_set_error_gate")
 
     # ---------------------------------------------------------------- gated update
     def update(self, rho, u, T, p, massf, dt_chem, t_interval, status=None, T_frozen=0.0,

@@ -22,7 +22,10 @@
  *   energy          T from (rho, u, Y_new) by the reference's Newton iteration
  *                   (therm_perf_gas_mix.d:426-468) converges and agrees with T + the predicted
  *                   dT within T_tol (relative);
- *   magnitude       no predicted |dY| exceeds max_dY (when max_dY > 0).
+ *   magnitude       no predicted |dY| exceeds max_dY (when max_dY > 0);
+ *   predicted error when an error model is attached and its gate set: the error network's
+ *                   estimate of log10 of the largest |dY| error of the prediction (trained as a
+ *                   quantile) does not exceed log10(tol).
  * Accepted cells take Y_new, that T and p = rho R T; their dt_chem is left as it was.  A cell
  * that fails any check is integrated by the plain FP64 update from its original state, exactly
  * as chem_reactor_update_cells would.  Cells at or below T_frozen and cells of invalid density
@@ -45,7 +48,8 @@ extern "C" {
 #define GDTK_GATE_ENERGY 6
 #define GDTK_GATE_NEWTON 7
 #define GDTK_GATE_MAGNITUDE 8
-#define GDTK_GATE_COUNT 9
+#define GDTK_GATE_PREDICTED_ERROR 9
+#define GDTK_GATE_COUNT 10
 
 /* A network for reactor cr_i's gas model (its species and, for the element check, the species'
  * atomic constituents), parameters drawn from U(-1/sqrt(fan_in), 1/sqrt(fan_in)) with a
@@ -100,6 +104,27 @@ int chem_surrogate_update_cells(int sg, int ncell, const double* rho, const doub
                                 double* massf, double* dt_chem, int* status, double t_interval, double T_frozen,
                                 int flags, void* stream, int* gate, long long* counts, int monitor_stride,
                                 double* monitor);
+/* Error model: a second network (same BF16 kernels) attached to the surrogate.  Its input is the
+ * surrogate's standardised input and standardised output (nin_pad + nout_pad values), its output
+ * an estimate of log10 of the largest |dY| error of that output.  It is trained on samples with a
+ * pinball (quantile) loss, so with quantile 0.9 its estimate lies above the actual error for about
+ * 90% of the samples it was trained on. */
+int chem_surrogate_error_model_new(int sg, int width, int depth, unsigned long long seed);
+/* host dims[5]: nin, nout_pad, width, depth, n_params */
+int chem_surrogate_error_dims(int sg, int* dims);
+int chem_surrogate_error_get_params(int sg, float* params);
+int chem_surrogate_error_set_params(int sg, const float* params);
+/* One AdamW step of the error network on rows[0..batch) of raw X, Y (the surrogate's own
+ * parameters are not changed); loss_sum (may be NULL) += the summed pinball loss. */
+int chem_surrogate_error_train_step(int sg, int batch, const float* X, const float* Y, const int* rows, float lr,
+                                    float weight_decay, float quantile, float* loss_sum, void* stream);
+/* The gradient of the error network's mean pinball loss (grad: its n_params floats), no update. */
+int chem_surrogate_error_gradients(int sg, int batch, const float* X, const float* Y, const int* rows, float quantile,
+                                   float* grad, float* loss_sum, void* stream);
+/* The error network's estimate (log10 of the largest |dY| error) for raw features X[n][nin_pad]. */
+int chem_surrogate_predict_error(int sg, int n, const float* X, float* out, void* stream);
+/* Reject cells whose estimated error exceeds tol (mass-fraction units); tol <= 0 turns it off. */
+int chem_surrogate_set_error_gate(int sg, double tol);
 /* The network's BF16 GEMM, exposed for testing: D[M][N] = op(A)[M][K] op(B)[K][N] (+ bias[N]),
  * act 0 none, 1 GELU (pre receives the pre-activation when not NULL); A, B are bf16 arrays;
  * D (fp32) and Dh (bf16) may each be NULL; splits > 1 splits K (no bias or act then). */

@@ -51,14 +51,22 @@ def forward(layers, X, bf=False):
     return out, cache
 
 
-def loss_and_grads(layers, X, Y, w, bf=False):
-    """(L, [(dW_l, db_l)]) for standardised X (B, in), Y (B, out), output weights w (out,)."""
+def loss_and_grads(layers, X, Y, w, bf=False, quantile=None):
+    """(L, [(dW_l, db_l)]) for standardised X (B, in), Y (B, out), output weights w (out,): the
+    weighted squared error, or with `quantile` the pinball loss of output column 0
+    (mean of max(q r, (q - 1) r), r = Y - out)."""
     r = bf16 if bf else (lambda v: np.asarray(v, np.float64))
     B = X.shape[0]
     out, cache = forward(layers, X, bf)
-    d = out - Y
-    L = float(np.sum(w[None, :] * d * d)) / B
-    g = 2.0 * w[None, :] * d / B          # dL/d(out), the fp32 copy
+    if quantile is None:
+        d = out - Y
+        L = float(np.sum(w[None, :] * d * d)) / B
+        g = 2.0 * w[None, :] * d / B          # dL/d(out), the fp32 copy
+    else:
+        res = Y[:, 0] - out[:, 0]
+        L = float(np.sum(np.where(res > 0, quantile * res, (quantile - 1.0) * res))) / B
+        g = np.zeros_like(out)
+        g[:, 0] = np.where(res > 0, -quantile, 1.0 - quantile) / B
     grads = [None] * len(layers)
     for l in range(len(layers) - 1, -1, -1):
         h, _ = cache[l]
@@ -73,11 +81,11 @@ def loss_and_grads(layers, X, Y, w, bf=False):
     return L, grads
 
 
-def finite_difference_check(layers, X, Y, w, n_probe=20, eps=1e-6, seed=0):
+def finite_difference_check(layers, X, Y, w, n_probe=20, eps=1e-6, seed=0, quantile=None):
     """Largest relative difference between the analytic FP64 gradient and central differences
     at n_probe random parameters."""
     rng = np.random.Generator(np.random.PCG64(seed))
-    _, grads = loss_and_grads(layers, X, Y, w)
+    _, grads = loss_and_grads(layers, X, Y, w, quantile=quantile)
     worst = 0.0
     for _ in range(n_probe):
         l = int(rng.integers(len(layers)))
@@ -86,9 +94,9 @@ def finite_difference_check(layers, X, Y, w, n_probe=20, eps=1e-6, seed=0):
         idx = tuple(int(rng.integers(s)) for s in P.shape)
         old = P[idx]
         P[idx] = old + eps
-        Lp, _ = loss_and_grads(layers, X, Y, w)
+        Lp, _ = loss_and_grads(layers, X, Y, w, quantile=quantile)
         P[idx] = old - eps
-        Lm, _ = loss_and_grads(layers, X, Y, w)
+        Lm, _ = loss_and_grads(layers, X, Y, w, quantile=quantile)
         P[idx] = old
         fd = (Lp - Lm) / (2 * eps)
         an = grads[l][which][idx]

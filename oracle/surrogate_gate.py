@@ -14,7 +14,7 @@ from .luatable import array, read_lua_file
 ATOMIC_MASS = {"H": 1.00794e-3, "He": 4.002602e-3, "C": 12.0107e-3, "N": 14.0067e-3, "O": 15.9994e-3,
                "Ar": 39.948e-3}
 
-ACCEPTED, FROZEN, BAD_INPUT, DOMAIN, ELEMENTS, NEGATIVE, ENERGY, NEWTON, MAGNITUDE = range(9)
+ACCEPTED, FROZEN, BAD_INPUT, DOMAIN, ELEMENTS, NEGATIVE, ENERGY, NEWTON, MAGNITUDE, PREDICTED_ERROR = range(10)
 
 
 def element_matrix(gas_file):

@@ -326,3 +326,99 @@ def test_largest_batch_indexing():
     assert np.abs(gY[ok] - o["massf"][ok]).max() <= 1e-8
     gT = d["T"].cpu().numpy()[idx]
     assert (np.abs(gT[ok] - o["T"][ok]) / o["T"][ok]).max() <= 1e-7
+
+
+@pytest.fixture(scope="module")
+def with_error_model(rc, samples, trained):
+    """The trained network with an error model trained on the same samples (quantile 0.9)."""
+    sg, *_ = trained
+    X, Y, rows = samples
+    sg.add_error_model(width=128, depth=2, seed=4)
+    hist = sg.train_error_model(X, Y, rows, epochs=4, batch=8192, quantile=0.9)
+    return sg, hist
+
+
+def test_error_model_gradient_matches_cpu_oracle(rc, samples):
+    from gdtk_gb300.surrogate import ChemSurrogate
+    X, Y, rows = samples
+    sg = ChemSurrogate(rc, width=256, depth=4, seed=7)
+    sg.fit_normalisation(X, Y, rows)
+    sg.add_error_model(width=64, depth=2, seed=8)
+    batch = rows[:1024].contiguous()
+    grad, loss = sg.error_gradients(X, Y, batch, quantile=0.9)
+    grad = grad.cpu().numpy().astype(np.float64)
+    nrm = sg.get_normalisation()
+    xb, yb = X[batch.long()].cpu().numpy(), Y[batch.long()].cpu().numpy()
+    Xs = ((xb - nrm["x_shift"]) / nrm["x_scale"]).astype(np.float32)
+    Ys = ((yb - nrm["y_shift"]) / nrm["y_scale"]).astype(np.float32).astype(np.float64)
+    main = [(W.astype(np.float64), b.astype(np.float64)) for W, b in sg.unpack(sg.get_params())]
+    out, _ = mlp.forward(main, Xs, bf=True)
+    nsp = rc.nsp
+    err = np.abs((out[:, :nsp] - Ys[:, :nsp]) * nrm["y_scale"][:nsp]).max(axis=1)
+    tgt = np.zeros((1024, sg.err_nout_pad))
+    tgt[:, 0] = np.log10(err + 1e-12)
+    feat = np.concatenate([mlp.bf16(Xs), mlp.bf16(out)], axis=1)
+    dims = sg.error_layer_dims()
+    flat = sg.get_error_params().astype(np.float64)
+    layers, off = [], 0
+    ws = []
+    for l in range(len(dims) - 1):
+        ws.append(flat[off:off + dims[l] * dims[l + 1]].reshape(dims[l + 1], dims[l]))
+        off += dims[l] * dims[l + 1]
+    for l in range(len(dims) - 1):
+        layers.append((ws[l], flat[off:off + dims[l + 1]]))
+        off += dims[l + 1]
+    L, g = mlp.loss_and_grads(layers, feat, tgt, np.ones(sg.err_nout_pad), bf=True, quantile=0.9)
+    assert loss / 1024 == pytest.approx(L, rel=5e-3)
+    goff = 0
+    gw = []
+    for l in range(len(dims) - 1):
+        gw.append(grad[goff:goff + dims[l] * dims[l + 1]].reshape(dims[l + 1], dims[l]))
+        goff += dims[l] * dims[l + 1]
+    for l in range(len(dims) - 1):
+        gb = grad[goff:goff + dims[l + 1]]
+        goff += dims[l + 1]
+        for got, ref in ((gw[l], g[l][0]), (gb, g[l][1])):
+            rel = np.linalg.norm(got - ref) / max(np.linalg.norm(ref), 1e-30)
+            assert rel < 3e-2, (l, rel)
+
+
+def test_error_model_ranks_the_surrogate_errors(samples, with_error_model):
+    """On held-out samples the error model's estimate follows the actual error, and a cell it
+    accepts at 1e-3 has a smaller error than the magnitude cap alone guarantees."""
+    sg, hist = with_error_model
+    assert hist[-1] < hist[0]
+    X, Y, rows = samples
+    hold = rows[-20000:]
+    Xh, Yh = X[hold.long()].contiguous(), Y[hold.long()]
+    pred = sg.predict(Xh)
+    actual = torch.log10((pred[:, :sg.nout - 1] - Yh[:, :sg.nout - 1]).abs().amax(dim=1) + 1e-12).cpu().numpy()
+    est = sg.predict_error(Xh).cpu().numpy()
+    rank = lambda v: np.argsort(np.argsort(v))
+    assert np.corrcoef(rank(est), rank(actual))[0, 1] > 0.6
+    below = (actual <= est).mean()
+    assert 0.75 < below < 0.98   # the 0.9 quantile, approximately
+
+
+def test_error_gate_in_the_update(rc, with_error_model):
+    sg, _ = with_error_model
+    n = 16384
+    base = _fresh_cells(rc, n, seed=25)
+    ref = _clone(base)
+    rc.update(ref["rho"], ref["u"], ref["T"], ref["p"], ref["massf"], ref["dt_chem"], 1e-6, status=ref["status"])
+    out = {}
+    for tol in (0.0, 1e-3):
+        sg.set_gate(elem_tol=1e-4, neg_tol=1e-5, T_tol=1e-3, max_dY=0.0)
+        sg.set_error_gate(tol)
+        d = _clone(base)
+        gate = torch.empty(n, dtype=torch.int32, device="cuda")
+        res = sg.update(d["rho"], d["u"], d["T"], d["p"], d["massf"], d["dt_chem"], 1e-6, status=d["status"],
+                        gate=gate)
+        acc = (gate == 0) & (ref["status"] == 0)
+        e = (d["massf"][:, acc] - ref["massf"][:, acc]).abs().amax(dim=0)
+        out[tol] = dict(acc=float(acc.float().mean()), p999=float(torch.quantile(e.double(), 0.999)),
+                        rejected_by_model=res["gate"]["predicted_error"])
+    sg.set_error_gate(0.0)
+    assert out[0.0]["rejected_by_model"] == 0 and out[1e-3]["rejected_by_model"] > 0
+    assert out[1e-3]["acc"] > 0.3
+    assert out[1e-3]["p999"] < out[0.0]["p999"], out

@@ -26,6 +26,15 @@ def test_oracle_gradient_matches_finite_differences():
     assert mlp.finite_difference_check(layers, X, Y, w, n_probe=40) < 1e-6
 
 
+def test_oracle_pinball_gradient_matches_finite_differences():
+    rng = np.random.Generator(np.random.PCG64(4))
+    layers = _layers([24, 16, 8], 6)
+    X = rng.normal(size=(64, 24))
+    Y = np.zeros((64, 8))
+    Y[:, 0] = rng.normal(size=64) * 3.0   # away from the kinks of the piecewise-linear loss
+    assert mlp.finite_difference_check(layers, X, Y, np.ones(8), n_probe=40, quantile=0.9) < 1e-5
+
+
 def test_bf16_rounding_is_round_to_nearest_even():
     x = np.array([1.0, 1.0 + 2 ** -8, 1.0 + 3 * 2 ** -8, 1.0 + 2 ** -9, -2.5, 3.0e-5, 0.0])
     r = mlp.bf16(x)
