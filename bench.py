@@ -48,7 +48,7 @@ WORKLOADS = {
     # h2air-1M distribution, dt log-uniform in [0.5, 2] us, 5% held out); inference + gate + FP64
     # fallback on 4,194,304 fresh cells at dt = 1e-6 s, against the plain FP64 update of the same cells
     "h2air-surrogate": dict(gas="j92-gas.lua", chem="j92-chem.lua", n=4194304, dt=1.0e-6, kind="surrogate",
-                            seed=3, train_samples=16777216, epochs=30, batch=8192),
+                            seed=3, train_samples=16777216, epochs=30, batch=8192, error_epochs=8),
 }
 
 
@@ -377,7 +377,21 @@ def run_surrogate(args, w):
     hist = sg.train(X, Yt, train, epochs=epochs, batch=w["batch"], lr=2e-3)
     sync()
     t_train = time.perf_counter() - t1
+    # error model: the 0.9 quantile of log10 of the network's own |dY| error, on the same samples
+    sg.add_error_model(width=128, depth=2, seed=1)
+    sync()
+    t1 = time.perf_counter()
+    ehist = sg.train_error_model(X, Yt, train, epochs=w["error_epochs"], batch=w["batch"], quantile=0.9)
+    sync()
+    t_err = time.perf_counter() - t1
     eY, eT = sg.heldout_error(X, Yt, hold)
+    est = sg.predict_error(X[hold.long()].contiguous()).cpu().numpy()
+    le = np.log10(eY + 1e-12)
+    err_model_stats = {"epochs": w["error_epochs"], "train_s": t_err, "quantile": 0.9,
+                       "heldout_fraction_below_estimate": float((le <= est).mean()),
+                       "heldout_rank_correlation": float(np.corrcoef(np.argsort(np.argsort(est)),
+                                                                     np.argsort(np.argsort(le)))[0, 1]),
+                       "loss_first_epoch": ehist[0], "loss_last_epoch": ehist[-1]}
     steps_per_epoch = train.shape[0] // w["batch"]
     train_flop = 3 * 2 * sum(a * b for a, b in zip(sg.layer_dims()[:-1], sg.layer_dims()[1:])) * \
         steps_per_epoch * w["batch"] * epochs
@@ -415,14 +429,19 @@ def run_surrogate(args, w):
     plain_time = float(np.mean(plain_s))
 
     # surrogate + fallback at a sweep of gate settings; the first is the default (reported value)
-    settings = [("strict", dict(elem_tol=1e-4, neg_tol=1e-5, T_tol=1e-3, max_dY=5e-4)),
-                ("max_dY 2e-3", dict(elem_tol=1e-4, neg_tol=1e-5, T_tol=1e-3, max_dY=2e-3)),
-                ("no magnitude cap", dict(elem_tol=1e-4, neg_tol=1e-5, T_tol=1e-3, max_dY=0.0))]
+    checks = dict(elem_tol=1e-4, neg_tol=1e-5, T_tol=1e-3)
+    settings = [("error model 1e-4", dict(checks, max_dY=0.0), 1e-4),
+                ("error model 3e-4", dict(checks, max_dY=0.0), 3e-4),
+                ("error model 1e-3", dict(checks, max_dY=0.0), 1e-3),
+                ("magnitude cap 5e-4", dict(checks, max_dY=5e-4), 0.0),
+                ("magnitude cap 2e-3", dict(checks, max_dY=2e-3), 0.0),
+                ("checks only", dict(checks, max_dY=0.0), 0.0)]
     gate = torch.empty(n, dtype=torch.int32, device=dev)
     sweep = []
     clocks = ClockSampler(int(os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] or 0))
-    for si, (name, gs) in enumerate(settings):
+    for si, (name, gs, etol) in enumerate(settings):
         sg.set_gate(**gs)
+        sg.set_error_gate(etol)
         reps = (1 + args.steps) if si == 0 else 1
         times = []
         if si == 0:
@@ -442,7 +461,7 @@ def run_surrogate(args, w):
         e = (Y[:, acc] - plain_Y[:, acc]).abs().amax(dim=0).double()
         et = ((T[acc] - plain_T[acc]).abs() / plain_T[acc]).double()
         q = lambda v, x: float(torch.quantile(v[:min(v.shape[0], 1 << 24)], x)) if v.numel() else 0.0
-        sweep.append({"gate": name, **gs, "seconds": secs, "cell_updates_per_s": n / secs,
+        sweep.append({"gate": name, **gs, "error_model_tol": etol, "seconds": secs, "cell_updates_per_s": n / secs,
                       "speedup_vs_plain": plain_time / secs, "accepted_fraction": float(acc.float().mean()),
                       "rejected_fraction": res["fallback"] / n, "gate_counts": res["gate"],
                       "fallback_failed": res["fallback_failed"],
@@ -492,6 +511,7 @@ def run_surrogate(args, w):
         "training": {"sample_generation_s": t_gen, "train_s": t_train, "samples_per_s":
                      steps_per_epoch * w["batch"] * epochs / t_train, "tflops": train_flop / t_train / 1e12,
                      "loss_first_epoch": hist[0], "loss_last_epoch": hist[-1]},
+        "error_model": err_model_stats,
         "heldout": {"rows": int(len(eY)), "median_max_dY": float(np.median(eY)),
                     "p99_max_dY": float(np.percentile(eY, 99)), "max_dY": float(eY.max()),
                     "median_rel_dT": float(np.median(eT)), "p99_rel_dT": float(np.percentile(eT, 99))},

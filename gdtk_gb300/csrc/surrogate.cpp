@@ -276,6 +276,7 @@ struct Surrogate {
     void loss_and_grad(int B, const float* X, const float* Y, const int* rows, float* loss_sum, cudaStream_t s,
                        int sm) {
         gather(B, X, Y, rows, s);
+        net.ensure_train(B);   // before t_out is read as the output pointer
         net.forward(B, t_xh.p, true, net.t_out.p, s);
         ck(launch_mse_grad(B, nout_pad, net.t_out.p, t_y.p, d_lw.p, net.t_dout.p, net.t_dout16.p, loss_sum, s), "loss");
         net.backward(B, t_xh.p, s, sm);
@@ -294,6 +295,7 @@ struct Surrogate {
         e_tgt.ensure((size_t)B * err->nout_pad);
         ck(launch_error_features(B, t_xh.p, nin_pad, e_main.p, nout_pad, e_xh.p, s), "error features");
         ck(launch_error_targets(B, e_main.p, t_y.p, nout_pad, d_yd.p, nsp, e_tgt.p, err->nout_pad, s), "error targets");
+        err->ensure_train(B);
         err->forward(B, e_xh.p, true, err->t_out.p, s);
         ck(launch_pinball_grad(B, err->nout_pad, err->t_out.p, e_tgt.p, tau, err->t_dout.p, err->t_dout16.p, loss_sum,
                                s),
