@@ -288,8 +288,24 @@ __device__ __noinline__ void rate_constants(const double* TH, double Tq, double*
     if (T > GDTK_T_UPPER) T = GDTK_T_UPPER;
     const double lnT = log(T), rT = 1.0 / T, rT2 = rT * rT, t1 = lnT + 1.0, t2 = 1.0 - lnT;
     int e = 0;
+#if GDTK_MIX_THERMO
+    // every species takes the same curve segment and blend here: choose them once
+    int sa = 0, sb = 0;
+    double wb = 0.0;
+    if (T >= GDTK_MIX_TLO && T <= GDTK_MIX_THI && seg_of(TH, T, sa, sb, wb)) {
 #pragma unroll 1
-    for (int i = 0; i < GDTK_NSP; ++i) G[i * ks] = sp_G(TH, i, T, lnT, rT, rT2, t1, t2, e);
+        for (int i = 0; i < GDTK_NSP; ++i) {
+            const double* c = TH + i * GDTK_TH_STRIDE + GDTK_TH_SEG0 + 15;
+            double g = poly_G(c + 24 * sa, T, rT, rT2, t1, t2);
+            if (wb != 0.0) g = fma(wb, poly_G(c + 24 * sb, T, rT, rT2, t1, t2) - g, g);
+            G[i * ks] = g;
+        }
+    } else
+#endif
+    {
+#pragma unroll 1
+        for (int i = 0; i < GDTK_NSP; ++i) G[i * ks] = sp_G(TH, i, T, lnT, rT, rT2, t1, t2, e);
+    }
     if (e) *err = e;
     gen_kc(T, lnT, rT, G, ks, K, ks, etab, G + GDTK_NSP * ks, ks);
 }
