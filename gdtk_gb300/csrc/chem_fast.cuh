@@ -32,6 +32,7 @@
 namespace gdtk_fast {
 
 using gdtk::gdtk_exp;
+using gdtk::gdtk_div;
 
 // must match the host's CellBlock / FastArgs (codegen.h)
 struct CellBlock {
@@ -206,10 +207,10 @@ __device__ __noinline__ double T_from_u(const double* TH, const double* YR, int 
         lane_stat(lst, 4);
         if (it > 0) {
             T += dT;
-            if (fabs(dT) / T < TOL) return T;
+            if (gdtk_div(fabs(dT), T) < TOL) return T;
             if (it == 10) break;
         }
-        const double lnT = log(T), rT = 1.0 / T, rT2 = rT * rT;
+        const double lnT = log(T), rT = gdtk_div(1.0, T), rT2 = rT * rT;
         double f = 0.0, cv = 0.0;
 #if GDTK_MIX_THERMO
         int sa = 0, sb = 0;
@@ -241,7 +242,7 @@ __device__ __noinline__ double T_from_u(const double* TH, const double* YR, int 
                 cv = fma(yr, Cp - 1.0, cv);
             }
         }
-        dT = -(f - u_tgt) / cv;
+        dT = -gdtk_div(f - u_tgt, cv);
         ++*iters;
     }
     if (fabs(dT) > 1e-3) *err = ST_NEWTON;
@@ -286,7 +287,7 @@ __device__ __noinline__ void rate_constants(const double* TH, double Tq, double*
     double T = Tq;
     if (T < GDTK_T_LOWER) T = GDTK_T_LOWER;
     if (T > GDTK_T_UPPER) T = GDTK_T_UPPER;
-    const double lnT = log(T), rT = 1.0 / T, rT2 = rT * rT, t1 = lnT + 1.0, t2 = 1.0 - lnT;
+    const double lnT = log(T), rT = gdtk_div(1.0, T), rT2 = rT * rT, t1 = lnT + 1.0, t2 = 1.0 - lnT;
     int e = 0;
 #if GDTK_MIX_THERMO
     // every species takes the same curve segment and blend here: choose them once
@@ -317,7 +318,7 @@ __device__ __forceinline__ double estimate_step(const double (&c)[GDTK_NSP], con
 #pragma unroll
     for (int i = 0; i < GDTK_NSP; ++i) {
         if (c[i] > 0.0 && fabs(q[i] - L[i]) > 1.0e-30) {
-            double dt = (q[i] > 10000.0 * L[i]) ? c[i] / (L[i] + ZERO_EPS) : fabs(c[i] / (q[i] - L[i]));
+            double dt = (q[i] > 10000.0 * L[i]) ? gdtk_div(c[i], L[i] + ZERO_EPS) : fabs(gdtk_div(c[i], q[i] - L[i]));
             min_dt = fmin(min_dt, dt);
         }
     }
@@ -404,7 +405,7 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
                     } else {
                         have = true;
                         retried = false;
-                        rrho = 1.0 / rho;
+                        rrho = gdtk_div(1.0, rho);
                         n_steps = n_rhs = n_kc = n_newton = n_rej = n_est = 0;
                         phase = -1;
                     }
@@ -484,7 +485,7 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
                     double o = fma(h, fma(b56, K6, fma(b54, K4, fma(b53, K3, b51 * K1))), y0[i]);
                     double o4 = fma(h, fma(b46, K6, fma(b45, K5, fma(b44, K4, fma(b43, K3, b41 * K1)))), y0[i]);
                     double sk = fma(GDTK_ERRTOL, fmax(fabs(y0[i]), fabs(o)), GDTK_ERRTOL);
-                    double e = (o - o4) / sk;
+                    double e = gdtk_div(o - o4, sk);
                     err2 = fma(e, e, err2);
                     yn[i] = o;
                 }
@@ -536,14 +537,14 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
                 for (int i = 0; i < GDTK_NSP; ++i) {
                     const double y = y0[i];
                     const double ci_ = (s == 0) ? y : yn[i];
-                    const double pp = L[i] / (ci_ + ZERO_EPS);
+                    const double pp = gdtk_div(L[i], ci_ + ZERO_EPS);
                     const double x = pp * h;
                     double N, D;
                     alpha_nd(x + ZERO_EPS, N, D);
                     const double q0 = (s == 0) ? q[i] : Q0[i * ks];
                     const double pb = (s == 0) ? pp : 0.5 * (P0[i * ks] + pp);
                     const double num = h * (fma(N, q[i] - q0, D * q0) - D * (pb * y));
-                    const double v = y + num / fma(N, h * pb, D);
+                    const double v = y + gdtk_div(num, fma(N, h * pb, D));
                     if (s == 0) {
                         Q0[i * ks] = q[i];
                         P0[i * ks] = pp;
@@ -560,16 +561,16 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
             for (int i = 0; i < GDTK_NSP; ++i) {
                 double yc = yn[i];
                 if (yc < ZERO_EPS) continue;
-                double test = fabs(yc - YP0[i * ks]) / (GDTK_EPS2 * (yc + GDTK_DELTA));
+                double test = gdtk_div(fabs(yc - YP0[i * ks]), GDTK_EPS2 * (yc + GDTK_DELTA));
                 if (test > sigma) sigma = test;
             }
             if (sigma <= 0.0) dtS = 10.0 * h;
             else {
                 double x = sigma;
-                x = x - 0.5 * (x * x - sigma) / x;
-                x = x - 0.5 * (x * x - sigma) / x;
-                x = x - 0.5 * (x * x - sigma) / x;
-                dtS = h * ((1.0 / x) + 0.005);
+                x = x - 0.5 * gdtk_div(x * x - sigma, x);
+                x = x - 0.5 * gdtk_div(x * x - sigma, x);
+                x = x - 0.5 * gdtk_div(x * x - sigma, x);
+                dtS = h * (gdtk_div(1.0, x) + 0.005);
             }
             ok = conv;
         }
@@ -640,7 +641,7 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
                 double v = y0[i] * GDTK_M[i] * rrho;
                 return (v < 1.0e-30) ? 0.0 : v;
             };
-            double rtot = 1.0 / sum_pairwise(mf_of);
+            double rtot = gdtk_div(1.0, sum_pairwise(mf_of));
             double Rm = 0.0;
 #pragma unroll
             for (int i = 0; i < GDTK_NSP; ++i) {

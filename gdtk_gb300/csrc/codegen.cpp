@@ -13,6 +13,7 @@
 #include <cuda.h>
 #include <nvrtc.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -329,13 +330,70 @@ std::string generate_fast_source(const GasModelHost& gm, const MechanismHost& mh
     }
     o << "}\n#define GDTK_NFALLOFF " << nfall << "\n";
 
-    // ---- rate constants
+    // ---- rate constants.  In table form (the default) the Arrhenius reactions are one loop over a
+    // __constant__ table, which keeps the code the warps cycle through each step small (the kernel is
+    // otherwise often stalled on instruction fetch); pressure-dependent reactions stay unrolled.
+    const char* kc_env = std::getenv("GDTK_KC_UNROLLED");
+    const bool kc_table = !(kc_env && kc_env[0] == '1');
+    std::vector<int> table_rx;
+    for (int ir = 0; ir < nr && (int)table_rx.size() < 320; ++ir) {   // 320 records = 51 KB of constant bank
+        const ReactionHost& r = mh.reactions[ir];
+        int np = 0;
+        for (auto& pp : participants(r)) np += pp.nu != 0;
+        if (kc_table && !r.frc.pressure_dependent() && np <= 8) table_rx.push_back(ir);
+    }
+    if (!table_rx.empty()) {
+        o << "struct KcRec { double lnA, n, mC, lnAb, nb, mCb; int mode, np, nusum, idx; int sp[8]; double nu[8]; };\n";
+        o << "__constant__ KcRec GDTK_KC_TAB[" << table_rx.size() << "] = {\n";
+        for (int ir : table_rx) {
+            const ReactionHost& r = mh.reactions[ir];
+            auto parts = participants(r);
+            int np = 0, nusum = 0;
+            std::ostringstream sp, nu;
+            for (auto& pp : parts) {
+                if (pp.nu == 0) continue;
+                sp << (np ? ", " : "") << pp.isp;
+                nu << (np ? ", " : "") << lit((double)pp.nu);
+                nusum += pp.nu;
+                ++np;
+            }
+            if (np == 0) { sp << "0"; nu << "0.0"; }
+            // mode 0: k_f Arrhenius, k_b from K_c; 1: both Arrhenius; 2: k_b Arrhenius, k_f from K_c
+            const int mode = r.frc.model == RATE_ARRHENIUS ? (r.brc.model == RATE_FROM_EQ ? 0 : 1) : 2;
+            auto lnA = [](const RateConstHost& rc) { return rc.A > 0.0 ? std::log(rc.A) : -1.0e300; };
+            o << "  {" << lit(lnA(r.frc)) << ", " << lit(r.frc.n) << ", " << lit(-r.frc.C) << ", " << lit(lnA(r.brc))
+              << ", " << lit(r.brc.n) << ", " << lit(-r.brc.C) << ", " << mode << ", " << np << ", " << nusum << ", "
+              << ir << ", {" << sp.str() << "}, {" << nu.str() << "}},   // "
+              << (r.equation.empty() ? std::string("reaction") : r.equation) << "\n";
+        }
+        o << "};\n";
+    }
     o << "__device__ __forceinline__ void gen_kc(double T, double lnT, double rT, const double* g, int gs, double* K, "
          "int ks, const double* etab, const double* Mv, int ms) {\n";
     o << "  (void)T; (void)Mv; (void)ms;\n";
+    if (!table_rx.empty()) {
+        o << "#pragma unroll 1\n";
+        o << "  for (int t = 0; t < " << table_rx.size() << "; ++t) {   // reaction.d:26-52, 94-143\n";
+        o << "    const KcRec& R = GDTK_KC_TAB[t];\n";
+        o << "    double dg = 0.0;\n";
+        o << "    for (int k = 0; k < R.np; ++k) dg = fma(R.nu[k], g[R.sp[k] * gs], dg);\n";
+        o << "    const double lnKc = fma((double)R.nusum, " << lit(std::log(101325.0 / R_universal)) << " - lnT, -dg);\n";
+        o << "    double kf, kb;\n";
+        o << "    if (R.mode != 2) {\n";
+        o << "      const double lkf = fma(R.mC, rT, fma(R.n, lnT, R.lnA));\n";
+        o << "      kf = gdtk_exp(lkf, etab);\n";
+        o << "      kb = R.mode == 0 ? gdtk_exp(lkf - lnKc, etab) : gdtk_exp(fma(R.mCb, rT, fma(R.nb, lnT, R.lnAb)), etab);\n";
+        o << "    } else {\n";
+        o << "      const double lkb = fma(R.mCb, rT, fma(R.nb, lnT, R.lnAb));\n";
+        o << "      kb = gdtk_exp(lkb, etab);\n";
+        o << "      kf = gdtk_exp(lkb + lnKc, etab);\n";
+        o << "    }\n";
+        o << "    K[R.idx * ks] = kf;\n    K[(" << nr << " + R.idx) * ks] = kb;\n  }\n";
+    }
     int ifall = 0;
     for (int ir = 0; ir < nr; ++ir) {
         const ReactionHost& r = mh.reactions[ir];
+        if (std::find(table_rx.begin(), table_rx.end(), ir) != table_rx.end()) continue;
         auto parts = participants(r);
         if (ir > 0 && ir % 4 == 0) o << "  asm volatile(\"\" ::: \"memory\");\n";
         std::ostringstream dg;   // sum nu * G/RT
@@ -474,6 +532,7 @@ std::string compile_cubin(const std::string& src, int major, int minor, std::str
     nvrtcGetProgramLogSize(prog, &n);
     log.assign(n, '\0');
     if (n) nvrtcGetProgramLog(prog, &log[0]);
+    while (!log.empty() && log.back() == '\0') log.pop_back();
     if (rc != NVRTC_SUCCESS) {
         nvrtcDestroyProgram(&prog);
         throw std::runtime_error(std::string("NVRTC compilation of the mechanism kernel failed: ") +
@@ -496,7 +555,7 @@ std::string compile_fast_check(const GasModelHost& gm, const MechanismHost& mh, 
     std::string log;
     std::string src = generate_fast_source(gm, mh, 256, 1);
     std::string cubin = compile_cubin(src, major, minor, log);
-    return log;
+    return log + "\ncubin bytes: " + std::to_string(cubin.size()) + "\n";
 }
 
 FastKernel* build_fast_kernel(const GasModelHost& gm, const MechanismHost& mh, int req_block, int req_min_blocks) {

@@ -477,3 +477,42 @@ def test_troe_fixed_volume_reactor_on_the_gpu_against_eilmer3():
     assert abs(t_ign - t_ign_ref) <= 0.01 * t_ign_ref
     assert rel.max() < 0.03
     assert rel[-1] < 2e-3
+
+
+def test_kernel_division_against_ieee_division():
+    """gdtk_div (Newton-Raphson refinement of the hardware's approximate reciprocal with one
+    quotient correction) is within 1 ulp of the IEEE quotient over the whole normal range, and
+    equal to it for zero, subnormal, infinite and NaN operands and out-of-range quotients (which
+    take the IEEE division)."""
+    import ctypes
+    import gdtk_gb300
+    torch = torch_cuda()
+    rng = np.random.Generator(np.random.PCG64(17))
+    n = 1 << 20
+    a = rng.uniform(1.0, 2.0, n) * np.exp2(rng.integers(-1000, 1000, n)) * rng.choice([-1.0, 1.0], n)
+    b = rng.uniform(1.0, 2.0, n) * np.exp2(rng.integers(-1000, 1000, n)) * rng.choice([-1.0, 1.0], n)
+    # the chemistry kernels' operand ranges: concentrations, rates, (c + 1e-50), positive denominators
+    a[: n // 4] = rng.uniform(0.0, 1.0, n // 4) * 10.0 ** rng.uniform(-40, 10, n // 4)
+    b[: n // 4] = rng.uniform(0.0, 1.0, n // 4) * 10.0 ** rng.uniform(-40, 10, n // 4) + 1e-50
+    special = np.array([0.0, -0.0, 5e-324, -3e-310, 2.2250738585072014e-308, 1.7976931348623157e308, np.inf, -np.inf,
+                        np.nan, 1.0, -1.0, 3.0, 2.0 ** -999, 2.0 ** 1000])
+    sa, sb = np.meshgrid(special, special)
+    a = np.concatenate([a, sa.ravel()])
+    b = np.concatenate([b, sb.ravel()])
+    da, db = to_dev(torch, a, b)
+    qf = torch.empty_like(da)
+    qi = torch.empty_like(da)
+    assert gdtk_gb300.lib().gdtk_div_device(len(a), da.data_ptr(), db.data_ptr(), qf.data_ptr(), qi.data_ptr()) == 0
+    qf, qi = qf.cpu().numpy(), qi.cpu().numpy()
+    assert np.array_equal(np.isnan(qf), np.isnan(qi))
+    fin = ~np.isnan(qi)
+    bf = qf[fin].view(np.int64)
+    bi = qi[fin].view(np.int64)
+    same_sign = np.sign(qf[fin]) == np.sign(qi[fin])
+    ulp = np.abs(bf - bi)
+    assert np.all(same_sign | (qi[fin] == 0.0))
+    assert ulp.max() <= 1, "largest difference %d ulp" % ulp.max()
+    assert (ulp == 0).mean() > 0.99
+    # zero, subnormal and infinite quotients come from the IEEE division itself
+    edge = fin & ((qi == 0.0) | np.isinf(qi) | (np.abs(qi) < 2.2250738585072014e-308))
+    assert np.array_equal(qf[edge].view(np.int64), qi[edge].view(np.int64))
