@@ -294,7 +294,7 @@ __device__ __noinline__ void rate_constants(const double* TH, double Tq, double*
     int sa = 0, sb = 0;
     double wb = 0.0;
     if (T >= GDTK_MIX_TLO && T <= GDTK_MIX_THI && seg_of(TH, T, sa, sb, wb)) {
-#pragma unroll 1
+        GDTK_G_UNROLL
         for (int i = 0; i < GDTK_NSP; ++i) {
             const double* c = TH + i * GDTK_TH_STRIDE + GDTK_TH_SEG0 + 15;
             double g = poly_G(c + 24 * sa, T, rT, rT2, t1, t2);
@@ -304,7 +304,7 @@ __device__ __noinline__ void rate_constants(const double* TH, double Tq, double*
     } else
 #endif
     {
-#pragma unroll 1
+        GDTK_G_UNROLL
         for (int i = 0; i < GDTK_NSP; ++i) G[i * ks] = sp_G(TH, i, T, lnT, rT, rT2, t1, t2, e);
     }
     if (e) *err = e;

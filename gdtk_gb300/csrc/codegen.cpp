@@ -251,6 +251,15 @@ std::vector<double> fast_thermo_table(const GasModelHost& gm) {
 // The temperature range where every species takes the same curve segment and blend of
 // cea_thermo_curves.d:150-182 (so that the mixture's H/R is one polynomial there): species curves
 // with at least two segments and equal first three breaks and first blend range.
+// Unroll factors of the rate-constant loops (reaction table, species G/RT): two independent
+// iterations in flight give the FP64 pipe work while one waits on its table loads.
+int env_int(const char* name, int dflt) {
+    const char* e = std::getenv(name);
+    return (e && *e) ? std::max(1, std::atoi(e)) : dflt;
+}
+int kc_unroll() { return env_int("GDTK_KC_UNROLL", 1); }
+int g_unroll() { return env_int("GDTK_G_UNROLL", 1); }
+
 bool mix_thermo_range(const GasModelHost& gm, double& tlo, double& thi) {
     const int nsp = gm.n_species();
     if (nsp == 0) return false;
@@ -303,6 +312,7 @@ std::string generate_fast_source(const GasModelHost& gm, const MechanismHost& mh
         o << "#define GDTK_MIX_THERMO " << (mix ? 1 : 0) << "\n";
         if (mix) o << "#define GDTK_MIX_TLO " << lit(tlo) << "\n#define GDTK_MIX_THI " << lit(thi) << "\n";
         o << "#define GDTK_VEC " << fast_vec_doubles(gm, mh) << "\n";
+        o << "#define GDTK_G_UNROLL _Pragma(\"unroll " << g_unroll() << "\")\n";
     }
     o << kFastExpSource << "\n";
     auto arr = [&](const char* name, std::function<double(int)> f) {
@@ -372,7 +382,7 @@ std::string generate_fast_source(const GasModelHost& gm, const MechanismHost& mh
          "int ks, const double* etab, const double* Mv, int ms) {\n";
     o << "  (void)T; (void)Mv; (void)ms;\n";
     if (!table_rx.empty()) {
-        o << "#pragma unroll 1\n";
+        o << "#pragma unroll " << kc_unroll() << "\n";
         o << "  for (int t = 0; t < " << table_rx.size() << "; ++t) {   // reaction.d:26-52, 94-143\n";
         o << "    const KcRec& R = GDTK_KC_TAB[t];\n";
         o << "    double dg = 0.0;\n";
