@@ -504,7 +504,8 @@ def run_surrogate(args, w):
                    "train_samples": int(n_train), "heldout_fraction": 0.05, "epochs": epochs,
                    "batch": w["batch"], "l2": "inputs larger than L2 (no flush)"},
         "plain_fp64": {"cell_updates_per_s": n / plain_time, "seconds": plain_time,
-                       "roofline_frac": achieved / peak},
+                       "roofline_frac": achieved / peak,
+                       "cells_failed": int(((plain_st != 0) & (plain_st != 6)).sum().item())},
         "surrogate_speedup_vs_plain": d["speedup_vs_plain"],
         "sweep": sweep,
         "accuracy_vs_cpu_reference": cpu_err,

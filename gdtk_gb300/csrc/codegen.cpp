@@ -259,6 +259,12 @@ int env_int(const char* name, int dflt) {
 }
 int kc_unroll() { return env_int("GDTK_KC_UNROLL", 1); }
 int g_unroll() { return env_int("GDTK_G_UNROLL", 1); }
+// Reactions between compiler fences in gen_rhs (0: none); the fences bound how far the scheduler
+// hoists the k_f, k_b loads, and with them the registers held.
+int rhs_fence() {
+    const char* e = std::getenv("GDTK_RHS_FENCE");
+    return (e && *e) ? std::max(0, std::atoi(e)) : 4;
+}
 
 bool mix_thermo_range(const GasModelHost& gm, double& tlo, double& thi) {
     const int nsp = gm.n_species();
@@ -500,7 +506,7 @@ std::string generate_fast_source(const GasModelHost& gm, const MechanismHost& mh
         const ReactionHost& r = mh.reactions[ir];
         // A compiler barrier every few reactions stops the scheduler from hoisting every k_f/k_b
         // load to the top, which would hold 2 NR doubles live and spill registers.
-        if (ir > 0 && ir % 4 == 0) o << "  asm volatile(\"\" ::: \"memory\");\n";
+        if (ir > 0 && rhs_fence() > 0 && ir % rhs_fence() == 0) o << "  asm volatile(\"\" ::: \"memory\");\n";
         o << "  {\n    double wf = K[" << ir << " * ks], wb = K[" << (nr + ir) << " * ks];\n";
         if (r.collider) o << "    wf *= M" << set_of[ir] << "; wb *= M" << set_of[ir] << ";\n";
         for (auto& x : r.reac) o << "    wf *= " << ipow_expr("c[" + std::to_string(x.first) + "]", x.second) << ";\n";
