@@ -80,7 +80,7 @@ SIGNATURES = {
     "chem_reactor_fast_source": (ctypes.c_int, [ctypes.c_int, _c, ctypes.c_int]),
     "chem_reactor_jit_log": (ctypes.c_int, [ctypes.c_int, _c, ctypes.c_int]),
     "gdtk_measure_fp64_peak": (ctypes.c_int, [_d]),
-    "gdtk_div_device": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "gdtk_div_device": (ctypes.c_int, [ctypes.c_int] + [ctypes.c_void_p] * 5),
     # include/gdtk_surrogate.h
     "chem_surrogate_new": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_ulonglong]),
     "chem_surrogate_free": (ctypes.c_int, [ctypes.c_int]),

@@ -33,6 +33,7 @@ namespace gdtk_fast {
 
 using gdtk::gdtk_exp;
 using gdtk::gdtk_div;
+using gdtk::gdtk_div_nr;
 
 // must match the host's CellBlock / FastArgs (codegen.h)
 struct CellBlock {
@@ -242,7 +243,7 @@ __device__ __noinline__ double T_from_u(const double* TH, const double* YR, int 
                 cv = fma(yr, Cp - 1.0, cv);
             }
         }
-        dT = -gdtk_div(f - u_tgt, cv);
+        dT = -gdtk_div_nr(f - u_tgt, cv);
         ++*iters;
     }
     if (fabs(dT) > 1e-3) *err = ST_NEWTON;
@@ -537,14 +538,14 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
                 for (int i = 0; i < GDTK_NSP; ++i) {
                     const double y = y0[i];
                     const double ci_ = (s == 0) ? y : yn[i];
-                    const double pp = gdtk_div(L[i], ci_ + ZERO_EPS);
+                    const double pp = gdtk_div_nr(L[i], ci_ + ZERO_EPS);
                     const double x = pp * h;
                     double N, D;
                     alpha_nd(x + ZERO_EPS, N, D);
                     const double q0 = (s == 0) ? q[i] : Q0[i * ks];
                     const double pb = (s == 0) ? pp : 0.5 * (P0[i * ks] + pp);
                     const double num = h * (fma(N, q[i] - q0, D * q0) - D * (pb * y));
-                    const double v = y + gdtk_div(num, fma(N, h * pb, D));
+                    const double v = y + gdtk_div_nr(num, fma(N, h * pb, D));
                     if (s == 0) {
                         Q0[i * ks] = q[i];
                         P0[i * ks] = pp;
@@ -556,20 +557,23 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
                 }
                 if (s > 0 && conv) break;
             }
-            double sigma = 0.0;
+            // sigma = max_i |yc - yp0| / (eps2 (yc + delta)), the largest ratio found by comparing
+            // cross products (denominators are positive), then one division
+            double snum = 0.0, sden = 1.0;
 #pragma unroll
             for (int i = 0; i < GDTK_NSP; ++i) {
                 double yc = yn[i];
                 if (yc < ZERO_EPS) continue;
-                double test = gdtk_div(fabs(yc - YP0[i * ks]), GDTK_EPS2 * (yc + GDTK_DELTA));
-                if (test > sigma) sigma = test;
+                const double num = fabs(yc - YP0[i * ks]), den = GDTK_EPS2 * (yc + GDTK_DELTA);
+                if (num * sden > snum * den) { snum = num; sden = den; }
             }
+            const double sigma = gdtk_div(snum, sden);
             if (sigma <= 0.0) dtS = 10.0 * h;
             else {
                 double x = sigma;
-                x = x - 0.5 * gdtk_div(x * x - sigma, x);
-                x = x - 0.5 * gdtk_div(x * x - sigma, x);
-                x = x - 0.5 * gdtk_div(x * x - sigma, x);
+                x = x - 0.5 * gdtk_div_nr(x * x - sigma, x);
+                x = x - 0.5 * gdtk_div_nr(x * x - sigma, x);
+                x = x - 0.5 * gdtk_div_nr(x * x - sigma, x);
                 dtS = h * (gdtk_div(1.0, x) + 0.005);
             }
             ok = conv;

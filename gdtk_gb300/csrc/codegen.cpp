@@ -287,6 +287,64 @@ bool mix_thermo_range(const GasModelHost& gm, double& tlo, double& thi) {
     return thi > tlo;
 }
 
+// Largest |G_i / R T| of each species over [tlo, thi] (log-spaced samples plus the curve breaks),
+// from the same NASA-9 curves, blends and extrapolation the kernels use.
+std::vector<double> species_g_bound(const GasModelHost& gm, double tlo, double thi) {
+    const int nsp = gm.n_species();
+    PackedMech pm = pack(gm, nullptr);
+    MechView v;
+    v.bind(pm.I.data(), pm.D.data());
+    std::vector<double> Ts;
+    const int n = 4000;
+    for (int k = 0; k <= n; ++k) Ts.push_back(tlo * std::pow(thi / tlo, (double)k / n));
+    for (auto& c : gm.curves)
+        for (double b : c.breaks)
+            if (b > tlo && b < thi) { Ts.push_back(b); Ts.push_back(b * (1 - 1e-9)); Ts.push_back(b * (1 + 1e-9)); }
+    std::vector<double> out(nsp, 0.0);
+    for (int i = 0; i < nsp; ++i) {
+        const double Ri = R_universal / gm.M[i];
+        for (double T : Ts) {
+            int err = 0;
+            const double lT = std::log(T);
+            const double g = (cea_h(v, i, T, lT, err) - T * cea_s(v, i, T, lT, err)) / (Ri * T);
+            out[i] = (err || !std::isfinite(g)) ? 1e300 : std::max(out[i], std::fabs(g));
+        }
+    }
+    return out;
+}
+
+// Reactions whose k_b = k_f / K_c is formed as k_f (R T / P_atm)^(sum nu) prod_i E_i^nu_i with
+// E_i = exp(G_i / R T) formed once per species (GDTK_KB_EXP=1 keeps one exp per reaction).  Only where
+// every partial product stays inside exp(+-600) over the mechanism's temperature limits, so that no
+// product can overflow or underflow.
+std::vector<bool> kb_product_reactions(const GasModelHost& gm, const MechanismHost& mh) {
+    std::vector<bool> out(mh.reactions.size(), false);
+    const char* e = std::getenv("GDTK_KB_EXP");
+    if (e && e[0] == '1') return out;
+    const std::vector<double> gb = species_g_bound(gm, mh.T_lower, mh.T_upper);
+    const double lcf = std::max(std::fabs(std::log(mh.T_lower * R_universal / 101325.0)),
+                                std::fabs(std::log(mh.T_upper * R_universal / 101325.0)));
+    for (size_t ir = 0; ir < mh.reactions.size(); ++ir) {
+        const ReactionHost& r = mh.reactions[ir];
+        if (r.frc.pressure_dependent() || r.frc.model != RATE_ARRHENIUS || r.brc.model != RATE_FROM_EQ) continue;
+        double bound = 0.0;
+        int nusum = 0, np = 0;
+        for (auto& pp : participants(r)) {
+            bound += std::abs(pp.nu) * gb[pp.isp];
+            nusum += pp.nu;
+            np += pp.nu != 0;
+        }
+        bound += std::abs(nusum) * lcf;
+        out[ir] = np <= 8 && bound <= 600.0;
+    }
+    return out;
+}
+
+bool any_kb_products(const GasModelHost& gm, const MechanismHost& mh) {
+    for (bool b : kb_product_reactions(gm, mh)) if (b) return true;
+    return false;
+}
+
 // Per-thread method vector (doubles): the ODE method's stage storage, and room for the
 // species' Y_i R_i plus two sets of 8 mixture coefficients during T(rho, u).
 int fast_vec_doubles(const GasModelHost& gm, const MechanismHost& mh) {
@@ -296,7 +354,8 @@ int fast_vec_doubles(const GasModelHost& gm, const MechanismHost& mh) {
     if (mix_thermo_range(gm, tlo, thi)) vec = std::max(vec, nsp + 16);
     int nfall = 0;   // third-body concentrations of pressure-dependent rates, beside G/RT
     for (auto& r : mh.reactions) nfall += r.frc.pressure_dependent() ? 1 : 0;
-    return std::max(vec, nsp + nfall);
+    // G/RT, the falloff concentrations, then E_i and 1/E_i for the product-form k_b
+    return std::max(vec, (any_kb_products(gm, mh) ? 3 * nsp : nsp) + nfall);
 }
 
 std::string generate_fast_source(const GasModelHost& gm, const MechanismHost& mh, int block, int min_blocks) {
@@ -329,7 +388,7 @@ std::string generate_fast_source(const GasModelHost& gm, const MechanismHost& mh
     arr("GDTK_M", [&](int i) { return gm.M[i]; });
     arr("GDTK_RM", [&](int i) { return 1.0 / gm.M[i]; });
     arr("GDTK_R", [&](int i) { return R_universal / gm.M[i]; });
-    o << "namespace gdtk_fast {\nusing gdtk::gdtk_exp;\n";
+    o << "namespace gdtk_fast {\nusing gdtk::gdtk_exp;\nusing gdtk::gdtk_div_nr;\n";
 
     // ---- third-body concentrations of the pressure-dependent rate constants (rate_constant.d:114-121),
     // from the concentrations at which the rate constants are evaluated
@@ -358,28 +417,35 @@ std::string generate_fast_source(const GasModelHost& gm, const MechanismHost& mh
         for (auto& pp : participants(r)) np += pp.nu != 0;
         if (kc_table && !r.frc.pressure_dependent() && np <= 8) table_rx.push_back(ir);
     }
+    const std::vector<bool> kbp = kb_product_reactions(gm, mh);
+    bool any_kbp = false;
+    for (int ir : table_rx) any_kbp = any_kbp || kbp[ir];
     if (!table_rx.empty()) {
-        o << "struct KcRec { double lnA, n, mC, lnAb, nb, mCb; int mode, np, nusum, idx; int sp[8]; double nu[8]; };\n";
+        o << "struct KcRec { double lnA, n, mC, lnAb, nb, mCb; int mode, np, nusum, idx; int sp[8], anu[8]; "
+             "double nu[8]; };\n";
         o << "__constant__ KcRec GDTK_KC_TAB[" << table_rx.size() << "] = {\n";
         for (int ir : table_rx) {
             const ReactionHost& r = mh.reactions[ir];
             auto parts = participants(r);
             int np = 0, nusum = 0;
-            std::ostringstream sp, nu;
+            std::ostringstream sp, nu, anu;
             for (auto& pp : parts) {
                 if (pp.nu == 0) continue;
                 sp << (np ? ", " : "") << pp.isp;
                 nu << (np ? ", " : "") << lit((double)pp.nu);
+                anu << (np ? ", " : "") << std::abs(pp.nu);
                 nusum += pp.nu;
                 ++np;
             }
-            if (np == 0) { sp << "0"; nu << "0.0"; }
-            // mode 0: k_f Arrhenius, k_b from K_c; 1: both Arrhenius; 2: k_b Arrhenius, k_f from K_c
-            const int mode = r.frc.model == RATE_ARRHENIUS ? (r.brc.model == RATE_FROM_EQ ? 0 : 1) : 2;
+            if (np == 0) { sp << "0"; nu << "0.0"; anu << "0"; }
+            // mode 0: k_f Arrhenius, k_b from K_c; 1: both Arrhenius; 2: k_b Arrhenius, k_f from K_c;
+            // 3: as 0, with k_b = k_f / K_c from the species' E_i
+            int mode = r.frc.model == RATE_ARRHENIUS ? (r.brc.model == RATE_FROM_EQ ? 0 : 1) : 2;
+            if (mode == 0 && kbp[ir]) mode = 3;
             auto lnA = [](const RateConstHost& rc) { return rc.A > 0.0 ? std::log(rc.A) : -1.0e300; };
             o << "  {" << lit(lnA(r.frc)) << ", " << lit(r.frc.n) << ", " << lit(-r.frc.C) << ", " << lit(lnA(r.brc))
               << ", " << lit(r.brc.n) << ", " << lit(-r.brc.C) << ", " << mode << ", " << np << ", " << nusum << ", "
-              << ir << ", {" << sp.str() << "}, {" << nu.str() << "}},   // "
+              << ir << ", {" << sp.str() << "}, {" << anu.str() << "}, {" << nu.str() << "}},   // "
               << (r.equation.empty() ? std::string("reaction") : r.equation) << "\n";
         }
         o << "};\n";
@@ -387,10 +453,35 @@ std::string generate_fast_source(const GasModelHost& gm, const MechanismHost& mh
     o << "__device__ __forceinline__ void gen_kc(double T, double lnT, double rT, const double* g, int gs, double* K, "
          "int ks, const double* etab, const double* Mv, int ms) {\n";
     o << "  (void)T; (void)Mv; (void)ms;\n";
+    if (any_kbp) {   // E_i = exp(G_i / R T) and its reciprocal, after G/RT and the falloff concentrations
+        o << "  const double* E = g + (" << nsp << " + " << nfall << ") * gs;\n";
+        o << "  const double* Ei = E + " << nsp << " * gs;\n";
+        o << "#pragma unroll 1\n";
+        o << "  for (int i = 0; i < " << nsp << "; ++i) {\n";
+        o << "    const double e = gdtk_exp(g[i * gs], etab);\n";
+        o << "    const_cast<double*>(E)[i * gs] = e;\n";
+        o << "    const_cast<double*>(Ei)[i * gs] = gdtk_div_nr(1.0, e);\n  }\n";
+        o << "  const double cf = T * " << lit(R_universal / 101325.0) << ", rcf = rT * " << lit(101325.0 / R_universal)
+          << ";   // R T / P_atm and its reciprocal\n";
+    }
     if (!table_rx.empty()) {
         o << "#pragma unroll " << kc_unroll() << "\n";
         o << "  for (int t = 0; t < " << table_rx.size() << "; ++t) {   // reaction.d:26-52, 94-143\n";
         o << "    const KcRec& R = GDTK_KC_TAB[t];\n";
+        if (any_kbp) {
+            o << "    if (R.mode == 3) {   // k_b = k_f (R T / P_atm)^(sum nu) prod E_i^nu_i\n";
+            o << "      const double kf = gdtk_exp(fma(R.mC, rT, fma(R.n, lnT, R.lnA)), etab);\n";
+            o << "      double P = 1.0;\n";
+            o << "      const double c = R.nusum > 0 ? cf : rcf;\n";
+            o << "      for (int m = 0; m < abs(R.nusum); ++m) P *= c;\n";
+            o << "      for (int k = 0; k < R.np; ++k) {\n";
+            o << "        const double v = (R.nu[k] > 0.0 ? E : Ei)[R.sp[k] * gs];\n";
+            o << "        for (int m = 0; m < R.anu[k]; ++m) P *= v;\n      }\n";
+            o << "      K[R.idx * ks] = kf;\n      K[(" << nr << " + R.idx) * ks] = kf * P;\n      continue;\n    }\n";
+        }
+        bool all_kbp = true;
+        for (int ir : table_rx) all_kbp = all_kbp && kbp[ir];
+        if (all_kbp) o << "#if 0   // every table reaction takes the product form\n";
         o << "    double dg = 0.0;\n";
         o << "    for (int k = 0; k < R.np; ++k) dg = fma(R.nu[k], g[R.sp[k] * gs], dg);\n";
         o << "    const double lnKc = fma((double)R.nusum, " << lit(std::log(101325.0 / R_universal)) << " - lnT, -dg);\n";
@@ -404,7 +495,9 @@ std::string generate_fast_source(const GasModelHost& gm, const MechanismHost& mh
         o << "      kb = gdtk_exp(lkb, etab);\n";
         o << "      kf = gdtk_exp(lkb + lnKc, etab);\n";
         o << "    }\n";
-        o << "    K[R.idx * ks] = kf;\n    K[(" << nr << " + R.idx) * ks] = kb;\n  }\n";
+        o << "    K[R.idx * ks] = kf;\n    K[(" << nr << " + R.idx) * ks] = kb;\n";
+        if (all_kbp) o << "#endif\n";
+        o << "  }\n";
     }
     int ifall = 0;
     for (int ir = 0; ir < nr; ++ir) {

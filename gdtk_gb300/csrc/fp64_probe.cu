@@ -21,19 +21,21 @@ __global__ void dfma_loop(double* out, int iters, double a, double b) {
     out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
 }
 
-__global__ void div_pairs(int n, const double* a, const double* b, double* q_fast, double* q_ieee) {
+__global__ void div_pairs(int n, const double* a, const double* b, double* q_fast, double* q_nr, double* q_ieee) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     q_fast[i] = gdtk::gdtk_div(a[i], b[i]);
+    q_nr[i] = gdtk::gdtk_div_nr(a[i], b[i]);
     q_ieee[i] = a[i] / b[i];
 }
 
 }  // namespace
 
-extern "C" int gdtk_div_device(int n, const double* a, const double* b, double* q_fast, double* q_ieee) {
-    if (n < 0 || (n > 0 && (!a || !b || !q_fast || !q_ieee))) return -1;
+extern "C" int gdtk_div_device(int n, const double* a, const double* b, double* q_fast, double* q_nr,
+                               double* q_ieee) {
+    if (n < 0 || (n > 0 && (!a || !b || !q_fast || !q_nr || !q_ieee))) return -1;
     if (n == 0) return 0;
-    div_pairs<<<(n + 255) / 256, 256>>>(n, a, b, q_fast, q_ieee);
+    div_pairs<<<(n + 255) / 256, 256>>>(n, a, b, q_fast, q_nr, q_ieee);
     return cudaDeviceSynchronize() == cudaSuccess ? 0 : -1;
 }
 

@@ -192,10 +192,10 @@ int chem_reactor_last_launch(int cr_i, int* grid, int* block, int* smem_bytes, i
 const char* gdtk_last_error(void);
 /* Measures this GPU's FP64 FMA throughput (TFLOP/s) with a register-resident DFMA loop. */
 int gdtk_measure_fp64_peak(double* tflops);
-/* The chemistry kernels' FP64 division (gdtk_div: Newton-Raphson refinement of the hardware's
- * approximate reciprocal) and the IEEE division of the same device arrays a[n], b[n], for
- * testing; synchronises the device. */
-int gdtk_div_device(int n, const double* a, const double* b, double* q_fast, double* q_ieee);
+/* The chemistry kernels' FP64 divisions and the IEEE division of the same device arrays a[n], b[n],
+ * for testing: q_fast = gdtk_div (Newton-Raphson refinement of the hardware's approximate reciprocal
+ * with a quotient correction), q_nr = gdtk_div_nr (without the correction); synchronises the device. */
+int gdtk_div_device(int n, const double* a, const double* b, double* q_fast, double* q_nr, double* q_ieee);
 
 #ifdef __cplusplus
 }

@@ -482,9 +482,8 @@ def test_troe_fixed_volume_reactor_on_the_gpu_against_eilmer3():
 def test_kernel_division_against_ieee_division():
     """gdtk_div (Newton-Raphson refinement of the hardware's approximate reciprocal with one
     quotient correction) is within 1 ulp of the IEEE quotient over the whole normal range, and
-    equal to it for zero, subnormal, infinite and NaN operands and out-of-range quotients (which
-    take the IEEE division)."""
-    import ctypes
+    gdtk_div_nr (without the correction) within 2 ulp; both equal it for zero, subnormal and
+    infinite quotients (which take the IEEE division) and give NaN where it does."""
     import gdtk_gb300
     torch = torch_cuda()
     rng = np.random.Generator(np.random.PCG64(17))
@@ -500,19 +499,18 @@ def test_kernel_division_against_ieee_division():
     a = np.concatenate([a, sa.ravel()])
     b = np.concatenate([b, sb.ravel()])
     da, db = to_dev(torch, a, b)
-    qf = torch.empty_like(da)
-    qi = torch.empty_like(da)
-    assert gdtk_gb300.lib().gdtk_div_device(len(a), da.data_ptr(), db.data_ptr(), qf.data_ptr(), qi.data_ptr()) == 0
-    qf, qi = qf.cpu().numpy(), qi.cpu().numpy()
-    assert np.array_equal(np.isnan(qf), np.isnan(qi))
+    qf, qn, qi = torch.empty_like(da), torch.empty_like(da), torch.empty_like(da)
+    assert gdtk_gb300.lib().gdtk_div_device(len(a), da.data_ptr(), db.data_ptr(), qf.data_ptr(), qn.data_ptr(),
+                                            qi.data_ptr()) == 0
+    qi = qi.cpu().numpy()
     fin = ~np.isnan(qi)
-    bf = qf[fin].view(np.int64)
-    bi = qi[fin].view(np.int64)
-    same_sign = np.sign(qf[fin]) == np.sign(qi[fin])
-    ulp = np.abs(bf - bi)
-    assert np.all(same_sign | (qi[fin] == 0.0))
-    assert ulp.max() <= 1, "largest difference %d ulp" % ulp.max()
-    assert (ulp == 0).mean() > 0.99
-    # zero, subnormal and infinite quotients come from the IEEE division itself
     edge = fin & ((qi == 0.0) | np.isinf(qi) | (np.abs(qi) < 2.2250738585072014e-308))
-    assert np.array_equal(qf[edge].view(np.int64), qi[edge].view(np.int64))
+    for q, bound, exact in ((qf.cpu().numpy(), 1, 0.99), (qn.cpu().numpy(), 2, 0.5)):
+        assert np.array_equal(np.isnan(q), np.isnan(qi))
+        ulp = np.abs(q[fin].view(np.int64) - qi[fin].view(np.int64))
+        assert np.all((np.sign(q[fin]) == np.sign(qi[fin])) | (qi[fin] == 0.0))
+        print("max %d ulp, %.4f exact" % (ulp.max(), (ulp == 0).mean()))
+        assert ulp.max() <= bound, "largest difference %d ulp" % ulp.max()
+        assert (ulp == 0).mean() > exact
+        # zero, subnormal and infinite quotients come from the IEEE division itself
+        assert np.array_equal(q[edge].view(np.int64), qi[edge].view(np.int64))
