@@ -70,12 +70,25 @@ struct FastArgs {
 };
 
 // Lane-occupancy instrumentation: for phase k, count warp executions and the lanes active in them.
+// Generated with GDTK_PHASE_CLOCKS, each mark also adds the SM cycles since the warp's previous mark
+// to that mark's phase (st[16 + phase]): a per-phase split of every warp's time.
+#if GDTK_PHASE_CLOCKS
+__shared__ long long gdtk_pc_t0[32];
+__shared__ int gdtk_pc_ph[32];
+#endif
 __device__ __forceinline__ void lane_stat(unsigned long long* st, int k) {
     if (!st) return;
     const unsigned m = __activemask();
     if ((threadIdx.x & 31) == __ffs(m) - 1) {
         atomicAdd(st + 2 * k, 1ull);
         atomicAdd(st + 2 * k + 1, (unsigned long long)__popc(m));
+#if GDTK_PHASE_CLOCKS
+        const int w = threadIdx.x >> 5;
+        const long long t = clock64();
+        if (gdtk_pc_ph[w] >= 0) atomicAdd(st + 16 + gdtk_pc_ph[w], (unsigned long long)(t - gdtk_pc_t0[w]));
+        gdtk_pc_t0[w] = t;
+        gdtk_pc_ph[w] = k;
+#endif
     }
 }
 
@@ -170,15 +183,21 @@ __device__ __forceinline__ double sp_G(const double* TH, int i, double T, double
 // polynomial instead of one per species.  The sums are reassociated, so f and cv differ from the
 // per-species sums in the last bits only.
 #if GDTK_MIX_THERMO
+// One pass over the species with the 8 sums in registers: each sum still adds the species in
+// order 0..nsp-1, and the 8 chains are independent of one another.
 __device__ __forceinline__ void mix_coeffs(const double* TH, const double* YR, int ys, int seg, double* m) {
+    double acc[8];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        double acc = 0.0;
+    for (int k = 0; k < 8; ++k) acc[k] = 0.0;
 #pragma unroll 1
-        for (int i = 0; i < GDTK_NSP; ++i)
-            acc = fma(YR[i * ys], TH[i * GDTK_TH_STRIDE + GDTK_TH_SEG0 + 24 * seg + k], acc);
-        m[k * ys] = acc;
+    for (int i = 0; i < GDTK_NSP; ++i) {
+        const double yr = YR[i * ys];
+        const double* c = TH + i * GDTK_TH_STRIDE + GDTK_TH_SEG0 + 24 * seg;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) acc[k] = fma(yr, c[k], acc[k]);
     }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) m[k * ys] = acc[k];
 }
 // H/R and Cp/R = d(H/R)/dT of the mixture polynomial m (H/R = -a0/T + a1 lnT + a7 + a2 T + a3/2 T^2 + ...)
 __device__ __forceinline__ void mix_H_Cp(const double* m, int ys, double T, double lnT, double rT, double rT2,
@@ -363,6 +382,10 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
     const int ks = blockDim.x;
     double* K = S + threadIdx.x;                         // kf[NR], kb[NR]
     double* V = K + 2 * GDTK_NR * ks;                    // method vectors; also G/RT and Y_i R_i scratch
+#if GDTK_PHASE_CLOCKS
+    if ((threadIdx.x & 31) == 0) gdtk_pc_ph[threadIdx.x >> 5] = -1;
+    __syncwarp();
+#endif
 
     unsigned g = 0;
     int b = 0, ci = 0;
@@ -522,6 +545,7 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
                     lane_stat(a.lane_stats, 2);
                     gen_rhs(cin, q, L, K, ks);
                 }
+                lane_stat(a.lane_stats, 7);
                 ++n_rhs;
                 if (s == 0) {
                     if (phase == 0) {

@@ -378,6 +378,8 @@ std::string generate_fast_source(const GasModelHost& gm, const MechanismHost& mh
         if (mix) o << "#define GDTK_MIX_TLO " << lit(tlo) << "\n#define GDTK_MIX_THI " << lit(thi) << "\n";
         o << "#define GDTK_VEC " << fast_vec_doubles(gm, mh) << "\n";
         o << "#define GDTK_G_UNROLL _Pragma(\"unroll " << g_unroll() << "\")\n";
+        const char* pc = std::getenv("GDTK_PHASE_CLOCKS");
+        o << "#define GDTK_PHASE_CLOCKS " << ((pc && pc[0] == '1') ? 1 : 0) << "\n";
     }
     o << kFastExpSource << "\n";
     auto arr = [&](const char* name, std::function<double(int)> f) {
@@ -433,7 +435,7 @@ std::string generate_fast_source(const GasModelHost& gm, const MechanismHost& mh
                 if (pp.nu == 0) continue;
                 sp << (np ? ", " : "") << pp.isp;
                 nu << (np ? ", " : "") << lit((double)pp.nu);
-                anu << (np ? ", " : "") << std::abs(pp.nu);
+                anu << (np ? ", " : "") << pp.nu;   // signed: > 0 products, < 0 reactants
                 nusum += pp.nu;
                 ++np;
             }
@@ -475,8 +477,9 @@ std::string generate_fast_source(const GasModelHost& gm, const MechanismHost& mh
             o << "      const double c = R.nusum > 0 ? cf : rcf;\n";
             o << "      for (int m = 0; m < abs(R.nusum); ++m) P *= c;\n";
             o << "      for (int k = 0; k < R.np; ++k) {\n";
-            o << "        const double v = (R.nu[k] > 0.0 ? E : Ei)[R.sp[k] * gs];\n";
-            o << "        for (int m = 0; m < R.anu[k]; ++m) P *= v;\n      }\n";
+            o << "        const int nk = R.anu[k];\n";
+            o << "        const double v = (nk > 0 ? E : Ei)[R.sp[k] * gs];\n";
+            o << "        for (int m = 0; m < abs(nk); ++m) P *= v;\n      }\n";
             o << "      K[R.idx * ks] = kf;\n      K[(" << nr << " + R.idx) * ks] = kf * P;\n      continue;\n    }\n";
         }
         bool all_kbp = true;

@@ -83,8 +83,13 @@ GDTK_HD double gdtk_exp(double x, const double* tab) {
     const double L1 = 0x1.62e42fee00000p-7;      // ln2/64, leading 32 bits
     const double L2 = 0x1.a39ef35793c76p-39;     // ln2/64 - L1
     const double SHIFT = 0x1.8p52;               // round-to-integer shift
-    if (!(x > -745.1332191019412)) return x != x ? x : 0.0;
-    if (x > 709.782712893384) return x * 0x1p1023;   // +inf
+    // |x| < 512 (biased exponent below 1032), tested on the bits: the result is normal and the
+    // scaling below needs no range check.  NaN, infinities and the range ends take the compares.
+    const bool inner = ((gdtk_bits(x) >> 52) & 0x7ff) < 1032;
+    if (!inner) {
+        if (!(x > -745.1332191019412)) return x != x ? x : 0.0;
+        if (x > 709.782712893384) return x * 0x1p1023;   // +inf
+    }
     double t = gdtk_fma(x, INV_L, SHIFT);
     int k = (int)(uint32_t)(gdtk_bits(t) & 0xffffffff);
     double kd = t - SHIFT;
@@ -99,7 +104,7 @@ GDTK_HD double gdtk_exp(double x, const double* tab) {
     double T = tab[k & 63];
     double y = gdtk_fma(T, p, T);
     int m = k >> 6;
-    if (m >= -1020 && m <= 1022) return gdtk_from_bits(gdtk_bits(y) + ((int64_t)m << 52));
+    if (inner || (m >= -1020 && m <= 1022)) return gdtk_from_bits(gdtk_bits(y) + ((int64_t)m << 52));
     // near the ends of the range: scale in two exact-power steps (the second may round
     // into the subnormal range, as the true result does)
     int m1 = m / 2, m2 = m - m1;

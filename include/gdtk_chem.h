@@ -178,11 +178,12 @@ int gdtk_compile_fast_source_check(const char* gas_file, const char* chem_file, 
  * restores the default (largest block the shared-memory budget allows).  Compiles and loads the
  * variant now; later updates use it.  Used by the autotuner (gdtk_gb300/autotune.py). */
 int chem_reactor_configure(int cr_i, int block, int min_blocks);
-/* Diagnostics: when stats (device, unsigned long long[16]) is set, later fast-kernel launches
+/* Diagnostics: when stats (device, unsigned long long[24]) is set, later fast-kernel launches
  * add, for each phase k (0 iteration, 1 rate constants, 2 right-hand side, 3 step control,
- * 4 Newton iteration, 5 cell completion, 6 refill), the number of warp executions in
- * stats[2k] and of active lanes in them in stats[2k+1].  NULL turns it off.  No counterpart in
- * the reference. */
+ * 4 Newton iteration, 5 cell completion, 6 refill, 7 the alpha-QSS update after a right-hand
+ * side), the number of warp executions in stats[2k] and of active lanes in them in stats[2k+1].
+ * A kernel generated with GDTK_PHASE_CLOCKS=1 in the environment also adds each warp's SM cycles
+ * spent in phase k to stats[16 + k].  NULL turns it off.  No counterpart in the reference. */
 int chem_reactor_set_lane_stats(int cr_i, unsigned long long* stats);
 /* Reactor description: n species, n reactions, ODE method (0 rkf, 1 alpha-qss), tight coupling. */
 int chem_reactor_info(int cr_i, int* nsp, int* nr, int* method, int* tight);
