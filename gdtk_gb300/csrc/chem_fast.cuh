@@ -209,10 +209,20 @@ __device__ __forceinline__ void mix_H_Cp(const double* m, int ys, double T, doub
 }
 #endif
 
+// ln(T (1 + x)) from ln T: ln T + log1p(x) by its Taylor series to x^6 when |x| < 2^-10 (the
+// truncation is below 2^-60 |x|), else a fresh log.  The kernel carries ln T with each cell this way,
+// because a library log costs as much FP64 issue as about 36 FMAs.
+__device__ __forceinline__ double ln_step(double lnT, double x, double T) {
+    if (fabs(x) < 0x1p-10)
+        return lnT + x * fma(x, fma(x, fma(x, fma(x, fma(x, -1.0 / 6.0, 0.2), -0.25), 1.0 / 3.0), -0.5), 1.0);
+    return log(T);
+}
+
+// *lnT_io: ln T_guess on entry, ln of the returned T on exit.
 __device__ __noinline__ double T_from_u(const double* TH, const double* YR, int ys, double* S, double u_tgt,
-                                        double T_guess, int* err, int* iters, unsigned long long* lst) {
+                                        double T_guess, double* lnT_io, int* err, int* iters, unsigned long long* lst) {
     const double TOL = 1e-10;
-    double T = T_guess, dT = 0.0;
+    double T = T_guess, dT = 0.0, lnT = *lnT_io, rT = gdtk_div(1.0, T);
 #if GDTK_MIX_THERMO
     double* ma = S;
     double* mb = S + 8 * ys;
@@ -226,11 +236,14 @@ __device__ __noinline__ double T_from_u(const double* TH, const double* YR, int 
     for (int it = 0; it <= 10; ++it) {
         lane_stat(lst, 4);
         if (it > 0) {
+            const double x = dT * rT;   // dT / T of the previous iterate
             T += dT;
-            if (gdtk_div(fabs(dT), T) < TOL) return T;
+            lnT = ln_step(lnT, x, T);
+            if (gdtk_div(fabs(dT), T) < TOL) { *lnT_io = lnT; return T; }
             if (it == 10) break;
+            rT = gdtk_div(1.0, T);
         }
-        const double lnT = log(T), rT = gdtk_div(1.0, T), rT2 = rT * rT;
+        const double rT2 = rT * rT;
         double f = 0.0, cv = 0.0;
 #if GDTK_MIX_THERMO
         int sa = 0, sb = 0;
@@ -266,6 +279,7 @@ __device__ __noinline__ double T_from_u(const double* TH, const double* YR, int 
         ++*iters;
     }
     if (fabs(dT) > 1e-3) *err = ST_NEWTON;
+    *lnT_io = lnT;
     return T;
 }
 
@@ -302,12 +316,12 @@ __device__ __forceinline__ double sum_pairwise(F d) {
 // species G/RT go through the per-thread scratch vector G.
 // G: scratch of GDTK_NSP slots (stride ks); the third-body concentrations of the pressure-dependent
 // rate constants (gen_falloff_M) are read from the GDTK_NFALLOFF slots after it.
-__device__ __noinline__ void rate_constants(const double* TH, double Tq, double* K, int ks, const double* etab,
-                                            double* G, int* err) {
-    double T = Tq;
-    if (T < GDTK_T_LOWER) T = GDTK_T_LOWER;
-    if (T > GDTK_T_UPPER) T = GDTK_T_UPPER;
-    const double lnT = log(T), rT = gdtk_div(1.0, T), rT2 = rT * rT, t1 = lnT + 1.0, t2 = 1.0 - lnT;
+__device__ __noinline__ void rate_constants(const double* TH, double Tq, double lnTq, double* K, int ks,
+                                            const double* etab, double* G, int* err) {
+    double T = Tq, lnT = lnTq;   // lnTq = ln Tq
+    if (T < GDTK_T_LOWER) { T = GDTK_T_LOWER; lnT = GDTK_LN_T_LOWER; }
+    if (T > GDTK_T_UPPER) { T = GDTK_T_UPPER; lnT = GDTK_LN_T_UPPER; }
+    const double rT = gdtk_div(1.0, T), rT2 = rT * rT, t1 = lnT + 1.0, t2 = 1.0 - lnT;
     int e = 0;
 #if GDTK_MIX_THERMO
     // every species takes the same curve segment and blend here: choose them once
@@ -391,7 +405,7 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
     int b = 0, ci = 0;
     bool have = false, alive = true, retried = false, need_kc = false;
     int phase = 0, cycle = 0, attempt = 0, err = 0;
-    double rho = 0, rrho = 0, u = 0, T = 0, p = 0, dtS = 0, dtS0 = 0, dtSave = 0, h = 0, t = 0, tI = 0;
+    double rho = 0, rrho = 0, u = 0, T = 0, lnT = 0, p = 0, dtS = 0, dtS0 = 0, dtSave = 0, h = 0, t = 0, tI = 0;
     double y0[GDTK_NSP];
     int n_steps = 0, n_rhs = 0, n_kc = 0, n_newton = 0, n_rej = 0, n_est = 0;
     const unsigned FULL = 0xffffffffu;
@@ -444,6 +458,7 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
         if (phase == -1) {   // (re)start from the stored input state
             const CellBlock& B = BLK[b];
             T = B.T[ci]; p = B.p[ci]; dtS = dtS0; t = 0.0; err = 0;
+            lnT = log(T);
 #pragma unroll
             for (int i = 0; i < GDTK_NSP; ++i) {
                 double v = B.massf[(size_t)i * B.ncell + ci] * rho * GDTK_RM[i];
@@ -455,7 +470,7 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
         if (need_kc) {
             lane_stat(a.lane_stats, 1);
             if (GDTK_NFALLOFF) gen_falloff_M(y0, V + GDTK_NSP * ks, ks);
-            rate_constants(TH, T, K, ks, ETAB, V, &err);
+            rate_constants(TH, T, lnT, K, ks, ETAB, V, &err);
             ++n_kc;
             need_kc = false;
         }
@@ -631,7 +646,7 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
                     V[i * ks] = yr;
                     Rm += yr;
                 }
-                T = T_from_u(TH, V, ks, V + GDTK_NSP * ks, u, T, &err, &n_newton, a.lane_stats);
+                T = T_from_u(TH, V, ks, V + GDTK_NSP * ks, u, T, &lnT, &err, &n_newton, a.lane_stats);
                 p = rho * Rm * T;
                 need_kc = true;
             }
@@ -679,7 +694,7 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
             }
             int st = 0;
             if (a.flags & F_UPDATE_THERMO) {
-                T = T_from_u(TH, V, ks, V + GDTK_NSP * ks, u, T, &st, &n_newton, a.lane_stats);
+                T = T_from_u(TH, V, ks, V + GDTK_NSP * ks, u, T, &lnT, &st, &n_newton, a.lane_stats);
                 p = rho * Rm * T;
             }
             const CellBlock& B = BLK[b];
@@ -758,7 +773,7 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
                 }
                 int err = 0;
                 if (GDTK_NFALLOFF) gen_falloff_M(y, V + GDTK_NSP * ks, ks);
-                rate_constants(TH, T, K, ks, ETAB, V, &err);
+                rate_constants(TH, T, log(T), K, ks, ETAB, V, &err);
                 gen_rhs(y, q, L, K, ks);
                 h = estimate_step(y, q, L);
             }

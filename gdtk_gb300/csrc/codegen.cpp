@@ -368,6 +368,8 @@ std::string generate_fast_source(const GasModelHost& gm, const MechanismHost& mh
     o << "#define GDTK_MAX_ITERS " << mh.maxIters << "\n#define GDTK_MAX_SUBCYCLES " << mh.maxSubcycles << "\n";
     o << "#define GDTK_MAX_ATTEMPTS " << mh.maxAttempts << "\n";
     o << "#define GDTK_T_LOWER " << lit(mh.T_lower) << "\n#define GDTK_T_UPPER " << lit(mh.T_upper) << "\n";
+    o << "#define GDTK_LN_T_LOWER " << lit(std::log(mh.T_lower)) << "\n#define GDTK_LN_T_UPPER "
+      << lit(std::log(mh.T_upper)) << "\n";
     o << "#define GDTK_ERRTOL " << lit(mh.errTol) << "\n#define GDTK_EPS1 " << lit(mh.eps1) << "\n";
     o << "#define GDTK_EPS2 " << lit(mh.eps2) << "\n#define GDTK_DELTA " << lit(mh.delta) << "\n";
     o << "#define GDTK_BLOCK " << block << "\n#define GDTK_MIN_BLOCKS " << min_blocks << "\n";
