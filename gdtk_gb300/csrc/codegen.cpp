@@ -425,7 +425,8 @@ std::string generate_fast_source(const GasModelHost& gm, const MechanismHost& mh
     bool any_kbp = false;
     for (int ir : table_rx) any_kbp = any_kbp || kbp[ir];
     if (!table_rx.empty()) {
-        o << "struct KcRec { double lnA, n, mC, lnAb, nb, mCb; int mode, np, nusum, idx; int sp[8], anu[8]; "
+        // pw: k_f = A T^pw by multiplication (C = 0, integer |n| <= 4); 99: by exp of its logarithm
+        o << "struct KcRec { double lnA, n, mC, lnAb, nb, mCb, A; int mode, np, nusum, idx, pw; int sp[8], anu[8]; "
              "double nu[8]; };\n";
         o << "__constant__ KcRec GDTK_KC_TAB[" << table_rx.size() << "] = {\n";
         for (int ir : table_rx) {
@@ -447,9 +448,12 @@ std::string generate_fast_source(const GasModelHost& gm, const MechanismHost& mh
             int mode = r.frc.model == RATE_ARRHENIUS ? (r.brc.model == RATE_FROM_EQ ? 0 : 1) : 2;
             if (mode == 0 && kbp[ir]) mode = 3;
             auto lnA = [](const RateConstHost& rc) { return rc.A > 0.0 ? std::log(rc.A) : -1.0e300; };
+            std::string pws;
+            const int pw = power_arrhenius(r.frc, pws) ? (int)r.frc.n : 99;
             o << "  {" << lit(lnA(r.frc)) << ", " << lit(r.frc.n) << ", " << lit(-r.frc.C) << ", " << lit(lnA(r.brc))
-              << ", " << lit(r.brc.n) << ", " << lit(-r.brc.C) << ", " << mode << ", " << np << ", " << nusum << ", "
-              << ir << ", {" << sp.str() << "}, {" << anu.str() << "}, {" << nu.str() << "}},   // "
+              << ", " << lit(r.brc.n) << ", " << lit(-r.brc.C) << ", " << lit(r.frc.A) << ", " << mode << ", " << np
+              << ", " << nusum << ", " << ir << ", " << pw << ", {" << sp.str() << "}, {" << anu.str() << "}, {"
+              << nu.str() << "}},   // "
               << (r.equation.empty() ? std::string("reaction") : r.equation) << "\n";
         }
         o << "};\n";
@@ -474,7 +478,11 @@ std::string generate_fast_source(const GasModelHost& gm, const MechanismHost& mh
         o << "    const KcRec& R = GDTK_KC_TAB[t];\n";
         if (any_kbp) {
             o << "    if (R.mode == 3) {   // k_b = k_f (R T / P_atm)^(sum nu) prod E_i^nu_i\n";
-            o << "      const double kf = gdtk_exp(fma(R.mC, rT, fma(R.n, lnT, R.lnA)), etab);\n";
+            o << "      double kf;\n";
+            o << "      if (R.pw != 99) {   // A T^n, C = 0, integer n\n";
+            o << "        const double b = R.pw > 0 ? T : rT;\n        kf = R.A;\n";
+            o << "        for (int m = 0; m < abs(R.pw); ++m) kf *= b;\n";
+            o << "      } else {\n        kf = gdtk_exp(fma(R.mC, rT, fma(R.n, lnT, R.lnA)), etab);\n      }\n";
             o << "      double P = 1.0;\n";
             o << "      const double c = R.nusum > 0 ? cf : rcf;\n";
             o << "      for (int m = 0; m < abs(R.nusum); ++m) P *= c;\n";
