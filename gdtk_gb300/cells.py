@@ -148,6 +148,16 @@ class ReactorCells:
         corr = max(rhs - steps - est, 0.0) if self.method == "alpha-qss" else 0.0
         return F[0] * kc + F[1] * rhs + F[2] * steps + F[3] * corr + F[4] * newton
 
+    def set_lane_stats(self, stats):
+        """Diagnostics (chem_reactor_set_lane_stats): a cuda int64 tensor of 24 slots that later fast-kernel
+        launches add to -- per phase k, warp executions [2k], active lanes [2k + 1], and with a kernel
+        generated under GDTK_PHASE_CLOCKS=1 the SM cycles [16 + k].  None turns it off."""
+        if stats is not None:
+            import torch
+            if not (stats.is_cuda and stats.dtype == torch.int64 and stats.numel() >= 24 and stats.is_contiguous()):
+                raise ValueError("expected a contiguous cuda int64 tensor of at least 24 slots")
+        check(lib().chem_reactor_set_lane_stats(self.reactor.id, _ptr(stats)), "chem_reactor_set_lane_stats")
+
     def last_launch(self):
         v = [ctypes.c_int() for _ in range(4)]
         check(lib().chem_reactor_last_launch(self.reactor.id, *[ctypes.byref(x) for x in v]), "last_launch")

@@ -96,3 +96,42 @@ def test_mechanism_kernel_compiles_for_sm103a(name):
     assert "sm_103a" in log
     m = re.search(r"Used (\d+) registers", log)
     assert m and int(m.group(1)) <= 255
+
+
+def _kc_modes(source):
+    """Mode of every record of the generated rate-constant table (0: k_b from K_c by exp, 1: both
+    Arrhenius, 2: k_f from K_c, 3: k_b from the species' exp(G/RT) products)."""
+    if "GDTK_KC_TAB" not in source:
+        return []
+    tab = source[source.index("GDTK_KC_TAB"):source.index("};", source.index("GDTK_KC_TAB"))]
+    return [int(m) for m in re.findall(r"^\s*\{(?:[^,{]*,){7}\s*(\d),", tab, flags=re.M)]
+
+
+def _source(gas, chem):
+    L = gdtk_gb300.lib()
+    buf = ctypes.create_string_buffer(1 << 22)
+    assert L.gdtk_generate_fast_source(gas.encode(), chem.encode(), buf, len(buf)) > 0
+    return buf.value.decode()
+
+
+def test_rate_constant_table_forms(monkeypatch):
+    # H2-air: every reaction's k_b from the species' exp(G/RT) products; the exp form is compiled out
+    src = _source(mech("j92-gas.lua"), mech("j92-chem.lua"))
+    assert _kc_modes(src) == [3] * 33
+    assert "#if 0   // every table reaction takes the product form" in src
+    # both directions Arrhenius stay in the exp form
+    assert set(_kc_modes(_source(mech("gupta5-gas.lua"), mech("gupta5-chem.lua")))) == {1}
+    monkeypatch.setenv("GDTK_KB_EXP", "1")
+    assert _kc_modes(_source(mech("j92-gas.lua"), mech("j92-chem.lua"))) == [0] * 33
+    monkeypatch.delenv("GDTK_KB_EXP")
+    monkeypatch.setenv("GDTK_KC_UNROLLED", "1")
+    assert _kc_modes(_source(mech("j92-gas.lua"), mech("j92-chem.lua"))) == []
+
+
+def test_product_form_refused_where_it_could_overflow(tmp_path):
+    """At 300 K the N atom's G/RT is about 170, so N2 <=> 2N stays inside exp(+-600); with the lower
+    temperature limit at 20 K it reaches about 2,800 and the reaction keeps the exp form."""
+    assert set(_kc_modes(_source(mech("n2-gas.lua"), mech("n2-chem.lua")))) == {3}
+    cold = tmp_path / "n2-cold-chem.lua"
+    cold.write_text(open(mech("n2-chem.lua")).read().replace("lower=300.000000", "lower=20.000000"))
+    assert set(_kc_modes(_source(mech("n2-gas.lua"), str(cold)))) == {0}

@@ -514,3 +514,30 @@ def test_kernel_division_against_ieee_division():
         assert (ulp == 0).mean() > exact
         # zero, subnormal and infinite quotients come from the IEEE division itself
         assert np.array_equal(q[edge].view(np.int64), qi[edge].view(np.int64))
+
+
+@pytest.mark.parametrize("form", [{"GDTK_KB_EXP": "1"}, {"GDTK_KC_UNROLLED": "1"}, {"GDTK_PHASE_CLOCKS": "1"}])
+def test_alternate_kernel_forms_parity(form, monkeypatch):
+    """The generator's alternate forms (k_b by one exp per reaction, straight-line rate constants,
+    phase clocks compiled in) keep parity; the variables are read when a reactor's kernel is
+    generated, so each form gets a fresh reactor."""
+    from gdtk_gb300.cells import ReactorCells
+    from gdtk_gb300.workloads import h2air_cells
+    for k, v in form.items():
+        monkeypatch.setenv(k, v)
+    rc = ReactorCells(mech("j92-gas.lua"), mech("j92-chem.lua"))
+    orc = oracle.Oracle(mech("j92-gas.lua"), mech("j92-chem.lua"))
+    torch = torch_cuda()
+    stats = torch.zeros(24, dtype=torch.int64, device="cuda")
+    rc.set_lane_stats(stats)
+    T, p, Y = h2air_cells(rc.species_names, rc.mol_masses, 512, seed=3)
+    g, o, _, _ = run_pair(rc, orc, T, p, Y, 1.0e-6)
+    rc.set_lane_stats(None)
+    assert (g["status"] == 0).mean() > 0.95
+    assert_parity(g, o)
+    s = stats.cpu().numpy()
+    assert s[2] > 0 and s[4] > 0                       # rate-constant and right-hand-side executions counted
+    if "GDTK_PHASE_CLOCKS" in form:
+        assert (s[16:24][[1, 2, 4, 7]] > 0).all()      # cycles in rate constants, RHS, Newton, alpha update
+    else:
+        assert (s[16:24] == 0).all()
