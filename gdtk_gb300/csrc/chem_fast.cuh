@@ -1,17 +1,25 @@
 // chem_fast.cuh -- mechanism-specialised FP64 chemistry update for sm_103a.
 //
 // This file is compiled at run time by NVRTC, once per mechanism, after a generated prologue
-// (codegen.cpp) that defines the mechanism as compile-time constants and two straight-line
-// functions:
-//   gen_kc(lnT, rT, g, K, ks, etab)   k_f, k_b of every reaction into K[r*ks], K[(NR + r)*ks]
-//   gen_rhs(c, q, L, K, ks)           production q and loss L of every species at c
-// so that per-species vectors live in registers and every index and coefficient is an
-// immediate.  The algorithm is the reference's (kinetics/chemistry_update.d:139-326 and the
-// calls below it), with the arithmetic rearranged to spend fewer FP64 operations, which are
-// the binding resource on this GPU (FP64 issue is 1/64 of FP32):
-//   * rate constants in log form, ln k = ln A + n ln T - C/T, and k_b = k_f / K_c as one
-//     exponential of ln k_f + sum(nu G/RT) - sum(nu) ln(P_atm / RT)  (reaction.d:26-52,
-//     rate_constant.d:72-75), with exp by Tang's table method (fast_exp.h);
+// (codegen.cpp) that defines the mechanism as compile-time constants and two functions:
+//   gen_kc(T, lnT, rT, g, gs, K, ks, etab, Mv, ms)   k_f, k_b of every reaction into K[r*ks],
+//                                    K[(NR + r)*ks]: a loop over a __constant__ table of the
+//                                    Arrhenius reactions, pressure-dependent ones straight-line
+//   gen_rhs(c, q, L, K, ks)          production q and loss L of every species at c, straight-line
+// so that per-species vectors live in registers.  FP64 operations compile to several instructions
+// each on sm_103a, so code size matters as much as operation count: loops over constant tables
+// where they cost no extra FP64 work, straight-line code where registers must hold the vectors.
+// The algorithm is the reference's (kinetics/chemistry_update.d:139-326 and the calls below it),
+// with the arithmetic rearranged to spend fewer FP64 operations, which are the binding resource on
+// this GPU (FP64 issue is 1/64 of FP32):
+//   * rate constants in log form, ln k = ln A + n ln T - C/T (A T^n by multiplication when C = 0
+//     and n is a small integer), and k_b = k_f / K_c = k_f (R T / P_atm)^sum(nu) prod E_i^nu_i with
+//     E_i = exp(G_i / R T) formed once per species (reaction.d:26-52, rate_constant.d:72-75), or
+//     as one exponential per reaction where those products could leave the double range; exp by
+//     Tang's table method (fast_exp.h);
+//   * ln T carried with each cell and updated by a log1p series in the Newton iteration, so that
+//     the library log (as costly as about 36 FMAs) runs only at cell start and after large steps;
+//   * divisions by Newton-Raphson refinement of the hardware reciprocal (fast_exp.h);
 //   * the NASA-9 enthalpy, heat capacity and G/RT in Horner form with coefficients scaled
 //     once on the host (cea_thermo_curves.d:55-137);
 //   * the alpha-QSS predictor/corrector with alpha = N(s)/D(s), s = p h + eps, folded into the

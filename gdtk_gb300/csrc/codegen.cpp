@@ -1,10 +1,11 @@
-// codegen.cpp -- writes the mechanism as straight-line CUDA, compiles it with NVRTC for the
-// device at hand, and launches it.
+// codegen.cpp -- writes the mechanism as CUDA, compiles it with NVRTC for the device at hand, and
+// launches it.
 //
 // The generated part is small: compile-time sizes and tolerances, the species constants, and
-// two functions -- gen_kc (rate constants) and gen_rhs (production/loss rates) -- in which
-// every species index, stoichiometric coefficient, third-body efficiency and Arrhenius
-// parameter is a literal.  The integrator around them is chem_fast.cuh.  The reference
+// two functions -- gen_kc (rate constants: a loop over a __constant__ table of the Arrhenius
+// reactions, the pressure-dependent ones straight-line) and gen_rhs (production/loss rates,
+// straight-line) -- in which every species index, stoichiometric coefficient, third-body
+// efficiency and Arrhenius parameter is a literal or a table entry.  The integrator around them is chem_fast.cuh.  The reference
 // interprets its reaction objects at run time (kinetics/reaction_mechanism.d:82-96,
 // reaction.d:145-149, 267-311, 394-456); its legacy GPU path generated source in a similar
 // spirit, from prep-chem's compact notation (eilmer/utils/prep-cuda-gpu-chem-kernel.py).
