@@ -416,7 +416,9 @@ std::string generate_fast_source(const GasModelHost& gm, const MechanismHost& mh
     const char* kc_env = std::getenv("GDTK_KC_UNROLLED");
     const bool kc_table = !(kc_env && kc_env[0] == '1');
     std::vector<int> table_rx;
-    for (int ir = 0; ir < nr && (int)table_rx.size() < 320; ++ir) {   // 320 records = 51 KB of constant bank
+    // 256 records of 208 bytes = 53 KB of the 64 KB constant bank, leaving room for the species constants;
+    // reactions beyond them stay straight-line
+    for (int ir = 0; ir < nr && (int)table_rx.size() < 256; ++ir) {
         const ReactionHost& r = mh.reactions[ir];
         int np = 0;
         for (auto& pp : participants(r)) np += pp.nu != 0;
