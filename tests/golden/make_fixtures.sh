@@ -59,6 +59,7 @@ cp "$REF/src/kinetics/sample-input/H2-I2-inp.lua" "$OUT/h2i2-chem.lua"
 cp "$REF/src/kinetics/sample-input/N2-diss.lua" "$OUT/n2-diss-rate.lua"
 cp "$REF/src/gas/sample-data/O-thermo.lua" "$OUT/O-thermo.lua"
 cp "$REF/src/gas/sample-data/therm-perf-5-species-air.lua" "$OUT/tpg-air5-gas.lua"
+cp "$REF/src/gas/sample-data/five-species-air.lua" "$OUT/air5-2T-gas.lua"   # two_temperature_gas.d:704-738
 # The DRM19 example's comparison data (Eilmer3's fixed-volume reactor, CH4:O2:N2 = 1:2:7.52 at 2000 K
 # and 1 atm, 2000 steps of 2e-7 s): time and temperature columns.
 grep -v '^[A-Za-z#]' "$KIN/methane-combustion-w-drm19/eilmer3-result-for-comparison.data" | awk '{print $1, $4}' \

@@ -218,3 +218,20 @@ def test_troe_falloff_fixed_volume_reactor_against_eilmer3():
     assert abs(t_ign - t_ign_ref) <= 0.01 * t_ign_ref
     assert rel.max() < 0.03
     assert rel[-1] < 2e-3
+
+
+def test_two_temperature_air5():
+    """gas/thermo/two_temperature_gas.d:704-738: five-species air, Y = 0.2 each, at p = 1 MPa and
+    T = T_ve = 2000 K has u + u_ve = 11,801,825.6 J/kg and rho = 1.2840117 kg/m^3; the (rho, u)
+    update returns T, T_ve and p (all to 1e-6).  Groundwork of the multi-temperature reactor."""
+    from oracle.two_temperature import TwoTemperatureGas
+    g = TwoTemperatureGas(mech("air5-2T-gas.lua"))
+    Y = np.full(5, 0.2)
+    rho, u, u_ve = g.update_from_pT(1.0e6, 2000.0, 2000.0, Y)
+    assert u + u_ve == pytest.approx(11_801_825.6, rel=1e-6)
+    assert rho == pytest.approx(1.2840117, rel=1e-6)
+    for guess in (2000.0, 1500.0):
+        T, T_ve, p = g.update_from_rhou(rho, u, u_ve, Y, guess)
+        assert T == pytest.approx(2000.0, rel=1e-6)
+        assert T_ve == pytest.approx(2000.0, rel=1e-6)
+        assert p == pytest.approx(1.0e6, rel=1e-6)
