@@ -67,6 +67,24 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(x, device="cpu"):
+    """The largest of each rank's x (a float) over the default process group; x itself without one.
+    device: where the reduction tensor lives ("cpu" for gloo, the rank's cuda device for nccl)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(cells_per_rank, world_size, steps, max_ms):
+    """Whole-job cell-updates/s of `world_size` replicas that each updated `cells_per_rank` cells
+    `steps` times, timed by the slowest rank (max_ms for all the steps)."""
+    return cells_per_rank * world_size * steps / (max_ms * 1e-3)
+
+
 class ClockSampler:
     """nvidia-smi clock/throttle samples during the timed region."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
@@ -660,12 +678,9 @@ def main():
     clk = clocks.stop()
     total_ms = k0.elapsed_time(k1)
     launch_ms = [a.elapsed_time(b) for a, b in ev]
-    if ws > 1:
-        t = torch.tensor([total_ms], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, dev)
     ms_per_step = total_ms / args.steps
-    value = n * ws * args.steps / (total_ms * 1e-3)
+    value = replica_throughput(n, ws, args.steps, total_ms)
     status = st.cpu().numpy()
     tot = totals.cpu().numpy().astype(np.float64)
     flops = rc.algorithmic_flops(tot / args.steps)
@@ -688,7 +703,8 @@ def main():
             rc.update_host(hrho, hu, hT, hp, hY, hdt, w["dt"], status=hst, flags=flags)
             times.append(time.perf_counter() - t0)
         nsp = rc.nsp
-        e2e = {"value": n * ws / float(np.mean(times)), "unit": "cell-updates/s",
+        e2e_s = max_over_ranks(float(np.mean(times)), dev)
+        e2e = {"value": replica_throughput(n, ws, 1, e2e_s * 1e3), "unit": "cell-updates/s",
                "h2d_bytes_per_step": n * 8 * (5 + nsp), "d2h_bytes_per_step": n * (8 * (3 + nsp) + 4),
                "steps": e2e_steps}
 
