@@ -541,3 +541,43 @@ def test_alternate_kernel_forms_parity(form, monkeypatch):
         assert (s[16:24][[1, 2, 4, 7]] > 0).all()      # cycles in rate constants, RHS, Newton, alpha update
     else:
         assert (s[16:24] == 0).all()
+
+
+def test_full_size_h2air_update_properties(j92):
+    """The benchmark's full workload (1,048,576 H2-air cells, one update of 1 us from a fresh step
+    size) through the fast kernel, checked by properties that do not depend on its size: every cell
+    completes, mass fractions are non-negative and sum to 1, p = rho R_mix T, and u recomputed from
+    (p, T, Y) is the input u (the update holds rho and u fixed, and T solves u(T) = u to |dT|/T < 1e-10);
+    plus cell-by-cell parity with the oracle on a strided sample of 2,000 cells."""
+    import bench
+    torch = torch_cuda()
+    rc, orc = j92
+    w = bench.WORKLOADS["h2air-1M"]
+    T0, p0, Y0 = bench.make_cells(w, rc.species_names, rc.mol_masses)
+    n = T0.shape[0]
+    assert n == 1 << 20
+    dT, dp = to_dev(torch, T0, p0)
+    dY = torch.tensor(np.ascontiguousarray(Y0), dtype=torch.float64, device="cuda")
+    rho, u = rc.thermo_from_pT(dp, dT, dY)
+    dtc = torch.full((n,), -1.0, dtype=torch.float64, device="cuda")
+    st = torch.zeros(n, dtype=torch.int32, device="cuda")
+    rc.update(rho, u, dT, dp, dY, dtc, w["dt"], status=st)
+    torch.cuda.synchronize()
+    assert int((st != 0).sum()) == 0
+    assert float(dY.min()) >= 0.0
+    assert float((dY.sum(dim=0) - 1.0).abs().max()) <= 1e-13
+    R = torch.tensor(8.31451 / np.asarray(rc.mol_masses), dtype=torch.float64, device="cuda")
+    p_eos = rho * (dY * R[:, None]).sum(dim=0) * dT
+    assert float(((p_eos - dp).abs() / dp).max()) <= 1e-12
+    rho2, u2 = rc.thermo_from_pT(dp, dT, dY)
+    assert float(((rho2 - rho).abs() / rho).max()) <= 1e-12
+    assert float((u2 - u).abs().max()) <= 1e-2   # J/kg: c_v |dT| with |dT| below 1e-10 T
+    idx = np.linspace(0, n - 1, 2000).astype(np.int64)
+    o = orc.chem_update(rho.cpu().numpy()[idx], u.cpu().numpy()[idx], T0[idx], p0[idx], Y0[:, idx].T,
+                        np.full(len(idx), -1.0), w["dt"], counters=True)
+    g = dict(T=dT.cpu().numpy()[idx], p=dp.cpu().numpy()[idx], Y=dY.cpu().numpy()[:, idx],
+             status=st.cpu().numpy()[idx], counters=None)
+    assert np.array_equal(g["status"], o["status"])
+    assert np.abs(g["Y"] - o["massf"].T).max() <= Y_ABS
+    assert (np.abs(g["T"] - o["T"]) / o["T"]).max() <= TP_REL
+    assert (np.abs(g["p"] - o["p"]) / o["p"]).max() <= TP_REL
