@@ -79,6 +79,24 @@ def max_over_ranks(x, device="cpu"):
     return float(t.item())
 
 
+PHASES = ["iteration", "rate constants", "right-hand side", "step control", "Newton iteration", "cell completion",
+          "refill", "alpha-QSS update"]
+
+
+def lane_stats_summary(s):
+    """Per phase of the fast kernel (chem_reactor_set_lane_stats slots): warp executions, mean active
+    lanes, and the share of all warps' SM cycles when the kernel counted them (GDTK_PHASE_CLOCKS=1)."""
+    s = np.asarray(s, dtype=np.float64)
+    cyc = s[16:24]
+    out = {}
+    for k, name in enumerate(PHASES):
+        d = {"warp_executions": int(s[2 * k]), "active_lanes": float(s[2 * k + 1] / s[2 * k]) if s[2 * k] else 0.0}
+        if cyc.sum() > 0:
+            d["time_share"] = float(cyc[k] / cyc.sum())
+        out[name] = d
+    return out
+
+
 def replica_throughput(cells_per_rank, world_size, steps, max_ms):
     """Whole-job cell-updates/s of `world_size` replicas that each updated `cells_per_rank` cells
     `steps` times, timed by the slowest rank (max_ms for all the steps)."""
@@ -556,6 +574,10 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--lane-stats", action="store_true",
+                    help="after the timed region, one more update with the kernel's lane statistics attached; "
+                         "with GDTK_PHASE_CLOCKS=1 in the environment the line also gets each phase's share of "
+                         "warp time")
     args = ap.parse_args()
     w = dict(WORKLOADS[args.workload])
     if args.cells:
@@ -708,6 +730,16 @@ def main():
                "h2d_bytes_per_step": n * 8 * (5 + nsp), "d2h_bytes_per_step": n * (8 * (3 + nsp) + 4),
                "steps": e2e_steps}
 
+    # ---- diagnostics: lane occupancy and (with GDTK_PHASE_CLOCKS=1) time per phase, on an untimed update
+    lanes = None
+    if args.lane_stats:
+        stats = torch.zeros(24, dtype=torch.int64, device=dev)
+        rc.set_lane_stats(stats)
+        step()
+        torch.cuda.synchronize()
+        rc.set_lane_stats(None)
+        lanes = lane_stats_summary(stats.cpu().numpy())
+
     # ---- CPU baseline (reference algorithm on the host cores), rank 0 at N=1 only
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
@@ -744,6 +776,8 @@ def main():
             "clocks": clk,
             "gpu_launches": args.steps * 5,
         }
+        if lanes is not None:
+            line["lane_stats"] = lanes
         print(json.dumps(line))
     if ws > 1:
         dist.destroy_process_group()

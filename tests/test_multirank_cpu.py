@@ -79,3 +79,16 @@ def test_reference_arm_under_torchrun_prints_once_from_rank_0():
     assert len(lines) == 1, r.stdout
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
+
+
+def test_lane_stats_summary():
+    sys.path.insert(0, ROOT)
+    import bench
+    import numpy as np
+    s = np.zeros(24)
+    s[2], s[3] = 10, 300          # rate constants: 10 warp executions, 30 lanes each
+    s[17], s[18] = 750, 250       # cycles: rate constants 75%, right-hand side 25%
+    d = bench.lane_stats_summary(s)
+    assert d["rate constants"]["warp_executions"] == 10 and d["rate constants"]["active_lanes"] == 30.0
+    assert d["rate constants"]["time_share"] == 0.75 and d["right-hand side"]["time_share"] == 0.25
+    assert "time_share" not in bench.lane_stats_summary(np.zeros(24))["iteration"]
