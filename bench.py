@@ -57,7 +57,17 @@ def make_cells(w, names=None, M=None, n=None):
     n = n or w["n"]
     if w["kind"] == "air5":
         return air5_cells(n, seed=w["seed"])
-    return h2air_cells(names, M, n, seed=w["seed"])
+    return h2air_cells(names, M, n, seed=w["seed"], gas_file=os.path.join(MECH, w["gas"]))
+
+
+# Environment switches read when the mechanism kernel is generated (alternate code forms, phase clocks).
+CODEGEN_ENV = ("GDTK_KB_EXP", "GDTK_KC_UNROLLED", "GDTK_KC_UNROLL", "GDTK_G_UNROLL", "GDTK_RHS_FENCE",
+               "GDTK_PHASE_CLOCKS", "GDTK_CHEM_REFERENCE_ORDER")
+
+
+def codegen_env():
+    """The kernel-generation switches set in this process's environment (recorded in the line's config)."""
+    return {k: os.environ[k] for k in CODEGEN_ENV if os.environ.get(k)}
 
 
 def dist_env():
@@ -151,6 +161,40 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(self.rows)}
 
 
+def profile_record(name, workload):
+    """The entry for `workload` in profiles/<name> (summaries of committed ncu captures), or None."""
+    path = os.path.join(ROOT, "profiles", name)
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        return json.load(f).get(workload)
+
+
+def roofline_fp64(issued, n, kernel_ms, peak, ref_flops, traffic, work_per_cell):
+    """The FP64 roofline object of a chemistry-update line.
+
+    achieved / frac: FP64 FLOP the kernel issues (2 DFMA + DADD + DMUL thread instructions, per cell
+    from the committed ncu capture of the same workload in profiles/fp64_issued.json, times the cells
+    of one launch) over the CUDA-event launch time, against the DFMA probe's peak.  The reference-
+    operation figure (the reference's add/mul/div = 1, exp/log = 20, pow = 40 per unit of work, with
+    the kernel's own work counters) is reported beside it under its own name."""
+    kernel_s = kernel_ms * 1e-3
+    ref = {"achieved": ref_flops / kernel_s / 1e12, "frac": ref_flops / kernel_s / 1e12 / peak,
+           "flops_per_launch": ref_flops, "work_per_cell": list(map(float, work_per_cell)),
+           "convention": "reference operations per unit of work: add/sub/mul/div 1, exp/log 20, pow 40"}
+    out = {"bound": "fp64", "achieved": None, "peak": peak, "unit": "TFLOP/s", "frac": None, "traffic": traffic,
+           "basis": "issued FP64 FLOP: 2 x DFMA + DADD + DMUL thread instructions",
+           "peak_source": "measured: gdtk_measure_fp64_peak DFMA probe on this GPU (no FP64 entry in "
+                          "MEASURED_PEAKS.json)",
+           "kernel_ms": kernel_ms, "reference_operation_count": ref}
+    if issued:
+        f = issued["flop_per_cell"] * n
+        out.update(achieved=f / kernel_s / 1e12, frac=f / kernel_s / 1e12 / peak, issued_flops_per_launch=f,
+                   issued_source="profiles/fp64_issued.json (%d-cell ncu capture: %s)" %
+                                 (issued["cells"], issued["command"]))
+    return out
+
+
 def fp64_peak_reference():
     """The FP64 roofline denominator: measured on this GPU by the library's DFMA probe."""
     from gdtk_gb300.cells import measure_fp64_peak
@@ -191,14 +235,15 @@ def run_blocks(args, w):
     dev = torch.device("cuda", 0)
     t64 = lambda a: torch.tensor(np.ascontiguousarray(a), dtype=torch.float64, device=dev)
     # launch-shape autotuning on a sample of the same mixture (cached per mechanism and device)
-    sT, sp, sY = h2air_cells(rc.species_names, rc.mol_masses, 262144, seed=77)
+    sT, sp, sY = h2air_cells(rc.species_names, rc.mol_masses, 262144, seed=77, gas_file=rc.gmodel.file_name)
     dT, dp, dY = t64(sT), t64(sp), t64(sY)
     srho, su = rc.thermo_from_pT(dp, dT, dY)
     sample = dict(rho=srho, u=su, T=dT, p=dp, massf=dY, dt_chem=torch.full((262144,), -1.0, dtype=torch.float64,
                                                                          device=dev))
     choice, oflag, _ = autotune.tune(rc, sample, 1.0e-6, tag="h2air-262144")
     flags = UPDATE_THERMO | RETRY | oflag
-    spec = h2air_blocks(rc.species_names, rc.mol_masses, nblocks=w["nblocks"], seed=w["seed"])
+    spec = h2air_blocks(rc.species_names, rc.mol_masses, nblocks=w["nblocks"], seed=w["seed"],
+                        gas_file=rc.gmodel.file_name)
     blocks, init = [], []
     for b in spec:
         n = b["T"].shape[0]
@@ -435,7 +480,8 @@ def run_surrogate(args, w):
     torch.cuda.empty_cache()
 
     # ---- fresh cells
-    T0, p0, Y0 = h2air_cells(rc.species_names, rc.mol_masses, n, seed=w["seed"] * 1000 + 17)
+    T0, p0, Y0 = h2air_cells(rc.species_names, rc.mol_masses, n, seed=w["seed"] * 1000 + 17,
+                             gas_file=rc.gmodel.file_name)
     t64 = lambda a: torch.tensor(np.ascontiguousarray(a), dtype=torch.float64, device=dev)
     sT, sp, sY = t64(T0), t64(p0), t64(Y0)
     srho, su = rc.thermo_from_pT(sp, sT, sY)
@@ -579,6 +625,9 @@ def main():
                          "with GDTK_PHASE_CLOCKS=1 in the environment the line also gets each phase's share of "
                          "warp time")
     args = ap.parse_args()
+    # the timed kernel is never the phase-clock build: that one is generated only for the untimed
+    # lane-statistics update below
+    phase_clocks = os.environ.pop("GDTK_PHASE_CLOCKS", "") == "1"
     w = dict(WORKLOADS[args.workload])
     if args.cells:
         w["n"] = args.cells
@@ -733,11 +782,18 @@ def main():
     # ---- diagnostics: lane occupancy and (with GDTK_PHASE_CLOCKS=1) time per phase, on an untimed update
     lanes = None
     if args.lane_stats:
+        drc = rc
+        if phase_clocks:   # a separately generated, instrumented kernel for this diagnostic update only
+            os.environ["GDTK_PHASE_CLOCKS"] = "1"
+            drc = ReactorCells(os.path.join(MECH, w["gas"]), os.path.join(MECH, w["chem"]))
         stats = torch.zeros(24, dtype=torch.int64, device=dev)
-        rc.set_lane_stats(stats)
-        step()
+        drc.set_lane_stats(stats)
+        T.copy_(sT); p.copy_(sp); Y.copy_(sY); dtc.copy_(sdt)
+        drc.update(srho, su, T, p, Y, dtc, w["dt"], status=st, flags=flags)
         torch.cuda.synchronize()
-        rc.set_lane_stats(None)
+        drc.set_lane_stats(None)
+        if phase_clocks:
+            os.environ.pop("GDTK_PHASE_CLOCKS", None)
         lanes = lane_stats_summary(stats.cpu().numpy())
 
     # ---- CPU baseline (reference algorithm on the host cores), rank 0 at N=1 only
@@ -750,12 +806,10 @@ def main():
 
     if rank == 0:
         traffic = None
-        prof = os.path.join(ROOT, "profiles", "traffic.json")
-        if os.path.exists(prof):
-            with open(prof) as f:
-                tj = json.load(f).get(args.workload)
-            if tj:
-                traffic = tj["bytes_per_cell"] * n
+        tj = profile_record("traffic.json", args.workload)
+        if tj:
+            traffic = tj["bytes_per_cell"] * n
+        issued = profile_record("fp64_issued.json", args.workload)
         ok = int((status == 0).sum())
         line = {
             "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
@@ -764,13 +818,8 @@ def main():
             "config": {"workload": args.workload, "cells_per_gpu": n, "mechanism": w["chem"], "dt": w["dt"],
                        "method": rc.method, "tight_coupling": rc.tight, "dt_chem_in": -1.0,
                        "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas x%d" % ws,
-                       "cells_ok": ok, "cells_failed": int(n - ok)},
-            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                         "frac": achieved / peak, "traffic": traffic,
-                         "peak_source": "measured: gdtk_measure_fp64_peak DFMA probe on this GPU (no FP64 "
-                                        "entry in MEASURED_PEAKS.json)",
-                         "flops_per_launch": flops, "kernel_ms": kernel_ms,
-                         "work_per_cell": (tot / args.steps / n).tolist()},
+                       "cells_ok": ok, "cells_failed": int(n - ok), "codegen_env": codegen_env()},
+            "roofline": roofline_fp64(issued, n, kernel_ms, peak, flops, traffic, tot / args.steps / n),
             "cpu_baseline": cpu,
             "e2e": e2e,
             "clocks": clk,

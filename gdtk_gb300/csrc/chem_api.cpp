@@ -244,7 +244,7 @@ void run_fast(ReactorObj& r, FastArgs& a, int flags, cudaStream_t s) {
     if (!(flags & GDTK_CHEM_INDEX_ORDER) && a.total > 1) {
         r.order_key.ensure((size_t)a.total);
         r.order.ensure((size_t)a.total);
-        r.order_hist.ensure(256);
+        r.order_hist.ensure(ORDER_BUCKETS);
         check(launch_order(*r.fast, a, cuda().sm_count, r.order_key.p, r.order.p, r.order_hist.p, s),
               "ordering launch");
         a.order = r.order.p;

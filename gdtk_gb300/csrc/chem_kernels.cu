@@ -634,10 +634,9 @@ __global__ void __launch_bounds__(128) gas_service_kernel(GasServiceArgs a) {
 }
 
 // ---------------------------------------------------------------- longest-first ordering
-// Counting sort of cells into 256 cost buckets (bucket = key/8, descending), the visit order of
-// the persistent chemistry kernel.  Order within a bucket is arbitrary; only scheduling
+// Counting sort of cells into ORDER_BUCKETS cost buckets (bucket = key/8, descending), the visit
+// order of the persistent chemistry kernel.  Order within a bucket is arbitrary; only scheduling
 // depends on it, never a cell's result.
-constexpr int ORDER_BUCKETS = 256;
 
 __device__ __forceinline__ int order_bucket(float key) {
     int b = (int)(key * 0.125f);

@@ -54,7 +54,10 @@ int chem_scratch_doubles(int nsp, int nr, int neff, int method);
 cudaError_t launch_chem_update(const ChemUpdateArgs& a, int method, int scratch_doubles, int sm_count,
                                cudaStream_t stream, LaunchInfo* info);
 cudaError_t launch_gas_service(const GasServiceArgs& a, int sm_count, cudaStream_t stream);
-// Counting sort of n cells by cost key (descending) into order[n]; hist is 256 ints of scratch.
+// Cost buckets of the longest-first ordering: launch_bucket_order's hist scratch holds this many ints.
+constexpr int ORDER_BUCKETS = 256;
+
+// Counting sort of n cells by cost key (descending) into order[n]; hist is ORDER_BUCKETS ints of scratch.
 cudaError_t launch_bucket_order(const float* key, int n, int* order, int* hist, int sm_count, cudaStream_t stream);
 
 }  // namespace gdtk

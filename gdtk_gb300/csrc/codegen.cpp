@@ -644,15 +644,32 @@ std::string cache_dir() {
     return std::string(home && *home ? home : "/tmp") + "/.cache/gdtk_gb300";
 }
 
+std::string arch_option(int major, int minor) {
+    return "--gpu-architecture=sm_" + std::to_string(major) + std::to_string(minor) + (major >= 9 ? "a" : "");
+}
+const char* const kJitOptions[] = {"--std=c++17", "--fmad=true", "-default-device", "-lineinfo",
+                                   "--ptxas-options=-v"};
+
+// Key of the in-process and on-disk cubin caches: the source, the target, NVRTC's version and
+// every compile option, so a toolkit upgrade or an option change never loads a stale cubin.
+std::string cubin_cache_key(const std::string& src, int major, int minor) {
+    int vmaj = 0, vmin = 0;
+    nvrtcVersion(&vmaj, &vmin);
+    std::string opts = arch_option(major, minor);
+    for (const char* o : kJitOptions) opts += std::string(" ") + o;
+    const size_t h = std::hash<std::string>{}(src) ^ (std::hash<std::string>{}(opts) * 0x9e3779b97f4a7c15ull);
+    return std::to_string(h) + "_sm" + std::to_string(major) + std::to_string(minor) + "_nvrtc" +
+           std::to_string(vmaj) + "." + std::to_string(vmin);
+}
+
 std::string compile_cubin(const std::string& src, int major, int minor, std::string& log) {
-    std::string arch = "--gpu-architecture=sm_" + std::to_string(major) + std::to_string(minor) +
-                       (major >= 9 ? "a" : "");
-    const char* opts[] = {arch.c_str(), "--std=c++17", "--fmad=true", "-default-device", "-lineinfo",
-                          "--ptxas-options=-v"};
+    const std::string arch = arch_option(major, minor);
+    std::vector<const char*> opts{arch.c_str()};
+    for (const char* o : kJitOptions) opts.push_back(o);
     nvrtcProgram prog;
     if (nvrtcCreateProgram(&prog, src.c_str(), "gdtk_chem_fast.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS)
         throw std::runtime_error("nvrtcCreateProgram failed");
-    nvrtcResult rc = nvrtcCompileProgram(prog, (int)(sizeof(opts) / sizeof(opts[0])), opts);
+    nvrtcResult rc = nvrtcCompileProgram(prog, (int)opts.size(), opts.data());
     size_t n = 0;
     nvrtcGetProgramLogSize(prog, &n);
     log.assign(n, '\0');
@@ -692,17 +709,22 @@ FastKernel* build_fast_kernel(const GasModelHost& gm, const MechanismHost& mh, i
     const int nsp = gm.n_species(), nr = (int)mh.reactions.size();
     const int per_thread = 2 * nr + fast_vec_doubles(gm, mh);
     const int table = nsp * 120 + 64;
-    // Block size: as many resident threads as shared memory allows, up to 256 per SM.
-    const double budget = 227.0 * 1024 / 8;   // doubles of shared memory per SM
+    // Block size: as many resident threads as shared memory allows, up to 256 per SM.  Each resident
+    // block also holds the kernel's static shared arrays (at most kStaticSmem bytes, the phase-clock
+    // instrumentation) and the 1 KB the hardware reserves per block; one block may use up to 227 KB.
+    constexpr double kStaticSmem = 512.0, kReserved = 1024.0, kSmPerSm = 228.0 * 1024, kSmPerBlock = 227.0 * 1024;
+    auto fits = [&](int blk, int nblk) {
+        const double dyn = (table + (double)per_thread * blk) * 8.0;
+        return dyn + kStaticSmem <= kSmPerBlock && nblk * (dyn + kStaticSmem + kReserved) <= kSmPerSm;
+    };
     int block = 256, min_blocks = 1;
-    while (block > 32 && table + (double)per_thread * block > budget) block -= 32;
-    if (table + (double)per_thread * block > budget) throw std::runtime_error("mechanism too large for shared memory");
-    if (block <= 128 && 2 * (table + (double)per_thread * block) <= budget) min_blocks = 2;
+    while (block > 32 && !fits(block, 1)) block -= 32;
+    if (!fits(block, 1)) throw std::runtime_error("mechanism too large for shared memory");
+    if (block <= 128 && fits(block, 2)) min_blocks = 2;
     if (req_block > 0) {   // an explicit launch shape (autotuning)
         if (req_block % 32 || req_block > 1024) throw std::runtime_error("block size must be a multiple of 32, <= 1024");
         int mb = req_min_blocks > 0 ? req_min_blocks : 1;
-        if (mb * (table + (double)per_thread * req_block) > budget)
-            throw std::runtime_error("requested block shape does not fit in shared memory");
+        if (!fits(req_block, mb)) throw std::runtime_error("requested block shape does not fit in shared memory");
         block = req_block;
         min_blocks = mb;
     }
@@ -713,8 +735,7 @@ FastKernel* build_fast_kernel(const GasModelHost& gm, const MechanismHost& mh, i
     k->per_thread_doubles = per_thread;
     k->table_doubles = table;
     k->source = generate_fast_source(gm, mh, block, min_blocks);
-    std::string key = std::to_string(std::hash<std::string>{}(k->source)) + "_sm" + std::to_string(major) +
-                      std::to_string(minor);
+    std::string key = cubin_cache_key(k->source, major, minor);
     std::string cubin;
     {
         std::lock_guard<std::mutex> lk(g_jit_mu);

@@ -13,6 +13,7 @@
 #include <string>
 
 #include "../../include/gdtk_chem.h"
+#include "chem_launch.h"
 
 namespace gdtk {
 int update_cells_with_scratch(int cr_i, int ncell, const double* rho, const double* u, double* T, double* p,
@@ -25,7 +26,8 @@ namespace {
 
 constexpr int kMaxCells = 1 << 20;                 // cells per call
 constexpr size_t kCounterBytes = 256;              // work counter (padded to the alignment)
-constexpr size_t kHistBytes = 256 * sizeof(int);   // ordering histogram
+constexpr size_t kHistBytes = gdtk::ORDER_BUCKETS * sizeof(int);   // ordering histogram
+static_assert(kHistBytes % 16 == 0, "the key array after the histogram stays 16-byte aligned");
 constexpr size_t kScratchBytes = kCounterBytes + kHistBytes + (size_t)kMaxCells * (sizeof(float) + sizeof(int));
 
 // About 8 MiB, held by every GPU on which this library's device code is loaded, until exit.

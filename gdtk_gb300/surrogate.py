@@ -286,7 +286,8 @@ def generate_samples(rc, sg, n, seed=0, dt_range=(0.5e-6, 2.0e-6), block=65536, 
     import torch
     from .workloads import h2air_cells
     if cells is None:
-        cells = lambda m, s: h2air_cells(rc.species_names, rc.mol_masses, m, seed=s)
+        cells = lambda m, s: h2air_cells(rc.species_names, rc.mol_masses, m, seed=s,
+                                              gas_file=rc.gmodel.file_name)
     nblk = (n + block - 1) // block
     dev = torch.device("cuda")
     X = torch.empty((nblk * block, sg.nin_pad), dtype=torch.float32, device=dev)

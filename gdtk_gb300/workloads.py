@@ -23,16 +23,22 @@ def air5_cells(n, seed=0):
 
 
 def h2air_cells(names, mol_masses, n, seed=1, frozen_fraction=0.5, T_cold=(300.0, 600.0), T_hot=(1100.0, 2800.0),
-                p_range=(2.0e4, 5.0e5)):
+                p_range=(2.0e4, 5.0e5), gas_file=None, subset=None):
     """H2-air workload of uneven stiffness.
 
     A fraction `frozen_fraction` of the cells is cold (T ~ U[T_cold]), the rest hot
     (T ~ U[T_hot]); p = 10^U[log10 p_range].  Composition: a blend, weight lambda ~ U[0, 1],
-    of stoichiometric H2-air (X_H2 : X_O2 : X_N2 = 2 : 1 : 3.76) and its complete-combustion
-    products (X_H2O : X_N2 = 2 : 3.76), plus radicals (H, O, OH, HO2, H2O2, N, NO, NO2, HNO)
-    whose total mass fraction is 10^U[-6, -2] split by Dirichlet(0.5); renormalised.
-    Returns T (n,), p (n,), Y (nsp, n).
+    of stoichiometric H2-air (X_H2 : X_O2 : X_N2 = 2 : 1 : 3.76) and its equilibrium products at
+    the cell's (p, T) (the element composition of X_H2O : X_N2 = 2 : 3.76, by
+    gdtk_gb300.equilibrium from the NASA-9 data of `gas_file`), plus radicals (H, O, OH, HO2,
+    H2O2, N, NO, NO2, HNO) whose total mass fraction is 10^U[-6, -2] split by Dirichlet(0.5);
+    renormalised.  Returns T (n,), p (n,), Y (nsp, n).  With `subset` (indices into the n cells),
+    only those cells are returned, and the equilibrium products are evaluated for them alone; the
+    random draws are the same as for all n cells.
     """
+    if gas_file is None:
+        raise ValueError("h2air_cells needs the gas file (species thermo data) for the equilibrium products")
+    from .equilibrium import products_table
     rng = np.random.Generator(np.random.PCG64(seed))
     idx = {s: i for i, s in enumerate(names)}
     M = np.asarray(mol_masses, dtype=np.float64)
@@ -49,25 +55,30 @@ def h2air_cells(names, mol_masses, n, seed=1, frozen_fraction=0.5, T_cold=(300.0
         return y / y.sum()
 
     unburnt = massf_of({'H2': 2.0, 'O2': 1.0, 'N2': 3.76})
-    burnt = massf_of({'H2O': 2.0, 'N2': 3.76})
     lam = rng.uniform(0.0, 1.0, n)
-    Y = (1.0 - lam)[:, None] * unburnt[None, :] + lam[:, None] * burnt[None, :]
     rad_idx = [idx[s] for s in H2AIR_RADICALS if s in idx]
     share = 10.0 ** rng.uniform(-6.0, -2.0, n)
     w = rng.dirichlet(np.full(len(rad_idx), 0.5), n)
+    if subset is not None:
+        subset = np.asarray(subset, dtype=np.int64)
+        T, p, lam, share, w = T[subset], p[subset], lam[subset], share[subset], w[subset]
+    burnt = products_table(gas_file, massf_of({'H2O': 2.0, 'N2': 3.76}), M).massf(p, T).T   # (n, nsp)
+    Y = (1.0 - lam)[:, None] * unburnt[None, :] + lam[:, None] * burnt
     Y *= (1.0 - share)[:, None]
     Y[:, rad_idx] += share[:, None] * w
     Y = Y / Y.sum(axis=1, keepdims=True)
     return T, p, np.ascontiguousarray(Y.T)
 
 
-def h2air_blocks(names, mol_masses, nblocks=64, seed=2, n_min=2048, n_max=524288, dts=(1.0e-7, 1.0e-6, 1.0e-5)):
+def h2air_blocks(names, mol_masses, nblocks=64, seed=2, n_min=2048, n_max=524288, dts=(1.0e-7, 1.0e-6, 1.0e-5),
+                 gas_file=None, pick=None):
     """Uneven multi-block H2-air workload.
 
     Block sizes are log-uniform in [n_min, n_max]; each block draws its own update interval from
     `dts`, its own cold fraction, and its own sub-ranges of the cold (300-600 K) and hot
     (1100-2800 K) temperatures and of the pressure (2e4-5e5 Pa), and then its cells as in
-    h2air_cells.  Returns a list of dicts with T, p, Y (nsp, n) and dt.
+    h2air_cells.  Returns a list of dicts with T, p, Y (nsp, n) and dt.  With `pick(b, n)` -> indices,
+    block b holds only those of its n cells (and 'n' and 'cells' record the full size and the indices).
     """
     rng = np.random.Generator(np.random.PCG64(seed))
     sizes = np.round(10.0 ** rng.uniform(np.log10(n_min), np.log10(n_max), nblocks)).astype(np.int64)
@@ -78,10 +89,12 @@ def h2air_blocks(names, mol_masses, nblocks=64, seed=2, n_min=2048, n_max=524288
         hot = np.sort(rng.uniform(1100.0, 2800.0, 2))
         lp = np.sort(rng.uniform(np.log10(2.0e4), np.log10(5.0e5), 2))
         frac = float(rng.uniform(0.0, 1.0))
-        T, p, Y = h2air_cells(names, mol_masses, int(sizes[b]), seed=seed * 1000 + b, frozen_fraction=frac,
+        nb = int(sizes[b])
+        sub = None if pick is None else np.asarray(pick(b, nb), dtype=np.int64)
+        T, p, Y = h2air_cells(names, mol_masses, nb, seed=seed * 1000 + b, frozen_fraction=frac,
                               T_cold=(cold[0], cold[1] + 1e-9), T_hot=(hot[0], hot[1] + 1e-9),
-                              p_range=(10.0 ** lp[0], 10.0 ** lp[1] * (1 + 1e-12)))
-        out.append(dict(T=T, p=p, Y=Y, dt=dt))
+                              p_range=(10.0 ** lp[0], 10.0 ** lp[1] * (1 + 1e-12)), gas_file=gas_file, subset=sub)
+        out.append(dict(T=T, p=p, Y=Y, dt=dt, n=nb, cells=sub))
     return out
 
 

@@ -128,7 +128,7 @@ def test_air5_warm_start_parity(park5, kernel):
 def test_h2air_alpha_qss_tight_parity(j92, kernel):
     from gdtk_gb300.workloads import h2air_cells
     rc, orc = j92
-    T, p, Y = h2air_cells(rc.species_names, rc.mol_masses, 512, seed=3)
+    T, p, Y = h2air_cells(rc.species_names, rc.mol_masses, 512, seed=3, gas_file=rc.gmodel.file_name)
     g, o, _, _ = run_pair(rc, orc, T, p, Y, 1.0e-6, kernel=kernel)
     assert (g["status"] == 0).mean() > 0.95
     assert_parity(g, o)
@@ -220,7 +220,7 @@ def test_source_terms(j92):
     from gdtk_gb300.workloads import h2air_cells
     torch = torch_cuda()
     rc, orc = j92
-    T, p, Y = h2air_cells(rc.species_names, rc.mol_masses, 128, seed=8)
+    T, p, Y = h2air_cells(rc.species_names, rc.mol_masses, 128, seed=8, gas_file=rc.gmodel.file_name)
     dT, dp, dY = to_dev(torch, T, p, Y)
     rho, _ = rc.thermo_from_pT(dp, dT, dY)
     src = rc.source_terms(rho, dT, dY).cpu().numpy()
@@ -303,7 +303,7 @@ def test_block_batch_equals_per_block_updates(j92):
     sizes, dts = [300, 37, 1200], [1e-7, 1e-5, 1e-6]
     blocks, solo = [], []
     for k, (n, dt) in enumerate(zip(sizes, dts)):
-        T, p, Y = h2air_cells(rc.species_names, rc.mol_masses, n, seed=20 + k)
+        T, p, Y = h2air_cells(rc.species_names, rc.mol_masses, n, seed=20 + k, gas_file=rc.gmodel.file_name)
         dT, dp, dY = to_dev(torch, T, p, Y)
         rho, u = rc.thermo_from_pT(dp, dT, dY)
         mk = lambda: dict(rho=rho, u=u, T=dT.clone(), p=dp.clone(), massf=dY.clone(),
@@ -329,7 +329,7 @@ def test_block_batch_graph_replay_matches_direct_calls(j92):
     def make():
         out = []
         for k, (n, dt) in enumerate(zip([200, 50], [1e-6, 1e-5])):
-            T, p, Y = h2air_cells(rc.species_names, rc.mol_masses, n, seed=60 + k)
+            T, p, Y = h2air_cells(rc.species_names, rc.mol_masses, n, seed=60 + k, gas_file=rc.gmodel.file_name)
             dT, dp, dY = to_dev(torch, T, p, Y)
             rho, u = rc.thermo_from_pT(dp, dT, dY)
             out.append(dict(rho=rho, u=u, T=dT, p=dp, massf=dY,
@@ -363,7 +363,7 @@ def test_autotuner_picks_a_fitting_shape(j92, tmp_path, monkeypatch):
     monkeypatch.setenv("GDTK_JIT_CACHE", str(tmp_path))
     monkeypatch.setattr(autotune, "SHAPES", [(256, 1), (128, 1)])
     rc, orc = j92
-    T, p, Y = h2air_cells(rc.species_names, rc.mol_masses, 2048, seed=70)
+    T, p, Y = h2air_cells(rc.species_names, rc.mol_masses, 2048, seed=70, gas_file=rc.gmodel.file_name)
     dT, dp, dY = to_dev(torch, T, p, Y)
     rho, u = rc.thermo_from_pT(dp, dT, dY)
     sample = dict(rho=rho, u=u, T=dT, p=dp, massf=dY, dt_chem=torch.full((2048,), -1.0, dtype=torch.float64,
@@ -530,7 +530,7 @@ def test_alternate_kernel_forms_parity(form, monkeypatch):
     torch = torch_cuda()
     stats = torch.zeros(24, dtype=torch.int64, device="cuda")
     rc.set_lane_stats(stats)
-    T, p, Y = h2air_cells(rc.species_names, rc.mol_masses, 512, seed=3)
+    T, p, Y = h2air_cells(rc.species_names, rc.mol_masses, 512, seed=3, gas_file=rc.gmodel.file_name)
     g, o, _, _ = run_pair(rc, orc, T, p, Y, 1.0e-6)
     rc.set_lane_stats(None)
     assert (g["status"] == 0).mean() > 0.95

@@ -133,7 +133,7 @@ def test_training_reduces_heldout_error(trained):
 
 def _fresh_cells(rc, n, seed):
     from gdtk_gb300.workloads import h2air_cells
-    T, p, Y = h2air_cells(rc.species_names, rc.mol_masses, n, seed=seed)
+    T, p, Y = h2air_cells(rc.species_names, rc.mol_masses, n, seed=seed, gas_file=rc.gmodel.file_name)
     d = dict(T=torch.tensor(T, device="cuda"), p=torch.tensor(p, device="cuda"),
              massf=torch.tensor(np.ascontiguousarray(Y), device="cuda"))
     d["rho"], d["u"] = rc.thermo_from_pT(d["p"], d["T"], d["massf"])

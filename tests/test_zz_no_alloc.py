@@ -17,7 +17,7 @@ pytestmark = pytest.mark.gpu
 
 def _cells(torch, rc, n, seed):
     from gdtk_gb300.workloads import h2air_cells
-    T, p, Y = h2air_cells(rc.species_names, rc.mol_masses, n, seed=seed)
+    T, p, Y = h2air_cells(rc.species_names, rc.mol_masses, n, seed=seed, gas_file=rc.gmodel.file_name)
     dev = lambda a: torch.tensor(np.ascontiguousarray(a), dtype=torch.float64, device="cuda")
     dT, dp, dY = dev(T), dev(p), dev(Y)
     rho, u = rc.thermo_from_pT(dp, dT, dY)
@@ -59,10 +59,10 @@ def test_noalloc_matches_allocating_entry_point_twice():
         assert torch.equal(s["status"], ref["status"])
         ok = ref["status"] == 0
         assert bool(ok.all())
-        assert float((s["massf"] - ref["massf"]).abs().max()) <= 1e-8
-        assert float(((s["T"] - ref["T"]).abs() / ref["T"]).max()) <= 1e-7
-        assert float(((s["p"] - ref["p"]).abs() / ref["p"]).max()) <= 1e-7
-        assert torch.equal(s["dt_chem"], ref["dt_chem"])
+        # the same generated kernel integrates each cell on its own, so only the visit order may
+        # differ between the two calls, and no cell's result depends on it: bitwise equality
+        for k in ("massf", "T", "p", "dt_chem"):
+            assert torch.equal(s[k], ref[k]), k
 
 
 def test_noalloc_rejects_batches_beyond_its_scratch():
