@@ -64,6 +64,12 @@ __device__ __forceinline__ double arrhenius(double A, double n, double C, double
     return A * pow(T, n) * exp(-C / T);
 }
 
+// Arrhenius (rate_constant.d:72-75) or Arrhenius2 (112-115) from the record's three parameters.
+__device__ __forceinline__ double simple_rate(int model, const double* p, double T) {
+    if (model == RATE_ARRHENIUS2) return exp(p[0] + p[1] * T - p[2] / T);
+    return p[0] * pow(T, p[1]) * exp(-p[2] / T);
+}
+
 // Forward rate constant of a pressure-dependent reaction: the third-body concentration of its
 // efficiency list from the gas state's mass fractions (rate_constant.d:114-121), then
 // Lindemann-Hinshelwood (155-160), Troe (258-287) or Yungster-Rabinowitz (338-350).
@@ -138,12 +144,12 @@ __device__ void rate_constants(const MechView& m, double Tq, Vec kf, Vec kb, Vec
             Kc = K_p * ipow(P_atm / (R_universal * T), (int)nuSum);
         }
         if (r[RX_FRC] != RATE_FROM_EQ) {
-            double f = (r[RX_FRC] == RATE_ARRHENIUS) ? d[0] * pow(T, d[1]) * exp(-d[2] / T)
-                                                     : pressure_dependent_kf(m, r, d, T, mf, rho);
+            double f = (r[RX_FRC] == RATE_ARRHENIUS || r[RX_FRC] == RATE_ARRHENIUS2)
+                           ? simple_rate(r[RX_FRC], d, T) : pressure_dependent_kf(m, r, d, T, mf, rho);
             kf[ir] = f;
-            kb[ir] = (r[RX_BRC] == RATE_FROM_EQ) ? f / Kc : d[3] * pow(T, d[4]) * exp(-d[5] / T);
+            kb[ir] = (r[RX_BRC] == RATE_FROM_EQ) ? f / Kc : simple_rate(r[RX_BRC], d + 3, T);
         } else {
-            double b = d[3] * pow(T, d[4]) * exp(-d[5] / T);
+            double b = simple_rate(r[RX_BRC], d + 3, T);
             kb[ir] = b;
             kf[ir] = b * Kc;
         }

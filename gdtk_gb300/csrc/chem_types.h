@@ -15,7 +15,8 @@
 //   [SP + 56*isp + k]  species isp: M, R, T_low, T_high, Cp_low, Cp_high, h_low, h_high, s_low, s_high,
 //                      breaks[5], blends[4], -, coeffs[4][9]
 //   [RD + 16*ir]       reaction ir: fA, fn, fC, bA, bn, bC (kInf in fA..fC for the pressure-dependent
-//                      models), k0 A, n, C, Troe F_cent, a, T1, T2, T3 (or Yungster-Rabinowitz a, b, c in
+//                      models; logA, B, C for Arrhenius2), k0 A, n, C, Troe F_cent, a, T1, T2, T3 (or
+//                      Yungster-Rabinowitz a, b, c in
 //                      the a, T1, T2 slots), Troe flags (1 F_cent given, 2 T1 given, 4 T2 given), -
 //   [ED + nsp*s]       efficiency set s: values[nsp]
 #pragma once
@@ -43,10 +44,11 @@ enum { SP_M = 0, SP_R, SP_TLOW, SP_THIGH, SP_CPLOW, SP_CPHIGH, SP_HLOW, SP_HHIGH
 // reaction int-record fields
 enum { RX_COLLIDER = 0, RX_FRC, RX_BRC, RX_EFFSET, RX_NREAC, RX_NPROD, RX_NPART,
        RX_REAC_IDX = 8, RX_REAC_COEFF = 12, RX_PROD_IDX = 16, RX_PROD_COEFF = 20, RX_PART = 24, RX_PART_NU = 32 };
-// rate-constant models (kinetics/rate_constant.d): Arrhenius 52-80, from K_c, and the pressure-dependent
+// rate-constant models (kinetics/rate_constant.d): Arrhenius 52-80, from K_c, the pressure-dependent
 // Lindemann-Hinshelwood 123-160, Troe 162-290, Yungster-Rabinowitz 292-355 (third-body concentration of
-// the reaction's efficiency list, 114-121)
-enum { RATE_ARRHENIUS = 0, RATE_FROM_EQ = 1, RATE_LH = 2, RATE_TROE = 3, RATE_YR = 4 };
+// the reaction's efficiency list, 114-121), and Arrhenius2 / Arrhenius-logA 82-121,
+// k = exp(logA + B T - C/T), whose (logA, B, C) take the places of (A, n, C)
+enum { RATE_ARRHENIUS = 0, RATE_FROM_EQ = 1, RATE_LH = 2, RATE_TROE = 3, RATE_YR = 4, RATE_ARRHENIUS2 = 5 };
 // reaction double-record fields beyond the six Arrhenius parameters
 enum { RD_K0A = 6, RD_K0N, RD_K0C, RD_FCENT, RD_TA, RD_T1, RD_T2, RD_T3, RD_TFLAGS };
 enum { TROE_FCENT = 1, TROE_T1 = 2, TROE_T2 = 4 };

@@ -136,6 +136,12 @@ std::vector<Part> participants(const ReactionHost& r) {
 
 // ln k = ln A + n ln T - C / T as an expression; empty if A == 0.
 std::string log_arrhenius(const RateConstHost& rc) {
+    if (rc.model == RATE_ARRHENIUS2) {   // ln k = logA + B T - C/T (rate_constant.d:112-115)
+        std::string e = lit(rc.A);
+        if (rc.n != 0.0) e = "fma(" + lit(rc.n) + ", T, " + e + ")";
+        if (rc.C != 0.0) e = "fma(" + lit(-rc.C) + ", rT, " + e + ")";
+        return e;
+    }
     if (rc.A <= 0.0) return "";
     std::string e = lit(std::log(rc.A));
     if (rc.n != 0.0) e = "fma(" + lit(rc.n) + ", lnT, " + e + ")";
@@ -145,7 +151,7 @@ std::string log_arrhenius(const RateConstHost& rc) {
 
 // k = A T^n as products when C == 0 and n is a small integer (no exponential needed).
 bool power_arrhenius(const RateConstHost& rc, std::string& out) {
-    if (rc.C != 0.0 || rc.n != std::floor(rc.n) || std::fabs(rc.n) > 4) return false;
+    if (rc.model != RATE_ARRHENIUS || rc.C != 0.0 || rc.n != std::floor(rc.n) || std::fabs(rc.n) > 4) return false;
     int n = (int)rc.n;
     if (n == 0) { out = lit(rc.A); return true; }
     out = lit(rc.A) + " * " + ipow_expr(n > 0 ? "T" : "rT", n > 0 ? n : -n);
@@ -422,7 +428,9 @@ std::string generate_fast_source(const GasModelHost& gm, const MechanismHost& mh
         const ReactionHost& r = mh.reactions[ir];
         int np = 0;
         for (auto& pp : participants(r)) np += pp.nu != 0;
-        if (kc_table && !r.frc.pressure_dependent() && np <= 8) table_rx.push_back(ir);
+        // the table holds ln A, n, C records; Arrhenius2 rate constants stay straight-line
+        const bool arr2 = r.frc.model == RATE_ARRHENIUS2 || r.brc.model == RATE_ARRHENIUS2;
+        if (kc_table && !r.frc.pressure_dependent() && !arr2 && np <= 8) table_rx.push_back(ir);
     }
     const std::vector<bool> kbp = kb_product_reactions(gm, mh);
     bool any_kbp = false;
@@ -545,7 +553,7 @@ std::string generate_fast_source(const GasModelHost& gm, const MechanismHost& mh
             o << "    const double Mc = Mv[" << ifall++ << " * ms];\n";
             o << pressure_dependent_code(r.frc);
             o << "    const double kb = kf * gdtk_exp(-" << lnKc << ", etab);\n";
-        } else if (r.frc.model == RATE_ARRHENIUS) {
+        } else if (r.frc.simple()) {
             std::string pw;
             if (power_arrhenius(r.frc, pw)) {
                 o << "    const double kf = " << pw << ";\n";
@@ -556,7 +564,7 @@ std::string generate_fast_source(const GasModelHost& gm, const MechanismHost& mh
                 else o << "    const double lkf = " << l << ";\n    const double kf = gdtk_exp(lkf, etab);\n";
                 if (r.brc.model == RATE_FROM_EQ) o << "    const double kb = gdtk_exp(lkf - " << lnKc << ", etab);\n";
             }
-            if (r.brc.model == RATE_ARRHENIUS) {
+            if (r.brc.simple()) {
                 std::string pb;
                 if (power_arrhenius(r.brc, pb)) o << "    const double kb = " << pb << ";\n";
                 else {

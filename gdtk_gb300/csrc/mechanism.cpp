@@ -36,6 +36,13 @@ RateConstHost rate_const(const LuaValue& t) {
     if (model == "Arrhenius") {
         r.model = RATE_ARRHENIUS;
         arrhenius_params(t, r.A, r.n, r.C);
+    } else if (model == "Arrhenius2" || model == "Arrhenius-logA") {   // rate_constant.d:82-121, 574-577
+        r.model = RATE_ARRHENIUS2;
+        r.A = t.get("logA").number();
+        r.n = t.get("B").number();
+        r.C = t.get("C").number();
+        if (t.has("rctIndex") && t.get("rctIndex").number() != -1)
+            throw std::runtime_error("rate constants on a temperature other than T need a multi-temperature gas");
     } else if (model == "fromEqConst") {
         r.model = RATE_FROM_EQ;
     } else if (model == "Lindemann-Hinshelwood" || model == "Troe" || model == "Yungster-Rabinowitz") {
@@ -61,9 +68,8 @@ RateConstHost rate_const(const LuaValue& t) {
             r.T2 = t.get("c").number();
         }
     } else {
-        // kinetics/rate_constant.d:570-597 also knows Arrhenius2, Park, Marrone-Treanor and MMT
-        // (multi-temperature or alternative forms); this engine implements the single-temperature
-        // Arrhenius, third-body and pressure-dependent path.
+        // kinetics/rate_constant.d:570-597 also knows Park, Marrone-Treanor and MMT, which take the
+        // rate-controlling temperature of a multi-temperature gas
         throw std::runtime_error("rate-constant model '" + model + "' is not supported by this engine");
     }
     return r;
@@ -319,7 +325,8 @@ void flop_model(const GasModelHost& gm, const MechanismHost& mh, double out[5]) 
         for (auto& x : r.prod) part.push_back(x.first);
         std::sort(part.begin(), part.end());
         part.erase(std::unique(part.begin(), part.end()), part.end());
-        // rate constants (rate_constant.d:72-75, reaction.d:26-52, 94-143)
+        // rate constants (rate_constant.d:72-75, 112-115, reaction.d:26-52, 94-143)
+        auto arr_of = [&](const RateConstHost& rc) { return rc.model == RATE_ARRHENIUS2 ? EXP + 4 : POW + EXP + 3; };
         const double arr = POW + EXP + 3;
         // pressure-dependent forward rates (rate_constant.d:114-121, 155-160, 258-287, 338-350): two
         // Arrhenius terms, the third-body sum (4 per efficiency) and the blending
@@ -335,10 +342,11 @@ void flop_model(const GasModelHost& gm, const MechanismHost& mh, double out[5]) 
         } else if (r.frc.model == RATE_YR) {
             fwd = tb + 2 + LOG + 2 * EXP + 7 + 3 + 4;
         }
+        if (r.frc.model == RATE_ARRHENIUS2) fwd = arr_of(r.frc);
         if (r.frc.model == RATE_FROM_EQ || r.brc.model == RATE_FROM_EQ)
-            kc += (r.frc.model == RATE_FROM_EQ ? arr : fwd) + 4.0 * part.size() + (EXP + 2) + 3 + 1 + 1;
+            kc += (r.frc.model == RATE_FROM_EQ ? arr_of(r.brc) : fwd) + 4.0 * part.size() + (EXP + 2) + 3 + 1 + 1;
         else
-            kc += fwd + arr;
+            kc += fwd + arr_of(r.brc);
         if (r.collider) {
             if (std::find(sets.begin(), sets.end(), r.eff) == sets.end()) {
                 sets.push_back(r.eff);

@@ -5,6 +5,7 @@
 #include <string>
 #include <vector>
 
+#include "chem_types.h"
 #include "lua_table.h"
 
 namespace gdtk {
@@ -27,12 +28,14 @@ struct GasModelHost {
 };
 
 struct RateConstHost {
-    int model = 0;   // RATE_ARRHENIUS, RATE_FROM_EQ, RATE_LH, RATE_TROE or RATE_YR
-    double A = 0, n = 0, C = 0;            // Arrhenius; k_inf for the pressure-dependent models
+    int model = 0;   // RATE_ARRHENIUS, RATE_FROM_EQ, RATE_LH, RATE_TROE, RATE_YR or RATE_ARRHENIUS2
+    double A = 0, n = 0, C = 0;            // Arrhenius; k_inf for the pressure-dependent models;
+                                           // logA, B, C for Arrhenius2 (k = exp(logA + B T - C/T))
     double A0 = 0, n0 = 0, C0 = 0;         // k_0 of the pressure-dependent models
     double Fcent = 0, a = 0, T1 = 0, T2 = 0, T3 = 0;   // Troe (a, T1, T2 hold a, b, c for Yungster-Rabinowitz)
     int troe_flags = 0;                    // TROE_FCENT | TROE_T1 | TROE_T2: parameters given
-    bool pressure_dependent() const { return model >= 2; }
+    bool pressure_dependent() const { return model == RATE_LH || model == RATE_TROE || model == RATE_YR; }
+    bool simple() const { return model == RATE_ARRHENIUS || model == RATE_ARRHENIUS2; }   // no third body
 };
 
 struct ReactionHost {

@@ -135,6 +135,8 @@ class Oracle:
                         return 0, float(d['A']), float(d['n']), float(d['C'])
                     if d['model'] == 'fromEqConst':
                         return 1, 0.0, 0.0, 0.0
+                    if d['model'] in ('Arrhenius2', 'Arrhenius-logA'):   # rate_constant.d:82-121
+                        return 5, float(d['logA']), float(d['B']), float(d['C'])
                     if d['model'] in pd_models:   # k_inf here, k_0 and the blending below
                         k = d['kInf']
                         return pd_models[d['model']], float(k['A']), float(k['n']), float(k['C'])
@@ -147,7 +149,7 @@ class Oracle:
                 ir = L.oracle_add_reaction(self.h, int(r['collider']), fm, fA, fn, fC, bm, bA, bn, bC,
                                            len(ri), _ip(ri), _ip(rcf), len(pi), _ip(pi), _ip(pcf), len(ei), _ip(ei),
                                            _dp(ev))
-                if fm >= 2:   # rate_constant.d:135-145, 181-229, 310-333
+                if fm in pd_models.values():   # rate_constant.d:135-145, 181-229, 310-333
                     d = r['frc']
                     k0 = d['k0']
                     flags = 0

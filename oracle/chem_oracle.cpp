@@ -129,8 +129,9 @@ struct CEACurve {
     }
 };
 
-// model 0 Arrhenius, 1 fromEqConst, and the pressure-dependent 2 Lindemann-Hinshelwood, 3 Troe,
-// 4 Yungster-Rabinowitz (A, n, C are then k_inf; yr a, b, c are held in a, T1, T2)
+// model 0 Arrhenius, 1 fromEqConst, the pressure-dependent 2 Lindemann-Hinshelwood, 3 Troe,
+// 4 Yungster-Rabinowitz (A, n, C are then k_inf; yr a, b, c are held in a, T1, T2), and
+// 5 Arrhenius2 / Arrhenius-logA (A, n, C hold logA, B, C)
 struct RateConst {
     int model = 0;
     double A = 0, n = 0, C = 0;
@@ -155,6 +156,10 @@ inline double ipow(double x, int n) {
 // rate_constant.d:72-75
 inline double arrhenius(const RateConst& rc, double T) { return rc.A * std::pow(T, rc.n) * std::exp(-rc.C / T); }
 inline double arrhenius0(const RateConst& rc, double T) { return rc.A0 * std::pow(T, rc.n0) * std::exp(-rc.C0 / T); }
+// rate_constant.d:112-115 (ArrheniusRateConstant2.eval)
+inline double arrhenius2(const RateConst& rc, double T) { return std::exp(rc.A + rc.n * T - rc.C / T); }
+inline double simple_rate(const RateConst& rc, double T) { return rc.model == 5 ? arrhenius2(rc, T) : arrhenius(rc, T); }
+inline bool pressure_dependent_model(int model) { return model >= 2 && model <= 4; }
 
 // Pressure-dependent rate constants with third-body concentration M (rate_constant.d:114-121 forms
 // M = sum eff * massf * rho / M_i): Lindemann-Hinshelwood 155-160, Troe 258-287, Yungster-Rabinowitz 338-350.
@@ -282,18 +287,18 @@ struct Work {
         gibbs(T);
         for (size_t ir = 0; ir < m.reactions.size(); ++ir) {
             const Reaction& r = m.reactions[ir];
-            if (r.frc.model == 0 || r.frc.model >= 2) {
-                if (r.frc.model == 0) {
-                    kf[ir] = arrhenius(r.frc, T);
+            if (r.frc.model != 1) {
+                if (!pressure_dependent_model(r.frc.model)) {
+                    kf[ir] = simple_rate(r.frc, T);
                 } else {
                     double M = 0.0;
                     for (auto& e : r.eff) M += e.second * tbc[e.first];
                     kf[ir] = pressure_dependent(r.frc, T, M);
                 }
                 if (r.brc.model == 1) kb[ir] = kf[ir] / Kc(r, T);
-                else kb[ir] = arrhenius(r.brc, T);
+                else kb[ir] = simple_rate(r.brc, T);
             } else {
-                kb[ir] = arrhenius(r.brc, T);
+                kb[ir] = simple_rate(r.brc, T);
                 kf[ir] = kb[ir] * Kc(r, T);
             }
         }
@@ -708,7 +713,9 @@ int oracle_species_thermo(void* h, int isp, double T, double* Cp, double* hh, do
 int oracle_rate_constants(void* h, double T, const double* conc, double* kf, double* kb) {
     Model* m = (Model*)h;
     Work w(*m);
-    try { w.rate_constants(T, conc); } catch (Failure& f) { return f.code; }
+    // without concentrations the third bodies of pressure-dependent rates are zero
+    std::vector<double> zero(m->nsp, 0.0);
+    try { w.rate_constants(T, conc ? conc : zero.data()); } catch (Failure& f) { return f.code; }
     for (size_t i = 0; i < m->reactions.size(); ++i) { kf[i] = w.kf[i]; kb[i] = w.kb[i]; }
     return 0;
 }

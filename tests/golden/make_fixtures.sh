@@ -52,6 +52,8 @@ prep gupta5 "$KIN/air-chemistry-1T/air-5sp-1T.inp"                     "$KIN/air
 # pressure-dependent (Troe) reactions: F_cent given (Stanford-2011), and a, T3, T1, T2 (DRM19 methane)
 prep stanford "$KIN/hydrogen-ignition-delay/Stanford-2011-species.inp"  "$KIN/hydrogen-ignition-delay/Stanford-2011.lua"
 prep drm19  "$KIN/methane-combustion-w-drm19/drm19-prep-gas.inp"       "$KIN/methane-combustion-w-drm19/drm19-prep-chem.inp"
+# Arrhenius2, Lindemann-Hinshelwood and Yungster-Rabinowitz forms (no reference example uses them)
+prep h2o2forms "$KIN/hydrogen-ignition-delay/Jachimowski-1992-species.inp" "$HERE/inputs/h2o2-rate-forms.lua"
 
 # Sample data of the reference's unit tests (known-answer tests).
 cp "$REF/src/kinetics/sample-input/H2-I2-HI.lua" "$OUT/h2i2-gas.lua"

@@ -135,3 +135,27 @@ def test_product_form_refused_where_it_could_overflow(tmp_path):
     cold = tmp_path / "n2-cold-chem.lua"
     cold.write_text(open(mech("n2-chem.lua")).read().replace("lower=300.000000", "lower=20.000000"))
     assert set(_kc_modes(_source(mech("n2-gas.lua"), str(cold)))) == {0}
+
+
+def test_rate_forms_fixture_generates_and_compiles():
+    """Arrhenius2 (rate_constant.d:82-121), Lindemann-Hinshelwood and Yungster-Rabinowitz forms: the
+    reader takes them, Arrhenius2 stays out of the ln A / n / C table, and the kernel compiles."""
+    gas, chem = mech("h2o2forms-gas.lua"), mech("h2o2forms-chem.lua")
+    src = _source(gas, chem)
+    assert len(_kc_modes(src)) == 6              # r3..r7 and r13 in the table; r1, r2, r11, lh, yr straight-line
+    assert "fma(%s, T, " % float.hex(2.0e-5) in src            # the B T term of r2 (hex literal)
+    assert "#define GDTK_NFALLOFF 2" in src
+    log = gdtk_gb300.compile_fast_source_check(gas, chem)
+    assert "sm_103a" in log
+
+
+def test_arrhenius_logA_is_the_same_model(tmp_path):
+    # createRateConstant (rate_constant.d:574-577) maps 'Arrhenius-logA' and 'Arrhenius2' to one class
+    alias = tmp_path / "alias-chem.lua"
+    alias.write_text(open(mech("h2o2forms-chem.lua")).read().replace("model='Arrhenius2'", "model='Arrhenius-logA'"))
+    gas = mech("h2o2forms-gas.lua")
+    assert _source(gas, str(alias)) == _source(gas, mech("h2o2forms-chem.lua"))
+    conc = np.linspace(0.5, 6.5, 13)
+    a = oracle.Oracle(gas, str(alias)).rate_constants(1500.0, conc)
+    b = oracle.Oracle(gas, mech("h2o2forms-chem.lua")).rate_constants(1500.0, conc)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])

@@ -581,3 +581,34 @@ def test_full_size_h2air_update_properties(j92):
     assert np.abs(g["Y"] - o["massf"].T).max() <= Y_ABS
     assert (np.abs(g["T"] - o["T"]) / o["T"]).max() <= TP_REL
     assert (np.abs(g["p"] - o["p"]) / o["p"]).max() <= TP_REL
+
+
+@pytest.mark.parametrize("kernel", sorted(KERNELS))
+def test_arrhenius2_lindemann_yungster_rabinowitz_parity(kernel):
+    # the h2o2forms fixture: Arrhenius2 (one with a B T term), Lindemann-Hinshelwood and
+    # Yungster-Rabinowitz forward rates beside Arrhenius and third-body reactions (rate_constant.d:82-355)
+    from gdtk_gb300.cells import ReactorCells
+    from gdtk_gb300.workloads import h2air_cells
+    gas, chem = mech("h2o2forms-gas.lua"), mech("h2o2forms-chem.lua")
+    rc, orc = ReactorCells(gas, chem), oracle.Oracle(gas, chem)
+    T, p, Y = h2air_cells(rc.species_names, rc.mol_masses, 512, seed=13, gas_file=gas)
+    g, o, _, _ = run_pair(rc, orc, T, p, Y, 1.0e-6, kernel=kernel)
+    assert (g["status"] == 0).mean() > 0.95
+    assert_parity(g, o)
+
+
+def test_rate_forms_tickrates_match_oracle():
+    from gdtk_gb300.gas import GasModel, GasState, ReactionMechanism
+    gm = GasModel(mech("h2o2forms-gas.lua"))
+    rm = ReactionMechanism(gm, mech("h2o2forms-chem.lua"))
+    orc = oracle.Oracle(mech("h2o2forms-gas.lua"), mech("h2o2forms-chem.lua"))
+    gs = GasState(gm)
+    gs.T = 1700.0
+    gs.p = 2.0e5
+    gs.molef = {'H2': 0.25, 'O2': 0.15, 'N2': 0.45, 'H2O': 0.05, 'OH': 0.02, 'H': 0.02, 'O': 0.01, 'HO2': 0.03,
+                'H2O2': 0.02}
+    gs.update_thermo_from_pT()
+    f = np.array(rm.forward_tickrates(gs))
+    b = np.array(rm.backward_tickrates(gs))
+    _, _, wf, wb = orc.split_rates(1700.0, np.array(gs.conc))
+    assert np.allclose(f, wf, rtol=1e-13, atol=0) and np.allclose(b, wb, rtol=1e-13, atol=0)

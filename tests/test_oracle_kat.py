@@ -235,3 +235,36 @@ def test_two_temperature_air5():
         assert T == pytest.approx(2000.0, rel=1e-6)
         assert T_ve == pytest.approx(2000.0, rel=1e-6)
         assert p == pytest.approx(1.0e6, rel=1e-6)
+
+
+def test_arrhenius2_and_falloff_forms_restated():
+    """The oracle's Arrhenius2 (rate_constant.d:112-115), Lindemann-Hinshelwood (155-160) and
+    Yungster-Rabinowitz (338-350) forward rate constants, from the formulas with the fixture's
+    parameters as prep_chem wrote them."""
+    from oracle.luatable import read_lua_file
+    o = oracle.Oracle(mech("h2o2forms-gas.lua"), mech("h2o2forms-chem.lua"))
+    rx = read_lua_file(mech("h2o2forms-chem.lua"))["reaction"]
+    T = 1700.0
+    conc = np.linspace(0.5, 6.5, o.nsp)            # mol/m^3, any positive state
+    kf, kb = o.rate_constants(T, conc)
+    for k in (1, 2, 8):                            # r1, r2, r11: Arrhenius2
+        f = rx[k]["frc"]
+        assert f["model"] == "Arrhenius2"
+        assert close(np.exp(f["logA"] + f["B"] * T - f["C"] / T), kf[k - 1], 1e-14)
+
+    def arr(d):
+        return d["A"] * T ** d["n"] * np.exp(-d["C"] / T)
+
+    def third_body(r):
+        eff = r["efficiencies"]
+        return sum(eff[i] * conc[i] for i in eff)
+
+    lh, yr = rx[10], rx[11]
+    assert lh["frc"]["model"] == "Lindemann-Hinshelwood" and yr["frc"]["model"] == "Yungster-Rabinowitz"
+    kinf, k0, M = arr(lh["frc"]["kInf"]), arr(lh["frc"]["k0"]), third_body(lh)
+    assert close(k0 * kinf * M / (k0 * M + kinf), kf[9], 1e-13)
+    f = yr["frc"]
+    kinf, k0, M = arr(f["kInf"]), arr(f["k0"]), third_body(yr)
+    pr = k0 * M / kinf
+    fc = f["a"] * np.exp(-f["b"] / T) + (1.0 - f["a"]) * np.exp(-f["c"] / T)
+    assert close(kinf * (pr / (1.0 + pr)) * fc / (1.0 + np.log(pr) ** 2), kf[10], 1e-13)
