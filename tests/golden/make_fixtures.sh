@@ -66,5 +66,8 @@ cp "$REF/src/gas/sample-data/five-species-air.lua" "$OUT/air5-2T-gas.lua"   # tw
 # and 1 atm, 2000 steps of 2e-7 s): time and temperature columns.
 grep -v '^[A-Za-z#]' "$KIN/methane-combustion-w-drm19/eilmer3-result-for-comparison.data" | awk '{print $1, $4}' \
     > "$HERE/drm19-fvr-eilmer3-T.txt"
-chmod u+w "$OUT"/*.lua
+# The reference's Python binding (CFFI, dlopen("libgas.so")), unmodified, for the drop-in test of the C ABI
+# (tests/test_gpu_ref_binding.py).
+cp "$REF/src/lib/gdtk/gas.py" "$HERE/ref_gdtk/gdtk/gas.py"
+chmod u+w "$OUT"/*.lua "$HERE/ref_gdtk/gdtk/gas.py"
 echo "fixtures written to $OUT"

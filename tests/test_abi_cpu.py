@@ -159,3 +159,26 @@ def test_arrhenius_logA_is_the_same_model(tmp_path):
     a = oracle.Oracle(gas, str(alias)).rate_constants(1500.0, conc)
     b = oracle.Oracle(gas, mech("h2o2forms-chem.lua")).rate_constants(1500.0, conc)
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+GAS_MODEL_INFO = r'''
+import json
+from gdtk.gas import GasModel
+gm = GasModel("j92-gas.lua")
+print(json.dumps(dict(type=gm.type_str, n=gm.n_species, modes=gm.n_modes, names=gm.species_names,
+                      M=list(gm.mol_masses))))
+'''
+
+
+@pytest.mark.parametrize("standin", [False, True])
+def test_reference_gas_py_opens_this_library(tmp_path, standin):
+    """The reference's unmodified gdtk/gas.py loads this library as its libgas.so and reads a gas model
+    (the calls that need no GPU), with the real cffi and with the stand-in the GPU machines use."""
+    if not standin:
+        pytest.importorskip("cffi")
+    from test_gpu_ref_binding import run_with_reference_binding
+    out = run_with_reference_binding(GAS_MODEL_INFO, tmp_path, standin=standin)
+    names, species = oracle.load_gas(mech("j92-gas.lua"))
+    assert out["names"] == names and out["n"] == 13 and out["modes"] == 0
+    assert np.array_equal(np.array(out["M"]), np.array([s["M"] for s in species]))
+    assert out["type"] in ("CompositeGas", "ThermallyPerfectGas")
