@@ -326,3 +326,46 @@ def generate_samples(rc, sg, n, seed=0, dt_range=(0.5e-6, 2.0e-6), block=65536, 
             log("samples %d / %d" % (min(nblk, g0 + blocks_per_launch) * block, nblk * block))
     torch.cuda.synchronize()
     return X, Y, valid, t_update
+
+
+def calibrate_error_gate(rc, sg, T0, p0, Y0, dt, max_dY=5.0e-5, max_rel_dT=5.0e-4, flags=UPDATE_THERMO | RETRY):
+    """Sets the error-model gate from a calibration batch so that its accepted cells meet the bounds.
+
+    The cells (device tensors T0, p0 (n,), Y0 (nsp, n), fresh step sizes) are updated by the plain
+    FP64 update and by the surrogate with the error gate off.  Each accepted cell's error against
+    the FP64 result (largest |dY|, and |dT| / T of the final temperature) is ranked by the error
+    network's estimate for that cell; the gate is set to the largest estimate below which every
+    calibration cell is within max_dY and max_rel_dT (split-conformal calibration of a maximum; the
+    bounds are set below the target error so that unseen cells keep a margin).  Returns a dict
+    with the threshold, the accepted fraction on the calibration cells and their largest errors."""
+    import torch
+    n = T0.shape[0]
+    dev = T0.device
+    rho, u = rc.thermo_from_pT(p0, T0, Y0)
+    st = torch.zeros(n, dtype=torch.int32, device=dev)
+    Tp, pp, Yp, dtc = T0.clone(), p0.clone(), Y0.clone(), torch.full((n,), -1.0, dtype=torch.float64, device=dev)
+    rc.update(rho, u, Tp, pp, Yp, dtc, dt, status=st, flags=flags)
+    X, _, valid = sg.make_samples(T0, p0, Y0, dt, Tp, Yp, st)
+    est = sg.predict_error(X).double()
+    sg.set_error_gate(0.0)
+    Ts, ps, Ys, dts = T0.clone(), p0.clone(), Y0.clone(), torch.full((n,), -1.0, dtype=torch.float64, device=dev)
+    gate = torch.empty(n, dtype=torch.int32, device=dev)
+    sst = torch.zeros(n, dtype=torch.int32, device=dev)
+    sg.update(rho, u, Ts, ps, Ys, dts, dt, status=sst, flags=flags, gate=gate)
+    acc = (gate == 0) & (st == 0) & (valid != 0)
+    eY = (Ys - Yp).abs().amax(dim=0)
+    eT = (Ts - Tp).abs() / Tp
+    idx = torch.nonzero(acc).flatten()
+    order = idx[torch.argsort(est[idx])]
+    bad = (eY[order] > max_dY) | (eT[order] > max_rel_dT)
+    k = int(torch.nonzero(bad).flatten()[0]) if bool(bad.any()) else order.shape[0]
+    if k == 0:
+        log10_tol = -30.0
+    else:   # between the last estimate kept and the first excluded
+        hi = float(est[order[k]]) if k < order.shape[0] else float(est[order[k - 1]]) + 1e-6
+        log10_tol = 0.5 * (float(est[order[k - 1]]) + hi)
+    sg.set_error_gate(10.0 ** log10_tol)
+    kept = order[:k]
+    return dict(cells=n, log10_tol=log10_tol, tol=10.0 ** log10_tol, accepted_fraction=k / n,
+                max_dY=float(eY[kept].max()) if k else 0.0, max_rel_dT=float(eT[kept].max()) if k else 0.0,
+                bounds=dict(max_dY=max_dY, max_rel_dT=max_rel_dT))
