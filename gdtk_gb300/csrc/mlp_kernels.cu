@@ -308,14 +308,20 @@ __global__ void error_features_kernel(int B, const __nv_bfloat16* xh, int nin, c
     }
 }
 
-// tgt[r][0] = log10(max_s |(out[r][s] - y[r][s]) y_scale[s]| + 1e-12) over the nsp mass-fraction
-// outputs (the raw-unit error of the standardised prediction out against the target y); other
-// columns of the w-wide row are zero.
+// tgt[r][0] = log10(e + 1e-12), e = max(max_s |(out[r][s] - y[r][s]) y_scale[s]|, T_weight |dT error| / T):
+// the raw-unit error of the standardised prediction out against the target y over the nsp mass
+// fractions, and the temperature increment's error (output nsp) relative to the sample's T =
+// exp(X[rows[r]][0]) weighted by T_weight (0.1 makes a relative T error of 1e-3 count as a mass-
+// fraction error of 1e-4).  Other columns of the w-wide row are zero.
 __global__ void error_targets_kernel(int B, const float* out, const float* y, int ld, const float* y_scale, int nsp,
-                                     float* tgt, int w) {
+                                     const float* X, const int* rows, int xld, float T_weight, float* tgt, int w) {
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < B; r += gridDim.x * blockDim.x) {
         float e = 0.f;
         for (int k = 0; k < nsp; ++k) e = fmaxf(e, fabsf((out[(size_t)r * ld + k] - y[(size_t)r * ld + k]) * y_scale[k]));
+        const size_t row = rows ? (size_t)rows[r] : (size_t)r;
+        const float T = expf(X[row * xld]);
+        const float eT = fabsf((out[(size_t)r * ld + nsp] - y[(size_t)r * ld + nsp]) * y_scale[nsp]) / T;
+        e = fmaxf(e, T_weight * eT);
         tgt[(size_t)r * w] = log10f(e + 1e-12f);
         for (int c = 1; c < w; ++c) tgt[(size_t)r * w + c] = 0.f;
     }
@@ -435,9 +441,11 @@ cudaError_t launch_error_features(int B, const __nv_bfloat16* xh, int nin, const
 }
 
 cudaError_t launch_error_targets(int B, const float* out, const float* y, int ld, const float* y_scale, int nsp,
-                                 float* tgt, int w, cudaStream_t s) {
+                                 const float* X, const int* rows, int xld, float T_weight, float* tgt, int w,
+                                 cudaStream_t s) {
     if (B <= 0) return cudaSuccess;
-    error_targets_kernel<<<grid_for((size_t)B), 256, 0, s>>>(B, out, y, ld, y_scale, nsp, tgt, w);
+    error_targets_kernel<<<grid_for((size_t)B), 256, 0, s>>>(B, out, y, ld, y_scale, nsp, X, rows, xld, T_weight, tgt,
+                                                             w);
     return cudaGetLastError();
 }
 

@@ -51,12 +51,14 @@ cudaError_t launch_gather_rows(int n, const int* idx, const float* X, int ldx, c
 cudaError_t launch_affine_columns(int n, int w, const float* shift, const float* scale, float* x, cudaStream_t s);
 
 // The surrogate's error network: input rows [xh (nin bf16), out (nout fp32 -> bf16)]; targets
-// log10 of the largest raw |dY| error of out against y over the nsp mass fractions; pinball
-// (quantile tau) loss gradient of column 0; column copy.
+// log10 of the larger of the largest raw |dY| error of out against y over the nsp mass fractions
+// and T_weight times the relative error of the temperature increment (T = exp(X[rows[r]][0]));
+// pinball (quantile tau) loss gradient of column 0; column copy.
 cudaError_t launch_error_features(int B, const __nv_bfloat16* xh, int nin, const float* out, int nout,
                                   __nv_bfloat16* feat, cudaStream_t s);
 cudaError_t launch_error_targets(int B, const float* out, const float* y, int ld, const float* y_scale, int nsp,
-                                 float* tgt, int w, cudaStream_t s);
+                                 const float* X, const int* rows, int xld, float T_weight, float* tgt, int w,
+                                 cudaStream_t s);
 cudaError_t launch_pinball_grad(int B, int w, const float* pred, const float* tgt, float tau, float* grad,
                                 __nv_bfloat16* gradh, float* loss_sum, cudaStream_t s);
 cudaError_t launch_copy_column(int n, const float* x, int ld, int col, float* out, cudaStream_t s);

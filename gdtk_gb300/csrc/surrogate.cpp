@@ -24,6 +24,10 @@
 namespace gdtk {
 namespace {
 
+// Weight of the relative temperature-increment error in the error network's target (a relative T error
+// of 1e-3 counts as a mass-fraction error of 1e-4, the two accuracy bars of the surrogate).
+constexpr float kErrorTWeight = 0.1f;
+
 static_assert(GDTK_GATE_COUNT == GATE_COUNT, "gate codes");
 
 void ck(cudaError_t e, const char* what) {
@@ -283,8 +287,9 @@ struct Surrogate {
     }
 
     // The error network's pinball loss at quantile tau and its gradient (err->grad): inputs are
-    // the increment network's standardised input and output, the target is log10 of the largest
-    // |dY| error of that output on the sample.
+    // the increment network's standardised input and output, the target is log10 of that output's
+    // error on the sample: the larger of its largest |dY| error and 0.1 times its relative error in
+    // the temperature increment (a relative T error of 1e-3 weighs as a mass-fraction error of 1e-4).
     void error_loss_and_grad(int B, const float* X, const float* Y, const int* rows, float tau, float* loss_sum,
                              cudaStream_t s, int sm) {
         gather(B, X, Y, rows, s);
@@ -294,7 +299,8 @@ struct Surrogate {
         e_xh.ensure((size_t)B * nin_e);
         e_tgt.ensure((size_t)B * err->nout_pad);
         ck(launch_error_features(B, t_xh.p, nin_pad, e_main.p, nout_pad, e_xh.p, s), "error features");
-        ck(launch_error_targets(B, e_main.p, t_y.p, nout_pad, d_yd.p, nsp, e_tgt.p, err->nout_pad, s), "error targets");
+        ck(launch_error_targets(B, e_main.p, t_y.p, nout_pad, d_yd.p, nsp, X, rows, nin_pad, kErrorTWeight, e_tgt.p,
+                                err->nout_pad, s), "error targets");
         err->ensure_train(B);
         err->forward(B, e_xh.p, true, err->t_out.p, s);
         ck(launch_pinball_grad(B, err->nout_pad, err->t_out.p, e_tgt.p, tau, err->t_dout.p, err->t_dout16.p, loss_sum,

@@ -185,8 +185,9 @@ class ChemSurrogate:
 
     # ---------------------------------------------------------------- error model
     def add_error_model(self, width=128, depth=2, seed=0):
-        """Attach the error network (include/gdtk_surrogate.h): an estimate of log10 of the largest
-        |dY| error of this network's prediction, from its standardised input and output."""
+        """Attach the error network (include/gdtk_surrogate.h): an estimate of log10 of this network's
+        prediction error (the larger of the largest |dY| error and 0.1 x the relative dT error), from
+        its standardised input and output."""
         check(lib().chem_surrogate_error_model_new(self.id, int(width), int(depth), ctypes.c_ulonglong(seed)),
               "chem_surrogate_error_model_new")
         d = (ctypes.c_int * 5)()
@@ -242,7 +243,7 @@ class ChemSurrogate:
         return hist
 
     def predict_error(self, X):
-        """The error network's estimate, log10 of the largest |dY| error, per row of raw X."""
+        """The error network's estimate, log10 of the prediction error, per row of raw X."""
         import torch
         out = torch.empty(X.shape[0], dtype=torch.float32, device=X.device)
         check(lib().chem_surrogate_predict_error(self.id, int(X.shape[0]), _ptr(X), _ptr(out), _stream()),

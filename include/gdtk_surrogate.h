@@ -24,8 +24,9 @@
  *                   dT within T_tol (relative);
  *   magnitude       no predicted |dY| exceeds max_dY (when max_dY > 0);
  *   predicted error when an error model is attached and its gate set: the error network's
- *                   estimate of log10 of the largest |dY| error of the prediction (trained as a
- *                   quantile) does not exceed log10(tol).
+ *                   estimate of log10 of the prediction's error (the larger of its largest |dY|
+ *                   error and 0.1 times its relative error in dT; trained as a quantile) does
+ *                   not exceed log10(tol).
  * Accepted cells take Y_new, that T and p = rho R T; their dt_chem is left as it was.  A cell
  * that fails any check is integrated by the plain FP64 update from its original state, exactly
  * as chem_reactor_update_cells would.  Cells at or below T_frozen and cells of invalid density
@@ -106,7 +107,9 @@ int chem_surrogate_update_cells(int sg, int ncell, const double* rho, const doub
                                 double* monitor);
 /* Error model: a second network (same BF16 kernels) attached to the surrogate.  Its input is the
  * surrogate's standardised input and standardised output (nin_pad + nout_pad values), its output
- * an estimate of log10 of the largest |dY| error of that output.  It is trained on samples with a
+ * an estimate of log10 of that output's error: the larger of its largest |dY| error and 0.1 times
+ * its relative error in the temperature increment (so that 1e-3 in T weighs as 1e-4 in Y).  It is
+ * trained on samples with a
  * pinball (quantile) loss, so with quantile 0.9 its estimate lies above the actual error for about
  * 90% of the samples it was trained on. */
 int chem_surrogate_error_model_new(int sg, int width, int depth, unsigned long long seed);
@@ -121,7 +124,7 @@ int chem_surrogate_error_train_step(int sg, int batch, const float* X, const flo
 /* The gradient of the error network's mean pinball loss (grad: its n_params floats), no update. */
 int chem_surrogate_error_gradients(int sg, int batch, const float* X, const float* Y, const int* rows, float quantile,
                                    float* grad, float* loss_sum, void* stream);
-/* The error network's estimate (log10 of the largest |dY| error) for raw features X[n][nin_pad]. */
+/* The error network's estimate (log10 of the error defined above) for raw features X[n][nin_pad]. */
 int chem_surrogate_predict_error(int sg, int n, const float* X, float* out, void* stream);
 /* Reject cells whose estimated error exceeds tol (mass-fraction units); tol <= 0 turns it off. */
 int chem_surrogate_set_error_gate(int sg, double tol);

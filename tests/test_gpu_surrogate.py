@@ -358,6 +358,9 @@ def test_error_model_gradient_matches_cpu_oracle(rc, samples):
     out = ((raw - nrm["y_shift"]) / nrm["y_scale"]).astype(np.float32).astype(np.float64)
     nsp = rc.nsp
     err = np.abs((out[:, :nsp] - Ys[:, :nsp]) * nrm["y_scale"][:nsp]).max(axis=1)
+    # with the temperature increment's error relative to T, weighted 0.1 (1e-3 in T counts as 1e-4 in Y)
+    errT = np.abs((out[:, nsp] - Ys[:, nsp]) * nrm["y_scale"][nsp]) / np.exp(xb[:, 0].astype(np.float64))
+    err = np.maximum(err, 0.1 * errT)
     tgt = np.zeros((1024, sg.err_nout_pad))
     tgt[:, 0] = np.log10(err + 1e-12)
     feat = np.concatenate([mlp.bf16(Xs), mlp.bf16(out)], axis=1)
@@ -397,7 +400,9 @@ def test_error_model_ranks_the_surrogate_errors(samples, with_error_model):
     hold = rows[-20000:]
     Xh, Yh = X[hold.long()].contiguous(), Y[hold.long()]
     pred = sg.predict(Xh)
-    actual = torch.log10((pred[:, :sg.nout - 1] - Yh[:, :sg.nout - 1]).abs().amax(dim=1) + 1e-12).cpu().numpy()
+    eT = (pred[:, sg.nout - 1] - Yh[:, sg.nout - 1]).abs() / torch.exp(Xh[:, 0])
+    actual = torch.log10(torch.maximum((pred[:, :sg.nout - 1] - Yh[:, :sg.nout - 1]).abs().amax(dim=1), 0.1 * eT)
+                         + 1e-12).cpu().numpy()
     est = sg.predict_error(Xh).cpu().numpy()
     rank = lambda v: np.argsort(np.argsort(v))
     assert np.corrcoef(rank(est), rank(actual))[0, 1] > 0.6
