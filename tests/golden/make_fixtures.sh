@@ -26,6 +26,7 @@ mkdir -p "$WORK/dgd/data" "$WORK/dgd/lib"
 (cd "$REF/src/gas/species-database" && awk '$1 !~ "#" {print $1}' < species-list.txt | xargs cat defaults.lua) \
     > "$WORK/dgd/data/species-database.lua"
 cp "$REF/src/gas/species-database/species-list.txt" "$WORK/dgd/data/"
+cp "$REF/src/gas/species-database/collision-integrals/"*.lua "$WORK/dgd/data/"   # two-temperature gas files
 cp "$REF/src/kinetics/reaction.lua" "$REF/src/kinetics/lex_elems.lua" "$REF/src/kinetics/mechanism.lua" "$WORK/dgd/lib/"
 # The species check of reaction.lua (checkEquationSpecies) indexes every parsed participant, but the
 # '(+ M)' marker of a pressure-dependent reaction parses to a plain string, so prep_chem stops with
@@ -52,6 +53,17 @@ prep gupta5 "$KIN/air-chemistry-1T/air-5sp-1T.inp"                     "$KIN/air
 # pressure-dependent (Troe) reactions: F_cent given (Stanford-2011), and a, T3, T1, T2 (DRM19 methane)
 prep stanford "$KIN/hydrogen-ignition-delay/Stanford-2011-species.inp"  "$KIN/hydrogen-ignition-delay/Stanford-2011.lua"
 prep drm19  "$KIN/methane-combustion-w-drm19/drm19-prep-gas.inp"       "$KIN/methane-combustion-w-drm19/drm19-prep-chem.inp"
+# Two-temperature air (Park 1993, 5 species): gas, reactions (Park 2-T rates) and energy exchange
+# (Landau-Teller with Millikan-White and Park's high-temperature correction; Marrone-Treanor coupling),
+# the inputs of examples/lmr/3D/cylinder-larc, through prep_gas, prep_chem and prep_kinetics.
+LARC=$REF/examples/lmr/3D/cylinder-larc
+(cd "$WORK" && "$LUA" "$REF/src/gas/prep_gas.lua" "$LARC/gm-air-5sp-2T.inp" park2t-gas.lua > park2t-prep.log 2>&1 \
+    && "$LUA" "$REF/src/kinetics/prep_chem.lua" park2t-gas.lua "$LARC/rm-park-5sp-2T.inp" park2t-chem.lua \
+        >> park2t-prep.log 2>&1 \
+    && "$LUA" "$REF/src/kinetics/prep_kinetics.lua" park2t-gas.lua park2t-chem.lua "$LARC/eem-park-5sp-2T.inp" \
+        park2t-eem.lua >> park2t-prep.log 2>&1) || { cat "$WORK/park2t-prep.log"; exit 1; }
+grep -v '^-- Auto-generated' "$WORK/park2t-gas.lua" > "$OUT/park2t-gas.lua"
+cp "$WORK/park2t-chem.lua" "$WORK/park2t-eem.lua" "$OUT/"
 # Arrhenius2, Lindemann-Hinshelwood and Yungster-Rabinowitz forms (no reference example uses them)
 prep h2o2forms "$KIN/hydrogen-ignition-delay/Jachimowski-1992-species.inp" "$HERE/inputs/h2o2-rate-forms.lua"
 
