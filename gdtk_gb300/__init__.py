@@ -72,6 +72,12 @@ SIGNATURES = {
     "chem_reactor_set_lane_stats": (ctypes.c_int, [ctypes.c_int, _v]),
     "chem_reactor_configure": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "chem_reactor_info": (ctypes.c_int, [ctypes.c_int, _i, _i, _i, _i]),
+    "chem_reactor2t_new": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p]),
+    "chem_reactor2t_info": (ctypes.c_int, [ctypes.c_int, _i, _i, _i]),
+    "chem_reactor2t_thermo_from_pT_cells": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _v, _v, _v, _v, _v, _v, _v,
+                                                           _v]),
+    "chem_reactor2t_update_cells": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _v, _v, _v, _v, _v, _v, _v, _v, _v,
+                                                   ctypes.c_double, _v, _v]),
     "chem_reactor_last_launch": (ctypes.c_int, [ctypes.c_int, _i, _i, _i, _i]),
     "gdtk_last_error": (ctypes.c_char_p, []),
     "gdtk_generate_fast_source": (ctypes.c_int, [_c, _c, _c, ctypes.c_int]),

@@ -18,6 +18,8 @@ NVCC = os.environ.get("NVCC", "nvcc")
 
 SOURCES = [
     ("chem_kernels.cu", ["--fmad=false"]),
+    ("twotemp_kernels.cu", ["--fmad=false"]),
+    ("twotemp.cpp", []),
     ("codegen.cpp", []),
     ("fp64_probe.cu", []),
     ("noalloc.cu", []),
@@ -29,7 +31,7 @@ SOURCES = [
     ("lua_table.cpp", []),
 ]
 HEADERS = ["chem_types.h", "chem_launch.h", "cea_thermo.h", "lua_table.h", "mechanism.h", "codegen.h", "fast_exp.h",
-           "chem_fast.cuh", "mix_thermo.cuh", "api_internal.h", "mlp_launch.h", "surrogate_launch.h"]
+           "chem_fast.cuh", "mix_thermo.cuh", "api_internal.h", "mlp_launch.h", "surrogate_launch.h", "twotemp.h"]
 # sources compiled at run time by NVRTC, embedded in the library as string literals
 EMBEDDED = [("kFastCuhSource", "chem_fast.cuh"), ("kFastExpSource", "fast_exp.h")]
 

@@ -168,3 +168,39 @@ def measure_fp64_peak():
     v = ctypes.c_double()
     check(lib().gdtk_measure_fp64_peak(ctypes.byref(v)), "gdtk_measure_fp64_peak")
     return v.value
+
+
+class ReactorCells2T:
+    """A two-temperature gas with its multi-temperature reactor (chem_reactor2t_* of include/gdtk_chem.h):
+    cells are SoA FP64 cuda tensors, mass fractions (nsp, n); launches go on torch's current stream."""
+
+    def __init__(self, gas_file, chem_file, eem_file):
+        self.id = check(lib().chem_reactor2t_new(gas_file.encode(), chem_file.encode(), eem_file.encode()),
+                        "chem_reactor2t_new")
+        nsp, nr, neem = (ctypes.c_int() for _ in range(3))
+        check(lib().chem_reactor2t_info(self.id, ctypes.byref(nsp), ctypes.byref(nr), ctypes.byref(neem)),
+              "chem_reactor2t_info")
+        self.nsp, self.nr, self.neem = nsp.value, nr.value, neem.value
+
+    def thermo_from_pT(self, p, T, T_ve, massf):
+        """(rho, u, u_ve) of cells given p, T, T_ve and mass fractions."""
+        import torch
+        n = p.shape[0]
+        for t in (p, T, T_ve):
+            _f64(t, (n,))
+        _f64(massf, (self.nsp, n))
+        rho, u, u_ve = (torch.empty_like(p) for _ in range(3))
+        check(lib().chem_reactor2t_thermo_from_pT_cells(self.id, n, _ptr(p), _ptr(T), _ptr(T_ve), _ptr(massf),
+                                                        _ptr(rho), _ptr(u), _ptr(u_ve), _stream()),
+              "chem_reactor2t_thermo_from_pT_cells")
+        return rho, u, u_ve
+
+    def update(self, rho, T, T_ve, p, massf, dt_chem, t_interval, status=None, u=None, u_ve=None, steps=None):
+        """One update of every cell over t_interval, in place (T, T_ve, p, massf, dt_chem; u, u_ve out)."""
+        n = rho.shape[0]
+        for t in (rho, T, T_ve, p, dt_chem):
+            _f64(t, (n,))
+        _f64(massf, (self.nsp, n))
+        check(lib().chem_reactor2t_update_cells(self.id, n, _ptr(rho), _ptr(T), _ptr(T_ve), _ptr(p), _ptr(massf),
+                                                _ptr(u), _ptr(u_ve), _ptr(dt_chem), _ptr(status), float(t_interval),
+                                                _ptr(steps), _stream()), "chem_reactor2t_update_cells")

@@ -48,9 +48,10 @@ enum { RX_COLLIDER = 0, RX_FRC, RX_BRC, RX_EFFSET, RX_NREAC, RX_NPROD, RX_NPART,
 // Lindemann-Hinshelwood 123-160, Troe 162-290, Yungster-Rabinowitz 292-355 (third-body concentration of
 // the reaction's efficiency list, 114-121), and Arrhenius2 / Arrhenius-logA 82-121,
 // k = exp(logA + B T - C/T), whose (logA, B, C) take the places of (A, n, C)
-enum { RATE_ARRHENIUS = 0, RATE_FROM_EQ = 1, RATE_LH = 2, RATE_TROE = 3, RATE_YR = 4, RATE_ARRHENIUS2 = 5 };
+enum { RATE_ARRHENIUS = 0, RATE_FROM_EQ = 1, RATE_LH = 2, RATE_TROE = 3, RATE_YR = 4, RATE_ARRHENIUS2 = 5,
+       RATE_PARK = 6 };   // Park 2-T (rate_constant.d:364-393): A, n, C with T_eff = T^s T_ve^(1-s), s in RD_S
 // reaction double-record fields beyond the six Arrhenius parameters
-enum { RD_K0A = 6, RD_K0N, RD_K0C, RD_FCENT, RD_TA, RD_T1, RD_T2, RD_T3, RD_TFLAGS };
+enum { RD_K0A = 6, RD_K0N, RD_K0C, RD_FCENT, RD_TA, RD_T1, RD_T2, RD_T3, RD_TFLAGS, RD_S };
 enum { TROE_FCENT = 1, TROE_T1 = 2, TROE_T2 = 4 };
 enum { METHOD_RKF = 0, METHOD_ALPHA_QSS = 1 };
 

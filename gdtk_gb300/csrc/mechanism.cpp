@@ -43,6 +43,14 @@ RateConstHost rate_const(const LuaValue& t) {
         r.C = t.get("C").number();
         if (t.has("rctIndex") && t.get("rctIndex").number() != -1)
             throw std::runtime_error("rate constants on a temperature other than T need a multi-temperature gas");
+    } else if (model == "Park") {   // rate_constant.d:364-393, rate-controlling T^s T_mode^(1-s)
+        r.model = RATE_PARK;
+        r.A = t.get("A").number();
+        r.n = t.get("n").number();
+        r.C = t.get("C").number();
+        r.s = t.has("s") ? t.get("s").number() : std::nan("");   // checked with the gas model below
+        if (t.has("mode") && t.get("mode").number() != 0)
+            throw std::runtime_error("Park rate constants on an energy mode other than 0 need more than two temperatures");
     } else if (model == "fromEqConst") {
         r.model = RATE_FROM_EQ;
     } else if (model == "Lindemann-Hinshelwood" || model == "Troe" || model == "Yungster-Rabinowitz") {
@@ -76,14 +84,18 @@ RateConstHost rate_const(const LuaValue& t) {
 }
 }  // namespace
 
-GasModelHost load_gas_model(const std::string& path) {
+GasModelHost load_gas_model(const std::string& path, bool allow_two_temperature) {
     LuaValue g = read_lua_file(path);
     GasModelHost gm;
     std::string model = g.has("model") ? g.get("model").string() : "";
     if (model == "CompositeGas") {
         std::string phys = g.get("physical_model").string();
-        if (phys != "thermally-perfect-gas")
-            throw std::runtime_error("physical model '" + phys + "' is not supported (thermally-perfect-gas only)");
+        if (phys == "two-temperature-gas" && allow_two_temperature) {
+            gm.two_temperature = true;
+        } else if (phys != "thermally-perfect-gas") {
+            throw std::runtime_error("physical model '" + phys + "' is not supported here (thermally-perfect-gas" +
+                                     std::string(allow_two_temperature ? " or two-temperature-gas)" : ")"));
+        }
         gm.type_str = "CompositeGas";
     } else if (model == "ThermallyPerfectGas") {
         gm.type_str = "ThermallyPerfectGas";
@@ -101,6 +113,15 @@ GasModelHost load_gas_model(const std::string& path) {
         const LuaValue& e = db.get(name);
         if (e.is_nil()) throw std::runtime_error("no database entry for species " + name);
         gm.M.push_back(e.get("M").number());
+        if (gm.two_temperature) {   // two_temperature_gas.d:45-80: the particle kind sets the heat capacity
+            const std::string kind = e.get("type").kind == LuaValue::STRING ? e.get("type").string() : "";
+            if (name == "e-" || kind == "electron") gm.particle.push_back(PARTICLE_ELECTRON);
+            else if (kind == "atom") gm.particle.push_back(PARTICLE_ATOM);
+            else if (kind == "molecule")
+                gm.particle.push_back(e.get("molecule_type").kind == LuaValue::STRING &&
+                                      e.get("molecule_type").string() == "linear" ? PARTICLE_LINEAR : PARTICLE_NONLINEAR);
+            else throw std::runtime_error("TwoTemperatureGas: unknown particle type for species " + name);
+        }
         std::map<std::string, int> comp;   // atomicConstituents = { H=2, O=1 } (prep-gas species record)
         const LuaValue& ac = e.get("atomicConstituents");
         if (ac.kind == LuaValue::TABLE)
@@ -176,6 +197,15 @@ MechanismHost load_mechanism(const std::string& path, const GasModelHost& gm, bo
         if (r.has("equation")) rh.equation = r.get("equation").string();
         rh.frc = rate_const(r.get("frc"));
         rh.brc = rate_const(r.get("brc"));
+        if (rh.frc.model == RATE_PARK || rh.brc.model == RATE_PARK) {
+            if (!gm.two_temperature)
+                throw std::runtime_error("rate-constant model 'Park' is not supported for a one-temperature gas: it "
+                                         "needs a two-temperature gas model (rate_constant.d:364-393)");
+            if (!std::isfinite(rh.frc.s) && rh.frc.model == RATE_PARK)
+                throw std::runtime_error("Park rate constant without its exponent s");
+            if (rh.brc.model == RATE_PARK)
+                throw std::runtime_error("Park backward rate constants are not supported (forward with k_b from K_c)");
+        }
         if (rh.frc.model == RATE_FROM_EQ && rh.brc.model == RATE_FROM_EQ)
             throw std::runtime_error("a reaction needs at least one Arrhenius rate constant");
         if (rh.brc.pressure_dependent() || (rh.frc.pressure_dependent() && rh.brc.model != RATE_FROM_EQ))
@@ -294,6 +324,7 @@ PackedMech pack(const GasModelHost& gm, const MechanismHost* mh) {
         rd[RD_K0A] = r.frc.A0; rd[RD_K0N] = r.frc.n0; rd[RD_K0C] = r.frc.C0;
         rd[RD_FCENT] = r.frc.Fcent; rd[RD_TA] = r.frc.a; rd[RD_T1] = r.frc.T1; rd[RD_T2] = r.frc.T2;
         rd[RD_T3] = r.frc.T3; rd[RD_TFLAGS] = r.frc.troe_flags;
+        rd[RD_S] = r.frc.s;
     }
     for (int s = 0; s < neff; ++s) {
         int* ei = I + HI + nsp + RXI * nr + (1 + nsp) * s;

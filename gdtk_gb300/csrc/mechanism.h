@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "chem_types.h"
+#include "chem_types.h"
 #include "lua_table.h"
 
 namespace gdtk {
@@ -24,8 +25,13 @@ struct GasModelHost {
     std::vector<CeaCurveHost> curves;
     std::vector<std::string> elements;                    // in order of first appearance
     std::vector<std::map<std::string, int>> composition;  // per species: element -> atoms
+    // two-temperature gas (gas/thermo/two_temperature_gas.d): particle kind per species
+    bool two_temperature = false;
+    std::vector<int> particle;   // PARTICLE_ATOM, PARTICLE_LINEAR, PARTICLE_NONLINEAR or PARTICLE_ELECTRON
     int n_species() const { return (int)names.size(); }
 };
+
+enum { PARTICLE_ATOM = 0, PARTICLE_LINEAR = 1, PARTICLE_NONLINEAR = 2, PARTICLE_ELECTRON = 3 };
 
 struct RateConstHost {
     int model = 0;   // RATE_ARRHENIUS, RATE_FROM_EQ, RATE_LH, RATE_TROE, RATE_YR or RATE_ARRHENIUS2
@@ -34,6 +40,7 @@ struct RateConstHost {
     double A0 = 0, n0 = 0, C0 = 0;         // k_0 of the pressure-dependent models
     double Fcent = 0, a = 0, T1 = 0, T2 = 0, T3 = 0;   // Troe (a, T1, T2 hold a, b, c for Yungster-Rabinowitz)
     int troe_flags = 0;                    // TROE_FCENT | TROE_T1 | TROE_T2: parameters given
+    double s = 0;                          // Park: exponent of T in the rate-controlling temperature
     bool pressure_dependent() const { return model == RATE_LH || model == RATE_TROE || model == RATE_YR; }
     bool simple() const { return model == RATE_ARRHENIUS || model == RATE_ARRHENIUS2; }   // no third body
 };
@@ -63,7 +70,8 @@ struct PackedMech {
     int nsp = 0, nr = 0, neff = 0, method = 0;
 };
 
-GasModelHost load_gas_model(const std::string& path);
+// A thermally perfect gas; with allow_two_temperature also a two-temperature gas (two_temperature = true).
+GasModelHost load_gas_model(const std::string& path, bool allow_two_temperature = false);
 // reads `reaction` (and `config` when with_config) of a prep-chem file; checks species order.
 MechanismHost load_mechanism(const std::string& path, const GasModelHost& gm, bool with_config);
 PackedMech pack(const GasModelHost& gm, const MechanismHost* mech);

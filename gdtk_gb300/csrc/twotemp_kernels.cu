@@ -1,0 +1,465 @@
+// twotemp_kernels.cu -- the multi-temperature thermochemical reactor for a two-temperature gas, one
+// thread per cell, in the reference's operation order (compiled with --fmad=false, library exp/pow/log).
+//
+// kinetics/multi_temperature_thermochemical_reactor.d:137-294 (opCall) and :334-431 (Cash-Karp RKF
+// on the concentrations and u_ve), with
+//   * rate constants once per subcycle at the clamped T (reaction_mechanism.d:49-63): Gibbs energies
+//     at p = P_atm and T_ve = T (:204-218, two_temperature_gas.d:469-482), forward Arrhenius or Park
+//     (rate_constant.d:72-75, 364-393: T_eff = T^s T_ve^(1-s)), backward k_f(T, T_ve = T) / K_c(T)
+//     (reaction.d:94-143, 26-52);
+//   * tick rates and q - L (reaction.d:290-311, 416-440; reaction_mechanism.d:74-96);
+//   * energy exchange (energy_exchange_system.d:93-104): Landau-Teller (energy_exchange_mechanism.d:
+//     83-101) with Millikan-White / Park high-temperature relaxation times (relaxation_time.d:27-175),
+//     evaluated once per subcycle on the subcycle's gas state, and Marrone-Treanor coupling with
+//     impartial dissociation (energy_exchange_mechanism.d:228-241, exchange_chemistry_coupling.d:
+//     27-121) on the current stage's tick rates;
+//   * T from u by direct inversion and T_ve by Newton iteration (two_temperature_gas.d:95-117, 656-700).
+// A cell that fails keeps its input state and gets the reference's failure as its status.
+#include <cuda_runtime.h>
+
+#include <cmath>
+
+#include "cea_thermo.h"
+#include "chem_types.h"
+#include "twotemp.h"
+
+namespace gdtk {
+namespace {
+
+constexpr double R_universal = 8.31451;       // gas/physical_constants.d:13
+constexpr double P_atm = 101.325e3;           // gas/physical_constants.d:16
+constexpr double Boltzmann = 1.380658e-23;    // gas/physical_constants.d:18
+constexpr double Avogadro = 6.02214e23;       // gas/physical_constants.d:19
+constexpr double PI_D = 3.141592653589793;
+constexpr double T_REF = 298.15;              // two_temperature_gas.d:26
+constexpr double SMALL_MOLE_FRACTION = 1.0e-15;   // gas_model.d:42
+constexpr double IGAMMA_SWITCH = 1.0e-7;      // exchange_chemistry_coupling.d:24
+constexpr double IGAMMA_OVERFLOW = 0.001;     // exchange_chemistry_coupling.d:25
+constexpr double H_MIN = 1.0e-15;             // multi_temperature_thermochemical_reactor.d:31
+constexpr double ALLOWABLE_MASSF_ERROR = 1.0e-3;
+constexpr int NV = GDTK_MAX_SPECIES + 1;
+constexpr int MAX_EEM = 64;
+
+struct Gas2T {
+    MechView m;
+    const Species2T* sp;
+    int electron;
+    __device__ double R(int i) const { return m.sp(i)[SP_R]; }
+    // two_temperature_gas.d:427-445, 538-545, 558-590
+    __device__ double e_ve(int i, double Tve, double logTve, int& err) const {
+        if (i == electron) return 1.5 * R(i) * Tve;
+        return cea_h(m, i, Tve, logTve, err) - sp[i].cp_tr * (Tve - T_REF) - sp[i].h_f;
+    }
+    __device__ double cv_ve(int i, double Tve, int& err) const {
+        if (i == electron) return 1.5 * R(i);
+        return cea_Cp(m, i, Tve, err) - sp[i].cp_tr;
+    }
+    __device__ double e_tr(int i, double T) const {
+        if (i == electron) return 0.0;
+        return sp[i].cp_tr * (T - T_REF) + sp[i].h_f - R(i) * T;
+    }
+    __device__ double e_ve_mix(const double* Y, double Tve, int& err) const {
+        const double lt = log(Tve);
+        double e = 0.0;
+        for (int i = 0; i < m.nsp; ++i) e += Y[i] * e_ve(i, Tve, lt, err);
+        return e;
+    }
+    __device__ double e_tr_mix(const double* Y, double T) const {
+        double e = 0.0;
+        for (int i = 0; i < m.nsp; ++i)
+            if (i != electron) e += Y[i] * e_tr(i, T);
+        return e;
+    }
+    __device__ double cv_ve_mix(const double* Y, double Tve, int& err) const {
+        double c = 0.0;
+        for (int i = 0; i < m.nsp; ++i) c += Y[i] * cv_ve(i, Tve, err);
+        return c;
+    }
+    __device__ double pressure(double rho, const double* Y, double T, double Tve) const {
+        double p = 0.0;
+        for (int i = 0; i < m.nsp; ++i) p += rho * Y[i] * R(i) * (i == electron ? Tve : T);
+        return p;
+    }
+    // updateFromRhoU: T directly, T_ve by Newton from the guess in Tve (40 iterations, |dT| < 1e-9 K,
+    // or the guess itself when its energy is within 1e-5 J/kg); false when the iteration fails.
+    __device__ bool from_rhou(double rho, double u, double u_ve, const double* Y, double& T, double& Tve,
+                              double& p) const {
+        double sumA = 0.0, sumB = 0.0;
+        for (int i = 0; i < m.nsp; ++i) {
+            if (i == electron) continue;
+            sumA += Y[i] * (sp[i].cp_tr * T_REF - sp[i].h_f);
+            sumB += Y[i] * (sp[i].cp_tr - R(i));
+        }
+        T = (u + sumA) / sumB;
+        int err = 0;
+        double Tg = Tve;
+        double f = e_ve_mix(Y, Tg, err) - u_ve;
+        if (fabs(f) >= 1e-5) {
+            int count = 0;
+            double dT = 0.0;
+            for (int it = 0; it < 40; ++it) {
+                const double Cv = cv_ve_mix(Y, Tg, err);
+                dT = -f / Cv;
+                Tg += dT;
+                if (fabs(dT) < 1.0e-9) break;
+                f = e_ve_mix(Y, Tg, err) - u_ve;
+                ++count;
+            }
+            if (count == 40 && fabs(dT) > 1e-3) return false;
+        }
+        if (err) return false;
+        Tve = Tg;
+        p = pressure(rho, Y, T, Tve);
+        return true;
+    }
+};
+
+__device__ __forceinline__ double pow_int(double x, int n) {   // small positive coefficients
+    double r = 1.0;
+    for (int k = 0; k < n; ++k) r *= x;
+    return r;
+}
+
+// Forward rate constant of reaction ir at (T, T_ve): Arrhenius at T, Park at T^s T_ve^(1-s).
+__device__ double forward_rc(const int* r, const double* d, double T, double Tve) {
+    if (r[RX_FRC] == RATE_PARK) {
+        const double Te = pow(T, d[RD_S]) * pow(Tve, 1.0 - d[RD_S]);
+        return d[0] * pow(Te, d[1]) * exp(-d[2] / Te);
+    }
+    return d[0] * pow(T, d[1]) * exp(-d[2] / T);
+}
+
+struct Reactor2T {
+    Gas2T g;
+    const Eem2T* eem;
+    int neem;
+    double tol;
+    int max_subcycles, max_attempts;
+
+    // reaction.d:94-143 (multi-temperature branch) at the clamped T; gs: Gibbs scratch [nsp]
+    __device__ void rate_constants(double Tq, double Tve, double* kf, double* kb, double* gs, int& err) const {
+        const MechView& m = g.m;
+        double T = Tq;
+        if (T < m.T_lower()) T = m.T_lower();
+        if (T > m.T_upper()) T = m.T_upper();
+        const double logT = log(T);
+        for (int i = 0; i < m.nsp; ++i) gs[i] = cea_h(m, i, T, logT, err) - T * cea_s(m, i, T, logT, err);
+        for (int ir = 0; ir < m.nr; ++ir) {
+            const int* r = m.rx(ir);
+            const double* d = m.rxd(ir);
+            double Kc = 1.0;
+            if (r[RX_FRC] == RATE_FROM_EQ || r[RX_BRC] == RATE_FROM_EQ) {
+                double dG = 0.0, nuSum = 0.0;
+                for (int k = 0; k < r[RX_NPART]; ++k) {
+                    const int isp = r[RX_PART + k], nu = r[RX_PART_NU + k];
+                    dG += nu * gs[isp] * m.sp(isp)[SP_M];
+                    nuSum += nu;
+                }
+                const double K_p = exp(-dG / (R_universal * T));
+                Kc = K_p * pow(P_atm / (R_universal * T), nuSum);
+            }
+            if (r[RX_FRC] != RATE_FROM_EQ) {
+                kf[ir] = forward_rc(r, d, T, Tve);
+                kb[ir] = (r[RX_BRC] == RATE_FROM_EQ) ? forward_rc(r, d, T, T) / Kc
+                                                     : d[3] * pow(T, d[4]) * exp(-d[5] / T);
+            } else {
+                kb[ir] = d[3] * pow(T, d[4]) * exp(-d[5] / T);
+                kf[ir] = kb[ir] * Kc;   // the backward rate constant at the state itself (reaction.d:131)
+            }
+        }
+    }
+
+    // Tick rates at conc into wf, wb, and q, L (reaction_mechanism.d:82-95).
+    __device__ void split_rates(const double* c, const double* kf, const double* kb, double* wf, double* wb,
+                                double* q, double* L) const {
+        const MechView& m = g.m;
+        for (int i = 0; i < m.nsp; ++i) { q[i] = 0.0; L[i] = 0.0; }
+        for (int ir = 0; ir < m.nr; ++ir) {
+            const int* r = m.rx(ir);
+            double mc = 1.0;
+            if (r[RX_COLLIDER]) {
+                const int* ei = m.eff_i(r[RX_EFFSET]);
+                const double* ev = m.eff_d(r[RX_EFFSET]);
+                mc = 0.0;
+                for (int k = 0; k < ei[0]; ++k) mc += ev[ei[1 + k]] * c[ei[1 + k]];
+            }
+            double f = kf[ir] * mc, b = kb[ir] * mc;
+            for (int k = 0; k < r[RX_NREAC]; ++k) f *= pow_int(c[r[RX_REAC_IDX + k]], r[RX_REAC_COEFF + k]);
+            for (int k = 0; k < r[RX_NPROD]; ++k) b *= pow_int(c[r[RX_PROD_IDX + k]], r[RX_PROD_COEFF + k]);
+            wf[ir] = f;
+            wb[ir] = b;
+            for (int k = 0; k < r[RX_NPART]; ++k) {
+                const int isp = r[RX_PART + k], nu = r[RX_PART_NU + k];
+                if (nu > 0) { q[isp] += nu * f; L[isp] += nu * b; }
+                else if (nu < 0) { q[isp] += -nu * b; L[isp] += -nu * f; }
+            }
+        }
+    }
+
+    __device__ double nu_of(int ir, int isp) const {
+        const int* r = g.m.rx(ir);
+        for (int k = 0; k < r[RX_NPART]; ++k)
+            if (r[RX_PART + k] == isp) return (double)r[RX_PART_NU + k];
+        return 0.0;
+    }
+
+    // Relaxation time of a Landau-Teller mechanism (relaxation_time.d:27-175); -1 for a rare collider.
+    __device__ double tau(const Eem2T& e, double T, double p, const double* molef, const double* numden) const {
+        if (molef[e.q] <= SMALL_MOLE_FRACTION) return -1.0;
+        const double pBath = molef[e.q] * p / P_atm;
+        const double t_mw = (1.0 / pBath) * exp(e.a * (pow(T, -1. / 3.) - e.b) - 18.42);
+        if (e.rt == RT_MILLIKAN_WHITE) return t_mw;
+        const double sigma = (e.rt == RT_PARK_HTC) ? e.sigma : e.sigma * (50e3 / T) * (50e3 / T);
+        const double cs = sqrt(8.0 * Boltzmann * T / PI_D / e.mu);
+        return t_mw + 1.0 / (sigma * cs * numden[e.q]);
+    }
+
+    // Impartial dissociation's energy removed per dissociation (exchange_chemistry_coupling.d:93-112).
+    __device__ static double gvanish(double T, double Tv, double D, double Th) {
+        const double iG = (T - Tv) / (T * Tv);
+        if (fabs(iG) < IGAMMA_SWITCH)
+            return 0.5 * (D - Th * R_universal) + iG * (Th * Th * R_universal * R_universal - D * D) / 12.0 / R_universal;
+        if (iG > IGAMMA_OVERFLOW)
+            return R_universal * Th / (exp(Th * iG) - 1.0) - D * exp(-D / R_universal * iG);
+        return R_universal * Th / (exp(Th * iG) - 1.0) - D / (exp(D / R_universal * iG) - 1.0);
+    }
+
+    // dy/dt at y (species rates and the energy exchange into u_ve); lt[k]: the Landau-Teller term of
+    // mechanism k on this subcycle's state (0 for others); gv[k]: its Marrone-Treanor G_vanish.
+    __device__ void rates(const double* y, const double* kf, const double* kb, const double* lt, const double* gv,
+                          double rho, double* wf, double* wb, double* q, double* L, double* out) const {
+        const int nsp = g.m.nsp;
+        split_rates(y, kf, kb, wf, wb, q, L);
+        for (int i = 0; i < nsp; ++i) out[i] = q[i] - L[i];
+        double rate = 0.0;
+        for (int k = 0; k < neem; ++k) {
+            const Eem2T& e = eem[k];
+            if (e.kind == EEM_LANDAU_TELLER) {
+                rate += lt[k];
+            } else {
+                const double nu = nu_of(e.reaction, e.p);
+                const double f = wf[e.reaction], b = wb[e.reaction];
+                const double prod = nu > 0 ? nu * f : (nu < 0 ? -nu * b : 0.0);
+                const double loss = nu > 0 ? nu * b : (nu < 0 ? -nu * f : 0.0);
+                const double ga = 0.5 * (e.D - e.Thetav * R_universal);
+                rate += (prod * ga - loss * gv[k]) / rho;
+            }
+        }
+        out[nsp] = rate;
+    }
+};
+
+__global__ void __launch_bounds__(128) two_temperature_update_kernel(const TwoTArgs a) {
+    Reactor2T R;
+    R.g.m.bind(a.mech_i, a.mech_d);
+    R.g.sp = a.species;
+    R.g.electron = a.electron;
+    R.eem = a.eem;
+    R.neem = a.neem;
+    R.tol = a.tol;
+    R.max_subcycles = a.max_subcycles;
+    R.max_attempts = a.max_attempts;
+    const MechView& m = R.g.m;
+    const int nsp = m.nsp, nr = m.nr, nv = nsp + 1;
+    unsigned long long my_steps = 0;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < a.ncell; c += gridDim.x * blockDim.x) {
+        double Y0[GDTK_MAX_SPECIES], Y[GDTK_MAX_SPECIES], y0[NV], yOut[NV], yT[NV], K[6][NV], yErr[NV];
+        double kf[GDTK_MAX_REACTIONS], kb[GDTK_MAX_REACTIONS], wf[GDTK_MAX_REACTIONS], wb[GDTK_MAX_REACTIONS];
+        double q[GDTK_MAX_SPECIES], L[GDTK_MAX_SPECIES], gs[GDTK_MAX_SPECIES], lt[MAX_EEM], gv[MAX_EEM];
+        double molef[GDTK_MAX_SPECIES], numden[GDTK_MAX_SPECIES];
+        const double rho = a.rho[c];
+        double T = a.T[c], Tve = a.Tve[c], p = a.p[c];
+        for (int i = 0; i < nsp; ++i) { Y0[i] = a.massf[(size_t)i * a.ncell + c]; Y[i] = Y0[i]; }
+        int fail = 0, err = 0;
+        if (isnan(rho) || rho <= 0.0) fail = CELL_BAD_INPUT;
+        double dt_suggest = a.dt_chem[c], dtSave = dt_suggest, u = 0.0, u_ve = 0.0;
+        const double tI = a.t_interval;
+        if (!fail) {
+            const double u_total = R.g.e_tr_mix(Y, T) + R.g.e_ve_mix(Y, Tve, err);
+            double t = 0.0, h;
+            for (int i = 0; i < nsp; ++i) {
+                const double v = Y[i] * rho / m.sp(i)[SP_M];
+                y0[i] = v < 1.0e-30 ? 0.0 : v;   // gas_model.d:237-256
+            }
+            y0[nsp] = R.g.e_ve_mix(Y, Tve, err);
+            R.rate_constants(T, Tve, kf, kb, gs, err);
+            if (dt_suggest > tI) {
+                h = tI;
+            } else if (dt_suggest <= 0.0) {   // reaction_mechanism.d:161-203
+                R.split_rates(y0, kf, kb, wf, wb, q, L);
+                double min_dt = 1.0e6;
+                for (int i = 0; i < nsp; ++i) {
+                    if (y0[i] > 0.0 && fabs(q[i] - L[i]) > 1.0e-30) {
+                        const double dt = (q[i] > 10000.0 * L[i]) ? y0[i] / (L[i] + 1.0e-50) : fabs(y0[i] / (q[i] - L[i]));
+                        min_dt = fmin(min_dt, dt);
+                    }
+                }
+                h = fmax(fmin(1.0e-3 * min_dt, 1.0e-10), 1.0e-15);
+            } else {
+                h = dt_suggest;
+            }
+            int cycle = 0;
+            for (; cycle < R.max_subcycles && !fail; ++cycle) {
+                // subcycle's rate constants, relaxation times and exchange terms on the gas state
+                R.rate_constants(T, Tve, kf, kb, gs, err);
+                double mol = 0.0;
+                for (int i = 0; i < nsp; ++i) mol += Y[i] / m.sp(i)[SP_M];
+                for (int i = 0; i < nsp; ++i) {
+                    molef[i] = (Y[i] / m.sp(i)[SP_M]) / mol;
+                    numden[i] = Avogadro * Y[i] * rho / m.sp(i)[SP_M];
+                }
+                const double logT = log(T), logTve = log(Tve);
+                for (int k = 0; k < R.neem; ++k) {
+                    const Eem2T& e = R.eem[k];
+                    lt[k] = 0.0;
+                    gv[k] = 0.0;
+                    if (e.kind == EEM_LANDAU_TELLER) {
+                        const double tk = R.tau(e, T, p, molef, numden);
+                        if (tk >= 0.0)
+                            lt[k] = Y[e.p] * (R.g.e_ve(e.p, T, logT, err) - R.g.e_ve(e.p, Tve, logTve, err)) / tk;
+                    } else {
+                        gv[k] = Reactor2T::gvanish(T, Tve, e.D, e.Thetav);
+                    }
+                }
+                dtSave = dt_suggest;
+                h = fmin(h, tI - t);
+                int attempt = 0;
+                for (; attempt < R.max_attempts; ++attempt) {
+                    // Cash-Karp (multi_temperature_thermochemical_reactor.d:334-431)
+                    const double a21 = 1. / 5., a31 = 3. / 40., a32 = 9. / 40., a41 = 3. / 10., a42 = -9. / 10.,
+                                 a43 = 6. / 5., a51 = -11. / 54., a52 = 5. / 2., a53 = -70. / 27., a54 = 35. / 27.,
+                                 a61 = 1631. / 55296., a62 = 175. / 512., a63 = 575. / 13824.,
+                                 a64 = 44275. / 110592., a65 = 253. / 4096.;
+                    const double b51 = 37. / 378., b53 = 250. / 621., b54 = 125. / 594., b56 = 512. / 1771.,
+                                 b41 = 2825. / 27648., b43 = 18575. / 48384., b44 = 13525. / 55296.,
+                                 b45 = 277. / 14336., b46 = 1.0 / 4.0;
+                    R.rates(y0, kf, kb, lt, gv, rho, wf, wb, q, L, K[0]);
+                    for (int i = 0; i < nv; ++i) yT[i] = y0[i] + h * a21 * K[0][i];
+                    R.rates(yT, kf, kb, lt, gv, rho, wf, wb, q, L, K[1]);
+                    for (int i = 0; i < nv; ++i) yT[i] = y0[i] + h * (a31 * K[0][i] + a32 * K[1][i]);
+                    R.rates(yT, kf, kb, lt, gv, rho, wf, wb, q, L, K[2]);
+                    for (int i = 0; i < nv; ++i) yT[i] = y0[i] + h * (a41 * K[0][i] + a42 * K[1][i] + a43 * K[2][i]);
+                    R.rates(yT, kf, kb, lt, gv, rho, wf, wb, q, L, K[3]);
+                    for (int i = 0; i < nv; ++i)
+                        yT[i] = y0[i] + h * (a51 * K[0][i] + a52 * K[1][i] + a53 * K[2][i] + a54 * K[3][i]);
+                    R.rates(yT, kf, kb, lt, gv, rho, wf, wb, q, L, K[4]);
+                    for (int i = 0; i < nv; ++i)
+                        yT[i] = y0[i] + h * (a61 * K[0][i] + a62 * K[1][i] + a63 * K[2][i] + a64 * K[3][i] +
+                                             a65 * K[4][i]);
+                    R.rates(yT, kf, kb, lt, gv, rho, wf, wb, q, L, K[5]);
+                    for (int i = 0; i < nv; ++i)
+                        yOut[i] = y0[i] + h * (b51 * K[0][i] + b53 * K[2][i] + b54 * K[3][i] + b56 * K[5][i]);
+                    for (int i = 0; i < nv; ++i)
+                        yErr[i] = yOut[i] - (y0[i] + h * (b41 * K[0][i] + b43 * K[2][i] + b44 * K[3][i] +
+                                                          b45 * K[4][i] + b46 * K[5][i]));
+                    double e2 = 0.0;
+                    for (int i = 0; i < nv; ++i) {
+                        const double sk = R.tol + R.tol * fmax(fabs(y0[i]), fabs(yOut[i]));
+                        e2 += (yErr[i] / sk) * (yErr[i] / sk);
+                    }
+                    const double en = sqrt(e2 / nv);
+                    bool ok;
+                    if (en <= 1.0) {
+                        double scale = (en == 0.0) ? 10.0 : 0.9 * pow(en, -0.2);
+                        if (en != 0.0) scale = fmin(fmax(scale, 0.2), 10.0);
+                        dt_suggest = scale * h;
+                        ok = true;
+                    } else {
+                        dt_suggest = fmax(0.9 * pow(en, -0.2), 0.2) * h;
+                        ok = false;
+                    }
+                    ++my_steps;
+                    bool passed = true;
+                    if (ok) {
+                        double tot = 0.0;
+                        for (int i = 0; i < nsp; ++i) {
+                            const double v = yOut[i] * m.sp(i)[SP_M] / rho;
+                            Y[i] = v < 1.0e-30 ? 0.0 : v;   // conc2massf (gas_model.d:258-271)
+                            tot += Y[i];
+                        }
+                        if (fabs(tot - 1.0) > ALLOWABLE_MASSF_ERROR) passed = false;
+                    }
+                    if (ok && passed) {
+                        t += h;
+                        for (int i = 0; i < nv; ++i) y0[i] = yOut[i];
+                        const double hMax = h * (1.0 + 10.0 / 100.0);
+                        if (dt_suggest > h) h = fmin(dt_suggest, hMax);
+                        break;
+                    }
+                    h /= 10.0;
+                    if (h < H_MIN) { fail = CELL_H_MIN; break; }
+                }
+                if (fail) break;
+                if (attempt == R.max_attempts) { fail = CELL_MAX_ATTEMPTS; break; }
+                u_ve = y0[nsp];
+                u = u_total - u_ve;
+                if (!R.g.from_rhou(rho, u, u_ve, Y, T, Tve, p)) { fail = CELL_NEWTON_FAIL; break; }
+                if (t >= tI) {
+                    if (cycle == 0) dtSave = dt_suggest;
+                    break;
+                }
+            }
+            if (!fail && cycle == R.max_subcycles) fail = CELL_MAX_SUBCYCLES;
+            if (!fail && err) fail = CELL_CEA_RANGE;
+        }
+        if (fail) {
+            if (a.status) a.status[c] = fail;
+            continue;
+        }
+        double tot = 0.0;
+        for (int i = 0; i < nsp; ++i) tot += Y[i];
+        for (int i = 0; i < nsp; ++i) a.massf[(size_t)i * a.ncell + c] = Y[i] / tot;
+        a.T[c] = T;
+        a.Tve[c] = Tve;
+        a.p[c] = p;
+        if (a.u) a.u[c] = u;
+        if (a.u_ve) a.u_ve[c] = u_ve;
+        a.dt_chem[c] = dtSave;
+        if (a.status) a.status[c] = CELL_OK;
+        (void)nr;
+    }
+    if (a.steps && my_steps) atomicAdd(a.steps, my_steps);
+}
+
+__global__ void two_temperature_thermo_pT_kernel(const Thermo2TArgs a) {
+    Gas2T g;
+    g.m.bind(a.mech_i, a.mech_d);
+    g.sp = a.species;
+    g.electron = a.electron;
+    const int nsp = g.m.nsp;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < a.ncell; c += gridDim.x * blockDim.x) {
+        double Y[GDTK_MAX_SPECIES];
+        for (int i = 0; i < nsp; ++i) Y[i] = a.massf[(size_t)i * a.ncell + c];
+        const double T = a.T[c], Tve = a.Tve[c];
+        double denom = 0.0;   // two_temperature_gas.d updateDensity
+        for (int i = 0; i < nsp; ++i) denom += Y[i] * g.R(i) * (i == g.electron ? Tve : T);
+        int err = 0;
+        a.rho[c] = a.p[c] / denom;
+        a.u[c] = g.e_tr_mix(Y, T);
+        a.u_ve[c] = g.e_ve_mix(Y, Tve, err);
+    }
+}
+
+int grid_for_cells(int n, int block, int sm_count) {
+    long long g = ((long long)n + block - 1) / block;
+    const long long cap = (long long)sm_count * 16;
+    if (g > cap) g = cap;
+    return g < 1 ? 1 : (int)g;
+}
+
+}  // namespace
+
+cudaError_t launch_two_temperature_update(const TwoTArgs& a, int sm_count, cudaStream_t s) {
+    if (a.ncell <= 0) return cudaSuccess;
+    if (a.neem > MAX_EEM) return cudaErrorInvalidValue;
+    two_temperature_update_kernel<<<grid_for_cells(a.ncell, 128, sm_count), 128, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_two_temperature_thermo_pT(const Thermo2TArgs& a, int sm_count, cudaStream_t s) {
+    if (a.ncell <= 0) return cudaSuccess;
+    two_temperature_thermo_pT_kernel<<<grid_for_cells(a.ncell, 128, sm_count), 128, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace gdtk

@@ -146,6 +146,26 @@ int chem_reactor_update_cells_host(int cr_i, int ncell, const double* rho, const
  * (reaction_mechanism.d:98-105): source[isp * ncell + cell].  Device pointers. */
 int chem_reactor_source_terms_cells(int cr_i, int ncell, const double* rho, const double* T, const double* massf,
                                     double* source, int* status, void* stream);
+/* ---- Two-temperature gas (gas/thermo/two_temperature_gas.d) and its multi-temperature thermochemical
+ * reactor (kinetics/multi_temperature_thermochemical_reactor.d), the path thermochemical_reactor_new
+ * (gas_cwrap.d:892-904, via init_thermochemical_reactor.d) takes for a gas with one energy mode.
+ * gas_file: prep-gas output with physical_model 'two-temperature-gas'; chem_file: prep-chem output
+ * (Arrhenius and Park rate constants, odeStep rkf); eem_file: prep-kinetics output (Landau-Teller
+ * exchange with Millikan-White / ParkHTC / ParkHTC2 relaxation times, Marrone-Treanor coupling with
+ * impartial dissociation).  Returns a handle or -1. */
+int chem_reactor2t_new(const char* gas_file, const char* chem_file, const char* eem_file);
+int chem_reactor2t_info(int h, int* nsp, int* nr, int* neem);
+/* rho, u (translation-rotation) and u_ve (vibration-electronic) from p, T, T_ve and the mass fractions
+ * (two_temperature_gas.d:84-92 updateFromPT).  Device pointers, massf[isp * ncell + cell]. */
+int chem_reactor2t_thermo_from_pT_cells(int h, int ncell, const double* p, const double* T, const double* T_ve,
+                                        const double* massf, double* rho, double* u, double* u_ve, void* stream);
+/* One reactor update of every cell over t_interval (opCall, multi_temperature_thermochemical_reactor.d:
+ * 137-294): in/out T, T_ve, p, massf, dt_chem (<= 0: estimate the first step); out u, u_ve (may be
+ * NULL), status (may be NULL; the reference's failures as in chem_reactor_update_cells, a failed cell
+ * keeping its input state); steps (may be NULL) += RKF step attempts.  Device pointers, stream-ordered. */
+int chem_reactor2t_update_cells(int h, int ncell, const double* rho, double* T, double* T_ve, double* p,
+                                double* massf, double* u, double* u_ve, double* dt_chem, int* status,
+                                double t_interval, unsigned long long* steps, void* stream);
 /* Gas-state thermo over many cells (therm_perf_gas_mix.d:57-73).  Device pointers. */
 int gas_model_update_thermo_from_pT_cells(int gm_i, int ncell, const double* p, const double* T,
                                           const double* massf, double* rho, double* u, int* status, void* stream);

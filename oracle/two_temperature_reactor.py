@@ -28,8 +28,8 @@ from .luatable import read_lua_file
 from .two_temperature import TwoTemperatureGas, R_UNIVERSAL
 
 P_ATM = 101325.0
-AVOGADRO = 6.02214076e23        # gas/physical_constants.d
-BOLTZMANN = 1.380649e-23        # gas/physical_constants.d
+AVOGADRO = 6.02214e23           # gas/physical_constants.d:19
+BOLTZMANN = 1.380658e-23        # gas/physical_constants.d:18
 SMALL_MOLE_FRACTION = 1.0e-15   # gas/gas_model.d:42
 IGAMMA_SWITCH = 1.0e-7          # exchange_chemistry_coupling.d:24
 IGAMMA_OVERFLOW = 0.001         # exchange_chemistry_coupling.d:25

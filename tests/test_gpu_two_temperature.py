@@ -1,0 +1,83 @@
+"""The two-temperature reactor on the GPU (chem_reactor2t_*), cell by cell against the oracle
+(oracle/two_temperature_reactor.py, restating kinetics/multi_temperature_thermochemical_reactor.d),
+on Park's 5-species 2-T air with Landau-Teller exchange and Marrone-Treanor coupling (the inputs of
+examples/lmr/3D/cylinder-larc through prep-gas, prep-chem and prep-kinetics).
+
+Bars as for the one-temperature reactor: |dY| <= 1e-8, T, T_ve and p within 1e-7 relative.
+"""
+import numpy as np
+import pytest
+
+from conftest import mech
+from test_gpu_parity import torch_cuda, to_dev
+
+pytestmark = pytest.mark.gpu
+
+FILES = (mech("park2t-gas.lua"), mech("park2t-chem.lua"), mech("park2t-eem.lua"))
+
+
+def _cells(n, seed):
+    """Non-equilibrium air: T ~ U[3000, 12000] K, T_ve ~ U[300 K, 1.2 T], p = 10^U[3, 4.7] Pa,
+    Y ~ Dirichlet(2, 1, 0.3, 0.3, 0.3) over (N2, O2, N, O, NO)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    T = rng.uniform(3000.0, 12000.0, n)
+    Tve = rng.uniform(300.0, 1.2 * T)
+    p = 10.0 ** rng.uniform(3.0, 4.7, n)
+    Y = rng.dirichlet([2.0, 1.0, 0.3, 0.3, 0.3], n)
+    return T, Tve, p, np.ascontiguousarray(Y.T)
+
+
+def test_two_temperature_thermo_from_pT():
+    from oracle.two_temperature import TwoTemperatureGas
+    from gdtk_gb300.cells import ReactorCells2T
+    torch = torch_cuda()
+    rc = ReactorCells2T(*FILES)
+    gas = TwoTemperatureGas(FILES[0])
+    T, Tve, p, Y = _cells(256, seed=3)
+    dT, dTve, dp, dY = to_dev(torch, T, Tve, p, Y)
+    rho, u, uve = rc.thermo_from_pT(dp, dT, dTve, dY)
+    torch.cuda.synchronize()
+    ref = np.array([gas.update_from_pT(p[k], T[k], Tve[k], Y[:, k]) for k in range(256)])
+    assert np.allclose(rho.cpu().numpy(), ref[:, 0], rtol=1e-13, atol=0)
+    assert np.allclose(u.cpu().numpy(), ref[:, 1], rtol=1e-12, atol=1e-6)
+    assert np.allclose(uve.cpu().numpy(), ref[:, 2], rtol=1e-12, atol=1e-6)
+
+
+def test_two_temperature_update_matches_the_oracle():
+    from oracle.two_temperature_reactor import TwoTemperatureReactor, ReactorFailure
+    from gdtk_gb300.cells import ReactorCells2T
+    torch = torch_cuda()
+    rc = ReactorCells2T(*FILES)
+    orc = TwoTemperatureReactor(*FILES)
+    n, dt = 96, 1.0e-6
+    T, Tve, p, Y = _cells(n, seed=7)
+    dT, dTve, dp, dY = to_dev(torch, T, Tve, p, Y)
+    rho, u0, uve0 = rc.thermo_from_pT(dp, dT, dTve, dY)
+    dtc = torch.full((n,), -1.0, dtype=torch.float64, device="cuda")
+    st = torch.full((n,), -9, dtype=torch.int32, device="cuda")
+    u, uve = torch.empty_like(rho), torch.empty_like(rho)
+    steps = torch.zeros(1, dtype=torch.int64, device="cuda")
+    rc.update(rho, dT, dTve, dp, dY, dtc, dt, status=st, u=u, u_ve=uve, steps=steps)
+    torch.cuda.synchronize()
+    g = dict(T=dT.cpu().numpy(), Tve=dTve.cpu().numpy(), p=dp.cpu().numpy(), Y=dY.cpu().numpy(),
+             st=st.cpu().numpy(), u=u.cpu().numpy(), uve=uve.cpu().numpy(), dt=dtc.cpu().numpy())
+    rho_h = rho.cpu().numpy()
+    total = 0
+    for k in range(n):
+        try:
+            o = orc.update(rho_h[k], T[k], Tve[k], p[k], Y[:, k], dt)
+        except ReactorFailure as f:
+            assert g["st"][k] == f.code
+            continue
+        total += o["steps"]
+        assert g["st"][k] == 0
+        assert np.abs(g["Y"][:, k] - o["massf"]).max() <= 1e-8
+        for key, ok in (("T", "T"), ("Tve", "Tve"), ("p", "p")):
+            assert abs(g[key][k] - o[ok]) <= 1e-7 * abs(o[ok]), (k, key, g[key][k], o[ok])
+        assert abs(g["uve"][k] - o["u_ve"]) <= 1e-7 * max(abs(o["u_ve"]), 1.0)
+        assert g["dt"][k] == pytest.approx(o["dt_suggest"], rel=1e-6)
+    assert (g["st"] == 0).mean() > 0.95
+    # total energy is carried over: u + u_ve after the update equals it before
+    ok = g["st"] == 0
+    assert np.allclose((g["u"] + g["uve"])[ok], (u0 + uve0).cpu().numpy()[ok], rtol=1e-12, atol=1e-3)
+    assert int(steps.item()) >= total

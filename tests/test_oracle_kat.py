@@ -268,3 +268,41 @@ def test_arrhenius2_and_falloff_forms_restated():
     pr = k0 * M / kinf
     fc = f["a"] * np.exp(-f["b"] / T) + (1.0 - f["a"]) * np.exp(-f["c"] / T)
     assert close(kinf * (pr / (1.0 + pr)) * fc / (1.0 + np.log(pr) ** 2), kf[10], 1e-13)
+
+
+def test_two_temperature_reactor_against_a_tight_integration():
+    """The two-temperature reactor restatement (oracle/two_temperature_reactor.py) on Park 2-T air
+    against a Radau integration (rtol 1e-9) of the same system with every rate at the instantaneous
+    state.  The reference algorithm freezes the rate constants and the exchange terms over each RKF
+    step (errTol 1e-3), so it agrees to that order only; total energy is conserved exactly."""
+    from scipy.integrate import solve_ivp
+    from oracle.two_temperature_reactor import TwoTemperatureReactor
+    r = TwoTemperatureReactor(mech("park2t-gas.lua"), mech("park2t-chem.lua"), mech("park2t-eem.lua"))
+    rng = np.random.default_rng(0)
+    for _ in range(4):
+        T, p = rng.uniform(4000.0, 12000.0), 10.0 ** rng.uniform(3.0, 4.5)
+        Tve = rng.uniform(500.0, 1.2 * T)
+        Y = rng.dirichlet([2.0, 1.0, 0.3, 0.3, 0.3])
+        rho, u, uve = r.gas.update_from_pT(p, T, Tve, Y)
+        o = r.update(rho, T, Tve, p, Y, 1.0e-6)
+        assert close(o["u"] + o["u_ve"], u + uve, 1e-12)
+        c0 = Y * rho / r.M
+        guess = {"Tve": Tve}
+
+        def rhs(t, y):
+            c = np.maximum(y[:r.nsp], 0.0)
+            Ym = c * r.M / rho
+            Tn, Tven, pn = r.gas.update_from_rhou(rho, u + uve - y[r.nsp], y[r.nsp], Ym, guess["Tve"])
+            guess["Tve"] = Tven
+            st = dict(rho=rho, T=Tn, Tve=Tven, p=pn, massf=Ym)
+            r._rate_constants(st)
+            return r._rates(st, r._relaxation_times(st), np.concatenate([c, [y[r.nsp]]]))
+
+        sol = solve_ivp(rhs, (0.0, 1.0e-6), np.concatenate([c0, [uve]]), method="Radau", rtol=1e-9,
+                        atol=np.concatenate([np.full(r.nsp, 1e-14 * c0.max()), [1e-6]]))
+        y = sol.y[:, -1]
+        Yt = np.maximum(y[:r.nsp], 0.0) * r.M / rho
+        Yt /= Yt.sum()
+        Tt, Tvt, _ = r.gas.update_from_rhou(rho, u + uve - y[r.nsp], y[r.nsp], Yt, guess["Tve"])
+        assert abs(o["T"] - Tt) / Tt < 1.5e-2 and abs(o["Tve"] - Tvt) / Tvt < 1.5e-2
+        assert np.abs(o["massf"] - Yt).max() < 5e-3
