@@ -40,7 +40,19 @@ SIGNATURES = {
     "gas_model_gas_state_update_thermo_from_pT": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
     "gas_model_gas_state_update_thermo_from_rhou": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
     "gas_model_gas_state_update_thermo_from_rhoT": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
+    "gas_model_gas_state_update_thermo_from_rhop": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
+    "gas_model_gas_state_update_sound_speed": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
+    "gas_model_gas_state_Cv": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _d]),
+    "gas_model_gas_state_Cp": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _d]),
+    "gas_model_gas_state_dpdrho_const_T": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _d]),
     "gas_model_gas_state_R": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _d]),
+    "gas_model_gas_state_gamma": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _d]),
+    "gas_model_gas_state_internal_energy": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _d]),
+    "gas_model_gas_state_enthalpy": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _d]),
+    "gas_model_gas_state_entropy": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _d]),
+    "gas_model_gas_state_enthalpy_isp": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _d]),
+    "gas_model_gas_state_entropy_isp": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _d]),
+    "gas_model_gas_state_gibbs_free_energy_isp": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _d]),
     "gas_model_gas_state_molecular_mass": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _d]),
     "gas_model_massf2molef": (ctypes.c_int, [ctypes.c_int, _d, _d]),
     "gas_model_molef2massf": (ctypes.c_int, [ctypes.c_int, _d, _d]),

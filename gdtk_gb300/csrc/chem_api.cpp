@@ -8,6 +8,8 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <array>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <stdexcept>
@@ -144,6 +146,11 @@ struct ReactorObj {
     DevBuf<float> order_key;            // longest-first scheduling scratch
     DevBuf<int> order;
     DevBuf<int> order_hist;
+    // one warp per cell: for mechanisms beyond the thread-per-cell kernels' limits, or on request
+    bool large = false;                 // more than GDTK_MAX_SPECIES species or GDTK_MAX_REACTIONS reactions
+    int warp_doubles = 0;
+    DevBuf<int> csr;                    // [nsp + 1] starts, then reaction indices, then net coefficients
+    int csr_n = 0;
     ~ReactorObj() { if (counter) cudaFree(counter); }
 };
 
@@ -191,6 +198,7 @@ void run_service(const DeviceMech& dm, int mode, int clip, int n, double* rho, d
     a.n_mech_d = (int)dm.host.D.size();
     a.nsp_hint = dm.host.nsp;
     a.nr_hint = dm.host.nr;
+    a.neff_hint = dm.host.neff;
     a.ncell = n;
     a.mode = mode;
     a.clip = clip;
@@ -255,6 +263,31 @@ void run_fast(ReactorObj& r, FastArgs& a, int flags, cudaStream_t s) {
     r.last.blocks_per_sm = r.fast->blocks_per_sm;
 }
 
+// Each species' (reaction, net coefficient) entries in reaction order, for the warp-per-cell kernel.
+void prepare_warp_path(ReactorObj& r, const PackedMech& pm) {
+    r.large = pm.nsp > GDTK_MAX_SPECIES || pm.nr > GDTK_MAX_REACTIONS;
+    r.warp_doubles = chem_warp_doubles(pm.nsp, pm.nr, pm.neff, pm.method);
+    std::vector<int> start(pm.nsp + 1, 0), rx, nu;
+    std::vector<std::vector<std::pair<int, int>>> per(pm.nsp);
+    for (int ir = 0; ir < (int)r.mh.reactions.size(); ++ir) {
+        std::map<int, int> net;
+        for (auto& x : r.mh.reactions[ir].reac) net[x.first] -= x.second;
+        for (auto& x : r.mh.reactions[ir].prod) net[x.first] += x.second;
+        for (auto& kv : net)
+            if (kv.second != 0) per[kv.first].push_back({ir, kv.second});
+    }
+    for (int i = 0; i < pm.nsp; ++i) {
+        start[i + 1] = start[i] + (int)per[i].size();
+        for (auto& e : per[i]) { rx.push_back(e.first); nu.push_back(e.second); }
+    }
+    std::vector<int> all(start);
+    all.insert(all.end(), rx.begin(), rx.end());
+    all.insert(all.end(), nu.begin(), nu.end());
+    r.csr_n = (int)rx.size();
+    r.csr.ensure(all.size());
+    check(cudaMemcpy(r.csr.p, all.data(), all.size() * sizeof(int), cudaMemcpyHostToDevice), "cudaMemcpy");
+}
+
 int launch_update(ReactorObj& r, int ncell, const double* rho, const double* u, double* T, double* p, double* massf,
                   double* dt_chem, int* status, double t_interval, double T_frozen, int flags, cudaStream_t s,
                   int* cell_counters, unsigned long long* totals) {
@@ -265,6 +298,26 @@ int launch_update(ReactorObj& r, int ncell, const double* rho, const double* u, 
     if (!(t_interval > 0.0)) throw std::runtime_error("t_interval must be > 0");
     if (!r.counter) check(cudaMalloc(&r.counter, sizeof(unsigned)), "cudaMalloc");
     check(cudaMemsetAsync(r.counter, 0, sizeof(unsigned), s), "cudaMemsetAsync");
+    if ((flags & GDTK_CHEM_WARP_PER_CELL) || r.large) {
+        if (!r.csr.p) throw std::runtime_error("warp-per-cell tables were not uploaded");
+        ChemUpdateArgs a{};
+        a.mech_i = r.dev.I;
+        a.mech_d = r.dev.D;
+        a.n_mech_i = (int)r.dev.host.I.size();
+        a.n_mech_d = (int)r.dev.host.D.size();
+        a.ncell = ncell;
+        a.rho = rho; a.u = u; a.T = T; a.p = p; a.massf = massf; a.dt_chem = dt_chem; a.status = status;
+        a.t_interval = t_interval;
+        a.T_frozen = T_frozen;
+        a.flags = flags & (CHEM_FLAG_UPDATE_THERMO | CHEM_FLAG_RETRY);
+        a.counter = r.counter;
+        a.cell_counters = cell_counters;
+        a.totals = totals;
+        const int nsp = r.dev.host.nsp;
+        check(launch_chem_update_warp(a, r.mh.method, r.csr.p, r.csr.p + nsp + 1, r.csr.p + nsp + 1 + r.csr_n,
+                                      r.warp_doubles, cuda().sm_count, s, &r.last), "warp-per-cell update launch");
+        return 0;
+    }
     if (flags & GDTK_CHEM_REFERENCE_ORDER) {
         ChemUpdateArgs a{};
         a.mech_i = r.dev.I;
@@ -524,6 +577,103 @@ int gas_model_gas_state_update_thermo_from_pT(int gm_i, int gs_i) { return therm
 int gas_model_gas_state_update_thermo_from_rhou(int gm_i, int gs_i) { return thermo_update(gm_i, gs_i, 1); }
 int gas_model_gas_state_update_thermo_from_rhoT(int gm_i, int gs_i) { return thermo_update(gm_i, gs_i, 4); }
 
+int gas_model_gas_state_update_thermo_from_rhop(int gm_i, int gs_i) {
+    return guarded([&] {
+        auto& s = state(gs_i);
+        bool valid = std::isfinite(s.rho) && std::isfinite(s.p);   // gas_cwrap.d:544-566
+        if (s.massf.size() > 1)
+            for (double y : s.massf) valid = valid && std::isfinite(y);
+        if (!valid) throw std::runtime_error("Gas state is not valid for rhop update.");
+        return thermo_update(gm_i, gs_i, 7);
+    });
+}
+
+}  // extern "C"
+
+namespace {
+// Mode-5 properties of a gas state at its (T, p, massf): Cv, Cp, R, u, h, s, a, dp/drho at constant T.
+std::array<double, 8> state_properties(int gm_i, int gs_i) {
+    auto& m = model(gm_i);
+    auto& s = state(gs_i);
+    if ((int)s.massf.size() != m.gm.n_species()) throw std::runtime_error("gas state does not belong to this model");
+    GasStateObj tmp = s;
+    std::array<double, 8> out{};
+    int st = state_service(m.device(), m.stage, 5, 0, tmp, out.data(), 8, nullptr, 0);
+    if (st) throw std::runtime_error(status_text(st));
+    return out;
+}
+
+int state_property(int gm_i, int gs_i, int k, double* result) {
+    return guarded([&] {
+        if (!result) throw std::runtime_error("null result pointer");
+        *result = state_properties(gm_i, gs_i)[k];
+        return 0;
+    });
+}
+
+// Mode-6 value `which` (0 h, 1 s, 2 g) of species isp.
+int species_property(int gm_i, int gs_i, int isp, int which, double* result) {
+    return guarded([&] {
+        auto& m = model(gm_i);
+        auto& s = state(gs_i);
+        const int nsp = m.gm.n_species();
+        if ((int)s.massf.size() != nsp) throw std::runtime_error("gas state does not belong to this model");
+        if (isp < 0 || isp >= nsp) throw std::runtime_error("species index out of range");
+        if (!result) throw std::runtime_error("null result pointer");
+        GasStateObj tmp = s;
+        std::vector<double> out(3 * (size_t)nsp);
+        int st = state_service(m.device(), m.stage, 6, 0, tmp, out.data(), 3 * nsp, nullptr, 0);
+        if (st) throw std::runtime_error(status_text(st));
+        *result = out[(size_t)which * nsp + isp];
+        return 0;
+    });
+}
+}  // namespace
+
+extern "C" {
+
+int gas_model_gas_state_update_sound_speed(int gm_i, int gs_i) {
+    return guarded([&] {
+        auto& s = state(gs_i);
+        bool valid = std::isfinite(s.rho) && std::isfinite(s.p) && std::isfinite(s.T);   // gas_cwrap.d:610-631
+        if (s.massf.size() > 1)
+            for (double y : s.massf) valid = valid && std::isfinite(y);
+        if (!valid) throw std::runtime_error("Gas state is not valid for sound_speed update.");
+        s.a = state_properties(gm_i, gs_i)[6];
+        return 0;
+    });
+}
+
+int gas_model_gas_state_Cv(int gm_i, int gs_i, double* result) { return state_property(gm_i, gs_i, 0, result); }
+int gas_model_gas_state_Cp(int gm_i, int gs_i, double* result) { return state_property(gm_i, gs_i, 1, result); }
+int gas_model_gas_state_dpdrho_const_T(int gm_i, int gs_i, double* result) {
+    return state_property(gm_i, gs_i, 7, result);
+}
+int gas_model_gas_state_internal_energy(int gm_i, int gs_i, double* result) {
+    return state_property(gm_i, gs_i, 3, result);
+}
+int gas_model_gas_state_enthalpy(int gm_i, int gs_i, double* result) { return state_property(gm_i, gs_i, 4, result); }
+int gas_model_gas_state_entropy(int gm_i, int gs_i, double* result) { return state_property(gm_i, gs_i, 5, result); }
+
+int gas_model_gas_state_gamma(int gm_i, int gs_i, double* result) {
+    return guarded([&] {   // gas_model.d:205: Cp / Cv
+        if (!result) throw std::runtime_error("null result pointer");
+        auto v = state_properties(gm_i, gs_i);
+        *result = v[1] / v[0];
+        return 0;
+    });
+}
+
+int gas_model_gas_state_enthalpy_isp(int gm_i, int gs_i, int isp, double* result) {
+    return species_property(gm_i, gs_i, isp, 0, result);
+}
+int gas_model_gas_state_entropy_isp(int gm_i, int gs_i, int isp, double* result) {
+    return species_property(gm_i, gs_i, isp, 1, result);
+}
+int gas_model_gas_state_gibbs_free_energy_isp(int gm_i, int gs_i, int isp, double* result) {
+    return species_property(gm_i, gs_i, isp, 2, result);
+}
+
 int gas_model_gas_state_R(int gm_i, int gs_i, double* result) {
     return guarded([&] {
         auto& m = model(gm_i).gm;
@@ -595,6 +745,7 @@ int thermochemical_reactor_new(int gm_i, const char* filename1, const char* file
         PackedMech pm = pack(m.gm, &r->mh);
         r->scratch = chem_scratch_doubles(pm.nsp, pm.nr, pm.neff, pm.method);
         r->dev.upload(pm);
+        prepare_warp_path(*r, pm);
         std::lock_guard<std::mutex> lk(g_mu);
         g_reactors.push_back(std::move(r));
         return (int)g_reactors.size() - 1;
@@ -698,7 +849,10 @@ int chem_reactor_update_blocks(int cr_i, int nblock, const gdtk_cell_block* bloc
         auto& r = reactor(cr_i);
         require_cuda();
         if (nblock < 0 || (nblock > 0 && !blocks)) throw std::runtime_error("bad block table");
-        if (flags & GDTK_CHEM_REFERENCE_ORDER) throw std::runtime_error("the block API uses the fast kernel only");
+        if (flags & (GDTK_CHEM_REFERENCE_ORDER | GDTK_CHEM_WARP_PER_CELL) || r.large)
+            throw std::runtime_error("the block API uses the fast kernel only (a mechanism within " +
+                                     std::to_string(GDTK_MAX_SPECIES) + " species and " +
+                                     std::to_string(GDTK_MAX_REACTIONS) + " reactions)");
         cudaStream_t s = (cudaStream_t)stream;
         if (!r.fast) r.fast.reset(build_fast_kernel(model(r.gm).gm, r.mh, r.req_block, r.req_min_blocks));
         if (!r.counter) check(cudaMalloc(&r.counter, sizeof(unsigned)), "cudaMalloc");

@@ -582,15 +582,28 @@ __global__ void __launch_bounds__(256) chem_update_kernel(ChemUpdateArgs a) {
 // mode 2: source terms (rho, T, massf -> source[nsp])              reaction_mechanism.d:98-105
 // mode 3: tick rates (rho, T, massf -> forward[nr], backward[nr])  gas_cwrap.d:968-990
 // mode 4: update_thermo_from_rhoT (rho, T, massf -> p, u)          therm_perf_gas_mix.d:69-73
+// mode 5: mixture properties at (T, p): out1[k] = Cv, Cp, R, u, h, s, a, dp/drho at constant T
+//         (therm_perf_gas_mix.d:230-300 and 335-343, gas_model.d:205)
+// mode 6: per-species h, s, g at (T, p): out1[0..nsp), [nsp..2nsp), [2nsp..3nsp)
+//         (therm_perf_gas_mix.d:322-326 and 345-349, gas_model.d:180-186)
+// mode 7: update_thermo_from_rhop (rho, p, massf -> T, u)          therm_perf_gas_mix.d:75-79, 393-403
+// A thread's vectors sit in shared memory after the staged mechanism, or (large mechanisms, gscratch
+// set) in global memory beside the other threads' with the mechanism read from global memory.
 __global__ void __launch_bounds__(128) gas_service_kernel(GasServiceArgs a) {
-    int* si;
-    double* sd;
-    double* scratch;
-    stage_mechanism(a.mech_i, a.mech_d, a.n_mech_i, a.n_mech_d, si, sd, scratch);
     MechView m;
-    m.bind(si, sd);
+    Vec S;
+    if (a.gscratch) {
+        m.bind(a.mech_i, a.mech_d);
+        S = Vec{a.gscratch + blockIdx.x * blockDim.x + threadIdx.x, (int)(gridDim.x * blockDim.x)};
+    } else {
+        int* si;
+        double* sd;
+        double* scratch;
+        stage_mechanism(a.mech_i, a.mech_d, a.n_mech_i, a.n_mech_d, si, sd, scratch);
+        m.bind(si, sd);
+        S = Vec{scratch + threadIdx.x, (int)blockDim.x};
+    }
     const int nsp = m.nsp, nr = m.nr;
-    Vec S{scratch + threadIdx.x, (int)blockDim.x};
     Vec mf = S, c = S + nsp, q = S + 2 * nsp, L = S + 3 * nsp, kf = S + 4 * nsp, kb = kf + nr, meff = kb + nr;
     for (int cell = blockIdx.x * blockDim.x + threadIdx.x; cell < a.ncell; cell += gridDim.x * blockDim.x) {
         for (int i = 0; i < nsp; ++i) mf[i] = a.massf[(size_t)i * a.ncell + cell];
@@ -610,6 +623,39 @@ __global__ void __launch_bounds__(128) gas_service_kernel(GasServiceArgs a) {
             for (int i = 0; i < nsp; ++i) uu += mf[i] * (cea_h(m, i, T, logT, err) - m.sp(i)[SP_R] * T);
             a.u[cell] = uu;
             a.p[cell] = rho * gas_constant(m, mf) * T;
+        } else if (a.mode == 5) {
+            const double T = a.T[cell], logT = log(T), lp = log(a.p[cell] / P_atm);
+            double cv = 0.0, cp = 0.0, R = 0.0, uu = 0.0, hh = 0.0, ss = 0.0;
+            for (int i = 0; i < nsp; ++i) {
+                const double Ri = m.sp(i)[SP_R], Cpi = cea_Cp(m, i, T, err), hi = cea_h(m, i, T, logT, err);
+                cv += mf[i] * (Cpi - Ri);
+                cp += mf[i] * Cpi;
+                R += mf[i] * Ri;
+                uu += mf[i] * (hi - Ri * T);
+                hh += mf[i] * hi;
+                ss += mf[i] * (cea_s(m, i, T, logT, err) - Ri * lp);
+            }
+            double* o = a.out1 + cell;
+            const size_t st = (size_t)a.ncell;
+            o[0] = cv; o[st] = cp; o[2 * st] = R; o[3 * st] = uu; o[4 * st] = hh; o[5 * st] = ss;
+            o[6 * st] = sqrt((cp / cv) * (R * T));   // frozen sound speed, therm_perf_gas_mix.d:230-240
+            o[7 * st] = R * T;
+        } else if (a.mode == 6) {
+            const double T = a.T[cell], logT = log(T), lp = log(a.p[cell] / P_atm);
+            for (int i = 0; i < nsp; ++i) {
+                const double hi = cea_h(m, i, T, logT, err);
+                const double si = cea_s(m, i, T, logT, err) - m.sp(i)[SP_R] * lp;
+                a.out1[(size_t)i * a.ncell + cell] = hi;
+                a.out1[(size_t)(nsp + i) * a.ncell + cell] = si;
+                a.out1[(size_t)(2 * nsp + i) * a.ncell + cell] = hi - T * si;
+            }
+        } else if (a.mode == 7) {
+            const double T = a.p[cell] / (gas_constant(m, mf) * a.rho[cell]);
+            const double logT = log(T);
+            double uu = 0.0;
+            for (int i = 0; i < nsp; ++i) uu += mf[i] * (cea_h(m, i, T, logT, err) - m.sp(i)[SP_R] * T);
+            a.T[cell] = T;
+            a.u[cell] = uu;
         } else if (a.mode == 1) {
             int it = 0;
             double T = T_from_u(m, mf, a.u[cell], a.T[cell], err, it);
@@ -680,6 +726,514 @@ __global__ void order_scatter(const float* key, int n, int* hist, int* order) {
         order[atomicAdd(&hist[order_bucket(key[i])], 1)] = i;
 }
 
+
+// ---------------------------------------------------------------- one warp per cell (large mechanisms)
+// The reference-order update (chem_update_kernel above) with one warp integrating one cell: species
+// and reactions are spread over the lanes, the cell's vectors live in the warp's share of shared
+// memory, and the mechanism tables are read from global memory (they need not fit in shared memory).
+// Every sum the reference takes over species in order (energies, gas constant, mass-fraction total,
+// RKF error norm) is taken by lane 0 in that order from per-species terms the lanes computed, and q, L
+// gather each species' terms in reaction order through a species -> reactions list, so each value is
+// the reference-order kernel's.  Minima and maxima (step estimate, sigma) are order-free.
+constexpr unsigned FULL_MASK = 0xffffffffu;
+
+struct WarpLayout {
+    int y0, yout, q, L, mf, g, tmp, kf, kb, wf, wb, meff, ext, total;
+    __device__ __host__ void make(int nsp, int nr, int neff, int method) {
+        y0 = 0; yout = nsp; q = 2 * nsp; L = 3 * nsp; mf = 4 * nsp; g = 5 * nsp; tmp = 6 * nsp;
+        kf = 8 * nsp; kb = kf + nr; wf = kb + nr; wb = wf + nr; meff = wb + nr;
+        ext = meff + (neff > 0 ? neff : 1);
+        total = ext + (method == METHOD_RKF ? 7 * nsp : 4 * nsp);
+    }
+};
+
+struct WarpCtx {
+    MechView m;
+    const int* csr_start;   // [nsp + 1]: species isp's entries csr_start[isp] .. csr_start[isp + 1]
+    const int* csr_rx;      // reaction index, ascending within a species
+    const int* csr_nu;      // net stoichiometric coefficient of the species in that reaction
+    int lane;
+};
+
+__device__ __forceinline__ double bcast(double v) { return __shfl_sync(FULL_MASK, v, 0); }
+
+// lane 0 sums v[0..n) in order; every lane gets the result
+__device__ __forceinline__ double serial_sum(const WarpCtx& w, const double* v, int n) {
+    double s = 0.0;
+    if (w.lane == 0)
+        for (int i = 0; i < n; ++i) s += v[i];
+    return bcast(s);
+}
+
+__device__ __forceinline__ int warp_or(int e) { return __any_sync(FULL_MASK, e != 0) ? (e ? e : 1) : 0; }
+
+__device__ void w_rate_constants(const WarpCtx& w, double Tq, double* kf, double* kb, double* g, const double* mf,
+                                 double rho, int& err) {
+    const MechView& m = w.m;
+    double T = Tq;
+    if (T < m.T_lower()) T = m.T_lower();
+    if (T > m.T_upper()) T = m.T_upper();
+    const double logT = log(T);
+    int e = 0;
+    for (int i = w.lane; i < m.nsp; i += 32) {
+        double h = cea_h(m, i, T, logT, e);
+        double sv = cea_s(m, i, T, logT, e);
+        g[i] = h - T * sv;
+    }
+    __syncwarp();
+    Vec mfv{const_cast<double*>(mf), 1};
+    for (int ir = w.lane; ir < m.nr; ir += 32) {
+        const int* r = m.rx(ir);
+        const double* d = m.rxd(ir);
+        double Kc = 1.0;
+        if (r[RX_FRC] == RATE_FROM_EQ || r[RX_BRC] == RATE_FROM_EQ) {
+            double dG = 0.0, nuSum = 0.0;
+            for (int k = 0; k < r[RX_NPART]; ++k) {
+                int isp = r[RX_PART + k];
+                int nu = r[RX_PART_NU + k];
+                dG += nu * g[isp] * m.sp(isp)[SP_M];
+                nuSum += nu;
+            }
+            double K_p = exp(-dG / (R_universal * T));
+            Kc = K_p * ipow(P_atm / (R_universal * T), (int)nuSum);
+        }
+        if (r[RX_FRC] != RATE_FROM_EQ) {
+            double f = (r[RX_FRC] == RATE_ARRHENIUS || r[RX_FRC] == RATE_ARRHENIUS2)
+                           ? simple_rate(r[RX_FRC], d, T) : pressure_dependent_kf(m, r, d, T, mfv, rho);
+            kf[ir] = f;
+            kb[ir] = (r[RX_BRC] == RATE_FROM_EQ) ? f / Kc : simple_rate(r[RX_BRC], d + 3, T);
+        } else {
+            double b = simple_rate(r[RX_BRC], d + 3, T);
+            kb[ir] = b;
+            kf[ir] = b * Kc;
+        }
+    }
+    __syncwarp();
+    const int any = warp_or(e);
+    if (any) err = CELL_CEA_RANGE;
+}
+
+// tick rates, then q and L per species in reaction order (reaction_mechanism.d:82-96)
+__device__ void w_split_rates(const WarpCtx& w, const double* c, double* q, double* L, const double* kf,
+                              const double* kb, double* wf, double* wb, double* meff) {
+    const MechView& m = w.m;
+    for (int s = w.lane; s < m.neff; s += 32) {
+        const int* ei = m.eff_i(s);
+        const double* ev = m.eff_d(s);
+        double term = 0.0;
+        for (int k = 0; k < ei[0]; ++k) {
+            int isp = ei[1 + k];
+            term += ev[isp] * c[isp];
+        }
+        meff[s] = term;
+    }
+    __syncwarp();
+    for (int ir = w.lane; ir < m.nr; ir += 32) {
+        const int* r = m.rx(ir);
+        double f = kf[ir], b = kb[ir];
+        if (r[RX_COLLIDER]) { double t = meff[r[RX_EFFSET]]; f = f * t; b = b * t; }
+        for (int k = 0; k < r[RX_NREAC]; ++k) f *= ipow(c[r[RX_REAC_IDX + k]], r[RX_REAC_COEFF + k]);
+        for (int k = 0; k < r[RX_NPROD]; ++k) b *= ipow(c[r[RX_PROD_IDX + k]], r[RX_PROD_COEFF + k]);
+        wf[ir] = f;
+        wb[ir] = b;
+    }
+    __syncwarp();
+    for (int isp = w.lane; isp < m.nsp; isp += 32) {
+        double qs = 0.0, Ls = 0.0;
+        for (int k = w.csr_start[isp]; k < w.csr_start[isp + 1]; ++k) {
+            const int ir = w.csr_rx[k], nu = w.csr_nu[k];
+            if (nu > 0) { qs += nu * wf[ir]; Ls += nu * wb[ir]; }
+            else if (nu < 0) { qs += -nu * wb[ir]; Ls += -nu * wf[ir]; }
+        }
+        q[isp] = qs;
+        L[isp] = Ls;
+    }
+    __syncwarp();
+}
+
+__device__ double w_estimate(const WarpCtx& w, const double* c, const double* q, const double* L) {
+    const double MUCH_LARGER_FACTOR = 10000.0, ZERO_TOL = 1.0e-30, EPS1 = 1.0e-3;
+    double min_dt = 1.0e6;
+    for (int i = w.lane; i < w.m.nsp; i += 32) {
+        double ci = c[i], qi = q[i], Li = L[i], dt;
+        if (ci > 0.0 && (fabs(qi - Li) > ZERO_TOL)) {
+            if (qi > MUCH_LARGER_FACTOR * Li) dt = ci / (Li + ZERO_EPS);
+            else dt = fabs(ci / (qi - Li));
+            min_dt = fmin(min_dt, dt);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) min_dt = fmin(min_dt, __shfl_xor_sync(FULL_MASK, min_dt, o));
+    double dt_chem = EPS1 * min_dt;
+    dt_chem = fmin(dt_chem, 1.0e-10);
+    dt_chem = fmax(dt_chem, 1.0e-15);
+    return dt_chem;
+}
+
+// therm_perf_gas_mix.d:406-468 with the per-species terms in tmp[0..nsp) and tmp[nsp..2nsp)
+__device__ double w_T_from_u(const WarpCtx& w, const double* mf, double u_tgt, double T_guess, int& err, int& iters,
+                             double* tmp) {
+    const MechView& m = w.m;
+    const int n = m.nsp;
+    const double TOL = 1e-10;
+    auto energy = [&](double T) {
+        const double logT = log(T);
+        int e = 0;
+        for (int i = w.lane; i < n; i += 32) tmp[i] = mf[i] * (cea_h(m, i, T, logT, e) - m.sp(i)[SP_R] * T);
+        __syncwarp();
+        if (warp_or(e)) err = CELL_CEA_RANGE;
+        const double s = serial_sum(w, tmp, n);
+        __syncwarp();
+        return s;
+    };
+    auto cv = [&](double T) {
+        int e = 0;
+        for (int i = w.lane; i < n; i += 32) tmp[n + i] = mf[i] * (cea_Cp(m, i, T, e) - m.sp(i)[SP_R]);
+        __syncwarp();
+        if (warp_or(e)) err = CELL_CEA_RANGE;
+        const double s = serial_sum(w, tmp + n, n);
+        __syncwarp();
+        return s;
+    };
+    double T = T_guess;
+    double f = energy(T) - u_tgt;
+    double dT = 0.0;
+    for (int iter = 0; iter < 10; ++iter) {
+        ++iters;
+        double c = cv(T);
+        dT = -f / c;
+        T += dT;
+        if (fabs(dT) / T < TOL) return T;
+        f = energy(T) - u_tgt;
+    }
+    if (fabs(dT) > 1e-3) err = CELL_NEWTON_FAIL;
+    return T;
+}
+
+__device__ double w_gas_constant(const WarpCtx& w, const double* mf, double* tmp) {
+    for (int i = w.lane; i < w.m.nsp; i += 32) tmp[i] = mf[i] * w.m.sp(i)[SP_R];
+    __syncwarp();
+    const double r = serial_sum(w, tmp, w.m.nsp);
+    __syncwarp();
+    return r;
+}
+
+// lane 0: Phobos' pairwise sum of v[0..n), broadcast
+__device__ double w_sum_pairwise(const WarpCtx& w, double* v, int n) {
+    double s = 0.0;
+    if (w.lane == 0) s = sum_pairwise(Vec{v, 1}, n);
+    return bcast(s);
+}
+
+__device__ bool w_rkf_step(const WarpCtx& w, const double* y0, double h, double* yOut, double& hSuggest, double* q,
+                           double* L, const double* kf, const double* kb, double* wf, double* wb, double* meff,
+                           double* ext, double* tmp, int& nrhs) {
+    const double a21 = 1. / 5., a31 = 3. / 40., a32 = 9. / 40., a41 = 3. / 10., a42 = -9. / 10., a43 = 6. / 5.,
+        a51 = -11. / 54., a52 = 5. / 2., a53 = -70. / 27., a54 = 35. / 27., a61 = 1631. / 55296., a62 = 175. / 512.,
+        a63 = 575. / 13824., a64 = 44275. / 110592., a65 = 253. / 4096.;
+    const double b51 = 37. / 378., b53 = 250. / 621., b54 = 125. / 594., b56 = 512. / 1771., b41 = 2825. / 27648.,
+        b43 = 18575. / 48384., b44 = 13525. / 55296., b45 = 277. / 14336., b46 = 1.0 / 4.0;
+    const int n = w.m.nsp;
+    double *k1 = ext, *k2 = ext + n, *k3 = ext + 2 * n, *k4 = ext + 3 * n, *k5 = ext + 4 * n, *k6 = ext + 5 * n,
+           *yT = ext + 6 * n;
+    auto rates = [&](const double* c, double* out) {
+        w_split_rates(w, c, q, L, kf, kb, wf, wb, meff);
+        ++nrhs;
+        for (int i = w.lane; i < n; i += 32) out[i] = q[i] - L[i];
+        __syncwarp();
+    };
+    rates(y0, k1);
+    for (int i = w.lane; i < n; i += 32) yT[i] = y0[i] + h * (a21 * k1[i]);
+    __syncwarp();
+    rates(yT, k2);
+    for (int i = w.lane; i < n; i += 32) yT[i] = y0[i] + h * (a31 * k1[i] + a32 * k2[i]);
+    __syncwarp();
+    rates(yT, k3);
+    for (int i = w.lane; i < n; i += 32) yT[i] = y0[i] + h * (a41 * k1[i] + a42 * k2[i] + a43 * k3[i]);
+    __syncwarp();
+    rates(yT, k4);
+    for (int i = w.lane; i < n; i += 32) yT[i] = y0[i] + h * (a51 * k1[i] + a52 * k2[i] + a53 * k3[i] + a54 * k4[i]);
+    __syncwarp();
+    rates(yT, k5);
+    for (int i = w.lane; i < n; i += 32)
+        yT[i] = y0[i] + h * (a61 * k1[i] + a62 * k2[i] + a63 * k3[i] + a64 * k4[i] + a65 * k5[i]);
+    __syncwarp();
+    rates(yT, k6);
+    const double atol = w.m.err_tol(), rtol = w.m.err_tol();
+    for (int i = w.lane; i < n; i += 32) {
+        double yo = y0[i] + h * (b51 * k1[i] + b53 * k3[i] + b54 * k4[i] + b56 * k6[i]);
+        yOut[i] = yo;
+        double ye = yo - (y0[i] + h * (b41 * k1[i] + b43 * k3[i] + b44 * k4[i] + b45 * k5[i] + b46 * k6[i]));
+        double sk = atol + rtol * fmax(fabs(y0[i]), fabs(yo));
+        tmp[i] = (ye / sk) * (ye / sk);
+    }
+    __syncwarp();
+    double err = serial_sum(w, tmp, n);
+    __syncwarp();
+    err = sqrt(err / n);
+    const double maxscale = 10.0, minscale = 0.2, safe = 0.9, alpha = 0.2;
+    double scale;
+    if (err <= 1.0) {
+        if (err == 0.0) scale = maxscale;
+        else {
+            scale = safe * pow(err, -alpha);
+            if (scale < minscale) scale = minscale;
+            if (scale > maxscale) scale = maxscale;
+        }
+        hSuggest = scale * h;
+        return true;
+    }
+    scale = fmax(safe * pow(err, -alpha), minscale);
+    hSuggest = scale * h;
+    return false;
+}
+
+__device__ bool w_aqss_step(const WarpCtx& w, const double* y0, double h, double* yOut, double& hSuggest, double* q,
+                            double* L, const double* kf, const double* kb, double* wf, double* wb, double* meff,
+                            double* ext, int& nrhs) {
+    const MechView& m = w.m;
+    const int n = m.nsp;
+    const double eps1 = m.eps1(), eps2 = m.eps2(), delta = m.delta();
+    double *q0 = ext, *p0 = ext + n, *yp0 = ext + 2 * n, *yp = ext + 3 * n;
+    w_split_rates(w, y0, q, L, kf, kb, wf, wb, meff);
+    ++nrhs;
+    for (int i = w.lane; i < n; i += 32) {
+        double y = y0[i];
+        double qi = q[i];
+        double pi = L[i] / (y + ZERO_EPS);
+        double a = alpha_of(pi, h);
+        double v = y + (h * (qi - pi * y)) / (1.0 + a * h * pi);
+        q0[i] = qi; p0[i] = pi; yp[i] = v; yp0[i] = v;
+    }
+    __syncwarp();
+    bool converged = false;
+    for (int corr = 0; corr < m.max_iters(); ++corr) {
+        w_split_rates(w, yp, q, L, kf, kb, wf, wb, meff);
+        ++nrhs;
+        bool conv = true;
+        for (int i = w.lane; i < n; i += 32) {
+            double y = y0[i];
+            double pp = L[i] / (yp[i] + ZERO_EPS);
+            double ab = alpha_of(pp, h);
+            double qt = ab * q[i] + (1 - ab) * q0[i];
+            double pb = 0.5 * (p0[i] + pp);
+            double yc = y + (h * (qt - pb * y)) / (1.0 + ab * h * pb);
+            yp[i] = yc;
+            if (!(yc < ZERO_EPS)) {
+                double test = fabs(yc - yp0[i]);
+                if (test >= (eps1 * (yc + delta))) conv = false;
+            }
+        }
+        __syncwarp();
+        converged = __all_sync(FULL_MASK, conv);
+        if (converged) break;
+    }
+    double sigma = 0.0;
+    for (int i = w.lane; i < n; i += 32) {
+        double yc = yp[i];
+        if (yc < ZERO_EPS) continue;
+        double test = fabs(yc - yp0[i]) / (eps2 * (yc + delta));
+        if (test > sigma) sigma = test;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const double other = __shfl_xor_sync(FULL_MASK, sigma, o);
+        if (other > sigma) sigma = other;
+    }
+    double h_new;
+    if (sigma <= 0.0) h_new = 10.0 * h;
+    else {
+        double x = sigma;
+        x = x - 0.5 * (x * x - sigma) / x;
+        x = x - 0.5 * (x * x - sigma) / x;
+        x = x - 0.5 * (x * x - sigma) / x;
+        h_new = h * ((1.0 / x) + 0.005);
+    }
+    hSuggest = h_new;
+    if (converged)
+        for (int i = w.lane; i < n; i += 32) yOut[i] = yp[i];
+    __syncwarp();
+    return converged;
+}
+
+template <int METHOD>
+__global__ void __launch_bounds__(128) chem_warp_kernel(ChemUpdateArgs a, const int* csr_start, const int* csr_rx,
+                                                        const int* csr_nu, int warp_doubles) {
+    extern __shared__ double smem_w[];
+    WarpCtx w;
+    w.m.bind(a.mech_i, a.mech_d);
+    w.csr_start = csr_start;
+    w.csr_rx = csr_rx;
+    w.csr_nu = csr_nu;
+    w.lane = threadIdx.x & 31;
+    const MechView& m = w.m;
+    WarpLayout lay;
+    lay.make(m.nsp, m.nr, m.neff, METHOD);
+    double* S = smem_w + (size_t)(threadIdx.x >> 5) * warp_doubles;
+    double *y0 = S + lay.y0, *yout = S + lay.yout, *q = S + lay.q, *L = S + lay.L, *mf = S + lay.mf, *g = S + lay.g,
+           *tmp = S + lay.tmp, *kf = S + lay.kf, *kb = S + lay.kb, *wf = S + lay.wf, *wb = S + lay.wb,
+           *meff = S + lay.meff, *ext = S + lay.ext;
+    const int nsp = m.nsp;
+    const unsigned ncell = (unsigned)a.ncell;
+    const double tI = a.t_interval;
+    while (true) {
+        unsigned c = 0;
+        if (w.lane == 0) c = atomicAdd(a.counter, 1u);
+        c = __shfl_sync(FULL_MASK, c, 0);
+        if (c >= ncell) break;
+        const double rho = a.rho[c], u = a.u[c], T0 = a.T[c], p0 = a.p[c];
+        double dtS0 = a.dt_chem[c];
+        if (T0 <= a.T_frozen) {
+            if (w.lane == 0 && a.status) a.status[c] = CELL_FROZEN;
+            continue;
+        }
+        if (isnan(rho) || rho <= 0.0) {
+            if (w.lane == 0 && a.status) a.status[c] = CELL_BAD_INPUT;
+            continue;
+        }
+        bool retried = false;
+        int n_steps = 0, n_rhs = 0, n_kc = 0, n_newton = 0, n_rej = 0, n_est = 0;
+        int final_status = 0;
+        double T = 0, p = 0, dtS = 0, dtSave = 0, h = 0, t = 0;
+        bool restart = true;
+        while (restart) {   // one pass, or two after a retryable failure (fluidfvcell.d:924-941)
+            restart = false;
+            int err = 0;
+            T = T0; p = p0; dtS = dtS0; t = 0.0;
+            for (int i = w.lane; i < nsp; i += 32) {
+                double v = a.massf[(size_t)i * ncell + c] * rho / m.sp(i)[SP_M];
+                y0[i] = (v < MIN_MOLES) ? 0.0 : v;
+                mf[i] = a.massf[(size_t)i * ncell + c];
+            }
+            __syncwarp();
+            w_rate_constants(w, T, kf, kb, g, mf, rho, err);
+            ++n_kc;
+            if (dtS > tI) h = tI;
+            else if (dtS <= 0.0) {
+                w_split_rates(w, y0, q, L, kf, kb, wf, wb, meff);
+                ++n_rhs;
+                ++n_est;
+                h = w_estimate(w, y0, q, L);
+            } else h = dtS;
+            int cycle = 0, fail = 0;
+            bool done = false, need_kc = false;
+            while (!fail && !done) {
+                dtSave = dtS;   // start of a subcycle
+                h = fmin(h, tI - t);
+                int attempt = 0;
+                while (true) {
+                    if (need_kc) {   // rate constants at the state of the last step, before the next one
+                        w_rate_constants(w, T, kf, kb, g, mf, rho, err);
+                        ++n_kc;
+                        need_kc = false;
+                    }
+                    ++n_steps;
+                    bool ok = (METHOD == METHOD_RKF)
+                                  ? w_rkf_step(w, y0, h, yout, dtS, q, L, kf, kb, wf, wb, meff, ext, tmp, n_rhs)
+                                  : w_aqss_step(w, y0, h, yout, dtS, q, L, kf, kb, wf, wb, meff, ext, n_rhs);
+                    if (ok) {   // mass-fraction test on conc2massf(concOut)
+                        for (int i = w.lane; i < nsp; i += 32) {
+                            double mfv = yout[i] * m.sp(i)[SP_M] / rho;
+                            tmp[i] = (mfv < MIN_MASS_FRACTION) ? 0.0 : mfv;
+                        }
+                        __syncwarp();
+                        double tot = w_sum_pairwise(w, tmp, nsp);
+                        __syncwarp();
+                        if (fabs(tot - 1.0) > ALLOWABLE_MASSF_ERROR) ok = false;
+                    }
+                    if (ok) {
+                        t += h;
+                        for (int i = w.lane; i < nsp; i += 32) y0[i] = yout[i];
+                        __syncwarp();
+                        double hMax = h * (1.0 + DT_INCREASE_PERCENT / 100.0);
+                        if (dtS > h) h = fmin(dtS, hMax);
+                        if (m.tight()) {   // chemistry_update.d:265-269
+                            for (int i = w.lane; i < nsp; i += 32) {
+                                double mfv = y0[i] * m.sp(i)[SP_M] / rho;
+                                mf[i] = (mfv < MIN_MASS_FRACTION) ? 0.0 : mfv;
+                            }
+                            __syncwarp();
+                            T = w_T_from_u(w, mf, u, T, err, n_newton, tmp);
+                            p = rho * w_gas_constant(w, mf, tmp) * T;
+                            need_kc = true;
+                        }
+                        if (err) fail = err;
+                        else if (t >= tI) {
+                            if (cycle == 0) dtSave = dtS;
+                            done = true;
+                        } else {
+                            ++cycle;
+                            if (cycle == m.max_subcycles()) fail = CELL_MAX_SUBCYCLES;
+                        }
+                        break;
+                    }
+                    ++n_rej;
+                    h /= DT_REDUCTION_FACTOR;
+                    if (err) { fail = err; break; }
+                    if (h < H_MIN) { fail = CELL_H_MIN; break; }
+                    if (++attempt == m.max_attempts()) { fail = CELL_MAX_ATTEMPTS; break; }
+                }
+            }
+            if (fail) {
+                const bool retryable = fail == CELL_H_MIN || fail == CELL_MAX_ATTEMPTS || fail == CELL_MAX_SUBCYCLES;
+                if ((a.flags & CHEM_FLAG_RETRY) && retryable && !retried) {
+                    retried = true;
+                    dtS0 = -1.0;
+                    restart = true;
+                    continue;
+                }
+                final_status = fail;
+            }
+        }
+        if (final_status) {
+            if (w.lane == 0 && a.status) a.status[c] = final_status;
+        } else {   // chemistry_update.d:290-325, then fluidfvcell.d:956
+            for (int i = w.lane; i < nsp; i += 32) {
+                double mfv = y0[i] * m.sp(i)[SP_M] / rho;
+                q[i] = (mfv < MIN_MASS_FRACTION) ? 0.0 : mfv;
+            }
+            __syncwarp();
+            double tot = w_sum_pairwise(w, q, nsp);
+            __syncwarp();
+            for (int i = w.lane; i < nsp; i += 32) q[i] = q[i] / tot;
+            __syncwarp();
+            int st = 0;
+            if (a.flags & CHEM_FLAG_UPDATE_THERMO) {
+                T = w_T_from_u(w, q, u, T, st, n_newton, tmp);
+                p = rho * w_gas_constant(w, q, tmp) * T;
+            }
+            if (st) {
+                if (w.lane == 0 && a.status) a.status[c] = st;
+            } else {
+                for (int i = w.lane; i < nsp; i += 32) a.massf[(size_t)i * ncell + c] = q[i];
+                if (w.lane == 0) {
+                    a.T[c] = T;
+                    a.p[c] = p;
+                    a.dt_chem[c] = dtSave;
+                    if (a.status) a.status[c] = CELL_OK;
+                }
+            }
+        }
+        if (w.lane == 0) {
+            if (a.cell_counters) {
+                a.cell_counters[0 * (size_t)ncell + c] = n_steps;
+                a.cell_counters[1 * (size_t)ncell + c] = n_rhs;
+                a.cell_counters[2 * (size_t)ncell + c] = n_kc;
+                a.cell_counters[3 * (size_t)ncell + c] = n_newton;
+                a.cell_counters[4 * (size_t)ncell + c] = n_rej;
+                a.cell_counters[5 * (size_t)ncell + c] = n_est;
+            }
+            if (a.totals) {
+                atomicAdd(a.totals + 0, (unsigned long long)n_steps);
+                atomicAdd(a.totals + 1, (unsigned long long)n_rhs);
+                atomicAdd(a.totals + 2, (unsigned long long)n_kc);
+                atomicAdd(a.totals + 3, (unsigned long long)n_newton);
+                atomicAdd(a.totals + 4, (unsigned long long)n_rej);
+                atomicAdd(a.totals + 5, (unsigned long long)n_est);
+            }
+        }
+        __syncwarp();
+    }
+}
+
 }  // namespace
 
 cudaError_t launch_bucket_order(const float* key, int n, int* order, int* hist, int sm_count, cudaStream_t stream) {
@@ -695,6 +1249,43 @@ cudaError_t launch_bucket_order(const float* key, int n, int* order, int* hist, 
 }
 
 // ---------------------------------------------------------------- host-side launchers
+
+int chem_warp_doubles(int nsp, int nr, int neff, int method) {
+    WarpLayout l;
+    l.make(nsp, nr, neff, method);
+    return l.total;
+}
+
+cudaError_t launch_chem_update_warp(const ChemUpdateArgs& a, int method, const int* csr_start, const int* csr_rx,
+                                    const int* csr_nu, int warp_doubles, int sm_count, cudaStream_t stream,
+                                    LaunchInfo* info) {
+    if (a.ncell <= 0) return cudaSuccess;
+    const size_t limit = 227 * 1024;
+    int block = 128;
+    while (block > 32 && (size_t)warp_doubles * 8 * (block / 32) > limit) block /= 2;
+    const size_t smem = (size_t)warp_doubles * 8 * (block / 32);
+    if (smem > limit) return cudaErrorInvalidConfiguration;
+    const void* fn = (method == METHOD_RKF) ? (const void*)chem_warp_kernel<METHOD_RKF>
+                                            : (const void*)chem_warp_kernel<METHOD_ALPHA_QSS>;
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, block, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    long long want = ((long long)a.ncell * 32 + block - 1) / block;
+    long long grid = (long long)sm_count * per_sm;
+    if (want < grid) grid = want;
+    if (grid < 1) grid = 1;
+    if (info) { info->grid = (int)grid; info->block = block; info->smem = (int)smem; info->blocks_per_sm = per_sm; }
+    if (method == METHOD_RKF)
+        chem_warp_kernel<METHOD_RKF><<<(unsigned)grid, block, smem, stream>>>(a, csr_start, csr_rx, csr_nu, warp_doubles);
+    else
+        chem_warp_kernel<METHOD_ALPHA_QSS><<<(unsigned)grid, block, smem, stream>>>(a, csr_start, csr_rx, csr_nu,
+                                                                                     warp_doubles);
+    return cudaGetLastError();
+}
+
 int chem_scratch_doubles(int nsp, int nr, int neff, int method) {
     Layout l;
     l.make(nsp, nr, neff, method);
@@ -734,20 +1325,36 @@ cudaError_t launch_chem_update(const ChemUpdateArgs& a, int method, int scratch_
 }
 
 cudaError_t launch_gas_service(const GasServiceArgs& a, int sm_count, cudaStream_t stream) {
+    if (a.ncell <= 0) return cudaSuccess;
     const size_t mech = mech_smem_bytes(a.n_mech_i, a.n_mech_d);
-    const int nsp = a.nsp_hint, nr = a.nr_hint;
-    const size_t per_thread = (size_t)(4 * nsp + 2 * nr + 16) * 8;
+    const int nsp = a.nsp_hint, nr = a.nr_hint, neff = a.neff_hint > 0 ? a.neff_hint : 1;
+    const size_t per_thread = (size_t)(4 * nsp + 2 * nr + neff) * 8;   // mf, c, q, L, kf, kb, meff
     int block = 128;
     while (block > 32 && mech + per_thread * block > 200 * 1024) block /= 2;
     size_t smem = mech + per_thread * block;
-    cudaError_t e = cudaFuncSetAttribute((const void*)gas_service_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
-    if (e != cudaSuccess) return e;
+    if (smem <= 200 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute((const void*)gas_service_kernel,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        long long grid = ((long long)a.ncell + block - 1) / block;
+        if (grid > (long long)sm_count * 8) grid = (long long)sm_count * 8;
+        if (grid < 1) grid = 1;
+        gas_service_kernel<<<(unsigned)grid, block, smem, stream>>>(a);
+        return cudaGetLastError();
+    }
+    // Global-memory vectors: at most two 64-thread blocks per SM, in a stream-ordered allocation.
+    block = 64;
     long long grid = ((long long)a.ncell + block - 1) / block;
-    if (grid > (long long)sm_count * 8) grid = (long long)sm_count * 8;
-    if (grid < 1) grid = 1;
-    gas_service_kernel<<<(unsigned)grid, block, smem, stream>>>(a);
-    return cudaGetLastError();
+    if (grid > (long long)sm_count * 2) grid = (long long)sm_count * 2;
+    GasServiceArgs g = a;
+    void* buf = nullptr;
+    cudaError_t e = cudaMallocAsync(&buf, per_thread * (size_t)(grid * block), stream);
+    if (e != cudaSuccess) return e;
+    g.gscratch = static_cast<double*>(buf);
+    gas_service_kernel<<<(unsigned)grid, block, 0, stream>>>(g);
+    e = cudaGetLastError();
+    cudaError_t f = cudaFreeAsync(buf, stream);
+    return e != cudaSuccess ? e : f;
 }
 
 }  // namespace gdtk

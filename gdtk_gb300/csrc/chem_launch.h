@@ -32,7 +32,7 @@ struct GasServiceArgs {
     const int* mech_i;
     const double* mech_d;
     int n_mech_i, n_mech_d;
-    int nsp_hint, nr_hint;
+    int nsp_hint, nr_hint, neff_hint;
     int ncell;
     int mode;
     int clip;
@@ -44,6 +44,7 @@ struct GasServiceArgs {
     double* out1;
     double* out2;
     int* status;
+    double* gscratch;   // set by the launcher when a thread's vectors do not fit in shared memory
 };
 
 struct LaunchInfo {
@@ -54,6 +55,13 @@ int chem_scratch_doubles(int nsp, int nr, int neff, int method);
 cudaError_t launch_chem_update(const ChemUpdateArgs& a, int method, int scratch_doubles, int sm_count,
                                cudaStream_t stream, LaunchInfo* info);
 cudaError_t launch_gas_service(const GasServiceArgs& a, int sm_count, cudaStream_t stream);
+// One warp per cell (mechanisms too large for the thread-per-cell kernels): the reference-order update with
+// species and reactions over the lanes.  csr_*: each species' (reaction, net coefficient) entries in
+// reaction order; warp_doubles = chem_warp_doubles(...), the shared-memory doubles of one warp.
+int chem_warp_doubles(int nsp, int nr, int neff, int method);
+cudaError_t launch_chem_update_warp(const ChemUpdateArgs& a, int method, const int* csr_start, const int* csr_rx,
+                                    const int* csr_nu, int warp_doubles, int sm_count, cudaStream_t stream,
+                                    LaunchInfo* info);
 // Cost buckets of the longest-first ordering: launch_bucket_order's hist scratch holds this many ints.
 constexpr int ORDER_BUCKETS = 256;
 

@@ -21,10 +21,12 @@
 //   [ED + nsp*s]       efficiency set s: values[nsp]
 #pragma once
 
-#define GDTK_MAX_SPECIES 32
+#define GDTK_MAX_SPECIES 32        // thread-per-cell kernels (fast, reference-order, surrogate, 2-T)
 #define GDTK_MAX_REACTIONS 128
+#define GDTK_MAX_SPECIES_ANY 128   // the reader; beyond GDTK_MAX_SPECIES / _REACTIONS the update runs one
+#define GDTK_MAX_REACTIONS_ANY 1024   // warp per cell
 #define GDTK_MAX_SEGMENTS 4
-#define GDTK_MAX_EFFSETS 16
+#define GDTK_MAX_EFFSETS 128
 #define GDTK_MAX_TERMS 4
 #define GDTK_MAX_PARTICIPANTS 8
 

@@ -366,6 +366,10 @@ int fast_vec_doubles(const GasModelHost& gm, const MechanismHost& mh) {
 }
 
 std::string generate_fast_source(const GasModelHost& gm, const MechanismHost& mh, int block, int min_blocks) {
+    if (gm.n_species() > GDTK_MAX_SPECIES || (int)mh.reactions.size() > GDTK_MAX_REACTIONS)
+        throw std::runtime_error("the mechanism-specialised kernel takes up to " + std::to_string(GDTK_MAX_SPECIES) +
+                                 " species and " + std::to_string(GDTK_MAX_REACTIONS) +
+                                 " reactions; larger mechanisms run one warp per cell");
     const int nsp = gm.n_species();
     const int nr = (int)mh.reactions.size();
     std::ostringstream o;
@@ -715,6 +719,7 @@ FastKernel* build_fast_kernel(const GasModelHost& gm, const MechanismHost& mh, i
     cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int nsp = gm.n_species(), nr = (int)mh.reactions.size();
+    if (nsp > GDTK_MAX_SPECIES || nr > GDTK_MAX_REACTIONS) generate_fast_source(gm, mh, 32, 1);   // throws the reason
     const int per_thread = 2 * nr + fast_vec_doubles(gm, mh);
     const int table = nsp * 120 + 64;
     // Block size: as many resident threads as shared memory allows, up to 256 per SM.  Each resident

@@ -106,8 +106,8 @@ GasModelHost load_gas_model(const std::string& path, bool allow_two_temperature)
         throw std::runtime_error("gas model '" + model + "' is not supported (thermally perfect gas only)");
     }
     gm.names = species_list(g.get("species"));
-    if (gm.names.empty() || (int)gm.names.size() > GDTK_MAX_SPECIES)
-        throw std::runtime_error("species count out of range (1.." + std::to_string(GDTK_MAX_SPECIES) + ")");
+    if (gm.names.empty() || (int)gm.names.size() > GDTK_MAX_SPECIES_ANY)
+        throw std::runtime_error("species count out of range (1.." + std::to_string(GDTK_MAX_SPECIES_ANY) + ")");
     const LuaValue& db = g.get("db");
     for (auto& name : gm.names) {
         const LuaValue& e = db.get(name);
@@ -234,8 +234,8 @@ MechanismHost load_mechanism(const std::string& path, const GasModelHost& gm, bo
         }
         mh.reactions.push_back(rh);
     }
-    if ((int)mh.reactions.size() > GDTK_MAX_REACTIONS)
-        throw std::runtime_error("too many reactions (max " + std::to_string(GDTK_MAX_REACTIONS) + ")");
+    if ((int)mh.reactions.size() > GDTK_MAX_REACTIONS_ANY)
+        throw std::runtime_error("too many reactions (max " + std::to_string(GDTK_MAX_REACTIONS_ANY) + ")");
     return mh;
 }
 

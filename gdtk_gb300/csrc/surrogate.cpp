@@ -370,6 +370,9 @@ int chem_surrogate_new(int cr_i, int width, int depth, unsigned long long seed) 
         if (width < 8 || width % 8 || width > 4096) throw std::runtime_error("surrogate width must be a multiple of 8 in 8..4096");
         if (depth < 1 || depth > 16) throw std::runtime_error("surrogate depth must be in 1..16");
         ReactorInternals ri = reactor_internals(cr_i);
+        if (ri.nsp > GDTK_MAX_SPECIES)
+            throw std::runtime_error("the surrogate takes mechanisms of up to " + std::to_string(GDTK_MAX_SPECIES) +
+                                     " species");
         auto S = std::make_unique<Surrogate>();
         S->cr = cr_i;
         S->nsp = ri.nsp;

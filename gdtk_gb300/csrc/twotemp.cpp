@@ -167,6 +167,9 @@ extern "C" int chem_reactor2t_new(const char* gas_file, const char* chem_file, c
                 throw std::runtime_error("the two-temperature reactor takes Arrhenius, Park and K_c rate constants");
         r->nsp = r->gm.n_species();
         r->nr = (int)r->mh.reactions.size();
+        if (r->nsp > GDTK_MAX_SPECIES || r->nr > GDTK_MAX_REACTIONS)
+            throw std::runtime_error("the two-temperature reactor takes up to " + std::to_string(GDTK_MAX_SPECIES) +
+                                     " species and " + std::to_string(GDTK_MAX_REACTIONS) + " reactions");
         std::vector<Eem2T> eem = load_energy_exchange(eem_file, r->gm, r->nr);
         r->neem = (int)eem.size();
         PackedMech pm = pack(r->gm, &r->mh);

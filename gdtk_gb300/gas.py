@@ -57,14 +57,61 @@ class GasModel:
         check(lib().gas_model_mol_masses(self.id, mm), "gas_model_mol_masses")
         return [mm[i] for i in range(self.n_species)]
 
+    # gas.py:210-243: each thermo update is followed by the sound-speed update.
     def update_thermo_from_pT(self, gstate):
         check(lib().gas_model_gas_state_update_thermo_from_pT(self.id, gstate.id), "update_thermo_from_pT")
+        self.update_sound_speed(gstate)
 
     def update_thermo_from_rhou(self, gstate):
         check(lib().gas_model_gas_state_update_thermo_from_rhou(self.id, gstate.id), "update_thermo_from_rhou")
+        self.update_sound_speed(gstate)
 
     def update_thermo_from_rhoT(self, gstate):
         check(lib().gas_model_gas_state_update_thermo_from_rhoT(self.id, gstate.id), "update_thermo_from_rhoT")
+        self.update_sound_speed(gstate)
+
+    def update_thermo_from_rhop(self, gstate):
+        check(lib().gas_model_gas_state_update_thermo_from_rhop(self.id, gstate.id), "update_thermo_from_rhop")
+        self.update_sound_speed(gstate)
+
+    def update_sound_speed(self, gstate):
+        check(lib().gas_model_gas_state_update_sound_speed(self.id, gstate.id), "update_sound_speed")
+
+    def _value(self, fn, gstate, *args):
+        v = ctypes.c_double()
+        check(getattr(lib(), fn)(self.id, gstate.id, *args, ctypes.byref(v)), fn)
+        return v.value
+
+    # gas.py:249-306
+    def Cv(self, gstate):
+        return self._value("gas_model_gas_state_Cv", gstate)
+
+    def Cp(self, gstate):
+        return self._value("gas_model_gas_state_Cp", gstate)
+
+    def dpdrho_const_T(self, gstate):
+        return self._value("gas_model_gas_state_dpdrho_const_T", gstate)
+
+    def gamma(self, gstate):
+        return self._value("gas_model_gas_state_gamma", gstate)
+
+    def internal_energy(self, gstate):
+        return self._value("gas_model_gas_state_internal_energy", gstate)
+
+    def enthalpy(self, gstate):
+        return self._value("gas_model_gas_state_enthalpy", gstate)
+
+    def entropy(self, gstate):
+        return self._value("gas_model_gas_state_entropy", gstate)
+
+    def enthalpy_isp(self, gstate, isp):
+        return self._value("gas_model_gas_state_enthalpy_isp", gstate, int(isp))
+
+    def entropy_isp(self, gstate, isp):
+        return self._value("gas_model_gas_state_entropy_isp", gstate, int(isp))
+
+    def gibbs_free_energy_isp(self, gstate, isp):
+        return self._value("gas_model_gas_state_gibbs_free_energy_isp", gstate, int(isp))
 
     def R(self, gstate):
         v = ctypes.c_double()
@@ -116,6 +163,14 @@ class GasState:
     p = property(lambda s: s._get("p"), lambda s, v: s._set("p", v))
     T = property(lambda s: s._get("T"), lambda s, v: s._set("T", v))
     u = property(lambda s: s._get("u"), lambda s, v: s._set("u", v))
+    a = property(lambda s: s._get("a"))
+    Cv = property(lambda s: s.gmodel.Cv(s))
+    Cp = property(lambda s: s.gmodel.Cp(s))
+    gamma = property(lambda s: s.gmodel.gamma(s))
+    R = property(lambda s: s.gmodel.R(s))
+    internal_energy = property(lambda s: s.gmodel.internal_energy(s))
+    enthalpy = property(lambda s: s.gmodel.enthalpy(s))
+    entropy = property(lambda s: s.gmodel.entropy(s))
 
     @property
     def massf(self):
@@ -164,6 +219,12 @@ class GasState:
 
     def update_thermo_from_rhoT(self):
         self.gmodel.update_thermo_from_rhoT(self)
+
+    def update_thermo_from_rhop(self):
+        self.gmodel.update_thermo_from_rhop(self)
+
+    def update_sound_speed(self):
+        self.gmodel.update_sound_speed(self)
 
 
 class PyGasState:
@@ -243,6 +304,14 @@ class PyGasState:
         if self.n_species > 1:
             self.copy_mass_fractions_into_dgs()
         self.gmodel.update_thermo_from_rhoT(self.dgs)
+        self.update_python_data()
+
+    def update_thermo_from_rhop(self):
+        self.dgs.rho = self.rho
+        self.dgs.p = self.p
+        if self.n_species > 1:
+            self.copy_mass_fractions_into_dgs()
+        self.gmodel.update_thermo_from_rhop(self.dgs)
         self.update_python_data()
 
 

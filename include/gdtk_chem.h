@@ -45,6 +45,11 @@ enum gdtk_cell_status {
 #define GDTK_CHEM_REFERENCE_ORDER 4 /* use the kernel that keeps the reference's operation order
                                        (default: the mechanism-specialised kernel, which rearranges
                                        the arithmetic to spend fewer FP64 operations) */
+#define GDTK_CHEM_WARP_PER_CELL 16  /* use the warp-per-cell kernel: the reference's operation order
+                                       with species and reactions spread over a warp's lanes.  It is
+                                       taken without the flag for mechanisms of more than 32 species or
+                                       128 reactions, which the thread-per-cell kernels do not take
+                                       (the reader accepts up to 128 species and 1024 reactions) */
 
 /* ---- 1. libgas-compatible subset (gas_cwrap.d) ---------------------------------------- */
 int cwrap_gas_init(void);                                                   /* gas_cwrap.d:40-55 */
@@ -64,7 +69,19 @@ int gas_state_copy_values(int gs_to_i, int gs_from_i);                      /* g
 int gas_model_gas_state_update_thermo_from_pT(int gm_i, int gs_i);          /* gas_cwrap.d:469-492 */
 int gas_model_gas_state_update_thermo_from_rhou(int gm_i, int gs_i);        /* gas_cwrap.d:494-517 */
 int gas_model_gas_state_update_thermo_from_rhoT(int gm_i, int gs_i);        /* gas_cwrap.d:519-542 */
+int gas_model_gas_state_update_thermo_from_rhop(int gm_i, int gs_i);        /* gas_cwrap.d:544-566 */
+int gas_model_gas_state_update_sound_speed(int gm_i, int gs_i);             /* gas_cwrap.d:610-631 */
+int gas_model_gas_state_Cv(int gm_i, int gs_i, double* result);             /* gas_cwrap.d:656-665 */
+int gas_model_gas_state_Cp(int gm_i, int gs_i, double* result);             /* gas_cwrap.d:667-676 */
+int gas_model_gas_state_dpdrho_const_T(int gm_i, int gs_i, double* result); /* gas_cwrap.d:678-687 */
 int gas_model_gas_state_R(int gm_i, int gs_i, double* result);              /* gas_cwrap.d:689-698 */
+int gas_model_gas_state_gamma(int gm_i, int gs_i, double* result);          /* gas_cwrap.d:700-709 */
+int gas_model_gas_state_internal_energy(int gm_i, int gs_i, double* result);/* gas_cwrap.d:722-731 */
+int gas_model_gas_state_enthalpy(int gm_i, int gs_i, double* result);       /* gas_cwrap.d:733-742 */
+int gas_model_gas_state_entropy(int gm_i, int gs_i, double* result);        /* gas_cwrap.d:744-753 */
+int gas_model_gas_state_enthalpy_isp(int gm_i, int gs_i, int isp, double* result);          /* :790-800 */
+int gas_model_gas_state_entropy_isp(int gm_i, int gs_i, int isp, double* result);           /* :802-812 */
+int gas_model_gas_state_gibbs_free_energy_isp(int gm_i, int gs_i, int isp, double* result); /* :814-824 */
 int gas_model_gas_state_molecular_mass(int gm_i, int gs_i, double* result); /* gas_cwrap.d:755-764 */
 int gas_model_massf2molef(int gm_i, double* massf, double* molef);          /* gas_cwrap.d:826-841 */
 int gas_model_molef2massf(int gm_i, double* molef, double* massf);          /* gas_cwrap.d:843-858 */

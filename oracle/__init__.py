@@ -120,6 +120,8 @@ class Oracle:
         self.nsp = len(self.names)
         self.M = np.array([s['M'] for s in self.species])
         self.h = L.oracle_model_new(self.nsp)
+        if not self.h:
+            raise ValueError("the oracle takes 1..128 species")
         for isp, s in enumerate(self.species):
             rc = L.oracle_set_species(self.h, isp, s['M'], s['nseg'], _dp(s['breaks']), _dp(s['blends']),
                                       _dp(np.ascontiguousarray(s['coeffs'].ravel())))
@@ -149,6 +151,8 @@ class Oracle:
                 ir = L.oracle_add_reaction(self.h, int(r['collider']), fm, fA, fn, fC, bm, bA, bn, bC,
                                            len(ri), _ip(ri), _ip(rcf), len(pi), _ip(pi), _ip(pcf), len(ei), _ip(ei),
                                            _dp(ev))
+                if ir < 0:
+                    raise ValueError("the oracle takes up to 1024 reactions")
                 if fm in pd_models.values():   # rate_constant.d:135-145, 181-229, 310-333
                     d = r['frc']
                     k0 = d['k0']

@@ -44,6 +44,10 @@
 #include <omp.h>
 #endif
 
+
+// Work-array sizes: the reader takes mechanisms up to these.
+constexpr int ORACLE_MAX_SPECIES = 128;
+constexpr int ORACLE_MAX_REACTIONS = 1024;
 namespace {
 
 constexpr double R_universal = 8.31451;      // physical_constants.d:13
@@ -220,7 +224,7 @@ struct Model {
 // Phobos std.algorithm.iteration.sumPairwise for a random-access range of doubles.
 double sum_pairwise(const double* d, int n) {
     if (n == 0) return 0.0;
-    double store[64];
+    double store[64];   // pairwise-summation stack (depth ~log2 n)
     size_t idx = 0;
     auto collapse = [&](size_t k) {
         size_t lastToKeep = idx - (size_t)__builtin_ctzll((unsigned long long)(k + 1));
@@ -245,13 +249,13 @@ struct Counters { long steps = 0, rhs = 0, kc = 0, newton = 0, rejects = 0; };
 
 struct Cell {   // the reference GasState fields used on this path
     double rho, u, T, p;
-    double massf[64];
+    double massf[ORACLE_MAX_SPECIES];
 };
 
 struct Work {
     const Model& m;
     Counters cnt;
-    double g[64], kf[256], kb[256], wf[256], wb[256];
+    double g[ORACLE_MAX_SPECIES], kf[ORACLE_MAX_REACTIONS], kb[ORACLE_MAX_REACTIONS], wf[ORACLE_MAX_REACTIONS], wb[ORACLE_MAX_REACTIONS];
     explicit Work(const Model& mm) : m(mm) {}
 
     // therm_perf_gas_mix.d:354-364 with Q.p = P_atm (reaction_mechanism.d:205-218)
@@ -336,14 +340,14 @@ struct Work {
         }
     }
     void rates(const double* c, double* out) {   // reaction_mechanism.d:75-81
-        double q[64], L[64];
+        double q[ORACLE_MAX_SPECIES], L[ORACLE_MAX_SPECIES];
         split_rates(c, q, L);
         for (int i = 0; i < m.nsp; ++i) out[i] = q[i] - L[i];
     }
     // reaction_mechanism.d:161-203
     double estimate_step(const double* c) {
         const double MUCH_LARGER_FACTOR = 10000.0, ZERO_EPS = 1.0e-50, ZERO_TOL = 1.0e-30, EPS1 = 1.0e-3;
-        double q[64], L[64];
+        double q[ORACLE_MAX_SPECIES], L[ORACLE_MAX_SPECIES];
         double min_dt = 1.0e6, dt;
         split_rates(c, q, L);
         for (int i = 0; i < m.nsp; ++i) {
@@ -366,7 +370,7 @@ struct Work {
         const double b51 = 37. / 378., b53 = 250. / 621., b54 = 125. / 594., b56 = 512. / 1771.,
             b41 = 2825. / 27648., b43 = 18575. / 48384., b44 = 13525. / 55296., b45 = 277. / 14336., b46 = 1.0 / 4.0;
         const int n = m.nsp;
-        double k1[64], k2[64], k3[64], k4[64], k5[64], k6[64], yT[64], yErr[64];
+        double k1[ORACLE_MAX_SPECIES], k2[ORACLE_MAX_SPECIES], k3[ORACLE_MAX_SPECIES], k4[ORACLE_MAX_SPECIES], k5[ORACLE_MAX_SPECIES], k6[ORACLE_MAX_SPECIES], yT[ORACLE_MAX_SPECIES], yErr[ORACLE_MAX_SPECIES];
         rates(y0, k1);
         for (int i = 0; i < n; ++i) yT[i] = y0[i] + h * (a21 * k1[i]);
         rates(yT, k2);
@@ -408,7 +412,7 @@ struct Work {
     bool aqss_step(const double* y0, double h, double* yOut, double& hSuggest) {
         const double ZERO_EPS = 1.0e-50;
         const int n = m.nsp;
-        double q0[64], L0[64], p0[64], alpha[64], yp[64], yp0[64], qp[64], Lp[64], pp[64], ab[64], qt[64], pb[64], yc[64];
+        double q0[ORACLE_MAX_SPECIES], L0[ORACLE_MAX_SPECIES], p0[ORACLE_MAX_SPECIES], alpha[ORACLE_MAX_SPECIES], yp[ORACLE_MAX_SPECIES], yp0[ORACLE_MAX_SPECIES], qp[ORACLE_MAX_SPECIES], Lp[ORACLE_MAX_SPECIES], pp[ORACLE_MAX_SPECIES], ab[ORACLE_MAX_SPECIES], qt[ORACLE_MAX_SPECIES], pb[ORACLE_MAX_SPECIES], yc[ORACLE_MAX_SPECIES];
         auto p_on_y = [&](const double* L, const double* y, double* p) {
             for (int i = 0; i < n; ++i) p[i] = L[i] / (y[i] + ZERO_EPS);
         };
@@ -473,7 +477,7 @@ struct Work {
     }
 
     // gas_model.d:237-253
-    double tb[64];
+    double tb[ORACLE_MAX_SPECIES];
     const double* third_body_terms(const Cell& Q) {   // rate_constant.d:117-119
         for (int i = 0; i < m.nsp; ++i) tb[i] = Q.massf[i] * Q.rho / m.M[i];
         return tb;
@@ -537,7 +541,7 @@ struct Work {
     void update_from_pT(Cell& Q) const {
         Q.rho = Q.p / (mass_average(Q, m.R.data()) * Q.T);
         double logT = std::log(Q.T);
-        double vals[64];
+        double vals[ORACLE_MAX_SPECIES];
         for (int i = 0; i < m.nsp; ++i) vals[i] = m.curves[i].eval_h(Q.T, logT) - m.R[i] * Q.T;
         Q.u = mass_average(Q, vals);
     }
@@ -545,7 +549,7 @@ struct Work {
     // chemistry_update.d:140-326
     void opCall(Cell& Q, double tInterval, double& dtSuggest) {
         Cell Qinit = Q;
-        double conc0[64], concOut[64];
+        double conc0[ORACLE_MAX_SPECIES], concOut[ORACLE_MAX_SPECIES];
         try {
             massf2conc(Q, conc0);
             rate_constants(Q.T, third_body_terms(Q));
@@ -624,7 +628,9 @@ struct Work {
 // C ABI used by tests/ and bench.py (ctypes).  Handles are heap pointers.
 extern "C" {
 
-void* oracle_model_new(int nsp) { Model* m = new Model(); m->nsp = nsp; m->M.resize(nsp); m->R.resize(nsp); m->curves.resize(nsp); return m; }
+void* oracle_model_new(int nsp) {
+    if (nsp < 1 || nsp > ORACLE_MAX_SPECIES) return nullptr;
+    Model* m = new Model(); m->nsp = nsp; m->M.resize(nsp); m->R.resize(nsp); m->curves.resize(nsp); return m; }
 void oracle_model_free(void* h) { delete (Model*)h; }
 
 // Per species: molar mass and its CEA curve (ThermPerfGasMixture ctor, therm_perf_gas_mix.d:30-47).
@@ -651,6 +657,7 @@ int oracle_add_reaction(void* h, int collider, int frc_model, double fA, double 
                         int nreac, const int* reac_idx, const int* reac_coeff,
                         int nprod, const int* prod_idx, const int* prod_coeff,
                         int neff, const int* eff_idx, const double* eff_val) {
+    if ((int)((Model*)h)->reactions.size() >= ORACLE_MAX_REACTIONS) return -1;
     Model* m = (Model*)h;
     Reaction r;
     r.collider = collider != 0;
@@ -755,7 +762,7 @@ int oracle_integrate_fixed(void* h, int method, double T, double* y, double dt, 
     Model mm = *m; mm.method = method;
     Work w(mm);
     w.rate_constants(T, y);
-    double t = 0.0, dummy, y1[64];
+    double t = 0.0, dummy, y1[ORACLE_MAX_SPECIES];
     int count = 0;
     while ((tMax - t) > 1.0e-9) {
         dt = std::min(dt, tMax - t);

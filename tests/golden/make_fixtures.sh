@@ -64,6 +64,18 @@ LARC=$REF/examples/lmr/3D/cylinder-larc
         park2t-eem.lua >> park2t-prep.log 2>&1) || { cat "$WORK/park2t-prep.log"; exit 1; }
 grep -v '^-- Auto-generated' "$WORK/park2t-gas.lua" > "$OUT/park2t-gas.lua"
 cp "$WORK/park2t-chem.lua" "$WORK/park2t-eem.lua" "$OUT/"
+# A large mechanism: the 75-species, 474-reaction C2H2/C2H4 model of examples/kinetics/acetylene-ignition-
+# delay (Chemkin format), converted by the reference's chemkin2eilmer (which runs prep-gas itself) and
+# prep_chem, as that example's prep-ignition.sh does.
+mkdir -p "$WORK/bin"
+printf '#!/bin/sh\nexec "%s" "%s" "$@"\n' "$LUA" "$REF/src/gas/prep_gas.lua" > "$WORK/bin/prep-gas"
+chmod +x "$WORK/bin/prep-gas"
+(cd "$WORK" && PATH="$WORK/bin:$PATH" "$LUA" "$REF/src/kinetics/chemkin2eilmer.lua" \
+        "$KIN/acetylene-ignition-delay/mech.txt" c2h2-gas.lua c2h2-reac.lua > c2h2-prep.log 2>&1 \
+    && "$LUA" "$REF/src/kinetics/prep_chem.lua" c2h2-gas.lua c2h2-reac.lua c2h2-chem.lua >> c2h2-prep.log 2>&1) \
+    || { cat "$WORK/c2h2-prep.log"; exit 1; }
+grep -v '^-- Auto-generated' "$WORK/c2h2-gas.lua" > "$OUT/c2h2-gas.lua"
+cp "$WORK/c2h2-chem.lua" "$OUT/c2h2-chem.lua"
 # Arrhenius2, Lindemann-Hinshelwood and Yungster-Rabinowitz forms (no reference example uses them)
 prep h2o2forms "$KIN/hydrogen-ignition-delay/Jachimowski-1992-species.inp" "$HERE/inputs/h2o2-rate-forms.lua"
 

@@ -32,7 +32,7 @@ def test_library_exports_every_declared_symbol():
     assert sorted(gdtk_gb300.SIGNATURES) == names
 
 
-@pytest.mark.parametrize("name", ["park5", "j92", "gupta5", "n2", "h2i2", "stanford", "drm19"])
+@pytest.mark.parametrize("name", ["park5", "j92", "gupta5", "n2", "h2i2", "stanford", "drm19", "c2h2"])
 def test_gas_model_reader_matches_oracle_reader(name):
     from gdtk_gb300.gas import GasModel
     gm = GasModel(mech(name + "-gas.lua"))
@@ -60,6 +60,22 @@ def test_unsupported_rate_model_is_refused(tmp_path):
     L = gdtk_gb300.lib()
     n = L.gdtk_generate_fast_source(mech("park5-gas.lua").encode(), str(bad).encode(), None, 0)
     assert n == -1 and "not supported" in gdtk_gb300.last_error()
+
+
+def test_large_mechanism_is_read_and_routed_to_the_warp_kernel():
+    """The 75-species, 474-reaction acetylene model: both readers take it, the oracle holds all of
+    it, and the mechanism-specialised (thread-per-cell) generator refuses it with the reason."""
+    gas, chem = mech("c2h2-gas.lua"), mech("c2h2-chem.lua")
+    names, _ = oracle.load_gas(gas)
+    assert len(names) == 75
+    rx, _ = oracle.load_mechanism(chem, names)
+    assert len(rx) == 474
+    orc = oracle.Oracle(gas, chem)
+    kf, kb = orc.rate_constants(1500.0, np.full(75, 1e-3))
+    assert kf.shape == (474,) and np.isfinite(kf).all() and np.isfinite(kb).all()
+    L = gdtk_gb300.lib()
+    assert L.gdtk_generate_fast_source(gas.encode(), chem.encode(), None, 0) == -1
+    assert "one warp per cell" in gdtk_gb300.last_error()
 
 
 def test_gpu_work_fails_loudly_without_gpu():

@@ -234,6 +234,45 @@ def test_source_terms(j92):
         assert np.abs(src[:, c] - want).max() <= 1e-12 * scale
 
 
+@pytest.mark.parametrize("name", ["park5", "c2h2"])
+def test_gas_state_properties_match_oracle(name):
+    """Cv, Cp, gamma, R, u, h, s, the frozen sound speed and per-species h, s, g of a gas state
+    (gas_cwrap.d:610-824 over therm_perf_gas_mix.d:230-364) from the oracle's species curves, and
+    the (rho, p) update (therm_perf_gas_mix.d:75-79)."""
+    from gdtk_gb300.gas import GasModel, GasState
+    gm = GasModel(mech(name + "-gas.lua"))
+    orc = oracle.Oracle(mech(name + "-gas.lua"))
+    nsp = gm.n_species
+    Y = np.random.default_rng(3).dirichlet(np.full(nsp, 0.5))
+    gs = GasState(gm)
+    gs.massf = list(Y)
+    T, p = 2345.0, 2.5e5
+    gs.T, gs.p = T, p
+    gs.update_thermo_from_pT()
+    R_i = 8.31451 / orc.M
+    th = np.array([orc.species_thermo(i, T) for i in range(nsp)])   # Cp, h, s per species
+    lp = np.log(p / 101325.0)
+    cv, cp = np.sum(Y * (th[:, 0] - R_i)), np.sum(Y * th[:, 0])
+    R = np.sum(Y * R_i)
+    want = dict(Cv=cv, Cp=cp, gamma=cp / cv, R=R, internal_energy=np.sum(Y * (th[:, 1] - R_i * T)),
+                enthalpy=np.sum(Y * th[:, 1]), entropy=np.sum(Y * (th[:, 2] - R_i * lp)),
+                a=np.sqrt(cp / cv * R * T))
+    for k, v in want.items():
+        assert np.isclose(getattr(gs, k), v, rtol=1e-12, atol=0), k
+    assert np.isclose(gm.dpdrho_const_T(gs), R * T, rtol=1e-12, atol=0)
+    for i in range(0, nsp, max(1, nsp // 9)):
+        h, s = gm.enthalpy_isp(gs, i), gm.entropy_isp(gs, i)
+        assert np.isclose(h, th[i, 1], rtol=1e-13, atol=0)
+        assert np.isclose(s, th[i, 2] - R_i[i] * lp, rtol=1e-13, atol=0)
+        assert gm.gibbs_free_energy_isp(gs, i) == h - T * s
+    g2 = GasState(gm)
+    g2.massf = list(Y)
+    g2.rho, g2.p = gs.rho, gs.p
+    g2.update_thermo_from_rhop()
+    assert np.isclose(g2.T, T, rtol=1e-13) and np.isclose(g2.u, gs.u, rtol=1e-12)
+    assert g2.a == gs.a or np.isclose(g2.a, gs.a, rtol=1e-13)
+
+
 def test_fixed_volume_reactor_through_gas_api():
     # examples/kinetics/fixed-volume-reactor-n2/test_fvreactor.py through the mirrored gdtk.gas API
     from gdtk_gb300.gas import GasModel, PyGasState as GasState, ThermochemicalReactor
