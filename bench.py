@@ -240,7 +240,7 @@ def run_blocks(args, w):
     srho, su = rc.thermo_from_pT(dp, dT, dY)
     sample = dict(rho=srho, u=su, T=dT, p=dp, massf=dY, dt_chem=torch.full((262144,), -1.0, dtype=torch.float64,
                                                                          device=dev))
-    choice, oflag, _ = autotune.tune(rc, sample, 1.0e-6, tag="h2air-262144")
+    choice, oflag, _ = autotune.tune(rc, sample, 1.0e-6, tag="h2air-262144", allow_warp=False)
     flags = UPDATE_THERMO | RETRY | oflag
     spec = h2air_blocks(rc.species_names, rc.mol_masses, nblocks=w["nblocks"], seed=w["seed"],
                         gas_file=rc.gmodel.file_name)

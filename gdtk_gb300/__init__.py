@@ -83,6 +83,7 @@ SIGNATURES = {
     "chem_reactor_flop_model": (ctypes.c_int, [ctypes.c_int, _d]),
     "chem_reactor_set_lane_stats": (ctypes.c_int, [ctypes.c_int, _v]),
     "chem_reactor_configure": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "chem_reactor_set_refill_chunk": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
     "chem_reactor_info": (ctypes.c_int, [ctypes.c_int, _i, _i, _i, _i]),
     "chem_reactor2t_new": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p]),
     "chem_reactor2t_info": (ctypes.c_int, [ctypes.c_int, _i, _i, _i]),

@@ -142,6 +142,7 @@ struct ReactorObj {
     LaunchInfo last{};
     std::unique_ptr<FastKernel> fast;   // mechanism-specialised kernel, compiled on first use
     int req_block = 0, req_min_blocks = 0;   // launch shape chosen by chem_reactor_configure
+    int refill_chunk = 0;                    // chem_reactor_set_refill_chunk
     unsigned long long* lane_stats = nullptr;   // when set, the fast kernel counts lane occupancy
     DevBuf<float> order_key;            // longest-first scheduling scratch
     DevBuf<int> order;
@@ -249,6 +250,7 @@ const char* status_text(int st) {
 // Fast-kernel launch of an assembled FastArgs, longest-first unless GDTK_CHEM_INDEX_ORDER.
 void run_fast(ReactorObj& r, FastArgs& a, int flags, cudaStream_t s) {
     a.lane_stats = r.lane_stats;
+    a.refill_chunk = r.refill_chunk;
     if (!(flags & GDTK_CHEM_INDEX_ORDER) && a.total > 1) {
         r.order_key.ensure((size_t)a.total);
         r.order.ensure((size_t)a.total);
@@ -403,6 +405,7 @@ int update_cells_with_scratch(int cr_i, int ncell, const double* rho, const doub
         a.flags = flags & (CHEM_FLAG_UPDATE_THERMO | CHEM_FLAG_RETRY);
         a.T_frozen = T_frozen;
         a.counter = counter;
+        a.refill_chunk = r.refill_chunk;
         CellBlock& b = a.blocks[0];
         b.ncell = ncell;
         b.first = 0;
@@ -1004,6 +1007,15 @@ int chem_reactor_configure(int cr_i, int block, int min_blocks) {
         r.req_block = block;
         r.req_min_blocks = min_blocks;
         r.fast = std::move(k);
+        return 0;
+    });
+}
+
+int chem_reactor_set_refill_chunk(int cr_i, int cells) {
+    return guarded([&] {
+        if (!(cells == 0 || cells == 1 || (cells >= 32 && cells <= (1 << 20))))
+            throw std::runtime_error("refill chunk must be 0, 1 or 32..1048576 cells");
+        reactor(cr_i).refill_chunk = cells;
         return 0;
     });
 }

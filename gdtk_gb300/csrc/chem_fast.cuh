@@ -67,7 +67,7 @@ struct FastArgs {
     int nblocks;
     int total;
     int flags;
-    int pad;
+    int refill_chunk;       // visit positions a warp reserves per atomic (<= 1: exactly the lanes that need one)
     double T_frozen;
     unsigned* counter;
     int* cell_counters;     // [6][total], global cell index
@@ -422,15 +422,34 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
     // All 32 lanes of a warp stay in this loop until the whole warp is out of work, so that
     // every iteration can re-converge them (__syncwarp) and lanes that refill with a new cell
     // run the same iteration as their neighbours instead of splitting the warp.
+    unsigned q_lo = 0, q_hi = 0;   // visit positions this warp has reserved and not yet handed out
     while (true) {
         const unsigned need = __ballot_sync(FULL, alive && !have);
-        if (need) {   // refill: one atomic per warp for all lanes that need a cell
+        if (need) {   // refill: at most one atomic per warp for all lanes that need a cell
             const int leader = __ffs(need) - 1;
-            unsigned base = 0;
-            if (lane == leader) base = atomicAdd(a.counter, (unsigned)__popc(need));
-            base = __shfl_sync(FULL, base, leader);
+            const unsigned n_need = __popc(need), rank = __popc(need & ((1u << lane) - 1u));
+            unsigned pos;
+            if (a.refill_chunk <= 1) {
+                unsigned base = 0;
+                if (lane == leader) base = atomicAdd(a.counter, n_need);
+                pos = __shfl_sync(FULL, base, leader) + rank;
+            } else {   // chunks of refill_chunk (>= 32) positions: the reserve, then a new chunk
+                const unsigned left = q_hi - q_lo;
+                unsigned nb = 0;
+                if (left < n_need) {
+                    if (lane == leader) nb = atomicAdd(a.counter, (unsigned)a.refill_chunk);
+                    nb = __shfl_sync(FULL, nb, leader);
+                }
+                pos = rank < left ? q_lo + rank : nb + (rank - left);
+                if (left < n_need) {
+                    q_lo = nb + (n_need - left);
+                    q_hi = nb + (unsigned)a.refill_chunk;
+                } else {
+                    q_lo += n_need;
+                }
+            }
             if (alive && !have) {
-                g = base + __popc(need & ((1u << lane) - 1u));
+                g = pos;
                 if (g >= (unsigned)a.total) {
                     alive = false;
                 } else {

@@ -31,7 +31,7 @@ struct FastArgs {
     int nblocks;
     int total;
     int flags;
-    int pad;
+    int refill_chunk;   // visit positions a warp reserves per atomic (<= 1: exactly the lanes that need a cell)
     double T_frozen;
     unsigned* counter;
     int* cell_counters;

@@ -215,6 +215,11 @@ int gdtk_compile_fast_source_check(const char* gas_file, const char* chem_file, 
  * restores the default (largest block the shared-memory budget allows).  Compiles and loads the
  * variant now; later updates use it.  Used by the autotuner (gdtk_gb300/autotune.py). */
 int chem_reactor_configure(int cr_i, int block, int min_blocks);
+/* Work-queue refill of the mechanism-specialised kernel: with cells = 0 or 1 a warp takes, with one
+ * atomic, exactly as many visit positions as it has lanes without a cell; with cells in 32..2^20 it
+ * reserves that many consecutive positions per atomic and hands them out to its own lanes before
+ * taking another chunk.  Only scheduling changes, never a cell's result.  Autotuner dimension. */
+int chem_reactor_set_refill_chunk(int cr_i, int cells);
 /* Diagnostics: when stats (device, unsigned long long[24]) is set, later fast-kernel launches
  * add, for each phase k (0 iteration, 1 rate constants, 2 right-hand side, 3 step control,
  * 4 Newton iteration, 5 cell completion, 6 refill, 7 the alpha-QSS update after a right-hand

@@ -408,14 +408,45 @@ def test_autotuner_picks_a_fitting_shape(j92, tmp_path, monkeypatch):
     sample = dict(rho=rho, u=u, T=dT, p=dp, massf=dY, dt_chem=torch.full((2048,), -1.0, dtype=torch.float64,
                                                                          device="cuda"))
     choice, oflag, results = autotune.tune(rc, sample, 1e-6, tag="test")
-    assert len(results) == 4 and (choice["block"], choice["min_blocks"]) in [(256, 1), (128, 1)]
+    # 2 shapes x 2 orders, 2 refill chunks on the best, one warp per cell
+    assert len(results) == 7
+    assert sorted({r["refill_chunk"] for r in results}) == [0] + autotune.CHUNKS
+    assert [r["cells_per_warp"] for r in results].count(1) == 1
+    if choice["cells_per_warp"] == 32:
+        assert (choice["block"], choice["min_blocks"]) in [(256, 1), (128, 1)]
     assert os.path.exists(os.path.join(str(tmp_path), "tune.json"))
-    again, _, _ = autotune.tune(rc, sample, 1e-6, tag="test")     # from the cache
-    assert again["block"] == choice["block"]
-    # results still match the oracle under the tuned shape
-    g, o, _, _ = run_pair(rc, orc, T[:256], p[:256], np.ascontiguousarray(Y[:, :256]), 1.0e-6)
+    again, again_flag, _ = autotune.tune(rc, sample, 1e-6, tag="test")     # from the cache
+    assert again["block"] == choice["block"] and again_flag == oflag
+    # results still match the oracle under the tuned variant
+    g, o, _, _ = run_pair(rc, orc, T[:256], p[:256], np.ascontiguousarray(Y[:, :256]), 1.0e-6, flags=3 | oflag)
     assert_parity(g, o)
-    autotune.check_shape(rc, 0, 0)   # back to the default shape for later tests
+    thread_only, tflag, tres = autotune.tune(rc, sample, 1e-6, tag="test", allow_warp=False)
+    assert thread_only["cells_per_warp"] == 32 and not tflag & autotune.WARP_PER_CELL and len(tres) == 6
+    autotune.check_shape(rc, 0, 0)   # back to the default shape and refill for later tests
+    autotune.set_refill_chunk(rc, 0)
+
+
+@pytest.mark.parametrize("chunk", [32, 128, 4096])
+def test_refill_chunk_changes_no_result(j92, chunk):
+    """The refill chunk only changes which warp takes which cell: bitwise the same cells."""
+    from gdtk_gb300 import autotune
+    from gdtk_gb300.workloads import h2air_cells
+    torch = torch_cuda()
+    rc, _ = j92
+    T, p, Y = h2air_cells(rc.species_names, rc.mol_masses, 5000, seed=72, gas_file=rc.gmodel.file_name)
+    outs = []
+    for cells in (0, chunk):
+        autotune.set_refill_chunk(rc, cells)
+        dT, dp, dY = to_dev(torch, T, p, Y)
+        rho, u = rc.thermo_from_pT(dp, dT, dY)
+        dtc = torch.full((5000,), -1.0, dtype=torch.float64, device="cuda")
+        st = torch.zeros(5000, dtype=torch.int32, device="cuda")
+        rc.update(rho, u, dT, dp, dY, dtc, 1.0e-6, status=st)
+        torch.cuda.synchronize()
+        outs.append((dT, dp, dY, dtc, st))
+    autotune.set_refill_chunk(rc, 0)
+    for a, b in zip(*outs):
+        assert torch.equal(a, b)
 
 
 def test_mixing_layer_split_steps_track_the_oracle(j92):
