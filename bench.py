@@ -47,16 +47,21 @@ WORKLOADS = {
     # learned surrogate: 4x256 GELU MLP trained on 16,777,216 samples of the FP64 update (cells of the
     # h2air-1M distribution, dt log-uniform in [0.5, 2] us, 5% held out); inference + gate + FP64
     # fallback on 4,194,304 fresh cells at dt = 1e-6 s, against the plain FP64 update of the same cells
+    # large mechanism: the reference's 75-species, 474-reaction C2H2/C2H4 model (alpha-QSS, one warp per
+    # cell) on shock-tube ignition states of its acetylene example, dt = 1e-6 s
+    "c2h2-262144": dict(gas="c2h2-gas.lua", chem="c2h2-chem.lua", n=262144, dt=1.0e-6, kind="c2h2", seed=5),
     "h2air-surrogate": dict(gas="j92-gas.lua", chem="j92-chem.lua", n=4194304, dt=1.0e-6, kind="surrogate",
                             seed=3, train_samples=16777216, epochs=30, batch=8192, error_epochs=8),
 }
 
 
 def make_cells(w, names=None, M=None, n=None):
-    from gdtk_gb300.workloads import air5_cells, h2air_cells
+    from gdtk_gb300.workloads import acetylene_cells, air5_cells, h2air_cells
     n = n or w["n"]
     if w["kind"] == "air5":
         return air5_cells(n, seed=w["seed"])
+    if w["kind"] == "c2h2":
+        return acetylene_cells(names, M, n, seed=w["seed"])
     return h2air_cells(names, M, n, seed=w["seed"], gas_file=os.path.join(MECH, w["gas"]))
 
 
@@ -919,13 +924,15 @@ def main():
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": args.workload, "cells_per_gpu": n, "mechanism": w["chem"], "dt": w["dt"],
                        "method": rc.method, "tight_coupling": rc.tight, "dt_chem_in": -1.0,
-                       "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas x%d" % ws,
+                       "l2": "inputs larger than L2 (no flush): %.0f MB of cell state" % (n * 8 * (5 + rc.nsp) / 1e6),
+                       "parallelism": "replicas x%d" % ws,
                        "cells_ok": ok, "cells_failed": int(n - ok), "codegen_env": codegen_env()},
             "roofline": roofline_fp64(issued, n, kernel_ms, peak, flops, traffic, tot / args.steps / n),
             "cpu_baseline": cpu,
             "e2e": e2e,
             "clocks": clk,
-            "gpu_launches": args.steps * 5,
+            # thread per cell: cost pre-pass, 3 ordering kernels, chemistry; one warp per cell: chemistry
+            "gpu_launches": args.steps * (1 if rc.nsp > 32 or rc.nr > 128 else 5),
         }
         if sur is not None:
             line["surrogate"] = sur

@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
 #include <array>
 #include <map>
 #include <memory>
@@ -150,8 +151,9 @@ struct ReactorObj {
     // one warp per cell: for mechanisms beyond the thread-per-cell kernels' limits, or on request
     bool large = false;                 // more than GDTK_MAX_SPECIES species or GDTK_MAX_REACTIONS reactions
     int warp_doubles = 0;
-    DevBuf<int> csr;                    // [nsp + 1] starts, then reaction indices, then net coefficients
-    int csr_n = 0;
+    DevBuf<int> wt_i;                   // warp-per-cell tables (WarpTables, chem_launch.h)
+    DevBuf<double> wt_d;
+    WarpTables wt{};
     ~ReactorObj() { if (counter) cudaFree(counter); }
 };
 
@@ -265,29 +267,80 @@ void run_fast(ReactorObj& r, FastArgs& a, int flags, cudaStream_t s) {
     r.last.blocks_per_sm = r.fast->blocks_per_sm;
 }
 
-// Each species' (reaction, net coefficient) entries in reaction order, for the warp-per-cell kernel.
+// Tables of the warp-per-cell kernel (layout in chem_launch.h) from the packed mechanism: reaction terms
+// and third bodies, the species -> (reaction, net coefficient) gather with whole species dealt to the 32
+// lanes longest first, and the efficiency lists transposed.
 void prepare_warp_path(ReactorObj& r, const PackedMech& pm) {
     r.large = pm.nsp > GDTK_MAX_SPECIES || pm.nr > GDTK_MAX_REACTIONS;
     r.warp_doubles = chem_warp_doubles(pm.nsp, pm.nr, pm.neff, pm.method);
-    std::vector<int> start(pm.nsp + 1, 0), rx, nu;
-    std::vector<std::vector<std::pair<int, int>>> per(pm.nsp);
-    for (int ir = 0; ir < (int)r.mh.reactions.size(); ++ir) {
-        std::map<int, int> net;
-        for (auto& x : r.mh.reactions[ir].reac) net[x.first] -= x.second;
-        for (auto& x : r.mh.reactions[ir].prod) net[x.first] += x.second;
-        for (auto& kv : net)
-            if (kv.second != 0) per[kv.first].push_back({ir, kv.second});
+    MechView m;
+    m.bind(pm.I.data(), pm.D.data());
+    const int nsp = pm.nsp, nr = pm.nr, neff = pm.neff;
+    std::vector<int> tstart(nr + 1, 0), terms, rxeff(nr, -1);
+    std::vector<std::vector<std::pair<int, int>>> per(nsp);   // species -> (reaction, nu), ascending reaction
+    auto term = [&](int isp, int coeff, int product) {
+        if (isp < 0 || isp >= nsp || coeff < 0 || coeff > 255) throw std::runtime_error("reaction term out of range");
+        terms.push_back(isp | coeff << 8 | product << 16);
+    };
+    for (int ir = 0; ir < nr; ++ir) {
+        const int* x = m.rx(ir);
+        for (int k = 0; k < x[RX_NREAC]; ++k) term(x[RX_REAC_IDX + k], x[RX_REAC_COEFF + k], 0);
+        for (int k = 0; k < x[RX_NPROD]; ++k) term(x[RX_PROD_IDX + k], x[RX_PROD_COEFF + k], 1);
+        tstart[ir + 1] = (int)terms.size();
+        if (x[RX_COLLIDER]) rxeff[ir] = x[RX_EFFSET];
+        for (int k = 0; k < x[RX_NPART]; ++k)
+            if (x[RX_PART_NU + k] != 0) per[x[RX_PART + k]].push_back({ir, x[RX_PART_NU + k]});
     }
-    for (int i = 0; i < pm.nsp; ++i) {
-        start[i + 1] = start[i] + (int)per[i].size();
-        for (auto& e : per[i]) { rx.push_back(e.first); nu.push_back(e.second); }
+    // longest species first onto the least-loaded lane (ties: lowest lane)
+    std::vector<int> order(nsp);
+    for (int i = 0; i < nsp; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return per[a].size() > per[b].size(); });
+    std::vector<std::vector<int>> lane_sp(32);
+    std::vector<size_t> load(32, 0);
+    for (int isp : order) {
+        int l = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        lane_sp[l].push_back(isp);
+        load[l] += per[isp].size();
     }
-    std::vector<int> all(start);
-    all.insert(all.end(), rx.begin(), rx.end());
-    all.insert(all.end(), nu.begin(), nu.end());
-    r.csr_n = (int)rx.size();
-    r.csr.ensure(all.size());
-    check(cudaMemcpy(r.csr.p, all.data(), all.size() * sizeof(int), cudaMemcpyHostToDevice), "cudaMemcpy");
+    std::vector<int> lane(33, 0), ent;
+    for (int l = 0; l < 32; ++l) {
+        for (int isp : lane_sp[l])
+            for (auto& e : per[isp]) {
+                if (e.second < -127 || e.second > 127) throw std::runtime_error("stoichiometric coefficient out of range");
+                ent.push_back(isp | e.first << 8 | (e.second + 128) << 24);
+            }
+        lane[l + 1] = (int)ent.size();
+    }
+    int maxlen = 0;
+    for (int s = 0; s < neff; ++s) maxlen = std::max(maxlen, m.eff_i(s)[0]);
+    std::vector<int> efflen(std::max(neff, 1), 0), effidx((size_t)maxlen * neff, 0);
+    std::vector<double> effval(std::max((size_t)maxlen * neff, (size_t)1), 0.0);
+    for (int s = 0; s < neff; ++s) {
+        const int* ei = m.eff_i(s);
+        const double* ev = m.eff_d(s);
+        efflen[s] = ei[0];
+        for (int k = 0; k < ei[0]; ++k) {
+            effidx[(size_t)k * neff + s] = ei[1 + k];
+            effval[(size_t)k * neff + s] = ev[ei[1 + k]];
+        }
+    }
+    std::vector<int> all;
+    auto put = [&](const std::vector<int>& v) { int off = (int)all.size(); all.insert(all.end(), v.begin(), v.end()); return off; };
+    WarpTables& t = r.wt;
+    t.off_tstart = put(tstart);
+    t.off_terms = put(terms);
+    t.off_rxeff = put(rxeff);
+    t.off_lane = put(lane);
+    t.off_ent = put(ent);
+    t.n_smem_ints = (int)all.size();
+    t.off_efflen = put(efflen);
+    t.off_effidx = put(effidx);
+    r.wt_i.ensure(all.size());
+    r.wt_d.ensure(effval.size());
+    check(cudaMemcpy(r.wt_i.p, all.data(), all.size() * sizeof(int), cudaMemcpyHostToDevice), "cudaMemcpy");
+    check(cudaMemcpy(r.wt_d.p, effval.data(), effval.size() * sizeof(double), cudaMemcpyHostToDevice), "cudaMemcpy");
+    t.gi = r.wt_i.p;
+    t.eff_val = r.wt_d.p;
 }
 
 int launch_update(ReactorObj& r, int ncell, const double* rho, const double* u, double* T, double* p, double* massf,
@@ -301,7 +354,7 @@ int launch_update(ReactorObj& r, int ncell, const double* rho, const double* u, 
     if (!r.counter) check(cudaMalloc(&r.counter, sizeof(unsigned)), "cudaMalloc");
     check(cudaMemsetAsync(r.counter, 0, sizeof(unsigned), s), "cudaMemsetAsync");
     if ((flags & GDTK_CHEM_WARP_PER_CELL) || r.large) {
-        if (!r.csr.p) throw std::runtime_error("warp-per-cell tables were not uploaded");
+        if (!r.wt.gi) throw std::runtime_error("warp-per-cell tables were not uploaded");
         ChemUpdateArgs a{};
         a.mech_i = r.dev.I;
         a.mech_d = r.dev.D;
@@ -315,9 +368,8 @@ int launch_update(ReactorObj& r, int ncell, const double* rho, const double* u, 
         a.counter = r.counter;
         a.cell_counters = cell_counters;
         a.totals = totals;
-        const int nsp = r.dev.host.nsp;
-        check(launch_chem_update_warp(a, r.mh.method, r.csr.p, r.csr.p + nsp + 1, r.csr.p + nsp + 1 + r.csr_n,
-                                      r.warp_doubles, cuda().sm_count, s, &r.last), "warp-per-cell update launch");
+        check(launch_chem_update_warp(a, r.mh.method, r.wt, r.warp_doubles, cuda().sm_count, s, &r.last),
+              "warp-per-cell update launch");
         return 0;
     }
     if (flags & GDTK_CHEM_REFERENCE_ORDER) {

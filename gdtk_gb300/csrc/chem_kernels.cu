@@ -729,12 +729,16 @@ __global__ void order_scatter(const float* key, int n, int* hist, int* order) {
 
 // ---------------------------------------------------------------- one warp per cell (large mechanisms)
 // The reference-order update (chem_update_kernel above) with one warp integrating one cell: species
-// and reactions are spread over the lanes, the cell's vectors live in the warp's share of shared
-// memory, and the mechanism tables are read from global memory (they need not fit in shared memory).
+// and reactions are spread over the lanes, and the cell's vectors live in the warp's share of shared
+// memory.  The right-hand side reads compact tables (WarpTables): each reaction's concentration terms
+// from shared memory, the third-body efficiency lists transposed in global memory (one list per lane,
+// consecutive words across lanes), and a species -> (reaction, coefficient) gather whose species are
+// dealt to the lanes longest first, so that the lanes' loops are about equally long.  Rate constants
+// and thermo read the packed mechanism from global memory (they need not fit in shared memory).
 // Every sum the reference takes over species in order (energies, gas constant, mass-fraction total,
 // RKF error norm) is taken by lane 0 in that order from per-species terms the lanes computed, and q, L
-// gather each species' terms in reaction order through a species -> reactions list, so each value is
-// the reference-order kernel's.  Minima and maxima (step estimate, sigma) are order-free.
+// gather each species' terms in reaction order, so each value is the reference-order kernel's.
+// Minima and maxima (step estimate, sigma) are order-free.
 constexpr unsigned FULL_MASK = 0xffffffffu;
 
 struct WarpLayout {
@@ -749,9 +753,14 @@ struct WarpLayout {
 
 struct WarpCtx {
     MechView m;
-    const int* csr_start;   // [nsp + 1]: species isp's entries csr_start[isp] .. csr_start[isp + 1]
-    const int* csr_rx;      // reaction index, ascending within a species
-    const int* csr_nu;      // net stoichiometric coefficient of the species in that reaction
+    const int* tstart;      // shared: reaction ir's terms tstart[ir] .. tstart[ir + 1]
+    const int* terms;       // shared: species | coeff << 8 | product << 16
+    const int* rxeff;       // shared: third-body efficiency list of each reaction, or -1
+    int ent_lo, ent_hi;     // this lane's gather entries
+    const int* ent;         // shared: species | reaction << 8 | (nu + 128) << 24
+    const int* efflen;      // global: length of each efficiency list
+    const int* effidx;      // global, [k][neff]: species of entry k of each list
+    const double* effval;   // global, [k][neff]: its efficiency
     int lane;
 };
 
@@ -817,37 +826,49 @@ __device__ void w_rate_constants(const WarpCtx& w, double Tq, double* kf, double
 __device__ void w_split_rates(const WarpCtx& w, const double* c, double* q, double* L, const double* kf,
                               const double* kb, double* wf, double* wb, double* meff) {
     const MechView& m = w.m;
-    for (int s = w.lane; s < m.neff; s += 32) {
-        const int* ei = m.eff_i(s);
-        const double* ev = m.eff_d(s);
+    const int neff = m.neff;
+    for (int s = w.lane; s < neff; s += 32) {   // reaction.d:450-456, in the list's order
+        const int len = w.efflen[s];
         double term = 0.0;
-        for (int k = 0; k < ei[0]; ++k) {
-            int isp = ei[1 + k];
-            term += ev[isp] * c[isp];
-        }
+        for (int k = 0; k < len; ++k) term += w.effval[k * neff + s] * c[w.effidx[k * neff + s]];
         meff[s] = term;
     }
+    for (int i = w.lane; i < m.nsp; i += 32) { q[i] = 0.0; L[i] = 0.0; }
     __syncwarp();
     for (int ir = w.lane; ir < m.nr; ir += 32) {
-        const int* r = m.rx(ir);
         double f = kf[ir], b = kb[ir];
-        if (r[RX_COLLIDER]) { double t = meff[r[RX_EFFSET]]; f = f * t; b = b * t; }
-        for (int k = 0; k < r[RX_NREAC]; ++k) f *= ipow(c[r[RX_REAC_IDX + k]], r[RX_REAC_COEFF + k]);
-        for (int k = 0; k < r[RX_NPROD]; ++k) b *= ipow(c[r[RX_PROD_IDX + k]], r[RX_PROD_COEFF + k]);
+        const int e = w.rxeff[ir];
+        if (e >= 0) { const double t = meff[e]; f = f * t; b = b * t; }
+        const int k1 = w.tstart[ir + 1];
+        for (int k = w.tstart[ir]; k < k1; ++k) {
+            const int t = w.terms[k];
+            const double v = ipow(c[t & 0xff], (t >> 8) & 0xff);
+            if (t >> 16) b *= v;
+            else f *= v;
+        }
         wf[ir] = f;
         wb[ir] = b;
     }
     __syncwarp();
-    for (int isp = w.lane; isp < m.nsp; isp += 32) {
-        double qs = 0.0, Ls = 0.0;
-        for (int k = w.csr_start[isp]; k < w.csr_start[isp + 1]; ++k) {
-            const int ir = w.csr_rx[k], nu = w.csr_nu[k];
-            if (nu > 0) { qs += nu * wf[ir]; Ls += nu * wb[ir]; }
-            else if (nu < 0) { qs += -nu * wb[ir]; Ls += -nu * wf[ir]; }
+    // q, L of this lane's species; a coefficient of +-1 needs no multiplication (1 * x == x)
+    int cur = -1;
+    double qs = 0.0, Ls = 0.0;
+    for (int k = w.ent_lo; k < w.ent_hi; ++k) {
+        const int e = w.ent[k];
+        const int isp = e & 0xff, ir = (e >> 8) & 0xffff, nu = ((e >> 24) & 0xff) - 128;
+        if (isp != cur) {
+            if (cur >= 0) { q[cur] = qs; L[cur] = Ls; }
+            cur = isp;
+            qs = 0.0;
+            Ls = 0.0;
         }
-        q[isp] = qs;
-        L[isp] = Ls;
+        const double f = wf[ir], b = wb[ir];
+        if (nu == 1) { qs += f; Ls += b; }
+        else if (nu == -1) { qs += b; Ls += f; }
+        else if (nu > 0) { qs += nu * f; Ls += nu * b; }
+        else { qs += -nu * b; Ls += -nu * f; }
     }
+    if (cur >= 0) { q[cur] = qs; L[cur] = Ls; }
     __syncwarp();
 }
 
@@ -1055,19 +1076,27 @@ __device__ bool w_aqss_step(const WarpCtx& w, const double* y0, double h, double
 }
 
 template <int METHOD>
-__global__ void __launch_bounds__(128) chem_warp_kernel(ChemUpdateArgs a, const int* csr_start, const int* csr_rx,
-                                                        const int* csr_nu, int warp_doubles) {
+__global__ void __launch_bounds__(512) chem_warp_kernel(ChemUpdateArgs a, WarpTables tb, int warp_doubles) {
     extern __shared__ double smem_w[];
+    int* ti = reinterpret_cast<int*>(smem_w);
+    for (int k = threadIdx.x; k < tb.n_smem_ints; k += blockDim.x) ti[k] = tb.gi[k];
+    __syncthreads();
     WarpCtx w;
     w.m.bind(a.mech_i, a.mech_d);
-    w.csr_start = csr_start;
-    w.csr_rx = csr_rx;
-    w.csr_nu = csr_nu;
     w.lane = threadIdx.x & 31;
+    w.tstart = ti + tb.off_tstart;
+    w.terms = ti + tb.off_terms;
+    w.rxeff = ti + tb.off_rxeff;
+    w.ent = ti + tb.off_ent;
+    w.ent_lo = ti[tb.off_lane + w.lane];
+    w.ent_hi = ti[tb.off_lane + w.lane + 1];
+    w.efflen = tb.gi + tb.off_efflen;
+    w.effidx = tb.gi + tb.off_effidx;
+    w.effval = tb.eff_val;
     const MechView& m = w.m;
     WarpLayout lay;
     lay.make(m.nsp, m.nr, m.neff, METHOD);
-    double* S = smem_w + (size_t)(threadIdx.x >> 5) * warp_doubles;
+    double* S = smem_w + (tb.n_smem_ints + 1) / 2 + (size_t)(threadIdx.x >> 5) * warp_doubles;
     double *y0 = S + lay.y0, *yout = S + lay.yout, *q = S + lay.q, *L = S + lay.L, *mf = S + lay.mf, *g = S + lay.g,
            *tmp = S + lay.tmp, *kf = S + lay.kf, *kb = S + lay.kb, *wf = S + lay.wf, *wb = S + lay.wb,
            *meff = S + lay.meff, *ext = S + lay.ext;
@@ -1256,33 +1285,38 @@ int chem_warp_doubles(int nsp, int nr, int neff, int method) {
     return l.total;
 }
 
-cudaError_t launch_chem_update_warp(const ChemUpdateArgs& a, int method, const int* csr_start, const int* csr_rx,
-                                    const int* csr_nu, int warp_doubles, int sm_count, cudaStream_t stream,
-                                    LaunchInfo* info) {
+cudaError_t launch_chem_update_warp(const ChemUpdateArgs& a, int method, const WarpTables& t, int warp_doubles,
+                                    int sm_count, cudaStream_t stream, LaunchInfo* info) {
     if (a.ncell <= 0) return cudaSuccess;
     const size_t limit = 227 * 1024;
-    int block = 128;
-    while (block > 32 && (size_t)warp_doubles * 8 * (block / 32) > limit) block /= 2;
-    const size_t smem = (size_t)warp_doubles * 8 * (block / 32);
-    if (smem > limit) return cudaErrorInvalidConfiguration;
+    const size_t tables = (size_t)((t.n_smem_ints + 1) / 2) * 8, per_warp = (size_t)warp_doubles * 8;
+    if (tables + per_warp > limit) return cudaErrorInvalidConfiguration;
     const void* fn = (method == METHOD_RKF) ? (const void*)chem_warp_kernel<METHOD_RKF>
                                             : (const void*)chem_warp_kernel<METHOD_ALPHA_QSS>;
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit);
     if (e != cudaSuccess) return e;
-    int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, block, smem);
-    if (e != cudaSuccess) return e;
-    if (per_sm < 1) return cudaErrorInvalidConfiguration;
-    long long want = ((long long)a.ncell * 32 + block - 1) / block;
+    // the block size (warps each holding one cell's vectors beside the block's copy of the tables) that
+    // keeps the most warps resident per SM; ties go to the larger block
+    int warps = 0, per_sm = 0;
+    for (int w : {16, 12, 8, 6, 4, 2, 1}) {
+        if (tables + per_warp * w > limit) continue;
+        int nb = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 32 * w, tables + per_warp * w);
+        if (e != cudaSuccess) return e;
+        if (nb * w > per_sm * warps) { warps = w; per_sm = nb; }
+    }
+    if (warps < 1 || per_sm < 1) return cudaErrorInvalidConfiguration;
+    const int block = 32 * warps;
+    const size_t smem = tables + per_warp * warps;
+    long long want = ((long long)a.ncell + warps - 1) / warps;
     long long grid = (long long)sm_count * per_sm;
     if (want < grid) grid = want;
     if (grid < 1) grid = 1;
     if (info) { info->grid = (int)grid; info->block = block; info->smem = (int)smem; info->blocks_per_sm = per_sm; }
     if (method == METHOD_RKF)
-        chem_warp_kernel<METHOD_RKF><<<(unsigned)grid, block, smem, stream>>>(a, csr_start, csr_rx, csr_nu, warp_doubles);
+        chem_warp_kernel<METHOD_RKF><<<(unsigned)grid, block, smem, stream>>>(a, t, warp_doubles);
     else
-        chem_warp_kernel<METHOD_ALPHA_QSS><<<(unsigned)grid, block, smem, stream>>>(a, csr_start, csr_rx, csr_nu,
-                                                                                     warp_doubles);
+        chem_warp_kernel<METHOD_ALPHA_QSS><<<(unsigned)grid, block, smem, stream>>>(a, t, warp_doubles);
     return cudaGetLastError();
 }
 

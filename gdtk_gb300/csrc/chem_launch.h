@@ -56,12 +56,30 @@ cudaError_t launch_chem_update(const ChemUpdateArgs& a, int method, int scratch_
                                cudaStream_t stream, LaunchInfo* info);
 cudaError_t launch_gas_service(const GasServiceArgs& a, int sm_count, cudaStream_t stream);
 // One warp per cell (mechanisms too large for the thread-per-cell kernels): the reference-order update with
-// species and reactions over the lanes.  csr_*: each species' (reaction, net coefficient) entries in
-// reaction order; warp_doubles = chem_warp_doubles(...), the shared-memory doubles of one warp.
+// species and reactions over the lanes.  Its tables (built by the host from the packed mechanism):
+//   ints [0, n_smem_ints), staged in shared memory by every block:
+//     [off_tstart + ir]  first concentration term of reaction ir (nr + 1 entries)
+//     [off_terms + k]    term k: species | coeff << 8 | (1 for a product) << 16; reactants first, each side
+//                        in the reaction's order
+//     [off_rxeff + ir]   efficiency list of reaction ir's third body, or -1
+//     [off_lane + l]     first gather entry of lane l (33 entries)
+//     [off_ent + k]      gather entry: species | reaction << 8 | (net coefficient + 128) << 24; a lane's
+//                        entries are whole species (balanced over the lanes by entry count), each species'
+//                        entries in ascending reaction order
+//   ints [off_efflen, ...) and doubles, read from global memory:
+//     [off_efflen + s]            length of efficiency list s
+//     [off_effidx + k*neff + s]   species of the k-th entry of list s (transposed: lanes read one list each)
+//     eff_val[k*neff + s]         its efficiency
+struct WarpTables {
+    const int* gi;
+    const double* eff_val;
+    int n_smem_ints;
+    int off_tstart, off_terms, off_rxeff, off_lane, off_ent, off_efflen, off_effidx;
+};
+// Shared-memory doubles of one warp's vectors.
 int chem_warp_doubles(int nsp, int nr, int neff, int method);
-cudaError_t launch_chem_update_warp(const ChemUpdateArgs& a, int method, const int* csr_start, const int* csr_rx,
-                                    const int* csr_nu, int warp_doubles, int sm_count, cudaStream_t stream,
-                                    LaunchInfo* info);
+cudaError_t launch_chem_update_warp(const ChemUpdateArgs& a, int method, const WarpTables& t, int warp_doubles,
+                                    int sm_count, cudaStream_t stream, LaunchInfo* info);
 // Cost buckets of the longest-first ordering: launch_bucket_order's hist scratch holds this many ints.
 constexpr int ORDER_BUCKETS = 256;
 

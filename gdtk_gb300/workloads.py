@@ -127,3 +127,27 @@ def h2air_mixing_layer(names, mol_masses, nx=2048, ny=1024, seed=4, thickness=16
     Y /= Y.sum(axis=1, keepdims=True)
     T = f * T_fuel + (1.0 - f) * T_ox
     return T, np.full(n, p), np.ascontiguousarray(Y.T)
+
+
+ACETYLENE_MIXTURE = {'C2H2': 0.02, 'O2': 0.025, 'Ar': 0.955}   # mole fractions, shock-tube mixture 25
+
+
+def acetylene_cells(names, mol_masses, n, seed=5, T_range=(1150.0, 1750.0), p_atm=0.6, share=(-6.0, -2.0)):
+    """Shock-tube ignition states of the 75-species C2H2/C2H4 mechanism (the reference's
+    examples/kinetics/acetylene-ignition-delay: the mixture above at 0.6 atm, 1150-1750 K).  Each
+    cell carries a 10^U[share] mass share of the other 72 species (Dirichlet(0.5)), standing for
+    cells at different stages of induction; T ~ U[T_range], p = p_atm atm.  Returns T, p, Y (nsp, n)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    M = np.asarray(mol_masses, dtype=np.float64)
+    x = np.zeros(len(names))
+    for s, v in ACETYLENE_MIXTURE.items():
+        x[names.index(s)] = v
+    y0 = x * M / (x * M).sum()
+    minor = [i for i, s in enumerate(names) if s not in ACETYLENE_MIXTURE]
+    Y = np.repeat(y0[None, :], n, axis=0)
+    w = 10.0 ** rng.uniform(share[0], share[1], n)
+    Y *= (1.0 - w)[:, None]
+    Y[:, minor] += w[:, None] * rng.dirichlet(np.full(len(minor), 0.5), n)
+    T = rng.uniform(T_range[0], T_range[1], n)
+    p = np.full(n, p_atm * 101325.0)
+    return T, p, np.ascontiguousarray(Y.T)
