@@ -268,52 +268,76 @@ void run_fast(ReactorObj& r, FastArgs& a, int flags, cudaStream_t s) {
 }
 
 // Tables of the warp-per-cell kernel (layout in chem_launch.h) from the packed mechanism: reaction terms
-// and third bodies, the species -> (reaction, net coefficient) gather with whole species dealt to the 32
-// lanes longest first, and the efficiency lists transposed.
+// and third bodies, scaled tick-rate slots for coefficients above 1, the q / L gather tasks dealt whole to
+// the 32 lanes longest first, and the efficiency lists transposed.
 void prepare_warp_path(ReactorObj& r, const PackedMech& pm) {
     r.large = pm.nsp > GDTK_MAX_SPECIES || pm.nr > GDTK_MAX_REACTIONS;
-    r.warp_doubles = chem_warp_doubles(pm.nsp, pm.nr, pm.neff, pm.method);
     MechView m;
     m.bind(pm.I.data(), pm.D.data());
     const int nsp = pm.nsp, nr = pm.nr, neff = pm.neff;
-    std::vector<int> tstart(nr + 1, 0), terms, rxeff(nr, -1);
-    std::vector<std::vector<std::pair<int, int>>> per(nsp);   // species -> (reaction, nu), ascending reaction
-    auto term = [&](int isp, int coeff, int product) {
-        if (isp < 0 || isp >= nsp || coeff < 0 || coeff > 255) throw std::runtime_error("reaction term out of range");
-        terms.push_back(isp | coeff << 8 | product << 16);
+    std::vector<int> tstart(nr + 1, 0), tmid(nr, 0), terms, rxeff(nr, -1), slot;
+    auto term = [&](int isp, int coeff) {
+        if (isp < 0 || isp >= nsp || coeff < 0 || coeff > 0xffffff) throw std::runtime_error("reaction term out of range");
+        terms.push_back(isp | coeff << 8);
     };
+    std::map<std::pair<int, int>, int> slot_of;   // (reaction, |nu|) -> slot
+    struct Entry { int ir, nu; };
+    std::vector<std::vector<Entry>> per(nsp);   // species -> (reaction, nu), ascending reaction
     for (int ir = 0; ir < nr; ++ir) {
         const int* x = m.rx(ir);
-        for (int k = 0; k < x[RX_NREAC]; ++k) term(x[RX_REAC_IDX + k], x[RX_REAC_COEFF + k], 0);
-        for (int k = 0; k < x[RX_NPROD]; ++k) term(x[RX_PROD_IDX + k], x[RX_PROD_COEFF + k], 1);
+        for (int k = 0; k < x[RX_NREAC]; ++k) term(x[RX_REAC_IDX + k], x[RX_REAC_COEFF + k]);
+        tmid[ir] = (int)terms.size();
+        for (int k = 0; k < x[RX_NPROD]; ++k) term(x[RX_PROD_IDX + k], x[RX_PROD_COEFF + k]);
         tstart[ir + 1] = (int)terms.size();
         if (x[RX_COLLIDER]) rxeff[ir] = x[RX_EFFSET];
-        for (int k = 0; k < x[RX_NPART]; ++k)
-            if (x[RX_PART_NU + k] != 0) per[x[RX_PART + k]].push_back({ir, x[RX_PART_NU + k]});
+        for (int k = 0; k < x[RX_NPART]; ++k) {
+            const int nu = x[RX_PART_NU + k];
+            if (nu == 0) continue;
+            const int a = nu < 0 ? -nu : nu;
+            if (a > 255) throw std::runtime_error("stoichiometric coefficient out of range");
+            if (a > 1 && !slot_of.count({ir, a})) {
+                slot_of[{ir, a}] = (int)slot.size();
+                slot.push_back(ir | a << 16);
+            }
+            per[x[RX_PART + k]].push_back({ir, nu});
+        }
     }
-    // longest species first onto the least-loaded lane (ties: lowest lane)
-    std::vector<int> order(nsp);
-    for (int i = 0; i < nsp; ++i) order[i] = i;
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return per[a].size() > per[b].size(); });
-    std::vector<std::vector<int>> lane_sp(32);
+    const int nslot = (int)slot.size();
+    // element of w_f[nr], w_b[nr], |nu| w_f[nslot], |nu| w_b[nslot] that a (reaction, nu) term adds to q or L:
+    // q gets nu w_f (nu > 0) or -nu w_b, L gets nu w_b (nu > 0) or -nu w_f (reaction_mechanism.d:82-96)
+    auto index = [&](const Entry& e, bool to_L) {
+        const int a = e.nu < 0 ? -e.nu : e.nu;
+        const bool use_b = (e.nu > 0) == to_L;
+        if (a == 1) return use_b ? nr + e.ir : e.ir;
+        const int j = slot_of[{e.ir, a}];
+        return 2 * nr + (use_b ? nslot : 0) + j;
+    };
+    if (2 * nr + 2 * nslot > 0x2000) throw std::runtime_error("too many tick-rate terms for the warp-per-cell gather");
+    // tasks: the q and the L of each species, longest first onto the least-loaded lane (ties: lowest lane)
+    std::vector<int> order(2 * nsp);
+    for (int t = 0; t < 2 * nsp; ++t) order[t] = t;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return per[a >> 1].size() > per[b >> 1].size(); });
+    std::vector<std::vector<int>> lane_tasks(32);
     std::vector<size_t> load(32, 0);
-    for (int isp : order) {
-        int l = (int)(std::min_element(load.begin(), load.end()) - load.begin());
-        lane_sp[l].push_back(isp);
-        load[l] += per[isp].size();
+    for (int t : order) {
+        if (per[t >> 1].empty()) continue;
+        const int l = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        lane_tasks[l].push_back(t);
+        load[l] += per[t >> 1].size();
     }
     std::vector<int> lane(33, 0), ent;
     for (int l = 0; l < 32; ++l) {
-        for (int isp : lane_sp[l])
-            for (auto& e : per[isp]) {
-                if (e.second < -127 || e.second > 127) throw std::runtime_error("stoichiometric coefficient out of range");
-                ent.push_back(isp | e.first << 8 | (e.second + 128) << 24);
-            }
+        for (int t : lane_tasks[l]) {
+            const int isp = t >> 1;
+            const bool to_L = t & 1;
+            for (auto& e : per[isp]) ent.push_back(isp | index(e, to_L) << 8 | (to_L ? 1 : 0) << 21);
+        }
         lane[l + 1] = (int)ent.size();
     }
     int maxlen = 0;
     for (int s = 0; s < neff; ++s) maxlen = std::max(maxlen, m.eff_i(s)[0]);
-    std::vector<int> efflen(std::max(neff, 1), 0), effidx((size_t)maxlen * neff, 0);
+    std::vector<int> efflen(std::max(neff, 1), 0), effidx(std::max((size_t)maxlen * neff, (size_t)1), 0);
     std::vector<double> effval(std::max((size_t)maxlen * neff, (size_t)1), 0.0);
     for (int s = 0; s < neff; ++s) {
         const int* ei = m.eff_i(s);
@@ -325,16 +349,24 @@ void prepare_warp_path(ReactorObj& r, const PackedMech& pm) {
         }
     }
     std::vector<int> all;
-    auto put = [&](const std::vector<int>& v) { int off = (int)all.size(); all.insert(all.end(), v.begin(), v.end()); return off; };
+    auto put = [&](const std::vector<int>& v) {
+        const int off = (int)all.size();
+        all.insert(all.end(), v.begin(), v.end());
+        return off;
+    };
     WarpTables& t = r.wt;
+    t.nslot = nslot;
     t.off_tstart = put(tstart);
+    t.off_tmid = put(tmid);
     t.off_terms = put(terms);
     t.off_rxeff = put(rxeff);
+    t.off_slot = put(slot);
     t.off_lane = put(lane);
     t.off_ent = put(ent);
     t.n_smem_ints = (int)all.size();
     t.off_efflen = put(efflen);
     t.off_effidx = put(effidx);
+    r.warp_doubles = chem_warp_doubles(nsp, nr, neff, pm.method, nslot);
     r.wt_i.ensure(all.size());
     r.wt_d.ensure(effval.size());
     check(cudaMemcpy(r.wt_i.p, all.data(), all.size() * sizeof(int), cudaMemcpyHostToDevice), "cudaMemcpy");

@@ -742,10 +742,11 @@ __global__ void order_scatter(const float* key, int n, int* hist, int* order) {
 constexpr unsigned FULL_MASK = 0xffffffffu;
 
 struct WarpLayout {
-    int y0, yout, q, L, mf, g, tmp, kf, kb, wf, wb, meff, ext, total;
-    __device__ __host__ void make(int nsp, int nr, int neff, int method) {
+    int y0, yout, q, L, mf, g, tmp, kf, kb, wf, wb, wsf, wsb, meff, ext, total;
+    __device__ __host__ void make(int nsp, int nr, int neff, int method, int nslot) {
         y0 = 0; yout = nsp; q = 2 * nsp; L = 3 * nsp; mf = 4 * nsp; g = 5 * nsp; tmp = 6 * nsp;
-        kf = 8 * nsp; kb = kf + nr; wf = kb + nr; wb = wf + nr; meff = wb + nr;
+        kf = 8 * nsp; kb = kf + nr; wf = kb + nr; wb = wf + nr; wsf = wb + nr; wsb = wsf + nslot;
+        meff = wsb + nslot;
         ext = meff + (neff > 0 ? neff : 1);
         total = ext + (method == METHOD_RKF ? 7 * nsp : 4 * nsp);
     }
@@ -753,11 +754,16 @@ struct WarpLayout {
 
 struct WarpCtx {
     MechView m;
-    const int* tstart;      // shared: reaction ir's terms tstart[ir] .. tstart[ir + 1]
-    const int* terms;       // shared: species | coeff << 8 | product << 16
+    const int* tstart;      // shared: reaction ir's terms tstart[ir] .. tstart[ir + 1], products from tmid[ir]
+    const int* tmid;
+    const int* terms;       // shared: species | coeff << 8
     const int* rxeff;       // shared: third-body efficiency list of each reaction, or -1
+    const int* slot;        // shared: reaction | |nu| << 16 of each scaled tick-rate slot
+    int nslot;
+    double* wsf;            // the warp's |nu| w_f and |nu| w_b of each slot
+    double* wsb;
     int ent_lo, ent_hi;     // this lane's gather entries
-    const int* ent;         // shared: species | reaction << 8 | (nu + 128) << 24
+    const int* ent;         // shared: species | index << 8 | L << 21 | source << 22
     const int* efflen;      // global: length of each efficiency list
     const int* effidx;      // global, [k][neff]: species of entry k of each list
     const double* effval;   // global, [k][neff]: its efficiency
@@ -839,36 +845,35 @@ __device__ void w_split_rates(const WarpCtx& w, const double* c, double* q, doub
         double f = kf[ir], b = kb[ir];
         const int e = w.rxeff[ir];
         if (e >= 0) { const double t = meff[e]; f = f * t; b = b * t; }
-        const int k1 = w.tstart[ir + 1];
-        for (int k = w.tstart[ir]; k < k1; ++k) {
-            const int t = w.terms[k];
-            const double v = ipow(c[t & 0xff], (t >> 8) & 0xff);
-            if (t >> 16) b *= v;
-            else f *= v;
-        }
+        const int k0 = w.tstart[ir], km = w.tmid[ir], k1 = w.tstart[ir + 1];
+        for (int k = k0; k < km; ++k) f *= ipow(c[w.terms[k] & 0xff], w.terms[k] >> 8);
+        for (int k = km; k < k1; ++k) b *= ipow(c[w.terms[k] & 0xff], w.terms[k] >> 8);
         wf[ir] = f;
         wb[ir] = b;
     }
     __syncwarp();
-    // q, L of this lane's species; a coefficient of +-1 needs no multiplication (1 * x == x)
+    for (int j = w.lane; j < w.nslot; j += 32) {   // (double)nu * w, as the reference forms it
+        const int sl = w.slot[j], ir = sl & 0xffff;
+        const double nu = (double)(sl >> 16);
+        w.wsf[j] = nu * wf[ir];
+        w.wsb[j] = nu * wb[ir];
+    }
+    __syncwarp();
+    // q, L: each of this lane's tasks adds its terms in reaction order from 0 (reaction_mechanism.d:82-96);
+    // an entry's index runs over w_f, w_b and the slots' |nu| w_f, |nu| w_b, which lie end to end
     int cur = -1;
-    double qs = 0.0, Ls = 0.0;
+    double sum = 0.0;
     for (int k = w.ent_lo; k < w.ent_hi; ++k) {
         const int e = w.ent[k];
-        const int isp = e & 0xff, ir = (e >> 8) & 0xffff, nu = ((e >> 24) & 0xff) - 128;
-        if (isp != cur) {
-            if (cur >= 0) { q[cur] = qs; L[cur] = Ls; }
-            cur = isp;
-            qs = 0.0;
-            Ls = 0.0;
+        const int key = e & 0x2000ff;   // species and the q / L bit
+        if (key != cur) {
+            if (cur >= 0) ((cur >> 21) ? L : q)[cur & 0xff] = sum;
+            cur = key;
+            sum = 0.0;
         }
-        const double f = wf[ir], b = wb[ir];
-        if (nu == 1) { qs += f; Ls += b; }
-        else if (nu == -1) { qs += b; Ls += f; }
-        else if (nu > 0) { qs += nu * f; Ls += nu * b; }
-        else { qs += -nu * b; Ls += -nu * f; }
+        sum += wf[(e >> 8) & 0x1fff];
     }
-    if (cur >= 0) { q[cur] = qs; L[cur] = Ls; }
+    if (cur >= 0) ((cur >> 21) ? L : q)[cur & 0xff] = sum;
     __syncwarp();
 }
 
@@ -1085,8 +1090,11 @@ __global__ void __launch_bounds__(512) chem_warp_kernel(ChemUpdateArgs a, WarpTa
     w.m.bind(a.mech_i, a.mech_d);
     w.lane = threadIdx.x & 31;
     w.tstart = ti + tb.off_tstart;
+    w.tmid = ti + tb.off_tmid;
     w.terms = ti + tb.off_terms;
     w.rxeff = ti + tb.off_rxeff;
+    w.slot = ti + tb.off_slot;
+    w.nslot = tb.nslot;
     w.ent = ti + tb.off_ent;
     w.ent_lo = ti[tb.off_lane + w.lane];
     w.ent_hi = ti[tb.off_lane + w.lane + 1];
@@ -1095,8 +1103,10 @@ __global__ void __launch_bounds__(512) chem_warp_kernel(ChemUpdateArgs a, WarpTa
     w.effval = tb.eff_val;
     const MechView& m = w.m;
     WarpLayout lay;
-    lay.make(m.nsp, m.nr, m.neff, METHOD);
+    lay.make(m.nsp, m.nr, m.neff, METHOD, tb.nslot);
     double* S = smem_w + (tb.n_smem_ints + 1) / 2 + (size_t)(threadIdx.x >> 5) * warp_doubles;
+    w.wsf = S + lay.wsf;
+    w.wsb = S + lay.wsb;
     double *y0 = S + lay.y0, *yout = S + lay.yout, *q = S + lay.q, *L = S + lay.L, *mf = S + lay.mf, *g = S + lay.g,
            *tmp = S + lay.tmp, *kf = S + lay.kf, *kb = S + lay.kb, *wf = S + lay.wf, *wb = S + lay.wb,
            *meff = S + lay.meff, *ext = S + lay.ext;
@@ -1279,9 +1289,9 @@ cudaError_t launch_bucket_order(const float* key, int n, int* order, int* hist, 
 
 // ---------------------------------------------------------------- host-side launchers
 
-int chem_warp_doubles(int nsp, int nr, int neff, int method) {
+int chem_warp_doubles(int nsp, int nr, int neff, int method, int nslot) {
     WarpLayout l;
-    l.make(nsp, nr, neff, method);
+    l.make(nsp, nr, neff, method, nslot);
     return l.total;
 }
 

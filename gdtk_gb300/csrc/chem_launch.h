@@ -59,13 +59,15 @@ cudaError_t launch_gas_service(const GasServiceArgs& a, int sm_count, cudaStream
 // species and reactions over the lanes.  Its tables (built by the host from the packed mechanism):
 //   ints [0, n_smem_ints), staged in shared memory by every block:
 //     [off_tstart + ir]  first concentration term of reaction ir (nr + 1 entries)
-//     [off_terms + k]    term k: species | coeff << 8 | (1 for a product) << 16; reactants first, each side
-//                        in the reaction's order
+//     [off_tmid + ir]    first product term of reaction ir
+//     [off_terms + k]    term k: species | coeff << 8; reactants, then products, each in the reaction's order
 //     [off_rxeff + ir]   efficiency list of reaction ir's third body, or -1
+//     [off_slot + j]     scaled tick-rate slot j: reaction | |nu| << 16, for each (reaction, |nu| >= 2) pair
 //     [off_lane + l]     first gather entry of lane l (33 entries)
-//     [off_ent + k]      gather entry: species | reaction << 8 | (net coefficient + 128) << 24; a lane's
-//                        entries are whole species (balanced over the lanes by entry count), each species'
-//                        entries in ascending reaction order
+//     [off_ent + k]      gather entry: species | index << 8 | (1 for L) << 21, adding element `index` of
+//                        the warp's w_f[nr], w_b[nr], |nu| w_f[nslot], |nu| w_b[nslot] (end to end) to q or
+//                        L of the species.  The tasks (one species' q, or its L) are dealt whole to the
+//                        lanes, longest first; a task's entries are in ascending reaction order
 //   ints [off_efflen, ...) and doubles, read from global memory:
 //     [off_efflen + s]            length of efficiency list s
 //     [off_effidx + k*neff + s]   species of the k-th entry of list s (transposed: lanes read one list each)
@@ -73,11 +75,11 @@ cudaError_t launch_gas_service(const GasServiceArgs& a, int sm_count, cudaStream
 struct WarpTables {
     const int* gi;
     const double* eff_val;
-    int n_smem_ints;
-    int off_tstart, off_terms, off_rxeff, off_lane, off_ent, off_efflen, off_effidx;
+    int n_smem_ints, nslot;
+    int off_tstart, off_tmid, off_terms, off_rxeff, off_slot, off_lane, off_ent, off_efflen, off_effidx;
 };
 // Shared-memory doubles of one warp's vectors.
-int chem_warp_doubles(int nsp, int nr, int neff, int method);
+int chem_warp_doubles(int nsp, int nr, int neff, int method, int nslot);
 cudaError_t launch_chem_update_warp(const ChemUpdateArgs& a, int method, const WarpTables& t, int warp_doubles,
                                     int sm_count, cudaStream_t stream, LaunchInfo* info);
 // Cost buckets of the longest-first ordering: launch_bucket_order's hist scratch holds this many ints.
