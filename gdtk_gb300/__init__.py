@@ -134,6 +134,7 @@ SIGNATURES = {
     "gdtk_mlp_gemm": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _v, ctypes.c_int, ctypes.c_int, _v,
                                      ctypes.c_int, ctypes.c_int, _v, ctypes.c_int, _v, _v, _v, ctypes.c_int,
                                      ctypes.c_int, _v]),
+    "gdtk_mlp_tcgen05": (ctypes.c_int, [ctypes.c_int, _v, _v]),
 }
 
 

@@ -24,6 +24,7 @@ SOURCES = [
     ("fp64_probe.cu", []),
     ("noalloc.cu", []),
     ("mlp_kernels.cu", []),
+    ("mlp_tcgen05.cu", []),
     ("surrogate_kernels.cu", []),
     ("surrogate.cpp", []),
     ("chem_api.cpp", []),

@@ -364,6 +364,10 @@ bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
 
 cudaError_t launch_gemm_bf16(const GemmArgs& g, cudaStream_t s) {
     if (g.M <= 0 || g.N <= 0 || g.K <= 0) return cudaSuccess;
+    if (tcgen05_gemm_eligible(g)) {   // the forward shapes: fifth-generation tensor cores
+        const cudaError_t e = launch_gemm_bf16_tcgen05(g, s);
+        if (e != cudaErrorNotSupported) return e;
+    }
     // 16-byte chunks along the contiguous dimension of each operand
     const int a_inner = g.trans_a ? g.M : g.K, b_inner = g.trans_b ? g.K : g.N;
     if (g.K % 8 || a_inner % 8 || b_inner % 8 || g.lda % 8 || g.ldb % 8 || !aligned16(g.A) || !aligned16(g.B))

@@ -35,6 +35,17 @@ struct GemmArgs {
 };
 
 cudaError_t launch_gemm_bf16(const GemmArgs& g, cudaStream_t s);
+
+// The tcgen05 (TMEM-accumulator) form, mlp_tcgen05.cu: taken by launch_gemm_bf16 for D = A W^T (+ bias)
+// (GELU) with A [M][K] and W [N][K] K-contiguous, K and N multiples of 16 in 16..256, alpha 1, beta 0,
+// no split; cudaErrorNotSupported when those do not hold or it is switched off (GDTK_MLP_TCGEN05=0 in the
+// environment, or tcgen05_gemm_set(0)).
+bool tcgen05_gemm_eligible(const GemmArgs& g);
+bool tcgen05_gemm_enabled();
+int tcgen05_gemm_set(int enable);                   // -1 leaves it; returns the previous setting
+unsigned long long tcgen05_gemm_launches();         // launches so far in this process
+cudaError_t tcgen05_gemm_error(int* error);         // 1/2: a load/MMA wait gave up (read and cleared)
+cudaError_t launch_gemm_bf16_tcgen05(const GemmArgs& g, cudaStream_t s);
 cudaError_t launch_column_sum(int M, int N, const float* x, float* partial, float* out, cudaStream_t s);
 cudaError_t launch_mse_grad(int M, int N, const float* pred, const float* y, const float* w, float* grad,
                             __nv_bfloat16* gradh, float* loss_sum, cudaStream_t s);

@@ -815,6 +815,15 @@ int chem_surrogate_set_error_gate(int sg, double tol) {
     });
 }
 
+int gdtk_mlp_tcgen05(int enable, unsigned long long* launches, int* error) {
+    return guard([&] {
+        const int prev = tcgen05_gemm_set(enable);
+        if (launches) *launches = tcgen05_gemm_launches();
+        if (error) ck(tcgen05_gemm_error(error), "gdtk_mlp_tcgen05");
+        return prev;
+    });
+}
+
 int gdtk_mlp_gemm(int M, int N, int K, const void* A, int lda, int trans_a, const void* B, int ldb, int trans_b,
                   const float* bias, int act, float* pre, float* D, void* Dh, int ldd, int splits, void* stream) {
     return guard([&] {

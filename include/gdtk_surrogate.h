@@ -133,6 +133,13 @@ int chem_surrogate_set_error_gate(int sg, double tol);
  * D (fp32) and Dh (bf16) may each be NULL; splits > 1 splits K (no bias or act then). */
 int gdtk_mlp_gemm(int M, int N, int K, const void* A, int lda, int trans_a, const void* B, int ldb, int trans_b,
                   const float* bias, int act, float* pre, float* D, void* Dh, int ldd, int splits, void* stream);
+/* The tcgen05 form of that GEMM (the network's forward shapes: A [M][K] and B stored [N][K], K and N
+ * multiples of 16 up to 256, no split): enable 1 uses it where it applies, 0 uses the mma.sync kernel
+ * everywhere, -1 leaves the setting (initially off only with GDTK_MLP_TCGEN05=0 in the environment).
+ * Returns the previous setting; *launches (if not NULL) receives the tcgen05 launches so far and *error
+ * (if not NULL, synchronising) the kernel's error flag, then cleared: 0, or 1 / 2 when a wait for its
+ * loads / its MMAs gave up. */
+int gdtk_mlp_tcgen05(int enable, unsigned long long* launches, int* error);
 
 #ifdef __cplusplus
 }
