@@ -50,6 +50,9 @@ WORKLOADS = {
     # large mechanism: the reference's 75-species, 474-reaction C2H2/C2H4 model (alpha-QSS, one warp per
     # cell) on shock-tube ignition states of its acetylene example, dt = 1e-6 s
     "c2h2-262144": dict(gas="c2h2-gas.lua", chem="c2h2-chem.lua", n=262144, dt=1.0e-6, kind="c2h2", seed=5),
+    # the surrogate network's forward layer alone: D = GELU(A W^T + b) over 1,048,576 rows, K = N = 256, BF16
+    # in and out, tcgen05 (TMEM) kernel against the mma.sync kernel on the same operands
+    "mlp-gemm-1M": dict(gas="j92-gas.lua", chem="j92-chem.lua", n=1048576, dt=0.0, kind="gemm", seed=6, K=256, N=256),
     "h2air-surrogate": dict(gas="j92-gas.lua", chem="j92-chem.lua", n=4194304, dt=1.0e-6, kind="surrogate",
                             seed=3, train_samples=16777216, epochs=30, batch=8192, error_epochs=8),
 }
@@ -557,6 +560,89 @@ def surrogate_leg(rc, srho, su, sT, sp, sY, dt, plain_ms, plain_T, plain_Y, plai
     }
 
 
+def run_gemm(args, w):
+    """The surrogate's forward layer on the tensor cores: tcgen05 kernel and mma.sync kernel, CUDA-event
+    timed over `steps` launches each (inputs and outputs 512 MB each, larger than L2)."""
+    import ctypes
+    import torch
+    import gdtk_gb300
+    from gdtk_gb300 import lib, check
+    gdtk_gb300.lib()
+    M, N, K = w["n"], w["N"], w["K"]
+    g = torch.Generator(device="cuda")
+    g.manual_seed(w["seed"])
+    A = torch.randn((M, K), generator=g, device="cuda").to(torch.bfloat16)
+    W = (torch.randn((N, K), generator=g, device="cuda") / 16.0).to(torch.bfloat16)
+    b = torch.randn(N, generator=g, device="cuda")
+    Dh = torch.empty((M, N), device="cuda", dtype=torch.bfloat16)
+    stream = torch.cuda.current_stream()
+    ptr = lambda t: ctypes.c_void_p(t.data_ptr())
+
+    def launch():
+        check(lib().gdtk_mlp_gemm(M, N, K, ptr(A), K, 0, ptr(W), K, 1, ptr(b), 1, None, None, ptr(Dh), N, 1,
+                                  ctypes.c_void_p(stream.cuda_stream)), "gdtk_mlp_gemm")
+
+    reps = 100   # launches per step: one launch is a fraction of a millisecond
+
+    def timed(tc):
+        lib().gdtk_mlp_tcgen05(1 if tc else 0, None, None)
+        for _ in range(args.warmup):
+            launch()
+        torch.cuda.synchronize()
+        n0 = ctypes.c_ulonglong()
+        lib().gdtk_mlp_tcgen05(-1, ctypes.byref(n0), None)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps * reps):
+            launch()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        n1, err = ctypes.c_ulonglong(), ctypes.c_int()
+        lib().gdtk_mlp_tcgen05(-1, ctypes.byref(n1), ctypes.byref(err))
+        if err.value:
+            raise RuntimeError("a tcgen05 wait gave up (%d)" % err.value)
+        return e0.elapsed_time(e1) / (args.steps * reps), n1.value - n0.value, Dh.clone()
+
+    clocks = ClockSampler(int(os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] or 0))
+    clocks.start()
+    ms_tc, n_tc, out_tc = timed(True)
+    clk = clocks.stop()
+    ms_ms, n_ms, out_ms = timed(False)
+    lib().gdtk_mlp_tcgen05(1, None, None)
+    if n_tc != args.steps * reps or n_ms != 0:
+        raise RuntimeError("unexpected kernel path (%d tcgen05 launches of %d)" % (n_tc, args.steps * reps))
+    diff = (out_tc.float() - out_ms.float()).abs().max().item()
+    flops = 2.0 * M * N * K
+    traffic = float(M * K * 2 + N * K * 2 + M * N * 2)
+    peaks = {}
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        with open(pk) as f:
+            peaks = json.load(f)
+    tf_peak = peaks.get("bf16_tflops", 1900.0)
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    tf = flops / (ms_tc * 1e-3) / 1e12
+    gbs = traffic / (ms_tc * 1e-3) / 1e9
+    return {
+        "metric": "BF16 GEMM + bias + GELU TFLOP/s (surrogate forward layer), 1 GB300", "value": tf,
+        "unit": "TFLOP/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_tc * reps,
+        "ms_per_launch": ms_tc, "launches_per_step": reps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+        "config": {"workload": args.workload, "M": M, "N": N, "K": K, "act": "gelu", "out": "bf16",
+                   "l2": "inputs and outputs larger than L2 (512 MB each, no flush)",
+                   "kernel": "gemm_tc_kernel: TMA loads, tcgen05.mma M=128 into TMEM, tcgen05.ld epilogue"},
+        # K = N = 256 puts the layer below the ridge point (128 FLOP per byte): HBM bounds it
+        "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
+                     "traffic": None, "algorithmic_bytes_per_launch": traffic,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)",
+                     "tensor": {"achieved": tf, "peak": tf_peak, "unit": "TFLOP/s", "frac": tf / tf_peak,
+                                "peak_source": "MEASURED_PEAKS.json bf16_tflops (measured, burst)"}},
+        "mma_sync": {"value": flops / (ms_ms * 1e-3) / 1e12, "unit": "TFLOP/s", "ms_per_launch": ms_ms,
+                     "speedup_of_tcgen05": ms_ms / ms_tc, "max_abs_diff_bf16_out": diff},
+        "cpu_baseline": None, "e2e": None, "clocks": clk, "gpu_launches": args.steps * reps,
+    }
+
+
 def run_surrogate(args, w):
     """Surrogate + FP64 fallback against the plain FP64 update on fresh cells (returns the JSON line)."""
     import torch
@@ -741,6 +827,15 @@ def main():
                                   "baseline inside the gdtk line"}))
             return 0
         print(json.dumps(run_layer(args, w)))
+        return 0
+
+    if w["kind"] == "gemm":
+        if args.impl == "reference" or rank != 0:
+            if args.impl == "reference" and rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable": "the surrogate network has no counterpart "
+                                  "in the reference"}))
+            return 0
+        print(json.dumps(run_gemm(args, w)))
         return 0
 
     if w["kind"] == "surrogate":
