@@ -28,7 +28,8 @@ namespace gdtk {
 namespace {
 
 constexpr int TC_M = 128;                           // rows per tile = TMEM lanes
-constexpr int TC_THREADS = 128;
+constexpr int EPI_WARPS = 16;                       // epilogue warps: 4 lane quarters x 4 column slices
+constexpr int TC_THREADS = 32 * (1 + EPI_WARPS);
 constexpr unsigned long long SPIN_LIMIT = 1ull << 22;   // mbarrier polls before a wait gives up
 
 __device__ int g_tc_error;
@@ -125,23 +126,42 @@ __device__ __forceinline__ float gelu_tc(float x) {   // tanh form, as the mma.s
     return 0.5f * x * (1.0f + tanhf(c * (x + 0.044715f * x * x * x)));
 }
 
+__device__ __forceinline__ void mbar_arrive(unsigned long long* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Warp 0 (one lane) loads and issues the MMAs; warps 1..EPI_WARPS drain the accumulators.  Two TMEM
+// accumulators alternate between tiles, so that the MMAs of tile i+1 (and the load of its A) run while
+// the epilogue warps drain tile i.  Epilogue warp w reads TMEM lanes 32 (w % 4) .. + 31 (the lanes a warp
+// may access) and the column slice (w - 1) / 4 of EPI_WARPS / 4 slices.
+// Barriers: load (A tile, + W the first time), full[b] (tcgen05.commit of accumulator b), empty[b]
+// (every epilogue warp has read accumulator b).
 __global__ void __launch_bounds__(TC_THREADS, 1)
     gemm_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmW, const TcArgs g) {
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char* sA = smem;
     unsigned char* sW = smem + g.a_bytes;
-    unsigned long long* bars = reinterpret_cast<unsigned long long*>(smem + g.a_bytes + g.w_bytes);   // load, mma
-    unsigned* tmem_slot = reinterpret_cast<unsigned*>(bars + 2);
+    unsigned long long* bars = reinterpret_cast<unsigned long long*>(smem + g.a_bytes + g.w_bytes);
+    unsigned long long* bar_load = bars;
+    unsigned long long* bar_full = bars + 1;    // [2]
+    unsigned long long* bar_empty = bars + 3;   // [2]
+    unsigned* tmem_slot = reinterpret_cast<unsigned*>(bars + 5);
+    int* s_state = reinterpret_cast<int*>(tmem_slot + 1);   // [0] failed, [1] commits issued
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     if (threadIdx.x == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
+        mbar_init(bar_load, 1);
+        mbar_init(&bar_full[0], 1);
+        mbar_init(&bar_full[1], 1);
+        mbar_init(&bar_empty[0], EPI_WARPS);
+        mbar_init(&bar_empty[1], EPI_WARPS);
+        s_state[0] = 0;
+        s_state[1] = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                     "r"(g.tmem_cols)
+                     "r"(2 * g.tmem_cols)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -149,83 +169,105 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     __syncthreads();
     tc_fence_after();
     const unsigned tmem = *tmem_slot;
-
-    // instruction descriptor: FP32 accumulator, BF16 A and B, both K-major, N >> 3, M >> 4
-    const unsigned idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(g.N >> 3) << 17) | ((unsigned)(TC_M >> 4) << 24);
-    const unsigned a_lbo = TC_M * 16, w_lbo = (unsigned)g.N * 16;   // bytes between K-groups of core matrices
-    const int kgroups = g.K / 8;
     const int ntiles = (g.M + TC_M - 1) / TC_M;
-    unsigned ph_load = 0, ph_mma = 0;
-    int failed = 0;   // 1: a load wait gave up, 2: an MMA wait gave up
-    bool first = true;
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        if (threadIdx.x == 0) {
-            mbar_expect_tx(&bars[0], (unsigned)(g.a_bytes + (first ? g.w_bytes : 0)));
-            for (int kg = 0; kg < kgroups; ++kg) tma_load_2d(sA + kg * a_lbo, &tmA, kg * 8, tile * TC_M, &bars[0]);
-            if (first)
-                for (int kg = 0; kg < kgroups; ++kg) tma_load_2d(sW + kg * w_lbo, &tmW, kg * 8, 0, &bars[0]);
-        }
-        first = false;
-        if (__syncthreads_or(!mbar_wait(&bars[0], ph_load))) { failed = 1; break; }
-        ph_load ^= 1;
-        if (threadIdx.x == 0) {
-            tc_fence_after();
-            for (int ks = 0; ks < g.K / 16; ++ks) {   // one K = 16 step covers two K-groups
-                const unsigned long long ad = smem_desc(smem_u32(sA) + 2u * ks * a_lbo, a_lbo, 128);
-                const unsigned long long bd = smem_desc(smem_u32(sW) + 2u * ks * w_lbo, w_lbo, 128);
-                mma_bf16(tmem, ad, bd, idesc, ks > 0 ? 1u : 0u);
+    const int my_tiles = blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            // instruction descriptor: FP32 accumulator, BF16 A and B, both K-major, N >> 3, M >> 4
+            const unsigned idesc =
+                (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(g.N >> 3) << 17) | ((unsigned)(TC_M >> 4) << 24);
+            const unsigned a_lbo = TC_M * 16, w_lbo = (unsigned)g.N * 16;   // bytes between K-groups
+            const int kgroups = g.K / 8;
+            int failed = 0, commits = 0;
+            unsigned load_parity = 0;
+            for (int i = 0; i < my_tiles && !failed; ++i) {
+                const int tile = blockIdx.x + i * gridDim.x, b = i & 1;
+                // A is free once the previous tile's MMAs are done (its commit)
+                if (i > 0 && !mbar_wait(&bar_full[(i - 1) & 1], ((i - 1) >> 1) & 1)) { failed = 2; break; }
+                mbar_expect_tx(bar_load, (unsigned)(g.a_bytes + (i == 0 ? g.w_bytes : 0)));
+                for (int kg = 0; kg < kgroups; ++kg) tma_load_2d(sA + kg * a_lbo, &tmA, kg * 8, tile * TC_M, bar_load);
+                if (i == 0)
+                    for (int kg = 0; kg < kgroups; ++kg) tma_load_2d(sW + kg * w_lbo, &tmW, kg * 8, 0, bar_load);
+                load_parity = i & 1;
+                if (!mbar_wait(bar_load, load_parity)) { failed = 1; break; }
+                // accumulator b is free once the epilogue has drained its previous tile
+                if (i >= 2 && !mbar_wait(&bar_empty[b], ((i >> 1) - 1) & 1)) { failed = 3; break; }
+                tc_fence_after();
+                const unsigned acc = tmem + (unsigned)b * g.tmem_cols;
+                for (int ks = 0; ks < g.K / 16; ++ks) {   // one K = 16 step covers two K-groups
+                    const unsigned long long ad = smem_desc(smem_u32(sA) + 2u * ks * a_lbo, a_lbo, 128);
+                    const unsigned long long bd = smem_desc(smem_u32(sW) + 2u * ks * w_lbo, w_lbo, 128);
+                    mma_bf16(acc, ad, bd, idesc, ks > 0 ? 1u : 0u);
+                }
+                mma_commit(&bar_full[b]);
+                ++commits;
             }
-            mma_commit(&bars[1]);
+            s_state[1] = commits;
+            if (failed) {
+                atomicExch(&g_tc_error, failed);
+                s_state[0] = 1;
+                if (failed == 1) mbar_wait(bar_load, load_parity);   // bounded: the loads still in flight
+            }
         }
-        if (__syncthreads_or(!mbar_wait(&bars[1], ph_mma))) { failed = 2; break; }
-        ph_mma ^= 1;
-        tc_fence_after();
-        const int row = tile * TC_M + warp * 32 + lane;
-        const unsigned trow = tmem + ((unsigned)(warp * 32) << 16);
-        for (int c = 0; c < g.N; c += 16) {
-            float v[16];
-            tmem_ld16(trow + (unsigned)c, v);
-            if (row < g.M) {
-                const size_t o = (size_t)row * g.ldd + c;
+    } else if (warp <= EPI_WARPS) {
+        const int quarter = warp & 3, slice = (warp - 1) >> 2, slices = EPI_WARPS / 4;
+        const int chunks = g.N / 16;   // 16-column chunks; this warp's are [slice, slice + 1) x chunks / slices
+        const int c0 = 16 * (slice * chunks / slices), c1 = 16 * ((slice + 1) * chunks / slices);
+        for (int i = 0; i < my_tiles; ++i) {
+            const int tile = blockIdx.x + i * gridDim.x, b = i & 1;
+            if (!mbar_wait(&bar_full[b], (i >> 1) & 1)) {
+                if (lane == 0) atomicExch(&g_tc_error, 4);
+                break;
+            }
+            tc_fence_after();
+            const int row = tile * TC_M + quarter * 32 + lane;
+            const unsigned trow = tmem + (unsigned)b * g.tmem_cols + ((unsigned)(quarter * 32) << 16);
+            for (int c = c0; c < c1; c += 16) {
+                float v[16];
+                tmem_ld16(trow + (unsigned)c, v);
+                if (row < g.M) {
+                    const size_t o = (size_t)row * g.ldd + c;
 #pragma unroll
-                for (int i = 0; i < 16; ++i) {
-                    if (g.bias) v[i] += g.bias[c + i];
-                    if (g.act == ACT_GELU) {
-                        if (g.pre) g.pre[o + i] = v[i];
-                        v[i] = gelu_tc(v[i]);
+                    for (int k = 0; k < 16; ++k) {
+                        if (g.bias) v[k] += __ldg(g.bias + c + k);
+                        if (g.act == ACT_GELU) {
+                            if (g.pre) g.pre[o + k] = v[k];
+                            v[k] = gelu_tc(v[k]);
+                        }
+                    }
+                    if (g.D) {
+                        float4* d4 = reinterpret_cast<float4*>(g.D + o);
+#pragma unroll
+                        for (int q = 0; q < 4; ++q)
+                            d4[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+                    }
+                    if (g.Dh) {
+                        __align__(16) __nv_bfloat16 h[16];
+#pragma unroll
+                        for (int k = 0; k < 16; ++k) h[k] = __float2bfloat16(v[k]);
+                        uint4* d = reinterpret_cast<uint4*>(g.Dh + o);
+                        d[0] = reinterpret_cast<const uint4*>(h)[0];
+                        d[1] = reinterpret_cast<const uint4*>(h)[1];
                     }
                 }
-                if (g.D) {
-                    float4* d4 = reinterpret_cast<float4*>(g.D + o);
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) d4[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
-                }
-                if (g.Dh) {
-                    __align__(16) __nv_bfloat16 h[16];
-#pragma unroll
-                    for (int i = 0; i < 16; ++i) h[i] = __float2bfloat16(v[i]);
-                    uint4* d = reinterpret_cast<uint4*>(g.Dh + o);
-                    d[0] = reinterpret_cast<const uint4*>(h)[0];
-                    d[1] = reinterpret_cast<const uint4*>(h)[1];
-                }
             }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&bar_empty[b]);
         }
-        tc_fence_before();
-        __syncthreads();
     }
-    if (failed) {
-        if (threadIdx.x == 0) {
-            atomicExch(&g_tc_error, failed);
-            // a second bounded wait for what is still in flight (the loads or the MMAs) before TMEM is freed
-            mbar_wait(&bars[failed == 1 ? 0 : 1], failed == 1 ? ph_load : ph_mma);
-        }
-        tc_fence_before();
-        __syncthreads();
-        tc_fence_after();
+    __syncthreads();
+    if (s_state[0] && threadIdx.x == 0 && s_state[1] > 0) {   // bounded wait for the last commit before freeing TMEM
+        const int last = s_state[1] - 1;
+        mbar_wait(&bar_full[last & 1], (last >> 1) & 1);
     }
+    tc_fence_before();
+    __syncthreads();
     tc_fence_after();
     if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(g.tmem_cols) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * g.tmem_cols)
+                     : "memory");
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
