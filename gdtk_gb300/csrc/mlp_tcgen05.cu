@@ -107,18 +107,26 @@ __device__ __forceinline__ void mma_commit(unsigned long long* bar) {
                  : "memory");
 }
 
-// 16 consecutive FP32 columns of this thread's TMEM lane
-__device__ __forceinline__ void tmem_ld16(unsigned taddr, float (&v)[16]) {
-    unsigned r[16];
+// Starts loading 16 consecutive FP32 columns of this thread's TMEM lane; the values are valid after
+// tmem_ld_wait.
+__device__ __forceinline__ void tmem_ld16(unsigned taddr, unsigned (&r)[16]) {
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
         "%15}, [%16];"
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
           "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
         : "r"(taddr));
+}
+
+// Waits for this thread's TMEM loads; the empty statements after it make every later use of r depend on
+// the wait.
+template <int Q>
+__device__ __forceinline__ void tmem_ld_wait(unsigned (&r)[Q][16]) {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+    for (int q = 0; q < Q; ++q)
+#pragma unroll
+        for (int i = 0; i < 16; ++i) asm volatile("" : "+r"(r[q][i])::"memory");
 }
 
 __device__ __forceinline__ float gelu_tc(float x) {   // tanh form, as the mma.sync kernel's epilogue
@@ -147,7 +155,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     unsigned long long* bar_empty = bars + 3;   // [2]
     unsigned* tmem_slot = reinterpret_cast<unsigned*>(bars + 5);
     int* s_state = reinterpret_cast<int*>(tmem_slot + 1);   // [0] failed, [1] commits issued
+    float* s_bias = reinterpret_cast<float*>(bars + 8);       // [N]
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int k = threadIdx.x; k < g.N; k += blockDim.x) s_bias[k] = g.bias ? g.bias[k] : 0.f;
 
     if (threadIdx.x == 0) {
         mbar_init(bar_load, 1);
@@ -223,14 +233,22 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             tc_fence_after();
             const int row = tile * TC_M + quarter * 32 + lane;
             const unsigned trow = tmem + (unsigned)b * g.tmem_cols + ((unsigned)(quarter * 32) << 16);
-            for (int c = c0; c < c1; c += 16) {
-                float v[16];
-                tmem_ld16(trow + (unsigned)c, v);
-                if (row < g.M) {
+            const int nq = (c1 - c0) >> 4;   // at most 4: N <= 256 over 4 column slices
+            unsigned r[4][16];
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                if (q < nq) tmem_ld16(trow + (unsigned)(c0 + 16 * q), r[q]);
+            tmem_ld_wait<4>(r);
+            if (row < g.M) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    if (q >= nq) break;
+                    const int c = c0 + 16 * q;
                     const size_t o = (size_t)row * g.ldd + c;
+                    float v[16];
 #pragma unroll
                     for (int k = 0; k < 16; ++k) {
-                        if (g.bias) v[k] += __ldg(g.bias + c + k);
+                        v[k] = __uint_as_float(r[q][k]) + s_bias[c + k];
                         if (g.act == ACT_GELU) {
                             if (g.pre) g.pre[o + k] = v[k];
                             v[k] = gelu_tc(v[k]);
@@ -239,8 +257,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     if (g.D) {
                         float4* d4 = reinterpret_cast<float4*>(g.D + o);
 #pragma unroll
-                        for (int q = 0; q < 4; ++q)
-                            d4[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+                        for (int k = 0; k < 4; ++k)
+                            d4[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
                     }
                     if (g.Dh) {
                         __align__(16) __nv_bfloat16 h[16];
@@ -352,7 +370,7 @@ cudaError_t launch_gemm_bf16_tcgen05(const GemmArgs& g, cudaStream_t s) {
     a.bias = g.bias; a.act = g.act; a.pre = g.pre; a.D = g.D; a.Dh = g.Dh; a.ldd = g.ldd;
     // at least 64 KB: whatever the operand sizes, every core matrix an MMA of this kernel addresses lies
     // inside the allocation
-    size_t smem = (size_t)a.a_bytes + a.w_bytes + 64;
+    size_t smem = (size_t)a.a_bytes + a.w_bytes + 64 + (size_t)g.N * 4;   // operands, barriers and state, bias
     if (smem < 64 * 1024) smem = 64 * 1024;
     static int sms = 0;
     if (!sms) {
