@@ -53,10 +53,12 @@ __device__ __forceinline__ void ldsm_x4_t(uint32_t (&r)[4], const void* p) {
                  : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]) : "r"(smem_addr(p)));
 }
 
-// GELU, tanh form: 0.5 x (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3))), and its derivative.
+// GELU, tanh form: 0.5 x (1 + tanh(u)), u = sqrt(2/pi) (x + 0.044715 x^3), evaluated as
+// x / (1 + exp(-2u)) (the tcgen05 kernel's epilogue uses the same expression), and its derivative.
 __device__ __forceinline__ float gelu_f(float x) {
-    const float c = 0.7978845608028654f;
-    return 0.5f * x * (1.0f + tanhf(c * (x + 0.044715f * x * x * x)));
+    const float m2c_log2e = -2.0f * 0.7978845608028654f * 1.4426950408889634f;
+    const float e = exp2f(m2c_log2e * (x + 0.044715f * x * x * x));
+    return __fdividef(x, 1.0f + e);
 }
 __device__ __forceinline__ float gelu_grad(float x) {
     const float c = 0.7978845608028654f;

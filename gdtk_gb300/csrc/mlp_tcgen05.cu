@@ -129,9 +129,13 @@ __device__ __forceinline__ void tmem_ld_wait(unsigned (&r)[Q][16]) {
         for (int i = 0; i < 16; ++i) asm volatile("" : "+r"(r[q][i])::"memory");
 }
 
-__device__ __forceinline__ float gelu_tc(float x) {   // tanh form, as the mma.sync kernel's epilogue
-    const float c = 0.7978845608028654f;
-    return 0.5f * x * (1.0f + tanhf(c * (x + 0.044715f * x * x * x)));
+// GELU, tanh form, as the mma.sync kernel's epilogue: 0.5 x (1 + tanh(u)) = x / (1 + exp(-2u)),
+// u = sqrt(2/pi) (x + 0.044715 x^3), with exp2f and __fdividef (each within 2 ulp); exp(-2u) -> inf gives
+// -0, exp(-2u) -> 0 gives x.
+__device__ __forceinline__ float gelu_tc(float x) {
+    const float m2c_log2e = -2.0f * 0.7978845608028654f * 1.4426950408889634f;
+    const float e = exp2f(m2c_log2e * (x + 0.044715f * x * x * x));
+    return __fdividef(x, 1.0f + e);
 }
 
 __device__ __forceinline__ void mbar_arrive(unsigned long long* bar) {
@@ -144,7 +148,7 @@ __device__ __forceinline__ void mbar_arrive(unsigned long long* bar) {
 // may access) and the column slice (w - 1) / 4 of EPI_WARPS / 4 slices.
 // Barriers: load (A tile, + W the first time), full[b] (tcgen05.commit of accumulator b), empty[b]
 // (every epilogue warp has read accumulator b).
-__global__ void __launch_bounds__(TC_THREADS, 1)
+__global__ void __maxnreg__(112)
     gemm_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmW, const TcArgs g) {
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char* sA = smem;
