@@ -148,7 +148,7 @@ __device__ __forceinline__ void mbar_arrive(unsigned long long* bar) {
 // may access) and the column slice (w - 1) / 4 of EPI_WARPS / 4 slices.
 // Barriers: load (A tile, + W the first time), full[b] (tcgen05.commit of accumulator b), empty[b]
 // (every epilogue warp has read accumulator b).
-__global__ void __maxnreg__(112)
+__global__ void __launch_bounds__(TC_THREADS, 1)
     gemm_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmW, const TcArgs g) {
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char* sA = smem;
@@ -238,16 +238,17 @@ __global__ void __maxnreg__(112)
             const int row = tile * TC_M + quarter * 32 + lane;
             const unsigned trow = tmem + (unsigned)b * g.tmem_cols + ((unsigned)(quarter * 32) << 16);
             const int nq = (c1 - c0) >> 4;   // at most 4: N <= 256 over 4 column slices
-            unsigned r[4][16];
+            for (int qb = 0; qb < nq; qb += 2) {   // two 16-column chunks in flight per wait
+                unsigned r[2][16];
+                __syncwarp();   // the TMEM loads are warp-collective
+                tmem_ld16(trow + (unsigned)(c0 + 16 * qb), r[0]);
+                if (qb + 1 < nq) tmem_ld16(trow + (unsigned)(c0 + 16 * qb + 16), r[1]);
+                tmem_ld_wait<2>(r);
+                if (row >= g.M) continue;
 #pragma unroll
-            for (int q = 0; q < 4; ++q)
-                if (q < nq) tmem_ld16(trow + (unsigned)(c0 + 16 * q), r[q]);
-            tmem_ld_wait<4>(r);
-            if (row < g.M) {
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    if (q >= nq) break;
-                    const int c = c0 + 16 * q;
+                for (int q = 0; q < 2; ++q) {
+                    if (qb + q >= nq) break;
+                    const int c = c0 + 16 * (qb + q);
                     const size_t o = (size_t)row * g.ldd + c;
                     float v[16];
 #pragma unroll
