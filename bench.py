@@ -325,7 +325,12 @@ def run_blocks(args, w):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "h2air-blocks64", "blocks": len(blocks), "cells": ncell,
                    "dt_per_block": [b["t_interval"] for b in blocks], "graph": "one CUDA-graph replay per split step",
-                   "launch_shape": {k: choice[k] for k in ("block", "min_blocks", "order")}, "cells_failed": failed,
+                   "launch_shape": {k: choice.get(k) for k in ("block", "min_blocks", "order", "refill_chunk",
+                                                                 "cells_per_warp")},
+                   "tuning_ms": {"%d/%d/%s/%d/%d" % (r["block"], r["min_blocks"], r["order"], r["refill_chunk"],
+                                                     r["cells_per_warp"]): round(r["ms"], 1)
+                                 for r in choice.get("results", [])},
+                   "cells_failed": failed,
                    "cells_by_status_last_step": by_status,
                    "l2": "inputs larger than L2 (no flush)"},
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
