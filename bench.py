@@ -47,6 +47,10 @@ WORKLOADS = {
     # learned surrogate: 4x256 GELU MLP trained on 16,777,216 samples of the FP64 update (cells of the
     # h2air-1M distribution, dt log-uniform in [0.5, 2] us, 5% held out); inference + gate + FP64
     # fallback on 4,194,304 fresh cells at dt = 1e-6 s, against the plain FP64 update of the same cells
+    # two-temperature reactor: Park's 5-species 2-T air (examples/lmr/3D/cylinder-larc inputs), Landau-Teller
+    # exchange and Marrone-Treanor coupling, non-equilibrium post-shock cells, dt = 1e-6 s
+    "air2t-262144": dict(gas="park2t-gas.lua", chem="park2t-chem.lua", eem="park2t-eem.lua", n=262144, dt=1.0e-6,
+                         kind="air2t", seed=7),
     # large mechanism: the reference's 75-species, 474-reaction C2H2/C2H4 model (alpha-QSS, one warp per
     # cell) on shock-tube ignition states of its acetylene example, dt = 1e-6 s
     "c2h2-262144": dict(gas="c2h2-gas.lua", chem="c2h2-chem.lua", n=262144, dt=1.0e-6, kind="c2h2", seed=5),
@@ -187,9 +191,11 @@ def roofline_fp64(issued, n, kernel_ms, peak, ref_flops, traffic, work_per_cell)
     operation figure (the reference's add/mul/div = 1, exp/log = 20, pow = 40 per unit of work, with
     the kernel's own work counters) is reported beside it under its own name."""
     kernel_s = kernel_ms * 1e-3
-    ref = {"achieved": ref_flops / kernel_s / 1e12, "frac": ref_flops / kernel_s / 1e12 / peak,
-           "flops_per_launch": ref_flops, "work_per_cell": list(map(float, work_per_cell)),
-           "convention": "reference operations per unit of work: add/sub/mul/div 1, exp/log 20, pow 40"}
+    ref = None
+    if ref_flops is not None:
+        ref = {"achieved": ref_flops / kernel_s / 1e12, "frac": ref_flops / kernel_s / 1e12 / peak,
+               "flops_per_launch": ref_flops, "work_per_cell": list(map(float, work_per_cell)),
+               "convention": "reference operations per unit of work: add/sub/mul/div 1, exp/log 20, pow 40"}
     out = {"bound": "fp64", "achieved": None, "peak": peak, "unit": "TFLOP/s", "frac": None, "traffic": traffic,
            "basis": "issued FP64 FLOP: 2 x DFMA + DADD + DMUL thread instructions",
            "peak_source": "measured: gdtk_measure_fp64_peak DFMA probe on this GPU (no FP64 entry in "
@@ -565,6 +571,87 @@ def surrogate_leg(rc, srho, su, sT, sp, sY, dt, plain_ms, plain_T, plain_Y, plai
     }
 
 
+def run_two_temperature(args, w):
+    """The two-temperature reactor over a batch of non-equilibrium air cells (chem_reactor2t_update_cells)."""
+    import torch
+    import gdtk_gb300
+    from gdtk_gb300.cells import ReactorCells2T
+    from gdtk_gb300.workloads import air2t_cells
+    gdtk_gb300.lib()
+    rc = ReactorCells2T(os.path.join(MECH, w["gas"]), os.path.join(MECH, w["chem"]), os.path.join(MECH, w["eem"]))
+    n = w["n"]
+    dev = torch.device("cuda", 0)
+    T0, Tve0, p0, Y0 = air2t_cells(n, seed=w["seed"])
+    t64 = lambda a: torch.tensor(np.ascontiguousarray(a), dtype=torch.float64, device=dev)
+    sT, sTve, sp, sY = t64(T0), t64(Tve0), t64(p0), t64(Y0)
+    rho, _, _ = rc.thermo_from_pT(sp, sT, sTve, sY)
+    T, Tve, p, Y = sT.clone(), sTve.clone(), sp.clone(), sY.clone()
+    dtc = torch.full((n,), -1.0, dtype=torch.float64, device=dev)
+    st = torch.zeros(n, dtype=torch.int32, device=dev)
+    u, uve = torch.empty_like(rho), torch.empty_like(rho)
+    steps = torch.zeros(1, dtype=torch.int64, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def reset():
+        T.copy_(sT); Tve.copy_(sTve); p.copy_(sp); Y.copy_(sY); dtc.fill_(-1.0)
+
+    for _ in range(args.warmup):
+        reset()
+        rc.update(rho, T, Tve, p, Y, dtc, w["dt"], status=st, u=u, u_ve=uve)
+    torch.cuda.synchronize()
+    peak = fp64_peak_reference()
+    clocks = ClockSampler(int(os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] or 0))
+    clocks.start()
+    steps.zero_()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    k0.record(stream)
+    for s in range(args.steps):
+        reset()
+        ev[s][0].record(stream)
+        rc.update(rho, T, Tve, p, Y, dtc, w["dt"], status=st, u=u, u_ve=uve, steps=steps)
+        ev[s][1].record(stream)
+    k1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    total_ms = k0.elapsed_time(k1)
+    kernel_ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
+    ok = int((st == 0).sum())
+    # end to end: pinned host arrays in, the update, results out, every step
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+    hrho, hT, hTve, hp, hY = pin(rho.cpu().numpy()), pin(T0), pin(Tve0), pin(p0), pin(Y0)
+    oT, oTve, op, oY = (torch.empty_like(x).pin_memory() for x in (hT, hTve, hp, hY))
+    e2e_times = []
+    for _ in range(max(1, min(args.steps, 3))):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        drho, dT_, dTve_, dp_, dY_ = (x.to(dev, non_blocking=True) for x in (hrho, hT, hTve, hp, hY))
+        ddt = torch.full((n,), -1.0, dtype=torch.float64, device=dev)
+        rc.update(drho, dT_, dTve_, dp_, dY_, ddt, w["dt"], status=st, u=u, u_ve=uve)
+        for h, d in ((oT, dT_), (oTve, dTve_), (op, dp_), (oY, dY_)):
+            h.copy_(d, non_blocking=True)
+        torch.cuda.synchronize()
+        e2e_times.append(time.perf_counter() - t0)
+    issued = profile_record("fp64_issued.json", args.workload)
+    attempts = float(steps.item()) / args.steps / n
+    return {
+        "metric": METRIC, "value": n * args.steps / (total_ms * 1e-3), "unit": "cell-updates/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": args.workload, "cells": n, "mechanism": w["chem"], "energy_exchange": w["eem"],
+                   "dt": w["dt"], "method": "rkf (multi-temperature reactor)", "cells_ok": ok,
+                   "rkf_attempts_per_cell": attempts, "l2": "inputs larger than L2 (no flush): %.0f MB of cell "
+                   "state" % (n * 8 * (6 + rc.nsp) / 1e6)},
+        "roofline": roofline_fp64(issued, n, kernel_ms, peak, None, None, None),
+        "cpu_baseline": None,
+        "cpu_baseline_note": "the two-temperature oracle is a pure-Python restatement, a checker, not a timing "
+                             "reference for the reference's compiled D reactor",
+        "e2e": {"value": n / float(np.mean(e2e_times)), "unit": "cell-updates/s",
+                "h2d_bytes_per_step": n * 8 * (4 + rc.nsp), "d2h_bytes_per_step": n * 8 * (3 + rc.nsp)},
+        "clocks": clk, "gpu_launches": args.steps,
+    }
+
+
 def run_gemm(args, w):
     """The surrogate's forward layer on the tensor cores: tcgen05 kernel and mma.sync kernel, CUDA-event
     timed over `steps` launches each (inputs and outputs 512 MB each, larger than L2)."""
@@ -832,6 +919,15 @@ def main():
                                   "baseline inside the gdtk line"}))
             return 0
         print(json.dumps(run_layer(args, w)))
+        return 0
+
+    if w["kind"] == "air2t":
+        if args.impl == "reference" or rank != 0:
+            if args.impl == "reference" and rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable": "the two-temperature oracle is a pure-Python "
+                                  "restatement, not a timing reference"}))
+            return 0
+        print(json.dumps(run_two_temperature(args, w)))
         return 0
 
     if w["kind"] == "gemm":

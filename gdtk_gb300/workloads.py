@@ -22,6 +22,18 @@ def air5_cells(n, seed=0):
     return T, p, np.ascontiguousarray(Y.T)
 
 
+def air2t_cells(n, seed=7):
+    """Two-temperature (thermal non-equilibrium) air behind a shock, Park's 5 species (N2, O2, N, O, NO):
+    T ~ U[3000, 12000] K, T_ve ~ U[300 K, 1.2 T], p = 10^U[3, 4.7] Pa, Y ~ Dirichlet(2, 1, 0.3, 0.3, 0.3).
+    Returns T, T_ve, p (n,) and Y (5, n)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    T = rng.uniform(3000.0, 12000.0, n)
+    Tve = rng.uniform(300.0, 1.2 * T)
+    p = 10.0 ** rng.uniform(3.0, 4.7, n)
+    Y = rng.dirichlet([2.0, 1.0, 0.3, 0.3, 0.3], n)
+    return T, Tve, p, np.ascontiguousarray(Y.T)
+
+
 def h2air_cells(names, mol_masses, n, seed=1, frozen_fraction=0.5, T_cold=(300.0, 600.0), T_hot=(1100.0, 2800.0),
                 p_range=(2.0e4, 5.0e5), gas_file=None, subset=None):
     """H2-air workload of uneven stiffness.

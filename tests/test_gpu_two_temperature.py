@@ -17,14 +17,9 @@ FILES = (mech("park2t-gas.lua"), mech("park2t-chem.lua"), mech("park2t-eem.lua")
 
 
 def _cells(n, seed):
-    """Non-equilibrium air: T ~ U[3000, 12000] K, T_ve ~ U[300 K, 1.2 T], p = 10^U[3, 4.7] Pa,
-    Y ~ Dirichlet(2, 1, 0.3, 0.3, 0.3) over (N2, O2, N, O, NO)."""
-    rng = np.random.Generator(np.random.PCG64(seed))
-    T = rng.uniform(3000.0, 12000.0, n)
-    Tve = rng.uniform(300.0, 1.2 * T)
-    p = 10.0 ** rng.uniform(3.0, 4.7, n)
-    Y = rng.dirichlet([2.0, 1.0, 0.3, 0.3, 0.3], n)
-    return T, Tve, p, np.ascontiguousarray(Y.T)
+    """Non-equilibrium air (gdtk_gb300.workloads.air2t_cells, the bench's air2t workload)."""
+    from gdtk_gb300.workloads import air2t_cells
+    return air2t_cells(n, seed=seed)
 
 
 def test_two_temperature_thermo_from_pT():
