@@ -7,7 +7,7 @@
 // int array
 //   [0..HI)            header: nsp, nr, neff, method, maxIters, tight, maxSubcycles, maxAttempts
 //   [HI + isp]         nseg of species isp                                 (nsp ints)
-//   [RX + 40*ir + k]   reaction ir: collider, frc_model, brc_model, eff_set, nreac, nprod, npart, -,
+//   [RX + 40*ir + k]   reaction ir: collider, frc_model, brc_model, eff_set, nreac, nprod, npart, frc_base,
 //                      reac_idx[4], reac_coeff[4], prod_idx[4], prod_coeff[4], part[8], part_nu[8]
 //   [EF + (1+nsp)*s]   efficiency set s: n, idx[nsp]
 // double array
@@ -17,7 +17,10 @@
 //   [RD + 16*ir]       reaction ir: fA, fn, fC, bA, bn, bC (kInf in fA..fC for the pressure-dependent
 //                      models; logA, B, C for Arrhenius2), k0 A, n, C, Troe F_cent, a, T1, T2, T3 (or
 //                      Yungster-Rabinowitz a, b, c in
-//                      the a, T1, T2 slots), Troe flags (1 F_cent given, 2 T1 given, 4 T2 given), -
+//                      the a, T1, T2 slots), Troe flags (1 F_cent given, 2 T1 given, 4 T2 given), Park s;
+//                      a (modified) Marrone-Treanor forward rate keeps its underlying Arrhenius or Park
+//                      rate (model in frc_base) in A, n, C and s, and T_D, U (aU), theta, U*, the
+//                      non-Boltzmann factor in the k_0 / Troe slots
 //   [ED + nsp*s]       efficiency set s: values[nsp]
 #pragma once
 
@@ -44,16 +47,19 @@ enum { HI = 8, RXI = 40, HD = 8, SPD = 56, RXD = 16 };
 enum { SP_M = 0, SP_R, SP_TLOW, SP_THIGH, SP_CPLOW, SP_CPHIGH, SP_HLOW, SP_HHIGH, SP_SLOW, SP_SHIGH,
        SP_BREAKS = 10, SP_BLENDS = 15, SP_COEFFS = 20 };
 // reaction int-record fields
-enum { RX_COLLIDER = 0, RX_FRC, RX_BRC, RX_EFFSET, RX_NREAC, RX_NPROD, RX_NPART,
+enum { RX_COLLIDER = 0, RX_FRC, RX_BRC, RX_EFFSET, RX_NREAC, RX_NPROD, RX_NPART, RX_BASE,
        RX_REAC_IDX = 8, RX_REAC_COEFF = 12, RX_PROD_IDX = 16, RX_PROD_COEFF = 20, RX_PART = 24, RX_PART_NU = 32 };
 // rate-constant models (kinetics/rate_constant.d): Arrhenius 52-80, from K_c, the pressure-dependent
 // Lindemann-Hinshelwood 123-160, Troe 162-290, Yungster-Rabinowitz 292-355 (third-body concentration of
 // the reaction's efficiency list, 114-121), and Arrhenius2 / Arrhenius-logA 82-121,
 // k = exp(logA + B T - C/T), whose (logA, B, C) take the places of (A, n, C)
 enum { RATE_ARRHENIUS = 0, RATE_FROM_EQ = 1, RATE_LH = 2, RATE_TROE = 3, RATE_YR = 4, RATE_ARRHENIUS2 = 5,
-       RATE_PARK = 6 };   // Park 2-T (rate_constant.d:364-393): A, n, C with T_eff = T^s T_ve^(1-s), s in RD_S
+       RATE_PARK = 6,   // Park 2-T (rate_constant.d:364-393): A, n, C with T_eff = T^s T_ve^(1-s), s in RD_S
+       RATE_MT = 7,     // Marrone-Treanor (rate_constant.d:395-452) over an Arrhenius or Park rate
+       RATE_MMT = 8 };  // modified Marrone-Treanor (rate_constant.d:454-566)
 // reaction double-record fields beyond the six Arrhenius parameters
 enum { RD_K0A = 6, RD_K0N, RD_K0C, RD_FCENT, RD_TA, RD_T1, RD_T2, RD_T3, RD_TFLAGS, RD_S };
+enum { RD_MT_TD = 6, RD_MT_U, RD_MT_THETA, RD_MT_USTAR, RD_MT_NB };   // U holds aU for the modified form
 enum { TROE_FCENT = 1, TROE_T1 = 2, TROE_T2 = 4 };
 enum { METHOD_RKF = 0, METHOD_ALPHA_QSS = 1 };
 

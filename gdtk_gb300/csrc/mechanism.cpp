@@ -51,6 +51,30 @@ RateConstHost rate_const(const LuaValue& t) {
         r.s = t.has("s") ? t.get("s").number() : std::nan("");   // checked with the gas model below
         if (t.has("mode") && t.get("mode").number() != 0)
             throw std::runtime_error("Park rate constants on an energy mode other than 0 need more than two temperatures");
+    } else if (model == "Marrone-Treanor" || model == "Modified-Marrone-Treanor") {   // rate_constant.d:395-566
+        RateConstHost b = rate_const(t.get("rate"));
+        if (b.model != RATE_ARRHENIUS && b.model != RATE_PARK)
+            throw std::runtime_error("a Marrone-Treanor rate constant needs an Arrhenius or Park rate beneath it");
+        r = b;
+        r.base = b.model;
+        r.model = model == "Marrone-Treanor" ? RATE_MT : RATE_MMT;
+        r.TD = t.get("T_D").number();
+        r.theta = t.get("theta").number();
+        if (r.model == RATE_MT) {
+            r.U = t.get("U").number();
+        } else {
+            r.aU = t.get("aU").number();
+            r.Ustar = t.get("Ustar").number();
+            if (t.has("non_boltzmann_correction")) {   // rate_constant.d:470-492: only the constant model
+                const LuaValue& nb = t.get("non_boltzmann_correction");
+                if (nb.get("model").string() != "constant")
+                    throw std::runtime_error("Invalid non Boltzmann correction factor for MMT");
+                r.nb = nb.get("factor").number();
+            }
+        }
+        if (t.has("mode") && t.get("mode").number() != 0)
+            throw std::runtime_error("Marrone-Treanor rate constants on an energy mode other than 0 need more than "
+                                     "two temperatures");
     } else if (model == "fromEqConst") {
         r.model = RATE_FROM_EQ;
     } else if (model == "Lindemann-Hinshelwood" || model == "Troe" || model == "Yungster-Rabinowitz") {
@@ -197,14 +221,21 @@ MechanismHost load_mechanism(const std::string& path, const GasModelHost& gm, bo
         if (r.has("equation")) rh.equation = r.get("equation").string();
         rh.frc = rate_const(r.get("frc"));
         rh.brc = rate_const(r.get("brc"));
-        if (rh.frc.model == RATE_PARK || rh.brc.model == RATE_PARK) {
+        auto two_t = [](const RateConstHost& c) {
+            return c.model == RATE_PARK || c.model == RATE_MT || c.model == RATE_MMT;
+        };
+        if (two_t(rh.frc) || two_t(rh.brc)) {
             if (!gm.two_temperature)
-                throw std::runtime_error("rate-constant model 'Park' is not supported for a one-temperature gas: it "
-                                         "needs a two-temperature gas model (rate_constant.d:364-393)");
-            if (!std::isfinite(rh.frc.s) && rh.frc.model == RATE_PARK)
+                throw std::runtime_error("rate-constant model '" +
+                                         std::string(rh.frc.model == RATE_PARK || rh.brc.model == RATE_PARK
+                                                         ? "Park" : "Marrone-Treanor") +
+                                         "' is not supported for a one-temperature gas: it needs a two-temperature "
+                                         "gas model (rate_constant.d:364-566)");
+            if (!std::isfinite(rh.frc.s) && (rh.frc.model == RATE_PARK || rh.frc.base == RATE_PARK))
                 throw std::runtime_error("Park rate constant without its exponent s");
-            if (rh.brc.model == RATE_PARK)
-                throw std::runtime_error("Park backward rate constants are not supported (forward with k_b from K_c)");
+            if (two_t(rh.brc))
+                throw std::runtime_error("Park and Marrone-Treanor backward rate constants are not supported "
+                                         "(forward with k_b from K_c)");
         }
         if (rh.frc.model == RATE_FROM_EQ && rh.brc.model == RATE_FROM_EQ)
             throw std::runtime_error("a reaction needs at least one Arrhenius rate constant");
@@ -325,6 +356,14 @@ PackedMech pack(const GasModelHost& gm, const MechanismHost* mh) {
         rd[RD_FCENT] = r.frc.Fcent; rd[RD_TA] = r.frc.a; rd[RD_T1] = r.frc.T1; rd[RD_T2] = r.frc.T2;
         rd[RD_T3] = r.frc.T3; rd[RD_TFLAGS] = r.frc.troe_flags;
         rd[RD_S] = r.frc.s;
+        if (r.frc.model == RATE_MT || r.frc.model == RATE_MMT) {
+            ri[RX_BASE] = r.frc.base;
+            rd[RD_MT_TD] = r.frc.TD;
+            rd[RD_MT_U] = r.frc.model == RATE_MT ? r.frc.U : r.frc.aU;
+            rd[RD_MT_THETA] = r.frc.theta;
+            rd[RD_MT_USTAR] = r.frc.Ustar;
+            rd[RD_MT_NB] = r.frc.nb;
+        }
     }
     for (int s = 0; s < neff; ++s) {
         int* ei = I + HI + nsp + RXI * nr + (1 + nsp) * s;

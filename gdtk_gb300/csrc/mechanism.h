@@ -34,13 +34,15 @@ struct GasModelHost {
 enum { PARTICLE_ATOM = 0, PARTICLE_LINEAR = 1, PARTICLE_NONLINEAR = 2, PARTICLE_ELECTRON = 3 };
 
 struct RateConstHost {
-    int model = 0;   // RATE_ARRHENIUS, RATE_FROM_EQ, RATE_LH, RATE_TROE, RATE_YR or RATE_ARRHENIUS2
+    int model = 0;   // RATE_* (chem_types.h)
     double A = 0, n = 0, C = 0;            // Arrhenius; k_inf for the pressure-dependent models;
                                            // logA, B, C for Arrhenius2 (k = exp(logA + B T - C/T))
     double A0 = 0, n0 = 0, C0 = 0;         // k_0 of the pressure-dependent models
     double Fcent = 0, a = 0, T1 = 0, T2 = 0, T3 = 0;   // Troe (a, T1, T2 hold a, b, c for Yungster-Rabinowitz)
     int troe_flags = 0;                    // TROE_FCENT | TROE_T1 | TROE_T2: parameters given
     double s = 0;                          // Park: exponent of T in the rate-controlling temperature
+    int base = 0;                          // (modified) Marrone-Treanor: model of the underlying rate in A, n, C, s
+    double TD = 0, U = 0, theta = 0, aU = 0, Ustar = 0, nb = 1;   // their parameters (nb: non-Boltzmann factor)
     bool pressure_dependent() const { return model == RATE_LH || model == RATE_TROE || model == RATE_YR; }
     bool simple() const { return model == RATE_ARRHENIUS || model == RATE_ARRHENIUS2; }   // no third body
 };

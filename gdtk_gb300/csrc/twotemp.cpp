@@ -80,12 +80,27 @@ std::vector<Eem2T> load_energy_exchange(const std::string& path, const GasModelH
             e.p = species_index(gm, m.get("p").string());
             e.reaction = (int)m.get("reaction_index").number();
             if (e.reaction < 0 || e.reaction >= nr) throw std::runtime_error("reaction_index out of range");
-            const LuaValue& cm = m.get("coupling_model");
-            if (cm.get("model").string() != "ImpartialDissociation")
-                throw std::runtime_error("chemistry-vibration coupling '" + cm.get("model").string() +
-                                         "' is not supported (ImpartialDissociation)");
-            e.D = cm.get("D").number();
+            const LuaValue& cm = m.get("coupling_model");   // exchange_chemistry_coupling.d:71-227, 262-276
+            const std::string model = cm.get("model").string();
             e.Thetav = cm.get("Thetav").number();
+            if (model == "ImpartialDissociation") {
+                e.coupling = CPL_IMPARTIAL;
+                e.D = cm.get("D").number();
+            } else if (model == "MarroneTreanorDissociation") {
+                e.coupling = CPL_MARRONE_TREANOR;
+                e.D = cm.get("D").number();
+                e.U = cm.get("U").number();
+            } else if (model == "ModifiedMarroneTreanorDissociation") {
+                e.coupling = CPL_MODIFIED_MARRONE_TREANOR;
+                e.D = cm.get("T_D").number();   // a temperature here
+                e.aU = cm.get("aU").number();
+                e.Ustar = cm.get("Ustar").number();
+                e.nb = cm.has("non_boltzmann") ? cm.get("non_boltzmann").number() : 0.0;
+            } else {
+                throw std::runtime_error("chemistry-vibration coupling '" + model + "' is not supported "
+                                         "(ImpartialDissociation, MarroneTreanorDissociation, "
+                                         "ModifiedMarroneTreanorDissociation)");
+            }
         } else {
             throw std::runtime_error("energy exchange rate '" + rate + "' is not supported (Landau-Teller, "
                                      "Marrone-Treanor)");
@@ -164,7 +179,8 @@ extern "C" int chem_reactor2t_new(const char* gas_file, const char* chem_file, c
                                      "(multi_temperature_thermochemical_reactor.d:88-101)");
         for (auto& rx : r->mh.reactions)
             if (rx.frc.pressure_dependent() || rx.frc.model == RATE_ARRHENIUS2 || rx.brc.model == RATE_ARRHENIUS2)
-                throw std::runtime_error("the two-temperature reactor takes Arrhenius, Park and K_c rate constants");
+                throw std::runtime_error("the two-temperature reactor takes Arrhenius, Park, Marrone-Treanor, "
+                                         "modified Marrone-Treanor and K_c rate constants");
         r->nsp = r->gm.n_species();
         r->nr = (int)r->mh.reactions.size();
         if (r->nsp > GDTK_MAX_SPECIES || r->nr > GDTK_MAX_REACTIONS)

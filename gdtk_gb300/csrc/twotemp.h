@@ -14,6 +14,7 @@ namespace gdtk {
 
 enum { EEM_LANDAU_TELLER = 0, EEM_MARRONE_TREANOR = 1 };
 enum { RT_MILLIKAN_WHITE = 0, RT_PARK_HTC = 1, RT_PARK_HTC2 = 2 };
+enum { CPL_IMPARTIAL = 0, CPL_MARRONE_TREANOR = 1, CPL_MODIFIED_MARRONE_TREANOR = 2 };
 
 // One energy-exchange mechanism (energy_exchange_mechanism.d).
 struct Eem2T {
@@ -22,11 +23,13 @@ struct Eem2T {
     int q;           // colliding species (Landau-Teller)
     int rt;          // RT_* (Landau-Teller)
     int reaction;    // reaction index (Marrone-Treanor)
-    int pad;
+    int coupling;    // CPL_* (Marrone-Treanor)
     double a, b;     // Millikan-White constants (relaxation_time.d:27-60)
     double sigma;    // Park high-temperature cross section [m^2]
     double mu;       // reduced mass of the p-q pair [kg]
-    double D, Thetav;   // Marrone-Treanor impartial dissociation (exchange_chemistry_coupling.d:71-121)
+    double D, Thetav;   // dissociation energy [J/mol] (T_D [K] for the modified form), vibrational temperature
+    double U;           // Marrone-Treanor U [K] (exchange_chemistry_coupling.d:133-175)
+    double aU, Ustar, nb;   // modified Marrone-Treanor (:181-227)
 };
 
 // Per-species two-temperature constants (two_temperature_gas.d:45-80).

@@ -5,14 +5,16 @@
 // on the concentrations and u_ve), with
 //   * rate constants once per subcycle at the clamped T (reaction_mechanism.d:49-63): Gibbs energies
 //     at p = P_atm and T_ve = T (:204-218, two_temperature_gas.d:469-482), forward Arrhenius or Park
-//     (rate_constant.d:72-75, 364-393: T_eff = T^s T_ve^(1-s)), backward k_f(T, T_ve = T) / K_c(T)
+//     (rate_constant.d:72-75, 364-393: T_eff = T^s T_ve^(1-s)) or (modified) Marrone-Treanor over either
+//     (rate_constant.d:395-566), backward k_f(T, T_ve = T) / K_c(T)
 //     (reaction.d:94-143, 26-52);
 //   * tick rates and q - L (reaction.d:290-311, 416-440; reaction_mechanism.d:74-96);
 //   * energy exchange (energy_exchange_system.d:93-104): Landau-Teller (energy_exchange_mechanism.d:
 //     83-101) with Millikan-White / Park high-temperature relaxation times (relaxation_time.d:27-175),
 //     evaluated once per subcycle on the subcycle's gas state, and Marrone-Treanor coupling with
-//     impartial dissociation (energy_exchange_mechanism.d:228-241, exchange_chemistry_coupling.d:
-//     27-121) on the current stage's tick rates;
+//     impartial, Marrone-Treanor or modified Marrone-Treanor dissociation (energy_exchange_mechanism.d:
+//     228-241, exchange_chemistry_coupling.d:41-227; G_appear and G_vanish on the subcycle's state) on
+//     the current stage's tick rates;
 //   * T from u by direct inversion and T_ve by Newton iteration (two_temperature_gas.d:95-117, 656-700).
 // A cell that fails keeps its input state and gets the reference's failure as its status.
 #include <cuda_runtime.h>
@@ -120,13 +122,42 @@ __device__ __forceinline__ double pow_int(double x, int n) {   // small positive
     return r;
 }
 
-// Forward rate constant of reaction ir at (T, T_ve): Arrhenius at T, Park at T^s T_ve^(1-s).
-__device__ double forward_rc(const int* r, const double* d, double T, double Tve) {
-    if (r[RX_FRC] == RATE_PARK) {
+// An Arrhenius (at T) or Park (at T^s T_ve^(1-s)) rate constant from the record's A, n, C, s.
+__device__ double base_rc(int model, const double* d, double T, double Tve) {
+    if (model == RATE_PARK) {
         const double Te = pow(T, d[RD_S]) * pow(Tve, 1.0 - d[RD_S]);
         return d[0] * pow(Te, d[1]) * exp(-d[2] / Te);
     }
     return d[0] * pow(T, d[1]) * exp(-d[2] / T);
+}
+
+// rate_constant.d:397-404
+__device__ __forceinline__ double Q_mt(double T, double D, double theta) {
+    const double num = 1 - exp(-D / T);
+    const double den = 1 - exp(-theta / T);
+    return num / den;
+}
+
+// Forward rate constant of reaction ir at (T, T_ve): Arrhenius, Park, or the (modified) Marrone-Treanor
+// non-equilibrium factor times the underlying one (rate_constant.d:438-447, 541-554).
+__device__ double forward_rc(const int* r, const double* d, double T, double Tve) {
+    const int model = r[RX_FRC];
+    if (model != RATE_MT && model != RATE_MMT) return base_rc(model, d, T, Tve);
+    const double kEQ = base_rc(r[RX_BASE], d, T, Tve);
+    const double TD = d[RD_MT_TD], th = d[RD_MT_THETA];
+    if (model == RATE_MT) {
+        const double U = d[RD_MT_U];
+        const double Gamma = 1. / (1. / Tve - 1. / T - 1. / U);
+        const double Q_T = Q_mt(T, TD, th), Q_Gamma = Q_mt(Gamma, TD, th), Q_Tv = Q_mt(Tve, TD, th),
+                     Q_U = Q_mt(-U, TD, th);
+        return kEQ * Q_T * Q_Gamma / (Q_Tv * Q_U);
+    }
+    const double Tinv = 1. / T, Tvinv = 1. / Tve;
+    const double Uinv = d[RD_MT_U] * Tinv + 1. / d[RD_MT_USTAR];
+    const double U = 1. / Uinv;
+    const double TF = 1. / (Tvinv - Tinv - Uinv);
+    const double Q_T = Q_mt(T, TD, th), Q_TF = Q_mt(TF, TD, th), Q_Tv = Q_mt(Tve, TD, th), Q_U = Q_mt(-U, TD, th);
+    return d[RD_MT_NB] * kEQ * Q_T * Q_TF / (Q_Tv * Q_U);
 }
 
 struct Reactor2T {
@@ -214,9 +245,8 @@ struct Reactor2T {
         return t_mw + 1.0 / (sigma * cs * numden[e.q]);
     }
 
-    // Impartial dissociation's energy removed per dissociation (exchange_chemistry_coupling.d:93-112).
-    __device__ static double gvanish(double T, double Tv, double D, double Th) {
-        const double iG = (T - Tv) / (T * Tv);
+    // Knab's equation (39) and its small-iG and overflow forms (exchange_chemistry_coupling.d:41-69).
+    __device__ static double L_knab(double iG, double D, double Th) {
         if (fabs(iG) < IGAMMA_SWITCH)
             return 0.5 * (D - Th * R_universal) + iG * (Th * Th * R_universal * R_universal - D * D) / 12.0 / R_universal;
         if (iG > IGAMMA_OVERFLOW)
@@ -224,10 +254,33 @@ struct Reactor2T {
         return R_universal * Th / (exp(Th * iG) - 1.0) - D / (exp(D / R_universal * iG) - 1.0);
     }
 
+    // Energy brought in (ga) and removed (gv) per dissociation at (T, T_ve), J/mol
+    // (exchange_chemistry_coupling.d:94-126 impartial, 152-174 Marrone-Treanor, 204-220 modified).
+    __device__ static void coupling(const Eem2T& e, double T, double Tv, double& ga, double& gv) {
+        const double th = e.Thetav;
+        if (e.coupling == CPL_IMPARTIAL) {
+            ga = 0.5 * (e.D - th * R_universal);
+            gv = L_knab((T - Tv) / (T * Tv), e.D, th);
+        } else if (e.coupling == CPL_MARRONE_TREANOR) {
+            gv = L_knab(1. / Tv - 1. / T - 1. / e.U, e.D, th);
+            const double T_F_inv = -1. / e.U;
+            ga = R_universal * th / (exp(th * T_F_inv) - 1.) - e.D / (exp(e.D / R_universal * T_F_inv) - 1.);
+        } else {
+            const double TD = e.D;
+            const double Uinv = e.aU / T + 1 / e.Ustar;
+            double T_F_inv = 1. / Tv - 1. / T - Uinv;
+            gv = R_universal * (th / (exp(th * T_F_inv) - 1.) - TD / (exp(TD * T_F_inv) - 1.)) + e.nb * R_universal * TD;
+            T_F_inv = -e.aU / T - 1 / e.Ustar;
+            ga = R_universal * (th / (exp(th * T_F_inv) - 1.) - TD / (exp(TD * T_F_inv) - 1.));
+        }
+    }
+
     // dy/dt at y (species rates and the energy exchange into u_ve); lt[k]: the Landau-Teller term of
-    // mechanism k on this subcycle's state (0 for others); gv[k]: its Marrone-Treanor G_vanish.
-    __device__ void rates(const double* y, const double* kf, const double* kb, const double* lt, const double* gv,
-                          double rho, double* wf, double* wb, double* q, double* L, double* out) const {
+    // mechanism k on this subcycle's state (0 for others); ga[k], gv[k]: its Marrone-Treanor G_appear and
+    // G_vanish on that state.
+    __device__ void rates(const double* y, const double* kf, const double* kb, const double* lt, const double* ga,
+                          const double* gv, double rho, double* wf, double* wb, double* q, double* L,
+                          double* out) const {
         const int nsp = g.m.nsp;
         split_rates(y, kf, kb, wf, wb, q, L);
         for (int i = 0; i < nsp; ++i) out[i] = q[i] - L[i];
@@ -241,8 +294,7 @@ struct Reactor2T {
                 const double f = wf[e.reaction], b = wb[e.reaction];
                 const double prod = nu > 0 ? nu * f : (nu < 0 ? -nu * b : 0.0);
                 const double loss = nu > 0 ? nu * b : (nu < 0 ? -nu * f : 0.0);
-                const double ga = 0.5 * (e.D - e.Thetav * R_universal);
-                rate += (prod * ga - loss * gv[k]) / rho;
+                rate += (prod * ga[k] - loss * gv[k]) / rho;
             }
         }
         out[nsp] = rate;
@@ -265,7 +317,7 @@ __global__ void __launch_bounds__(128) two_temperature_update_kernel(const TwoTA
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < a.ncell; c += gridDim.x * blockDim.x) {
         double Y0[GDTK_MAX_SPECIES], Y[GDTK_MAX_SPECIES], y0[NV], yOut[NV], yT[NV], K[6][NV], yErr[NV];
         double kf[GDTK_MAX_REACTIONS], kb[GDTK_MAX_REACTIONS], wf[GDTK_MAX_REACTIONS], wb[GDTK_MAX_REACTIONS];
-        double q[GDTK_MAX_SPECIES], L[GDTK_MAX_SPECIES], gs[GDTK_MAX_SPECIES], lt[MAX_EEM], gv[MAX_EEM];
+        double q[GDTK_MAX_SPECIES], L[GDTK_MAX_SPECIES], gs[GDTK_MAX_SPECIES], lt[MAX_EEM], ga[MAX_EEM], gv[MAX_EEM];
         double molef[GDTK_MAX_SPECIES], numden[GDTK_MAX_SPECIES];
         const double rho = a.rho[c];
         double T = a.T[c], Tve = a.Tve[c], p = a.p[c];
@@ -312,13 +364,14 @@ __global__ void __launch_bounds__(128) two_temperature_update_kernel(const TwoTA
                 for (int k = 0; k < R.neem; ++k) {
                     const Eem2T& e = R.eem[k];
                     lt[k] = 0.0;
+                    ga[k] = 0.0;
                     gv[k] = 0.0;
                     if (e.kind == EEM_LANDAU_TELLER) {
                         const double tk = R.tau(e, T, p, molef, numden);
                         if (tk >= 0.0)
                             lt[k] = Y[e.p] * (R.g.e_ve(e.p, T, logT, err) - R.g.e_ve(e.p, Tve, logTve, err)) / tk;
                     } else {
-                        gv[k] = Reactor2T::gvanish(T, Tve, e.D, e.Thetav);
+                        Reactor2T::coupling(e, T, Tve, ga[k], gv[k]);
                     }
                 }
                 dtSave = dt_suggest;
@@ -333,20 +386,20 @@ __global__ void __launch_bounds__(128) two_temperature_update_kernel(const TwoTA
                     const double b51 = 37. / 378., b53 = 250. / 621., b54 = 125. / 594., b56 = 512. / 1771.,
                                  b41 = 2825. / 27648., b43 = 18575. / 48384., b44 = 13525. / 55296.,
                                  b45 = 277. / 14336., b46 = 1.0 / 4.0;
-                    R.rates(y0, kf, kb, lt, gv, rho, wf, wb, q, L, K[0]);
+                    R.rates(y0, kf, kb, lt, ga, gv, rho, wf, wb, q, L, K[0]);
                     for (int i = 0; i < nv; ++i) yT[i] = y0[i] + h * a21 * K[0][i];
-                    R.rates(yT, kf, kb, lt, gv, rho, wf, wb, q, L, K[1]);
+                    R.rates(yT, kf, kb, lt, ga, gv, rho, wf, wb, q, L, K[1]);
                     for (int i = 0; i < nv; ++i) yT[i] = y0[i] + h * (a31 * K[0][i] + a32 * K[1][i]);
-                    R.rates(yT, kf, kb, lt, gv, rho, wf, wb, q, L, K[2]);
+                    R.rates(yT, kf, kb, lt, ga, gv, rho, wf, wb, q, L, K[2]);
                     for (int i = 0; i < nv; ++i) yT[i] = y0[i] + h * (a41 * K[0][i] + a42 * K[1][i] + a43 * K[2][i]);
-                    R.rates(yT, kf, kb, lt, gv, rho, wf, wb, q, L, K[3]);
+                    R.rates(yT, kf, kb, lt, ga, gv, rho, wf, wb, q, L, K[3]);
                     for (int i = 0; i < nv; ++i)
                         yT[i] = y0[i] + h * (a51 * K[0][i] + a52 * K[1][i] + a53 * K[2][i] + a54 * K[3][i]);
-                    R.rates(yT, kf, kb, lt, gv, rho, wf, wb, q, L, K[4]);
+                    R.rates(yT, kf, kb, lt, ga, gv, rho, wf, wb, q, L, K[4]);
                     for (int i = 0; i < nv; ++i)
                         yT[i] = y0[i] + h * (a61 * K[0][i] + a62 * K[1][i] + a63 * K[2][i] + a64 * K[3][i] +
                                              a65 * K[4][i]);
-                    R.rates(yT, kf, kb, lt, gv, rho, wf, wb, q, L, K[5]);
+                    R.rates(yT, kf, kb, lt, ga, gv, rho, wf, wb, q, L, K[5]);
                     for (int i = 0; i < nv; ++i)
                         yOut[i] = y0[i] + h * (b51 * K[0][i] + b53 * K[2][i] + b54 * K[3][i] + b56 * K[5][i]);
                     for (int i = 0; i < nv; ++i)

@@ -5,15 +5,17 @@ Follows kinetics/multi_temperature_thermochemical_reactor.d (RKF Cash-Karp on th
 concentrations and the vibrational-electronic energy, one rate-constant and relaxation-time
 evaluation per subcycle, T and T_ve from (rho, u, u_ve) after each successful step), with
   * rate constants, reaction.d:94-143 (multi-temperature branch) and rate_constant.d:52-80,
-    364-393 (Arrhenius; Park 2-T, T_eff = T^s T_ve^(1-s)); backward rates from K_c at T with the
+    364-393 (Arrhenius; Park 2-T, T_eff = T^s T_ve^(1-s)), 395-452 (Marrone-Treanor) and 494-566
+    (modified Marrone-Treanor) over an Arrhenius or Park rate; backward rates from K_c at T with the
     forward rate constant re-evaluated at T_ve = T; Gibbs energies at p = P_atm and T_ve = T
     (reaction_mechanism.d:49-63, 204-218; two_temperature_gas.d:469-482);
   * tick rates, reaction.d:267-311, 394-456 (pow(conc, coeff), anonymous colliders), and species
     rates q - L (reaction_mechanism.d:74-96);
   * energy exchange, energy_exchange_system.d:70-104 and energy_exchange_mechanism.d: Landau-Teller
     (:56-101) with Millikan-White, ParkHTC and ParkHTC2 relaxation times (relaxation_time.d:27-175),
-    and the Marrone-Treanor chemistry-vibration coupling (:195-253) with impartial dissociation
-    (exchange_chemistry_coupling.d:18-121); within a step the exchange sees the gas state of the
+    and the Marrone-Treanor chemistry-vibration coupling (:195-253) with impartial, Marrone-Treanor or
+    modified Marrone-Treanor dissociation (exchange_chemistry_coupling.d:18-227); within a step the
+    exchange sees the gas state of the
     step's start (T, T_ve, p, mass fractions), as the reference's does;
   * the two-temperature thermo of oracle/two_temperature.py (two_temperature_gas.d), pinned to the
     reference's known-answer test.
@@ -48,6 +50,11 @@ class ReactorFailure(Exception):
 
 def _ints(t):
     return [int(t[k]) for k in sorted(t)] if isinstance(t, dict) else [int(v) for v in t]
+
+
+def _Qmt(T, D, theta):
+    """rate_constant.d:397-404: the partition-function ratio of the Marrone-Treanor rates."""
+    return (1 - math.exp(-D / T)) / (1 - math.exp(-theta / T))
 
 
 def _pow_int(x, n):
@@ -85,6 +92,22 @@ class Reaction:
         if m == "Park":
             Tr = math.pow(T, rc["s"]) * math.pow(T_modes[int(rc["mode"])], 1.0 - rc["s"])
             return rc["A"] * math.pow(Tr, rc["n"]) * math.exp(-rc["C"] / Tr)
+        if m == "Marrone-Treanor":   # rate_constant.d:438-447
+            kEQ = Reaction.rate_constant(rc["rate"], T, T_modes)
+            Tv, TD, th, U = T_modes[int(rc["mode"])], rc["T_D"], rc["theta"], rc["U"]
+            Gamma = 1. / (1. / Tv - 1. / T - 1. / U)
+            return kEQ * _Qmt(T, TD, th) * _Qmt(Gamma, TD, th) / (_Qmt(Tv, TD, th) * _Qmt(-U, TD, th))
+        if m == "Modified-Marrone-Treanor":   # rate_constant.d:541-554
+            kEQ = Reaction.rate_constant(rc["rate"], T, T_modes)
+            Tv, TD, th = T_modes[int(rc["mode"])], rc["T_D"], rc["theta"]
+            Tinv = 1. / T
+            Tvinv = 1. / Tv
+            Uinv = rc["aU"] * Tinv + 1. / rc["Ustar"]
+            U = 1. / Uinv
+            TF = 1. / (Tvinv - Tinv - Uinv)
+            nbc = rc.get("non_boltzmann_correction")
+            nb = float(nbc["factor"]) if nbc else 1.0
+            return nb * kEQ * _Qmt(T, TD, th) * _Qmt(TF, TD, th) / (_Qmt(Tv, TD, th) * _Qmt(-U, TD, th))
         raise ValueError("rate-constant model %s is outside the two-temperature path" % m)
 
     def eval_rate_constants(self, T, T_modes, gibbs, M):
@@ -163,10 +186,18 @@ class TwoTemperatureReactor:
                 self.mechs.append(dict(kind="LT", p=p, q=q, rt=self._relaxation(m["relaxation_time"], p, q)))
             elif m["rate"] == "Marrone-Treanor":
                 cm = m["coupling_model"]
-                if cm["model"] != "ImpartialDissociation":
+                mech = dict(kind="MT", p=idx[m["p"]], r=int(m["reaction_index"]), coupling=cm["model"],
+                            Thetav=float(cm["Thetav"]))
+                if cm["model"] == "ImpartialDissociation":
+                    mech.update(D=float(cm["D"]))
+                elif cm["model"] == "MarroneTreanorDissociation":
+                    mech.update(D=float(cm["D"]), U=float(cm["U"]))
+                elif cm["model"] == "ModifiedMarroneTreanorDissociation":
+                    mech.update(T_D=float(cm["T_D"]), aU=float(cm["aU"]), Ustar=float(cm["Ustar"]),
+                                nb=float(cm.get("non_boltzmann", 0.0)))
+                else:
                     raise ValueError("coupling model %s is outside this restatement" % cm["model"])
-                self.mechs.append(dict(kind="MT", p=idx[m["p"]], r=int(m["reaction_index"]), D=float(cm["D"]),
-                                       Thetav=float(cm["Thetav"])))
+                self.mechs.append(mech)
             else:
                 raise ValueError("energy exchange rate %s is outside this restatement" % m["rate"])
 
@@ -192,6 +223,39 @@ class TwoTemperatureReactor:
         cs = math.sqrt(8.0 * BOLTZMANN * T / math.pi / rt["mu"])
         return tau_sub + 1.0 / (sigma * cs * numden[rt["q"]])
 
+    # ---- chemistry-vibration coupling (exchange_chemistry_coupling.d:41-227)
+    @staticmethod
+    def _coupling(m, T, Tv):
+        """(G_appear, G_vanish) of a Marrone-Treanor mechanism at (T, T_ve)."""
+        th = m["Thetav"]
+        if m["coupling"] == "ImpartialDissociation":   # :94-126
+            return 0.5 * (m["D"] - th * R_UNIVERSAL), TwoTemperatureReactor._gvanish(T, Tv, m["D"], th)
+        if m["coupling"] == "MarroneTreanorDissociation":   # :152-174
+            D, U = m["D"], m["U"]
+            iG = 1. / Tv - 1. / T - 1. / U
+            gv = TwoTemperatureReactor._L(iG, D, th)
+            T_F_inv = -1. / U
+            ga = R_UNIVERSAL * th / (math.exp(th * T_F_inv) - 1.) - D / (math.exp(D / R_UNIVERSAL * T_F_inv) - 1.)
+            return ga, gv
+        TD = m["T_D"]   # ModifiedMarroneTreanorDissociation, :204-220
+        Uinv = m["aU"] / T + 1 / m["Ustar"]
+        T_F_inv = 1. / Tv - 1. / T - Uinv
+        gv = R_UNIVERSAL * (th / (math.exp(th * T_F_inv) - 1.) - TD / (math.exp(TD * T_F_inv) - 1.)) \
+            + m["nb"] * R_UNIVERSAL * TD
+        T_F_inv = - m["aU"] / T - 1 / m["Ustar"]
+        ga = R_UNIVERSAL * (th / (math.exp(th * T_F_inv) - 1.) - TD / (math.exp(TD * T_F_inv) - 1.))
+        return ga, gv
+
+    @staticmethod
+    def _L(iG, D, Thetav):
+        """Equation (39) of Knab 1995 with its small-iG and overflow forms (exchange_chemistry_coupling.d:41-69)."""
+        if abs(iG) < IGAMMA_SWITCH:
+            return 0.5 * (D - Thetav * R_UNIVERSAL) + iG * (Thetav * Thetav * R_UNIVERSAL * R_UNIVERSAL - D * D) / 12.0 \
+                / R_UNIVERSAL
+        if iG > IGAMMA_OVERFLOW:
+            return R_UNIVERSAL * Thetav / (math.exp(Thetav * iG) - 1.0) - D * math.exp(-D / R_UNIVERSAL * iG)
+        return R_UNIVERSAL * Thetav / (math.exp(Thetav * iG) - 1.0) - D / (math.exp(D / R_UNIVERSAL * iG) - 1.0)
+
     # ---- Marrone-Treanor, impartial dissociation (exchange_chemistry_coupling.d:27-121)
     @staticmethod
     def _gvanish(T, Tv, D, Thetav):
@@ -216,8 +280,7 @@ class TwoTemperatureReactor:
                 rate += Y[m["p"]] * (ev_star - ev) / tau
             else:
                 r = self.reactions[m["r"]]
-                ga = 0.5 * (m["D"] - m["Thetav"] * R_UNIVERSAL)
-                gv = self._gvanish(T, Tv, m["D"], m["Thetav"])
+                ga, gv = self._coupling(m, T, Tv)
                 rate += (r.production(m["p"]) * ga - r.loss(m["p"]) * gv) / rho
         return rate
 

@@ -64,6 +64,38 @@ LARC=$REF/examples/lmr/3D/cylinder-larc
         park2t-eem.lua >> park2t-prep.log 2>&1) || { cat "$WORK/park2t-prep.log"; exit 1; }
 grep -v '^-- Auto-generated' "$WORK/park2t-gas.lua" > "$OUT/park2t-gas.lua"
 cp "$WORK/park2t-chem.lua" "$WORK/park2t-eem.lua" "$OUT/"
+# The Marrone-Treanor forms on the same air (rate_constant.d:395-560, exchange_chemistry_coupling.d:133-227;
+# no reference example uses them): N2 dissociation as a Marrone-Treanor rate (T_D/U = 3) over its Arrhenius
+# rate, coupled by MarroneTreanorDissociation; O2 dissociation as a Modified-Marrone-Treanor rate over its
+# Park rate with a constant non-Boltzmann factor, coupled by ModifiedMarroneTreanorDissociation; NO
+# dissociation unchanged.  The model parameters are test values; theta_v are the species' vibrational
+# temperatures.
+sed -e "s|fr={'Park', A=7.0e21, n=-1.60, C=113200.0, s=0.5},|fr={'Marrone-Treanor', D='N2', TD_on_U=3.0, theta_v=3393.44, rate={'Arrhenius', A=7.0e21, n=-1.60, C=113200.0}},|" \
+    -e "s|fr={'Park', A=2.0e21, n=-1.5, C=59500.0, s=0.5},|fr={'Modified-Marrone-Treanor', D_sp='O2', Thetav=2273.54, aU=0.15, Ustar=40000.0, rate={'Park', A=2.0e21, n=-1.5, C=59500.0, s=0.5}, non_boltzmann_correction={model='constant', factor=0.9}},|" \
+    "$LARC/rm-park-5sp-2T.inp" > "$WORK/rm-mt.inp"
+grep -q "Modified-Marrone-Treanor" "$WORK/rm-mt.inp" && grep -q "'Marrone-Treanor'" "$WORK/rm-mt.inp"
+sed '/^ChemistryCouplingMechanism{/,$d' "$LARC/eem-park-5sp-2T.inp" > "$WORK/eem-mt.inp"
+cat >> "$WORK/eem-mt.inp" <<'EOF2'
+ChemistryCouplingMechanism{
+    reaction_labels = {"r1"},
+    rate = "Marrone-Treanor",
+    coupling_model = {model="MarroneTreanorDissociation", TD_on_U=3.0, Thetav=3393.44}
+}
+ChemistryCouplingMechanism{
+    reaction_labels = {"r2"},
+    rate = "Marrone-Treanor",
+    coupling_model = {model="ModifiedMarroneTreanorDissociation", Thetav=2273.54, aU=0.15, Ustar=40000.0, non_boltzmann=0.1}
+}
+ChemistryCouplingMechanism{
+    reaction_labels = {"r3"},
+    rate = "Marrone-Treanor",
+    coupling_model = {model="ImpartialDissociation"}
+}
+EOF2
+(cd "$WORK" && "$LUA" "$REF/src/kinetics/prep_chem.lua" park2t-gas.lua rm-mt.inp park2tmt-chem.lua > park2tmt-prep.log 2>&1 \
+    && "$LUA" "$REF/src/kinetics/prep_kinetics.lua" park2t-gas.lua park2tmt-chem.lua eem-mt.inp park2tmt-eem.lua \
+        >> park2tmt-prep.log 2>&1) || { cat "$WORK/park2tmt-prep.log"; exit 1; }
+cp "$WORK/park2tmt-chem.lua" "$WORK/park2tmt-eem.lua" "$OUT/"
 # A large mechanism: the 75-species, 474-reaction C2H2/C2H4 model of examples/kinetics/acetylene-ignition-
 # delay (Chemkin format), converted by the reference's chemkin2eilmer (which runs prep-gas itself) and
 # prep_chem, as that example's prep-ignition.sh does.

@@ -14,6 +14,8 @@ from test_gpu_parity import torch_cuda, to_dev
 pytestmark = pytest.mark.gpu
 
 FILES = (mech("park2t-gas.lua"), mech("park2t-chem.lua"), mech("park2t-eem.lua"))
+# the same air with Marrone-Treanor / modified Marrone-Treanor dissociation rates and couplings
+FILES_MT = (mech("park2t-gas.lua"), mech("park2tmt-chem.lua"), mech("park2tmt-eem.lua"))
 
 
 def _cells(n, seed):
@@ -38,12 +40,13 @@ def test_two_temperature_thermo_from_pT():
     assert np.allclose(uve.cpu().numpy(), ref[:, 2], rtol=1e-12, atol=1e-6)
 
 
-def test_two_temperature_update_matches_the_oracle():
+@pytest.mark.parametrize("files", [FILES, FILES_MT], ids=["impartial", "marrone-treanor"])
+def test_two_temperature_update_matches_the_oracle(files):
     from oracle.two_temperature_reactor import TwoTemperatureReactor, ReactorFailure
     from gdtk_gb300.cells import ReactorCells2T
     torch = torch_cuda()
-    rc = ReactorCells2T(*FILES)
-    orc = TwoTemperatureReactor(*FILES)
+    rc = ReactorCells2T(*files)
+    orc = TwoTemperatureReactor(*files)
     n, dt = 96, 1.0e-6
     T, Tve, p, Y = _cells(n, seed=7)
     dT, dTve, dp, dY = to_dev(torch, T, Tve, p, Y)

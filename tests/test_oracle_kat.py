@@ -270,14 +270,16 @@ def test_arrhenius2_and_falloff_forms_restated():
     assert close(kinf * (pr / (1.0 + pr)) * fc / (1.0 + np.log(pr) ** 2), kf[10], 1e-13)
 
 
-def test_two_temperature_reactor_against_a_tight_integration():
+@pytest.mark.parametrize("chem,eem", [("park2t-chem.lua", "park2t-eem.lua"), ("park2tmt-chem.lua", "park2tmt-eem.lua")],
+                         ids=["impartial", "marrone-treanor"])
+def test_two_temperature_reactor_against_a_tight_integration(chem, eem):
     """The two-temperature reactor restatement (oracle/two_temperature_reactor.py) on Park 2-T air
     against a Radau integration (rtol 1e-9) of the same system with every rate at the instantaneous
     state.  The reference algorithm freezes the rate constants and the exchange terms over each RKF
     step (errTol 1e-3), so it agrees to that order only; total energy is conserved exactly."""
     from scipy.integrate import solve_ivp
     from oracle.two_temperature_reactor import TwoTemperatureReactor
-    r = TwoTemperatureReactor(mech("park2t-gas.lua"), mech("park2t-chem.lua"), mech("park2t-eem.lua"))
+    r = TwoTemperatureReactor(mech("park2t-gas.lua"), mech(chem), mech(eem))
     rng = np.random.default_rng(0)
     for _ in range(4):
         T, p = rng.uniform(4000.0, 12000.0), 10.0 ** rng.uniform(3.0, 4.5)
@@ -306,3 +308,30 @@ def test_two_temperature_reactor_against_a_tight_integration():
         Tt, Tvt, _ = r.gas.update_from_rhou(rho, u + uve - y[r.nsp], y[r.nsp], Yt, guess["Tve"])
         assert abs(o["T"] - Tt) / Tt < 1.5e-2 and abs(o["Tve"] - Tvt) / Tvt < 1.5e-2
         assert np.abs(o["massf"] - Yt).max() < 5e-3
+
+
+def test_marrone_treanor_forms_at_thermal_equilibrium():
+    """At T_ve = T the Marrone-Treanor factor of rate_constant.d:438-447 is 1 and the modified form's
+    (:541-554) is its non-Boltzmann factor; the Marrone-Treanor coupling's G_vanish equals its G_appear,
+    and the modified coupling's exceeds it by non_boltzmann R T_D (exchange_chemistry_coupling.d:152-220).
+    The parameters are those prep_chem / prep_kinetics wrote (T_D from the species' heats of formation,
+    U from T_D / U = 3)."""
+    from oracle.two_temperature_reactor import TwoTemperatureReactor, Reaction
+    from oracle.two_temperature import R_UNIVERSAL
+    r = TwoTemperatureReactor(mech("park2t-gas.lua"), mech("park2tmt-chem.lua"), mech("park2tmt-eem.lua"))
+    mt, mmt = r.reactions[0].frc, r.reactions[1].frc
+    assert mt["model"] == "Marrone-Treanor" and mmt["model"] == "Modified-Marrone-Treanor"
+    assert close(mt["U"], mt["T_D"] / 3.0, 1e-9)
+    for T in (3000.0, 7000.0, 12000.0):
+        assert close(Reaction.rate_constant(mt, T, [T]), Reaction.rate_constant(mt["rate"], T, [T]), 1e-12)
+        assert close(Reaction.rate_constant(mmt, T, [T]), 0.9 * Reaction.rate_constant(mmt["rate"], T, [T]), 1e-12)
+        # out of equilibrium the factors move the rate (cold vibration slows dissociation)
+        assert Reaction.rate_constant(mt, T, [0.5 * T]) < Reaction.rate_constant(mt["rate"], T, [0.5 * T])
+    kinds = {m["coupling"]: m for m in r.mechs if m["kind"] == "MT"}
+    assert set(kinds) == {"ImpartialDissociation", "MarroneTreanorDissociation", "ModifiedMarroneTreanorDissociation"}
+    for T in (3000.0, 9000.0):
+        ga, gv = r._coupling(kinds["MarroneTreanorDissociation"], T, T)
+        assert close(gv, ga, 1e-9)
+        m = kinds["ModifiedMarroneTreanorDissociation"]
+        ga, gv = r._coupling(m, T, T)
+        assert close(gv - ga, m["nb"] * R_UNIVERSAL * m["T_D"], 1e-9)
