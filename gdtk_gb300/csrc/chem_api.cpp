@@ -936,11 +936,21 @@ int chem_reactor_update_blocks(int cr_i, int nblock, const gdtk_cell_block* bloc
         auto& r = reactor(cr_i);
         require_cuda();
         if (nblock < 0 || (nblock > 0 && !blocks)) throw std::runtime_error("bad block table");
-        if (flags & (GDTK_CHEM_REFERENCE_ORDER | GDTK_CHEM_WARP_PER_CELL) || r.large)
-            throw std::runtime_error("the block API uses the fast kernel only (a mechanism within " +
-                                     std::to_string(GDTK_MAX_SPECIES) + " species and " +
-                                     std::to_string(GDTK_MAX_REACTIONS) + " reactions)");
+        if (flags & GDTK_CHEM_REFERENCE_ORDER)
+            throw std::runtime_error("the block API runs the fast or the warp-per-cell kernel, not the reference-order one");
         cudaStream_t s = (cudaStream_t)stream;
+        if ((flags & GDTK_CHEM_WARP_PER_CELL) || r.large) {   // one warp per cell: one launch per block, in order
+            if (cell_counters)
+                throw std::runtime_error("per-cell counters of the block API need the thread-per-cell kernel");
+            for (int k = 0; k < nblock; ++k) {
+                const gdtk_cell_block& in = blocks[k];
+                if (in.ncell < 0) throw std::runtime_error("negative block size");
+                if (in.ncell == 0) continue;
+                launch_update(r, in.ncell, in.rho, in.u, in.T, in.p, in.massf, in.dt_chem, in.status, in.t_interval,
+                              T_frozen, flags | GDTK_CHEM_WARP_PER_CELL, s, nullptr, totals);
+            }
+            return 0;
+        }
         if (!r.fast) r.fast.reset(build_fast_kernel(model(r.gm).gm, r.mh, r.req_block, r.req_min_blocks));
         if (!r.counter) check(cudaMalloc(&r.counter, sizeof(unsigned)), "cudaMalloc");
         long long done_cells = 0;

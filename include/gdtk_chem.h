@@ -123,7 +123,9 @@ int chem_reactor_update_cells_ex(int cr_i, int ncell, const double* rho, const d
  * launch (per 128 blocks) whose work counter walks the cells of all blocks in table order, so
  * ordering the table by expected cost (most steps first) shortens the tail.  `first` is set
  * by the library.  The table is passed in the launch parameters: the call can be captured in a
- * CUDA graph and replayed.  cell_counters, when given, is int[6][total cells] in table order. */
+ * CUDA graph and replayed.  cell_counters, when given, is int[6][total cells] in table order.
+ * Mechanisms beyond 32 species / 128 reactions (or GDTK_CHEM_WARP_PER_CELL in flags) run one warp
+ * per cell, one launch per block in table order (also capturable); cell_counters must then be NULL. */
 typedef struct gdtk_cell_block {
     int ncell;
     int first;
