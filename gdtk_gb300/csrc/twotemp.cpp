@@ -120,10 +120,8 @@ struct Reactor2TObj {
     int n_i = 0, n_d = 0;
     Species2T* d_sp = nullptr;
     Eem2T* d_eem = nullptr;
-    unsigned* d_counter = nullptr;
     int sm_count = 0;
     ~Reactor2TObj() {
-        if (d_counter) cudaFree(d_counter);
         if (d_i) cudaFree(d_i);
         if (d_d) cudaFree(d_d);
         if (d_sp) cudaFree(d_sp);
@@ -259,8 +257,6 @@ extern "C" int chem_reactor2t_update_cells(int h, int ncell, const double* rho, 
         a.tol = r.mh.errTol; a.max_subcycles = r.mh.maxSubcycles; a.max_attempts = r.mh.maxAttempts;
         a.ncell = ncell; a.rho = rho; a.T = T; a.Tve = T_ve; a.p = p; a.massf = massf; a.u = u; a.u_ve = u_ve;
         a.dt_chem = dt_chem; a.status = status; a.t_interval = t_interval; a.steps = steps;
-        if (!r.d_counter) ck(cudaMalloc(&r.d_counter, sizeof(unsigned)), "cudaMalloc");
-        a.counter = r.d_counter;
         ck(launch_two_temperature_update(a, r.sm_count, (cudaStream_t)stream), "two-temperature update launch");
         return 0;
     });

@@ -61,7 +61,6 @@ struct TwoTArgs {
     int* status;       // may be null
     double t_interval;
     unsigned long long* steps;   // optional: total RKF step attempts
-    unsigned* counter;           // work counter, set to 0 by the launcher
 };
 
 // p, T, T_ve, Y -> rho, u, u_ve (two_temperature_gas.d:84-92).
@@ -81,7 +80,6 @@ struct Thermo2TArgs {
     double* u_ve;
 };
 
-// A persistent grid (as many blocks as stay resident) takes cells from a.counter, which it zeroes first.
 cudaError_t launch_two_temperature_update(const TwoTArgs& a, int sm_count, cudaStream_t s);
 cudaError_t launch_two_temperature_thermo_pT(const Thermo2TArgs& a, int sm_count, cudaStream_t s);
 

@@ -301,18 +301,6 @@ struct Reactor2T {
     }
 };
 
-// The next cell for this thread: one atomic per group of lanes asking together.
-__device__ __forceinline__ unsigned next_cell(unsigned* counter) {
-    const unsigned mask = __activemask();
-    const int lane = threadIdx.x & 31, leader = __ffs(mask) - 1;
-    unsigned base = 0;
-    if (lane == leader) base = atomicAdd(counter, (unsigned)__popc(mask));
-    base = __shfl_sync(mask, base, leader);
-    return base + __popc(mask & ((1u << lane) - 1u));
-}
-
-// A persistent grid: each thread takes cells from the work counter until they run out, so that a lane whose
-// cell finished early starts another instead of idling until its warp's slowest cell is done.
 __global__ void __launch_bounds__(128) two_temperature_update_kernel(const TwoTArgs a) {
     Reactor2T R;
     R.g.m.bind(a.mech_i, a.mech_d);
@@ -326,10 +314,7 @@ __global__ void __launch_bounds__(128) two_temperature_update_kernel(const TwoTA
     const MechView& m = R.g.m;
     const int nsp = m.nsp, nr = m.nr, nv = nsp + 1;
     unsigned long long my_steps = 0;
-    while (true) {
-        const unsigned cu = next_cell(a.counter);
-        if (cu >= (unsigned)a.ncell) break;
-        const int c = (int)cu;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < a.ncell; c += gridDim.x * blockDim.x) {
         double Y0[GDTK_MAX_SPECIES], Y[GDTK_MAX_SPECIES], y0[NV], yOut[NV], yT[NV], K[6][NV], yErr[NV];
         double kf[GDTK_MAX_REACTIONS], kb[GDTK_MAX_REACTIONS], wf[GDTK_MAX_REACTIONS], wb[GDTK_MAX_REACTIONS];
         double q[GDTK_MAX_SPECIES], L[GDTK_MAX_SPECIES], gs[GDTK_MAX_SPECIES], lt[MAX_EEM], ga[MAX_EEM], gv[MAX_EEM];
@@ -519,16 +504,8 @@ int grid_for_cells(int n, int block, int sm_count) {
 
 cudaError_t launch_two_temperature_update(const TwoTArgs& a, int sm_count, cudaStream_t s) {
     if (a.ncell <= 0) return cudaSuccess;
-    if (a.neem > MAX_EEM || !a.counter) return cudaErrorInvalidValue;
-    int per_sm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, two_temperature_update_kernel, 128, 0);
-    if (e != cudaSuccess) return e;
-    long long grid = (long long)sm_count * (per_sm > 0 ? per_sm : 1);
-    const long long want = ((long long)a.ncell + 127) / 128;
-    if (want < grid) grid = want;
-    e = cudaMemsetAsync(a.counter, 0, sizeof(unsigned), s);
-    if (e != cudaSuccess) return e;
-    two_temperature_update_kernel<<<(unsigned)grid, 128, 0, s>>>(a);
+    if (a.neem > MAX_EEM) return cudaErrorInvalidValue;
+    two_temperature_update_kernel<<<grid_for_cells(a.ncell, 128, sm_count), 128, 0, s>>>(a);
     return cudaGetLastError();
 }
 
