@@ -62,6 +62,16 @@ def lib():
                                          ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int, _l]
         L.oracle_integrate_fixed.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, _d, ctypes.c_double, ctypes.c_double]
         L.oracle_max_threads.restype = ctypes.c_int
+        # the compiled two-temperature reactor (twotemp_oracle.cpp; see two_temperature_reactor.compiled)
+        L.oracle2t_new.restype = ctypes.c_void_p
+        L.oracle2t_new.argtypes = [ctypes.c_void_p, ctypes.c_int, _d, _d, _d, ctypes.c_int, ctypes.c_double,
+                                   ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int]
+        L.oracle2t_free.argtypes = [ctypes.c_void_p]
+        L.oracle2t_add_reaction.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _i, _i, ctypes.c_int, _i, _i,
+                                            ctypes.c_int, _i, _d, _d, _d]
+        L.oracle2t_add_eem.argtypes = [ctypes.c_void_p, _d]
+        L.oracle2t_update.argtypes = [ctypes.c_void_p, ctypes.c_int, _d, _d, _d, _d, _d, ctypes.c_double, _d, _d, _d,
+                                      _i, _l, ctypes.c_int]
         _lib = L
     return _lib
 

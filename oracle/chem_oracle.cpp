@@ -704,6 +704,19 @@ int oracle_set_config(void* h, double T_lower, double T_upper, int method, doubl
 
 int oracle_n_reactions(void* h) { return (int)((Model*)h)->reactions.size(); }
 
+// Species enthalpy at T given ln T, and Cp at T (per species, J/kg); nonzero on a CEA range failure.
+int oracle_species_h(void* h, int isp, double T, double logT, double* out) {
+    Model* m = (Model*)h;
+    try { *out = m->curves[isp].eval_h(T, logT); } catch (Failure& f) { return f.code; }
+    return 0;
+}
+
+int oracle_species_cp(void* h, int isp, double T, double* out) {
+    Model* m = (Model*)h;
+    try { *out = m->curves[isp].eval_Cp(T); } catch (Failure& f) { return f.code; }
+    return 0;
+}
+
 // Species thermo (per species, J/kg): Cp, h, s at T (s at p = P_atm).
 int oracle_species_thermo(void* h, int isp, double T, double* Cp, double* hh, double* s) {
     Model* m = (Model*)h;

@@ -431,3 +431,94 @@ class TwoTemperatureReactor:
             raise ReactorFailure(3, "Hit maximum number of subcycles while attempting 2-T thermochemical update.")
         mf = st["massf"] / math.fsum(st["massf"])
         return dict(T=st["T"], Tve=st["Tve"], p=st["p"], u=u, u_ve=u_ve, massf=mf, dt_suggest=dtSave, steps=steps)
+
+
+# ---- the compiled restatement (oracle/twotemp_oracle.cpp), for timing the CPU side at compiled speed
+_RC_CODE = {"Arrhenius": 0, "fromEqConst": 1, "Park": 6, "Marrone-Treanor": 7, "Modified-Marrone-Treanor": 8}
+_RT_CODE = {"MW": 0, "ParkHTC": 1, "ParkHTC2": 2}
+_CPL_CODE = {"ImpartialDissociation": 0, "MarroneTreanorDissociation": 1, "ModifiedMarroneTreanorDissociation": 2}
+
+
+def _rate_vec(rc):
+    """model, base model, rctIndex, A, n, C, s, T_D, U, theta, aU, Ustar, non-Boltzmann factor."""
+    m = rc["model"]
+    v = np.zeros(13)
+    v[0], v[1], v[2], v[12] = _RC_CODE[m], 0, -1, 1.0
+    base = rc
+    if m in ("Marrone-Treanor", "Modified-Marrone-Treanor"):
+        base = rc["rate"]
+        v[1] = _RC_CODE[base["model"]]
+        v[7], v[9] = rc["T_D"], rc["theta"]
+        if m == "Marrone-Treanor":
+            v[8] = rc["U"]
+        else:
+            v[10], v[11] = rc["aU"], rc["Ustar"]
+            nbc = rc.get("non_boltzmann_correction")
+            v[12] = float(nbc["factor"]) if nbc else 1.0
+    if base["model"] in ("Arrhenius", "fromEqConst"):
+        v[2] = int(base.get("rctIndex", -1))
+    if base["model"] in ("Arrhenius", "Park"):
+        v[3], v[4], v[5] = base["A"], base["n"], base["C"]
+    if base["model"] == "Park":
+        v[6] = base["s"]
+    return v
+
+
+class CompiledTwoTemperatureReactor:
+    """The same reactor in C++ (oracle/twotemp_oracle.cpp), built from a parsed TwoTemperatureReactor;
+    update_cells runs a batch of cells on the host's threads."""
+
+    def __init__(self, r):
+        from . import lib, _dp, _ip
+        self.r = r
+        self.nsp = r.nsp
+        M, cp_tr, h_f = (np.ascontiguousarray(x, np.float64) for x in (r.M, r.gas.cp_tr, r.gas.h_f))
+        self.h = lib().oracle2t_new(r.gas.curves.h, r.nsp, _dp(M), _dp(cp_tr), _dp(h_f), r.gas.electron,
+                                    r.T_lower, r.T_upper, r.tol, r.max_subcycles, r.max_attempts)
+        if not self.h:
+            raise ValueError("oracle2t_new failed")
+        for x in r.reactions:
+            ri = np.array([i for i, _ in x.reac], np.int32); rc = np.array([c for _, c in x.reac], np.int32)
+            pi = np.array([i for i, _ in x.prod], np.int32); pc = np.array([c for _, c in x.prod], np.int32)
+            ei = np.array([i for i, _ in x.eff], np.int32); ev = np.array([e for _, e in x.eff], np.float64)
+            fv, bv = _rate_vec(x.frc), _rate_vec(x.brc)
+            lib().oracle2t_add_reaction(self.h, int(x.collider), len(ri), _ip(ri), _ip(rc), len(pi), _ip(pi), _ip(pc),
+                                        len(ei), _ip(ei), _dp(ev), _dp(fv), _dp(bv))
+        for m in r.mechs:
+            v = np.zeros(19)
+            if m["kind"] == "LT":
+                rt = m["rt"]
+                v[0], v[1], v[2], v[3] = 0, m["p"], m["q"], _RT_CODE[rt["model"]]
+                if rt["model"] == "MW":
+                    v[4], v[5] = rt["a"], rt["b"]
+                else:
+                    v[6], v[7], v[8], v[9] = rt["sigma"], rt["mu"], rt["sub"]["a"], rt["sub"]["b"]
+            else:
+                v[0], v[1], v[10], v[11] = 1, m["p"], m["r"], _CPL_CODE[m["coupling"]]
+                v[13] = m["Thetav"]
+                v[12] = m.get("D", 0.0)
+                v[14] = m.get("U", 0.0)
+                v[15] = m.get("T_D", 0.0)
+                v[16], v[17], v[18] = m.get("aU", 0.0), m.get("Ustar", 0.0), m.get("nb", 0.0)
+            lib().oracle2t_add_eem(self.h, _dp(v))
+
+    def __del__(self):
+        from . import _lib
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.oracle2t_free(self.h)
+            self.h = None
+
+    def update_cells(self, rho, T, Tve, p, massf, t_interval, dt_suggest=None, nthreads=0):
+        """massf (n, nsp).  Returns dict(T, Tve, p, massf, u, u_ve, dt_suggest, status, steps)."""
+        from . import lib, _dp, _ip, _l
+        n = len(rho)
+        rho = np.ascontiguousarray(rho, np.float64)
+        T, Tve, p = (np.array(x, np.float64, copy=True) for x in (T, Tve, p))
+        mf = np.array(massf, np.float64, order="C", copy=True).reshape(n, self.nsp)
+        dt = np.full(n, -1.0) if dt_suggest is None else np.array(dt_suggest, np.float64, copy=True)
+        u, uve = np.zeros(n), np.zeros(n)
+        st = np.zeros(n, np.int32)
+        steps = np.zeros(n, np.int64)
+        lib().oracle2t_update(self.h, n, _dp(rho), _dp(T), _dp(Tve), _dp(p), _dp(mf), t_interval, _dp(dt), _dp(u),
+                              _dp(uve), _ip(st), steps.ctypes.data_as(_l), nthreads)
+        return dict(T=T, Tve=Tve, p=p, massf=mf, u=u, u_ve=uve, dt_suggest=dt, status=st, steps=steps)

@@ -335,3 +335,29 @@ def test_marrone_treanor_forms_at_thermal_equilibrium():
         m = kinds["ModifiedMarroneTreanorDissociation"]
         ga, gv = r._coupling(m, T, T)
         assert close(gv - ga, m["nb"] * R_UNIVERSAL * m["T_D"], 1e-9)
+
+
+@pytest.mark.parametrize("chem,eem", [("park2t-chem.lua", "park2t-eem.lua"), ("park2tmt-chem.lua", "park2tmt-eem.lua")],
+                         ids=["impartial", "marrone-treanor"])
+def test_compiled_two_temperature_reactor_equals_the_restatement(chem, eem):
+    """oracle/twotemp_oracle.cpp (the two-temperature workload's CPU timing reference) against the
+    Python restatement it transcribes: same status and RKF attempts per cell, T and T_ve to 1e-14,
+    mass fractions to 1e-15 (only the final normalising sum is taken differently)."""
+    from oracle.two_temperature_reactor import TwoTemperatureReactor, CompiledTwoTemperatureReactor, ReactorFailure
+    from gdtk_gb300.workloads import air2t_cells
+    r = TwoTemperatureReactor(mech("park2t-gas.lua"), mech(chem), mech(eem))
+    c = CompiledTwoTemperatureReactor(r)
+    n = 24
+    T, Tve, p, Y = air2t_cells(n, seed=13)
+    rho = np.array([r.gas.update_from_pT(p[k], T[k], Tve[k], Y[:, k])[0] for k in range(n)])
+    o = c.update_cells(rho, T, Tve, p, Y.T, 1e-6, nthreads=2)
+    for k in range(n):
+        try:
+            py = r.update(rho[k], T[k], Tve[k], p[k], Y[:, k], 1e-6)
+        except ReactorFailure as f:
+            assert o["status"][k] == f.code
+            continue
+        assert o["status"][k] == 0 and o["steps"][k] == py["steps"]
+        assert close(o["T"][k], py["T"], 1e-14) and close(o["Tve"][k], py["Tve"], 1e-14)
+        assert np.abs(o["massf"][k] - py["massf"]).max() <= 1e-15
+        assert close(o["u_ve"][k], py["u_ve"], 1e-13) and close(o["dt_suggest"][k], py["dt_suggest"], 1e-14)
