@@ -1146,7 +1146,7 @@ int chem_reactor_last_launch(int cr_i, int* grid, int* block, int* smem_bytes, i
 const char* gdtk_last_error(void) { return g_last_error.c_str(); }
 
 int gdtk_exp_host(int n, const double* x, double* y) {
-    static const double tab[64] = GDTK_EXP2_TABLE_INIT;
+    static const double tab[GDTK_EXP2_TABLE_SIZE] = GDTK_EXP2_TABLE_INIT;
     for (int i = 0; i < n; ++i) y[i] = gdtk_exp(x[i], tab);
     return 0;
 }

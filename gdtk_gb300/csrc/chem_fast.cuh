@@ -42,6 +42,7 @@ namespace gdtk_fast {
 using gdtk::gdtk_exp;
 using gdtk::gdtk_div;
 using gdtk::gdtk_div_nr;
+using gdtk::gdtk_add_div;
 
 // must match the host's CellBlock / FastArgs (codegen.h)
 struct CellBlock {
@@ -109,22 +110,71 @@ constexpr double ZERO_EPS = 1.0e-50;
 constexpr double H_MIN = 1.0e-15;
 constexpr double ALLOWABLE_MASSF_ERROR = 1.0e-3;
 
+// ---------------------------------------------------------------- compares on the integer pipe
+// An FP64 compare (DSETP) takes an FP64 issue slot, as costly as an FMA on this GPU, while the
+// bit patterns of doubles can be compared on the integer pipe: for doubles of the same sign the
+// patterns order like the values.  Each helper below gives exactly the IEEE result, NaN included,
+// for the operands its comment allows; the kernel's hot loops compare through them.
+constexpr long long ABS_BITS = 0x7fffffffffffffffLL;
+constexpr long long INF_BITS = 0x7ff0000000000000LL;
+__device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
+// x < c, any x, c > 0 finite
+__device__ __forceinline__ bool lt_pos(double x, double c) {
+    const long long b = dbits(x);
+    return b < dbits(c) && (b >= 0 || (b & ABS_BITS) <= INF_BITS);
+}
+// x > c, any x, c >= 0 finite
+__device__ __forceinline__ bool gt_pos(double x, double c) {
+    const long long b = dbits(x);
+    return b > dbits(c) && b <= INF_BITS;
+}
+// x >= c, any x, c > 0 finite
+__device__ __forceinline__ bool ge_pos(double x, double c) {
+    const long long b = dbits(x);
+    return b >= dbits(c) && b <= INF_BITS;
+}
+// fmin(x, c), any x, c > 0 finite
+__device__ __forceinline__ double min_pos(double x, double c) { return lt_pos(x, c) ? x : c; }
+// a > b for a, b >= +0 or NaN of either sign (not -0.0)
+__device__ __forceinline__ bool gt_nn(double a, double b) {
+    const unsigned long long ua = (unsigned long long)dbits(a), ub = (unsigned long long)dbits(b);
+    return ua > ub && ua <= (unsigned long long)INF_BITS && ub <= (unsigned long long)INF_BITS;
+}
+// a >= b for a, b >= +0 or NaN of either sign (not -0.0)
+__device__ __forceinline__ bool ge_nn(double a, double b) {
+    const unsigned long long ua = (unsigned long long)dbits(a), ub = (unsigned long long)dbits(b);
+    return ua >= ub && ua <= (unsigned long long)INF_BITS && ub <= (unsigned long long)INF_BITS;
+}
+// x != 0.0 (either sign of zero), any x
+__device__ __forceinline__ bool nonzero(double x) { return (dbits(x) & ABS_BITS) != 0; }
+// |x| as a double with the sign bit cleared (an integer operation)
+__device__ __forceinline__ double abs_bits(double x) { return __longlong_as_double(dbits(x) & ABS_BITS); }
+#if GDTK_MIX_THERMO
+// GDTK_MIX_TLO <= T <= GDTK_MIX_THI (both bounds positive), any T
+__device__ __forceinline__ bool in_mix_range(double T) {
+    const long long t = dbits(T);
+    return t >= dbits(GDTK_MIX_TLO) && t <= dbits(GDTK_MIX_THI);
+}
+#endif
+
 // ---------------------------------------------------------------- species thermo
 // Segment choice of cea_thermo_curves.d:150-182: coefficients sa blended towards sb by wb.
+// th[10] holds the segment count as integer bits; th[10 + i] and th[13 + i] the blend window
+// [break_i - blend_{i-1}/2, break_i + blend_{i-1}/2] around break i (i = 1..nseg-1, formed on the
+// host with the reference's arithmetic), th[16 + i] 1 / blend_{i-1}.  The bounds are positive, so
+// for any T but NaN (rejected first) the compares are exact on the bit patterns.
 __device__ __forceinline__ bool seg_of(const double* th, double T, int& sa, int& sb, double& wb) {
-    const int nseg = (int)th[10];
-    const double* br = th + 11;
-    const double* bl = th + 16;
-    const double* rbl = th + 20;
+    const int nseg = (int)dbits(th[10]);
+    const long long t = dbits(T);
     wb = 0.0;
-    if (nseg == 1) { sa = sb = 0; return T == T; }
-    if (T < (br[1] - 0.5 * bl[0])) { sa = sb = 0; return true; }
-    if (T > (br[nseg - 1] + 0.5 * bl[nseg - 2])) { sa = sb = nseg - 1; return true; }
+    if ((t & ABS_BITS) > INF_BITS) return false;   // NaN
+    if (nseg == 1) { sa = sb = 0; return true; }
+    if (t < dbits(th[11])) { sa = sb = 0; return true; }
+    if (t > dbits(th[12 + nseg])) { sa = sb = nseg - 1; return true; }
     for (int i = 1; i < nseg; ++i) {
-        double lo = br[i] - 0.5 * bl[i - 1];
-        double hi = br[i] + 0.5 * bl[i - 1];
-        if (T >= lo && T <= hi) { wb = rbl[i - 1] * (T - lo); sa = i - 1; sb = i; return true; }
-        if (T > hi && i < nseg - 1 && T < (br[i + 1] - 0.5 * bl[i])) { sa = sb = i; return true; }
+        const long long lo = dbits(th[10 + i]), hi = dbits(th[13 + i]);
+        if (t >= lo && t <= hi) { wb = th[16 + i] * (T - th[10 + i]); sa = i - 1; sb = i; return true; }
+        if (t > hi && i < nseg - 1 && t < dbits(th[11 + i])) { sa = sb = i; return true; }
     }
     sa = sb = 0;
     return false;
@@ -146,15 +196,15 @@ __device__ __forceinline__ double poly_G(const double* c, double T, double rT, d
 __device__ __forceinline__ void sp_H_Cp(const double* TH, int i, double T, double lnT, double rT, double rT2, double& H,
                                         double& Cp, int& err) {
     const double* th = TH + i * GDTK_TH_STRIDE;
-    if (T < th[0]) { H = th[2] - th[4] * (th[0] - T); Cp = th[4]; return; }
-    if (T > th[1]) { H = th[3] + th[5] * (T - th[1]); Cp = th[5]; return; }
+    if (lt_pos(T, th[0])) { H = th[2] - th[4] * (th[0] - T); Cp = th[4]; return; }
+    if (gt_pos(T, th[1])) { H = th[3] + th[5] * (T - th[1]); Cp = th[5]; return; }
     int sa, sb;
     double wb;
     if (!seg_of(th, T, sa, sb, wb)) { err = ST_CEA; H = 0.0; Cp = 1.0; return; }
     const double* ca = th + GDTK_TH_SEG0 + 24 * sa;
     H = poly_H(ca, T, lnT, rT);
     Cp = poly_Cp(ca + 8, T, rT, rT2);
-    if (wb != 0.0) {
+    if (nonzero(wb)) {
         const double* cb = th + GDTK_TH_SEG0 + 24 * sb;
         H = fma(wb, poly_H(cb, T, lnT, rT) - H, H);
         Cp = fma(wb, poly_Cp(cb + 8, T, rT, rT2) - Cp, Cp);
@@ -164,11 +214,11 @@ __device__ __forceinline__ void sp_H_Cp(const double* TH, int i, double T, doubl
 __device__ __forceinline__ double sp_G(const double* TH, int i, double T, double lnT, double rT, double rT2, double t1,
                                        double t2, int& err) {
     const double* th = TH + i * GDTK_TH_STRIDE;
-    if (T < th[0]) {
+    if (lt_pos(T, th[0])) {
         double H = th[2] - th[4] * (th[0] - T), S = th[6] - th[4] * (th[8] - lnT);
         return fma(H, rT, -S);
     }
-    if (T > th[1]) {
+    if (gt_pos(T, th[1])) {
         double H = th[3] + th[5] * (T - th[1]), S = th[7] + th[5] * (lnT - th[9]);
         return fma(H, rT, -S);
     }
@@ -176,7 +226,7 @@ __device__ __forceinline__ double sp_G(const double* TH, int i, double T, double
     double wb;
     if (!seg_of(th, T, sa, sb, wb)) { err = ST_CEA; return 0.0; }
     double g = poly_G(TH + i * GDTK_TH_STRIDE + GDTK_TH_SEG0 + 24 * sa + 15, T, rT, rT2, t1, t2);
-    if (wb != 0.0) g = fma(wb, poly_G(TH + i * GDTK_TH_STRIDE + GDTK_TH_SEG0 + 24 * sb + 15, T, rT, rT2, t1, t2) - g, g);
+    if (nonzero(wb)) g = fma(wb, poly_G(TH + i * GDTK_TH_STRIDE + GDTK_TH_SEG0 + 24 * sb + 15, T, rT, rT2, t1, t2) - g, g);
     return g;
 }
 
@@ -221,7 +271,7 @@ __device__ __forceinline__ void mix_H_Cp(const double* m, int ys, double T, doub
 // truncation is below 2^-60 |x|), else a fresh log.  The kernel carries ln T with each cell this way,
 // because a library log costs as much FP64 issue as about 36 FMAs.
 __device__ __forceinline__ double ln_step(double lnT, double x, double T) {
-    if (fabs(x) < 0x1p-10)
+    if ((dbits(x) & ABS_BITS) < dbits(0x1p-10))
         return lnT + x * fma(x, fma(x, fma(x, fma(x, fma(x, -1.0 / 6.0, 0.2), -0.25), 1.0 / 3.0), -0.5), 1.0);
     return log(T);
 }
@@ -247,20 +297,21 @@ __device__ __noinline__ double T_from_u(const double* TH, const double* YR, int 
             const double x = dT * rT;   // dT / T of the previous iterate
             T += dT;
             lnT = ln_step(lnT, x, T);
-            if (gdtk_div(fabs(dT), T) < TOL) { *lnT_io = lnT; return T; }
-            if (it == 10) break;
+            // |dT| / T < TOL (therm_perf_gas_mix.d:452) with the reciprocal the next iteration needs
             rT = gdtk_div(1.0, T);
+            if (lt_pos(abs_bits(dT) * rT, TOL)) { *lnT_io = lnT; return T; }
+            if (it == 10) break;
         }
         const double rT2 = rT * rT;
         double f = 0.0, cv = 0.0;
 #if GDTK_MIX_THERMO
         int sa = 0, sb = 0;
         double wb = 0.0;
-        if (T >= GDTK_MIX_TLO && T <= GDTK_MIX_THI && seg_of(TH, T, sa, sb, wb)) {
+        if (in_mix_range(T) && seg_of(TH, T, sa, sb, wb)) {
             if (sa != seg_a) { mix_coeffs(TH, YR, ys, sa, ma); seg_a = sa; }
             double H, C;
             mix_H_Cp(ma, ys, T, lnT, rT, rT2, H, C);
-            if (wb != 0.0) {
+            if (nonzero(wb)) {
                 if (sb != seg_b) { mix_coeffs(TH, YR, ys, sb, mb); seg_b = sb; }
                 double Hb, Cb;
                 mix_H_Cp(mb, ys, T, lnT, rT, rT2, Hb, Cb);
@@ -286,7 +337,7 @@ __device__ __noinline__ double T_from_u(const double* TH, const double* YR, int 
         dT = -gdtk_div_nr(f - u_tgt, cv);
         ++*iters;
     }
-    if (fabs(dT) > 1e-3) *err = ST_NEWTON;
+    if (gt_pos(abs_bits(dT), 1e-3)) *err = ST_NEWTON;
     *lnT_io = lnT;
     return T;
 }
@@ -327,20 +378,20 @@ __device__ __forceinline__ double sum_pairwise(F d) {
 __device__ __noinline__ void rate_constants(const double* TH, double Tq, double lnTq, double* K, int ks,
                                             const double* etab, double* G, int* err) {
     double T = Tq, lnT = lnTq;   // lnTq = ln Tq
-    if (T < GDTK_T_LOWER) { T = GDTK_T_LOWER; lnT = GDTK_LN_T_LOWER; }
-    if (T > GDTK_T_UPPER) { T = GDTK_T_UPPER; lnT = GDTK_LN_T_UPPER; }
+    if (lt_pos(T, GDTK_T_LOWER)) { T = GDTK_T_LOWER; lnT = GDTK_LN_T_LOWER; }
+    if (gt_pos(T, GDTK_T_UPPER)) { T = GDTK_T_UPPER; lnT = GDTK_LN_T_UPPER; }
     const double rT = gdtk_div(1.0, T), rT2 = rT * rT, t1 = lnT + 1.0, t2 = 1.0 - lnT;
     int e = 0;
 #if GDTK_MIX_THERMO
     // every species takes the same curve segment and blend here: choose them once
     int sa = 0, sb = 0;
     double wb = 0.0;
-    if (T >= GDTK_MIX_TLO && T <= GDTK_MIX_THI && seg_of(TH, T, sa, sb, wb)) {
+    if (in_mix_range(T) && seg_of(TH, T, sa, sb, wb)) {
         GDTK_G_UNROLL
         for (int i = 0; i < GDTK_NSP; ++i) {
             const double* c = TH + i * GDTK_TH_STRIDE + GDTK_TH_SEG0 + 15;
             double g = poly_G(c + 24 * sa, T, rT, rT2, t1, t2);
-            if (wb != 0.0) g = fma(wb, poly_G(c + 24 * sb, T, rT, rT2, t1, t2) - g, g);
+            if (nonzero(wb)) g = fma(wb, poly_G(c + 24 * sb, T, rT, rT2, t1, t2) - g, g);
             G[i * ks] = g;
         }
     } else
@@ -369,14 +420,15 @@ __device__ __forceinline__ double estimate_step(const double (&c)[GDTK_NSP], con
     return fmax(dt_chem, 1.0e-15);
 }
 
-// alpha = N/D (chemistry_update.d:599-604) as N(s)/D(s), s = p h + eps, the reference's
-// rational function with numerator and denominator multiplied by s^3.  For s >= 1e50 the ratio
-// is 1 to double precision in either form, so s is capped there, which keeps N and D finite
-// without a branch.
+// alpha = N/D (chemistry_update.d:599-604) as N(s)/D(s), s = p h, the reference's rational
+// function of r = 1 / (p h + eps) with numerator and denominator multiplied by s^3.  The form has
+// no division by s, so the reference's eps (1e-50, which guards its 1 / (p h)) changes nothing
+// above s = 1e-34 and is left out.  For s >= 1e50 the ratio is 1 to double precision in either
+// form, so s is capped there, which keeps N and D finite without a branch.
 __device__ __forceinline__ void alpha_nd(double s, double& N, double& D) {
-    s = fmin(s, 1.0e50);
+    s = min_pos(s, 1.0e50);
     N = fma(s, fma(s, 11.0 + s, 60.0), 180.0);
-    D = fma(s, fma(s, 12.0 + s, 60.0), 360.0);
+    D = fma(s, s, N + 180.0);   // s^3 + 12 s^2 + 60 s + 360 = N + s^2 + 180
 }
 
 // ---------------------------------------------------------------- the kernel
@@ -395,11 +447,11 @@ __constant__ double RKF_A[5][5] = {
 extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_chem_fast(const __grid_constant__ FastArgs a) {
     extern __shared__ double smem[];
     double* TH = smem;                                   // thermo table, nsp * stride
-    double* ETAB = smem + GDTK_NSP * GDTK_TH_STRIDE;     // exp table, 64
+    double* ETAB = smem + GDTK_NSP * GDTK_TH_STRIDE;     // exp table, GDTK_EXP2_TABLE_SIZE
     const CellBlock* BLK = a.blocks;
-    double* S = ETAB + 64;                               // per-thread vectors
+    double* S = ETAB + GDTK_EXP2_TABLE_SIZE;             // per-thread vectors
     for (int k = threadIdx.x; k < GDTK_NSP * GDTK_TH_STRIDE; k += blockDim.x) TH[k] = a.thermo[k];
-    for (int k = threadIdx.x; k < 64; k += blockDim.x) ETAB[k] = a.exp_table[k];
+    for (int k = threadIdx.x; k < GDTK_EXP2_TABLE_SIZE; k += blockDim.x) ETAB[k] = a.exp_table[k];
     __syncthreads();
     const int ks = blockDim.x;
     double* K = S + threadIdx.x;                         // kf[NR], kb[NR]
@@ -605,18 +657,19 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
                     const double y = y0[i];
                     const double ci_ = (s == 0) ? y : yn[i];
                     const double pp = gdtk_div_nr(L[i], ci_ + ZERO_EPS);
-                    const double x = pp * h;
                     double N, D;
-                    alpha_nd(x + ZERO_EPS, N, D);
+                    alpha_nd(pp * h, N, D);
                     const double q0 = (s == 0) ? q[i] : Q0[i * ks];
-                    const double pb = (s == 0) ? pp : 0.5 * (P0[i * ks] + pp);
-                    const double num = h * (fma(N, q[i] - q0, D * q0) - D * (pb * y));
-                    const double v = y + gdtk_div_nr(num, fma(N, h * pb, D));
+                    const double pb = (s == 0) ? pp : fma(0.5, pp, P0[i * ks]);   // P0 holds p0 / 2
+                    // y + h (N (q - q0) + D (q0 - pb y)) / (N h pb + D)
+                    const double num = h * fma(N, q[i] - q0, D * fma(-pb, y, q0));
+                    const double v = gdtk_add_div(y, num, fma(N, h * pb, D));
                     if (s == 0) {
                         Q0[i * ks] = q[i];
-                        P0[i * ks] = pp;
+                        P0[i * ks] = 0.5 * pp;
                         YP0[i * ks] = v;
-                    } else if (!(v < ZERO_EPS) && fabs(v - YP0[i * ks]) >= GDTK_EPS1 * (v + GDTK_DELTA)) {
+                    } else if (!lt_pos(v, ZERO_EPS) &&
+                               ge_nn(abs_bits(v - YP0[i * ks]), fma(GDTK_EPS1, v, GDTK_EPS1 * GDTK_DELTA))) {
                         conv = false;
                     }
                     yn[i] = v;
@@ -629,12 +682,12 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
 #pragma unroll
             for (int i = 0; i < GDTK_NSP; ++i) {
                 double yc = yn[i];
-                if (yc < ZERO_EPS) continue;
-                const double num = fabs(yc - YP0[i * ks]), den = GDTK_EPS2 * (yc + GDTK_DELTA);
-                if (num * sden > snum * den) { snum = num; sden = den; }
+                if (lt_pos(yc, ZERO_EPS)) continue;
+                const double num = abs_bits(yc - YP0[i * ks]), den = fma(GDTK_EPS2, yc, GDTK_EPS2 * GDTK_DELTA);
+                if (gt_nn(num * sden, snum * den)) { snum = num; sden = den; }
             }
             const double sigma = gdtk_div(snum, sden);
-            if (sigma <= 0.0) dtS = 10.0 * h;
+            if (!nonzero(sigma)) dtS = 10.0 * h;   // sigma <= 0 (sigma is >= 0 or NaN)
             else {
                 double x = sigma;
                 x = x - 0.5 * gdtk_div_nr(x * x - sigma, x);
@@ -650,9 +703,9 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
         if (ok) {   // mass-fraction test (chemistry_update.d:175-185)
             double tot = sum_pairwise([&](int i) {
                 double v = yn[i] * GDTK_M[i] * rrho;
-                return (v < 1.0e-30) ? 0.0 : v;
+                return lt_pos(v, 1.0e-30) ? 0.0 : v;
             });
-            if (fabs(tot - 1.0) > ALLOWABLE_MASSF_ERROR) ok = false;
+            if (gt_pos(abs_bits(tot - 1.0), ALLOWABLE_MASSF_ERROR)) ok = false;
         }
         int fail = 0;
         bool done = false;
@@ -668,7 +721,7 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
 #pragma unroll
                 for (int i = 0; i < GDTK_NSP; ++i) {
                     double v = y0[i] * GDTK_M[i] * rrho;
-                    v = (v < 1.0e-30) ? 0.0 : v;
+                    v = lt_pos(v, 1.0e-30) ? 0.0 : v;
                     double yr = v * GDTK_R[i];
                     V[i * ks] = yr;
                     Rm += yr;
@@ -709,7 +762,7 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
             lane_stat(a.lane_stats, 5);
             auto mf_of = [&](int i) {
                 double v = y0[i] * GDTK_M[i] * rrho;
-                return (v < 1.0e-30) ? 0.0 : v;
+                return lt_pos(v, 1.0e-30) ? 0.0 : v;
             };
             double rtot = gdtk_div(1.0, sum_pairwise(mf_of));
             double Rm = 0.0;
@@ -770,9 +823,9 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
     extern __shared__ double smem[];
     double* TH = smem;
     double* ETAB = smem + GDTK_NSP * GDTK_TH_STRIDE;
-    double* S = ETAB + 64;
+    double* S = ETAB + GDTK_EXP2_TABLE_SIZE;
     for (int k = threadIdx.x; k < GDTK_NSP * GDTK_TH_STRIDE; k += blockDim.x) TH[k] = a.thermo[k];
-    for (int k = threadIdx.x; k < 64; k += blockDim.x) ETAB[k] = a.exp_table[k];
+    for (int k = threadIdx.x; k < GDTK_EXP2_TABLE_SIZE; k += blockDim.x) ETAB[k] = a.exp_table[k];
     __syncthreads();
     const int ks = blockDim.x;
     double* K = S + threadIdx.x;

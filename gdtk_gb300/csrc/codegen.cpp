@@ -18,6 +18,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <fstream>
 #include <functional>
 #include <map>
@@ -236,9 +237,16 @@ std::vector<double> fast_thermo_table(const GasModelHost& gm) {
         th[7] = s[SP_SHIGH] / R;
         th[8] = std::log(s[SP_TLOW]);
         th[9] = std::log(s[SP_THIGH]);
-        th[10] = c.nseg;
-        for (int k = 0; k <= c.nseg; ++k) th[11 + k] = c.breaks[k];
-        for (int k = 0; k < c.nseg - 1; ++k) { th[16 + k] = c.blends[k]; th[20 + k] = 1. / c.blends[k]; }
+        // segment count as integer bits; per break k = 1..nseg-1 the blend window [lo, hi] of
+        // cea_thermo_curves.d:150-182 (break -/+ blend/2, the reference's arithmetic) and 1 / blend
+        const int64_t nseg_bits = c.nseg;
+        std::memcpy(&th[10], &nseg_bits, sizeof nseg_bits);
+        for (int k = 1; k < c.nseg; ++k) {
+            th[10 + k] = c.breaks[k] - 0.5 * c.blends[k - 1];
+            th[13 + k] = c.breaks[k] + 0.5 * c.blends[k - 1];
+            th[16 + k] = 1. / c.blends[k - 1];
+            if (!(th[10 + k] > 0.0)) throw std::runtime_error("thermo curve blend window below 0 K");
+        }
         for (int sg = 0; sg < c.nseg; ++sg) {
             const double* a = c.coeffs.data() + 9 * sg;
             double* h = th + 24 + 24 * sg;
@@ -721,7 +729,7 @@ FastKernel* build_fast_kernel(const GasModelHost& gm, const MechanismHost& mh, i
     const int nsp = gm.n_species(), nr = (int)mh.reactions.size();
     if (nsp > GDTK_MAX_SPECIES || nr > GDTK_MAX_REACTIONS) generate_fast_source(gm, mh, 32, 1);   // throws the reason
     const int per_thread = 2 * nr + fast_vec_doubles(gm, mh);
-    const int table = nsp * 120 + 64;
+    const int table = nsp * 120 + GDTK_EXP2_TABLE_SIZE;
     // Block size: as many resident threads as shared memory allows, up to 256 per SM.  Each resident
     // block also holds the kernel's static shared arrays (at most kStaticSmem bytes, the phase-clock
     // instrumentation) and the 1 KB the hardware reserves per block; one block may use up to 227 KB.
@@ -799,11 +807,11 @@ FastKernel* build_fast_kernel(const GasModelHost& gm, const MechanismHost& mh, i
     cu_check(d.occupancy(&k->blocks_per_sm, fn, block, smem_max), "cuOccupancyMaxActiveBlocksPerMultiprocessor");
     if (k->blocks_per_sm < 1) throw std::runtime_error("fast kernel cannot be resident (registers/shared memory)");
     std::vector<double> th = fast_thermo_table(gm);
-    static const double etab[64] = GDTK_EXP2_TABLE_INIT;
-    if (cudaMalloc(&k->d_thermo, th.size() * 8) != cudaSuccess || cudaMalloc(&k->d_exp, 64 * 8) != cudaSuccess)
+    static const double etab[GDTK_EXP2_TABLE_SIZE] = GDTK_EXP2_TABLE_INIT;
+    if (cudaMalloc(&k->d_thermo, th.size() * 8) != cudaSuccess || cudaMalloc(&k->d_exp, sizeof etab) != cudaSuccess)
         throw std::runtime_error("cudaMalloc failed");
     cudaMemcpy(k->d_thermo, th.data(), th.size() * 8, cudaMemcpyHostToDevice);
-    cudaMemcpy(k->d_exp, etab, 64 * 8, cudaMemcpyHostToDevice);
+    cudaMemcpy(k->d_exp, etab, sizeof etab, cudaMemcpyHostToDevice);
     (void)sms;
     return k.release();
 }
