@@ -206,6 +206,36 @@ def roofline_fp64(issued, n, kernel_ms, peak, ref_flops, traffic, work_per_cell)
         out.update(achieved=f / kernel_s / 1e12, frac=f / kernel_s / 1e12 / peak, issued_flops_per_launch=f,
                    issued_source="profiles/fp64_issued.json (%d-cell ncu capture: %s)" %
                                  (issued["cells"], issued["command"]))
+        # FP64 pipe issue: thread-level DFMA + DADD + DMUL instructions per second against the probe's
+        # FMA instruction rate (peak / 2); a kernel whose every FP64 slot held an FMA on an active lane
+        # would reach 1 on both bases, one whose slots held adds and multiplies reaches 1 here only
+        inst = (issued["dfma"] + issued["dadd"] + issued["dmul"]) / issued["cells"] * n
+        out["fp64_issue"] = {"thread_instructions_per_launch": inst,
+                             "frac": inst / kernel_s / (peak * 1e12 / 2.0),
+                             "basis": "DFMA + DADD + DMUL thread instructions (same capture) per second, "
+                                      "over the DFMA probe's instruction rate"}
+    return out
+
+
+def roofline_fp64_estimated(ref_flops, total_s, peak, extra=None):
+    """FP64 roofline of a workload of the H2-air mechanism without its own issued-FLOP capture: the
+    reference-operation count of its work counters, and from it the issued FLOP estimated with the
+    issued / reference ratio of the h2air-1M capture (same mechanism and kernel; the ratio depends on
+    the mix of rate-constant, right-hand-side and Newton work, so the figure is an estimate)."""
+    rec = profile_record("fp64_issued.json", "h2air-1M")
+    ref = {"achieved": ref_flops / total_s / 1e12, "frac": ref_flops / total_s / 1e12 / peak,
+           "flops": ref_flops,
+           "convention": "reference operations per unit of work: add/sub/mul/div 1, exp/log 20, pow 40"}
+    out = {"bound": "fp64", "achieved": None, "peak": peak, "unit": "TFLOP/s", "frac": None, "traffic": None,
+           "reference_operation_count": ref}
+    if rec and rec.get("reference_flop_per_cell"):
+        ratio = rec["flop_per_cell"] / rec["reference_flop_per_cell"]
+        out.update(achieved=ref["achieved"] * ratio, frac=ref["frac"] * ratio,
+                   basis="issued FP64 FLOP (2 x DFMA + DADD + DMUL), estimated as the reference-operation "
+                         "count x %.4f, the issued / reference ratio of the h2air-1M capture "
+                         "(profiles/fp64_issued.json)" % ratio)
+    if extra:
+        out.update(extra)
     return out
 
 
@@ -341,9 +371,8 @@ def run_blocks(args, w):
                    "l2": "inputs larger than L2 (no flush)"},
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                        "per_step": [round(float(x), 3) for x in lat]},
-        "roofline": {"bound": "fp64", "achieved": flops / (total_ms * 1e-3) / 1e12, "peak": peak, "unit": "TFLOP/s",
-                     "frac": flops / (total_ms * 1e-3) / 1e12 / peak, "traffic": None,
-                     "work_per_cell_update": (tot / (ncell * nsteps)).tolist()},
+        "roofline": roofline_fp64_estimated(flops, total_ms * 1e-3, peak,
+                                            {"work_per_cell_update": (tot / (ncell * nsteps)).tolist()}),
         "cpu_baseline": {"value": cpu_cells / cpu_secs, "unit": "cell-updates/s", "cores": oracle.max_threads(),
                          "kind": "port", "sample": "32 strided cells of each block over the 20 split steps"},
         "e2e": None, "clocks": clk, "gpu_launches": nsteps * 5,
@@ -439,8 +468,7 @@ def run_layer(args, w):
         "accuracy_vs_cpu_reference": {"columns": cols.tolist(), "cells": int(len(idx)), "max_abs_dY": dY,
                                       "max_rel_dT": relT},
         "accuracy_vs_tight_integration": tg,
-        "roofline": {"bound": "fp64", "achieved": flops / (total_ms * 1e-3) / 1e12, "peak": peak,
-                     "unit": "TFLOP/s", "frac": flops / (total_ms * 1e-3) / 1e12 / peak, "traffic": None},
+        "roofline": roofline_fp64_estimated(flops, total_ms * 1e-3, peak),
         "cpu_baseline": {"value": len(idx) * nsteps / cpu_secs, "unit": "cell-updates/s",
                          "cores": oracle.max_threads(), "kind": "port",
                          "sample": "%d full columns (%d cells) over the %d split steps" % (len(cols), len(idx), nsteps)},
@@ -918,7 +946,7 @@ def run_surrogate(args, w):
                    "train_samples": int(n_train), "heldout_fraction": 0.05, "epochs": epochs,
                    "batch": w["batch"], "l2": "inputs larger than L2 (no flush)"},
         "plain_fp64": {"cell_updates_per_s": n / plain_time, "seconds": plain_time,
-                       "roofline_frac": achieved / peak,
+                       "reference_operation_frac": achieved / peak,
                        "cells_failed": int(((plain_st != 0) & (plain_st != 6)).sum().item())},
         "surrogate_speedup_vs_plain": d["speedup_vs_plain"],
         "sweep": sweep,
@@ -930,9 +958,8 @@ def run_surrogate(args, w):
         "heldout": {"rows": int(len(eY)), "median_max_dY": float(np.median(eY)),
                     "p99_max_dY": float(np.percentile(eY, 99)), "max_dY": float(eY.max()),
                     "median_rel_dT": float(np.median(eT)), "p99_rel_dT": float(np.percentile(eT, 99))},
-        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak, "traffic": None,
-                     "kernel": "plain FP64 update of the same cells (the fallback's kernel)"},
+        "roofline": roofline_fp64_estimated(plain_flops, plain_time, peak,
+                                            {"kernel": "plain FP64 update of the same cells (the fallback's kernel)"}),
         "cpu_baseline": cpu, "e2e": None, "clocks": clk,
         # per 1M-cell chunk: features, 5 GEMMs, gate; fallback: gather, cost + 3 ordering kernels,
         # chemistry, scatter; monitor: repack, cost + 3 ordering kernels, chemistry, compare

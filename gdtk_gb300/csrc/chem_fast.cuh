@@ -256,14 +256,18 @@ __device__ __forceinline__ void mix_coeffs(const double* TH, const double* YR, i
     }
 #pragma unroll
     for (int k = 0; k < 8; ++k) m[k * ys] = acc[k];
+    // the Cp/R = d(H/R)/dT coefficients k h_k of the polynomial part, once per segment
+#pragma unroll
+    for (int k = 3; k < 7; ++k) m[(5 + k) * ys] = (double)(k - 1) * acc[k];
 }
-// H/R and Cp/R = d(H/R)/dT of the mixture polynomial m (H/R = -a0/T + a1 lnT + a7 + a2 T + a3/2 T^2 + ...)
+// H/R and Cp/R = d(H/R)/dT of the mixture polynomial m (H/R = -a0/T + a1 lnT + a7 + a2 T + a3/2 T^2 + ...;
+// m[8..11] = 2 h3, 3 h4, 4 h5, 5 h6)
 __device__ __forceinline__ void mix_H_Cp(const double* m, int ys, double T, double lnT, double rT, double rT2,
                                          double& H, double& Cp) {
     const double h0 = m[0], h1 = m[ys], h2 = m[2 * ys], h3 = m[3 * ys], h4 = m[4 * ys], h5 = m[5 * ys],
                  h6 = m[6 * ys], h7 = m[7 * ys];
     H = fma(T, fma(T, fma(T, fma(T, fma(T, h6, h5), h4), h3), h2), fma(h0, rT, fma(h1, lnT, h7)));
-    Cp = fma(T, fma(T, fma(T, fma(T, 5.0 * h6, 4.0 * h5), 3.0 * h4), 2.0 * h3), fma(-h0, rT2, fma(h1, rT, h2)));
+    Cp = fma(T, fma(T, fma(T, fma(T, m[11 * ys], m[10 * ys]), m[9 * ys]), m[8 * ys]), fma(-h0, rT2, fma(h1, rT, h2)));
 }
 #endif
 
@@ -276,20 +280,20 @@ __device__ __forceinline__ double ln_step(double lnT, double x, double T) {
     return log(T);
 }
 
-// *lnT_io: ln T_guess on entry, ln of the returned T on exit.
+// *lnT_io: ln T_guess on entry, ln of the returned T on exit.  ysum = sum_i Y_i R_i, added in species order.
+// S: 24 doubles (stride ys) of scratch for the mixture coefficients.
 __device__ __noinline__ double T_from_u(const double* TH, const double* YR, int ys, double* S, double u_tgt,
-                                        double T_guess, double* lnT_io, int* err, int* iters, unsigned long long* lst) {
+                                        double T_guess, double ysum, double* lnT_io, int* err, int* iters,
+                                        unsigned long long* lst) {
     const double TOL = 1e-10;
     double T = T_guess, dT = 0.0, lnT = *lnT_io, rT = gdtk_div(1.0, T);
 #if GDTK_MIX_THERMO
     double* ma = S;
-    double* mb = S + 8 * ys;
+    double* mb = S + 12 * ys;
     int seg_a = -1, seg_b = -1;
-    double ysum = 0.0;
-#pragma unroll 1
-    for (int i = 0; i < GDTK_NSP; ++i) ysum += YR[i * ys];
 #else
     (void)S;
+    (void)ysum;
 #endif
     for (int it = 0; it <= 10; ++it) {
         lane_stat(lst, 4);
@@ -700,10 +704,12 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
 #endif
         __syncwarp(hm);
         lane_stat(a.lane_stats, 3);
-        if (ok) {   // mass-fraction test (chemistry_update.d:175-185)
+        if (ok) {   // mass-fraction test (chemistry_update.d:175-185); the Y_i go to V for the thermo update
             double tot = sum_pairwise([&](int i) {
                 double v = yn[i] * GDTK_M[i] * rrho;
-                return lt_pos(v, 1.0e-30) ? 0.0 : v;
+                v = lt_pos(v, 1.0e-30) ? 0.0 : v;
+                V[i * ks] = v;
+                return v;
             });
             if (gt_pos(abs_bits(tot - 1.0), ALLOWABLE_MASSF_ERROR)) ok = false;
         }
@@ -716,17 +722,15 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
             double hMax = h * 1.1;
             if (dtS > h) h = fmin(dtS, hMax);
 #if GDTK_TIGHT
-            {   // chemistry_update.d:265-269; Y_i R_i go to V, free until the next step
+            {   // chemistry_update.d:265-269; Y_i (from the mass-fraction test) -> Y_i R_i in V, free until the next step
                 double Rm = 0.0;
 #pragma unroll
                 for (int i = 0; i < GDTK_NSP; ++i) {
-                    double v = y0[i] * GDTK_M[i] * rrho;
-                    v = lt_pos(v, 1.0e-30) ? 0.0 : v;
-                    double yr = v * GDTK_R[i];
+                    double yr = V[i * ks] * GDTK_R[i];
                     V[i * ks] = yr;
                     Rm += yr;
                 }
-                T = T_from_u(TH, V, ks, V + GDTK_NSP * ks, u, T, &lnT, &err, &n_newton, a.lane_stats);
+                T = T_from_u(TH, V, ks, V + GDTK_NSP * ks, u, T, Rm, &lnT, &err, &n_newton, a.lane_stats);
                 p = rho * Rm * T;
                 need_kc = true;
             }
@@ -774,7 +778,7 @@ extern "C" __global__ void __launch_bounds__(GDTK_BLOCK, GDTK_MIN_BLOCKS) gdtk_c
             }
             int st = 0;
             if (a.flags & F_UPDATE_THERMO) {
-                T = T_from_u(TH, V, ks, V + GDTK_NSP * ks, u, T, &lnT, &st, &n_newton, a.lane_stats);
+                T = T_from_u(TH, V, ks, V + GDTK_NSP * ks, u, T, Rm, &lnT, &st, &n_newton, a.lane_stats);
                 p = rho * Rm * T;
             }
             const CellBlock& B = BLK[b];

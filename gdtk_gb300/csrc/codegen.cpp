@@ -361,12 +361,12 @@ bool any_kb_products(const GasModelHost& gm, const MechanismHost& mh) {
 }
 
 // Per-thread method vector (doubles): the ODE method's stage storage, and room for the
-// species' Y_i R_i plus two sets of 8 mixture coefficients during T(rho, u).
+// species' Y_i R_i plus two sets of 12 mixture coefficients during T(rho, u).
 int fast_vec_doubles(const GasModelHost& gm, const MechanismHost& mh) {
     const int nsp = gm.n_species();
     int vec = (mh.method == METHOD_RKF ? 6 : 3) * nsp;
     double tlo, thi;
-    if (mix_thermo_range(gm, tlo, thi)) vec = std::max(vec, nsp + 16);
+    if (mix_thermo_range(gm, tlo, thi)) vec = std::max(vec, nsp + 24);
     int nfall = 0;   // third-body concentrations of pressure-dependent rates, beside G/RT
     for (auto& r : mh.reactions) nfall += r.frc.pressure_dependent() ? 1 : 0;
     // G/RT, the falloff concentrations, then E_i and 1/E_i for the product-form k_b
