@@ -268,8 +268,9 @@ def cpu_reference_run(w, T, p, Y, rho, u, max_seconds, nthreads=0):
     return dict(value=m / secs, cells=m, seconds=secs, threads=threads, out=out, idx=idx)
 
 
-def run_blocks(args, w):
-    """Uneven multi-block batch: one graph replay per split step (returns the JSON line)."""
+def run_blocks(args, w, tune=True, cpu=True):
+    """Uneven multi-block batch: one graph replay per split step (returns the JSON line).  tune=False
+    takes the default launch shape (256 threads, longest-first); cpu=False leaves out the CPU sample."""
     import torch
     import gdtk_gb300
     from gdtk_gb300 import autotune
@@ -278,13 +279,14 @@ def run_blocks(args, w):
     rc = ReactorCells(os.path.join(MECH, w["gas"]), os.path.join(MECH, w["chem"]))
     dev = torch.device("cuda", 0)
     t64 = lambda a: torch.tensor(np.ascontiguousarray(a), dtype=torch.float64, device=dev)
-    # launch-shape autotuning on a sample of the same mixture (cached per mechanism and device)
-    sT, sp, sY = h2air_cells(rc.species_names, rc.mol_masses, 262144, seed=77, gas_file=rc.gmodel.file_name)
-    dT, dp, dY = t64(sT), t64(sp), t64(sY)
-    srho, su = rc.thermo_from_pT(dp, dT, dY)
-    sample = dict(rho=srho, u=su, T=dT, p=dp, massf=dY, dt_chem=torch.full((262144,), -1.0, dtype=torch.float64,
-                                                                         device=dev))
-    choice, oflag, _ = autotune.tune(rc, sample, 1.0e-6, tag="h2air-262144", allow_warp=False)
+    choice, oflag = {}, 0
+    if tune:   # launch-shape autotuning on a sample of the same mixture (cached per mechanism and device)
+        sT, sp, sY = h2air_cells(rc.species_names, rc.mol_masses, 262144, seed=77, gas_file=rc.gmodel.file_name)
+        dT, dp, dY = t64(sT), t64(sp), t64(sY)
+        srho, su = rc.thermo_from_pT(dp, dT, dY)
+        sample = dict(rho=srho, u=su, T=dT, p=dp, massf=dY, dt_chem=torch.full((262144,), -1.0,
+                                                                             dtype=torch.float64, device=dev))
+        choice, oflag, _ = autotune.tune(rc, sample, 1.0e-6, tag="h2air-262144", allow_warp=False)
     flags = UPDATE_THERMO | RETRY | oflag
     spec = h2air_blocks(rc.species_names, rc.mol_masses, nblocks=w["nblocks"], seed=w["seed"],
                         gas_file=rc.gmodel.file_name)
@@ -339,10 +341,11 @@ def run_blocks(args, w):
         for vv, cc in zip(v, c):
             by_status[int(vv)] = by_status.get(int(vv), 0) + int(cc)
     # CPU baseline: the oracle over the same 20 split steps on a strided sample of every block
-    import oracle
-    orc = oracle.Oracle(os.path.join(MECH, w["gas"]), os.path.join(MECH, w["chem"]))
     cpu_cells, cpu_secs = 0, 0.0
-    for b, i in zip(blocks, init):
+    if cpu:
+        import oracle
+        orc = oracle.Oracle(os.path.join(MECH, w["gas"]), os.path.join(MECH, w["chem"]))
+    for b, i in zip(blocks, init) if cpu else ():
         n = b["rho"].shape[0]
         idx = np.arange(0, n, max(n // 32, 1))[:32]
         rho, u = i["rho"].cpu().numpy()[idx], i["u"].cpu().numpy()[idx]
@@ -374,7 +377,8 @@ def run_blocks(args, w):
         "roofline": roofline_fp64_estimated(flops, total_ms * 1e-3, peak,
                                             {"work_per_cell_update": (tot / (ncell * nsteps)).tolist()}),
         "cpu_baseline": {"value": cpu_cells / cpu_secs, "unit": "cell-updates/s", "cores": oracle.max_threads(),
-                         "kind": "port", "sample": "32 strided cells of each block over the 20 split steps"},
+                         "kind": "port", "sample": "32 strided cells of each block over the 20 split steps"}
+                        if cpu else None,
         "e2e": None, "clocks": clk, "gpu_launches": nsteps * 5,
     }
 
@@ -980,6 +984,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true", help="leave out the surrogate + fallback object")
+    ap.add_argument("--no-blocks", action="store_true", help="leave out the 64-block batch object")
     ap.add_argument("--lane-stats", action="store_true",
                     help="after the timed region, one more update with the kernel's lane statistics attached; "
                          "with GDTK_PHASE_CLOCKS=1 in the environment the line also gets each phase's share of "
@@ -1186,6 +1191,21 @@ def main():
         plain_T, plain_Y, plain_st = T.clone(), Y.clone(), st.clone()   # the last timed step's plain result
         sur = surrogate_leg(rc, srho, su, sT, sp, sY, w["dt"], ms_per_step, plain_T, plain_Y, plain_st)
 
+    # ---- the uneven multi-block batch (config of 64 blocks, per-split-step latency), default shape
+    blk = None
+    if rank == 0 and ws == 1 and args.workload == "h2air-1M" and not args.no_blocks:
+        b = run_blocks(args, WORKLOADS["h2air-blocks64"], tune=False, cpu=False)
+        lat = b["latency_ms"]
+        blk = {"workload": "h2air-blocks64", "cell_updates_per_s": b["value"], "cells": b["config"]["cells"],
+               "blocks": b["config"]["blocks"], "split_steps": b["steps"],
+               "ms_per_split_step": {"mean": b["ms_per_step"], "p50": lat["p50"], "p99": lat["p99"],
+                                     "p99_over_p50": lat["p99"] / lat["p50"]},
+               "per_split_step_ms": lat["per_step"], "cells_failed_last_step": b["config"]["cells_failed"],
+               "launch_shape": "default (256 threads x 1 block per SM, longest-first), no tuning",
+               "roofline_frac": b["roofline"]["frac"], "roofline_basis": b["roofline"].get("basis"),
+               "timing": "CUDA events around each graph replay of one split step, after one untimed split step",
+               "clocks": b["clocks"]}
+
     if rank == 0:
         traffic = None
         tj = profile_record("traffic.json", args.workload)
@@ -1211,6 +1231,8 @@ def main():
         }
         if sur is not None:
             line["surrogate"] = sur
+        if blk is not None:
+            line["blocks64"] = blk
         if lanes is not None:
             line["lane_stats"] = lanes
         print(json.dumps(line))
