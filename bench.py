@@ -451,15 +451,20 @@ def run_layer(args, w):
     from oracle.tight import integrate_cell
     zone = np.arange(ny // 2 - 30, ny // 2 + 30, 6)
     tg = {"gpu_dY": 0.0, "gpu_dT": 0.0, "cpu_dY": 0.0, "cpu_dT": 0.0, "cells": int(len(zone))}
+    tight_ref = []
     for j in zone:
         mf, Tt = integrate_cell(orc, crho[j], cu[j], T0[idx][j], Y0[:, idx][:, j], nsteps * w["dt"], rtol=1e-10,
                                 tight=True)
+        tight_ref.append((j, mf, Tt))
         tg["gpu_dY"] = max(tg["gpu_dY"], float(np.abs(gY[j] - mf).max()))
         tg["gpu_dT"] = max(tg["gpu_dT"], float(abs(gT[j] - Tt) / Tt))
         tg["cpu_dY"] = max(tg["cpu_dY"], float(np.abs(cY[j] - mf).max()))
         tg["cpu_dT"] = max(tg["cpu_dT"], float(abs(cT[j] - Tt) / Tt))
     status = st.cpu().numpy()
-    return {
+    sur = None
+    if not args.no_surrogate:
+        sur = layer_surrogate_leg(rc, w, rho, u, init, (T, Y), nsteps, total_ms, idx, (cT, cY), tight_ref, flags)
+    line = {
         "metric": METRIC, "value": n * nsteps / (total_ms * 1e-3), "unit": "cell-updates/s", "n_gpus": 1,
         "steps": nsteps, "warmup": 1, "ms_per_step": total_ms / nsteps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -478,17 +483,112 @@ def run_layer(args, w):
                          "sample": "%d full columns (%d cells) over the %d split steps" % (len(cols), len(idx), nsteps)},
         "e2e": None, "clocks": clk, "gpu_launches": nsteps * 5,
     }
+    if sur is not None:
+        line["surrogate"] = sur
+    return line
 
 
-def train_surrogate(rc, n_train, epochs, error_epochs, batch, seed=7):
+def layer_surrogate_leg(rc, w, rho, u, init, plain, nsteps, plain_ms, idx, cpu_final, tight_ref, flags):
+    """Surrogate + FP64 fallback over the mixing layer's split steps, against the plain GPU update, the
+    CPU reference on the sampled columns and the tight integrations (the surrogate half of the in-loop
+    comparison).  The network is trained on samples of the layer's own states: every 10th split step of
+    an untimed plain run, up to 200,000 unfrozen cells each, advanced by the FP64 update over dt drawn
+    log-uniform in [dt/2, 2 dt] (8,388,608 samples, 5% held out); its error gate is calibrated on 262,144
+    fresh draws from the same states (split-conformal, half the target bars, as in the default line)."""
+    import torch
+    from gdtk_gb300.surrogate import calibrate_error_gate
+    dev = rho.device
+    sync = torch.cuda.synchronize
+    dt, Tf = w["dt"], w["T_frozen"]
+    n = rho.shape[0]
+    t0 = time.perf_counter()
+    T, p, Y, dtc = (x.clone() for x in init)
+    st = torch.zeros(n, dtype=torch.int32, device=dev)
+    g = torch.Generator(device=dev)
+    g.manual_seed(11)
+    pool = []
+    for k in range(nsteps):
+        if k % 10 == 0:
+            live = torch.nonzero(T > Tf).flatten()
+            if live.numel():
+                sel = live[torch.randperm(live.numel(), generator=g, device=dev)[:200000]]
+                pool.append((T[sel].cpu().numpy(), p[sel].cpu().numpy(), Y[:, sel].cpu().numpy()))
+        rc.update(rho, u, T, p, Y, dtc, dt, status=st, T_frozen=Tf, flags=flags)
+    sync()
+    PT = np.concatenate([a[0] for a in pool])
+    Pp = np.concatenate([a[1] for a in pool])
+    PY = np.concatenate([a[2] for a in pool], axis=1)
+
+    def cells(m, seed):
+        r = np.random.Generator(np.random.PCG64(seed)).integers(0, PT.shape[0], m)
+        return PT[r].copy(), Pp[r].copy(), np.ascontiguousarray(PY[:, r])
+
+    sg, X, Yt, train, hold, tr = train_surrogate(rc, 8388608, 30, 8, 8192, seed=13, cells=cells,
+                                                 dt_range=(0.5 * dt, 2.0 * dt))
+    del X, Yt, train, hold
+    torch.cuda.empty_cache()
+    t64 = lambda a: torch.tensor(np.ascontiguousarray(a), dtype=torch.float64, device=dev)
+    cT, cp, cY = cells(262144, 977)
+    sg.set_gate(elem_tol=1e-4, neg_tol=1e-5, T_tol=2e-4, max_dY=0.0)
+    cal = calibrate_error_gate(rc, sg, t64(cT), t64(cp), t64(cY), dt)
+    t_setup = time.perf_counter() - t0
+    # the split steps from the initial state, surrogate + fallback (wall clock, device synchronised: the gate
+    # reads its rejected count on the host)
+    T, p, Y, dtc = (x.clone() for x in init)
+    gate = torch.empty(n, dtype=torch.int32, device=dev)
+    lat, acc_frac = [], []
+    for k in range(nsteps):
+        live = T > Tf
+        sync()
+        t1 = time.perf_counter()
+        sg.update(rho, u, T, p, Y, dtc, dt, status=st, T_frozen=Tf, flags=flags, gate=gate)
+        sync()
+        lat.append((time.perf_counter() - t1) * 1e3)
+        acc_frac.append(float(((gate == 0) & (st == 0) & live).sum()) / max(int(live.sum()), 1))
+    lat = np.array(lat)
+    pT, pY = plain
+    unfrozen = (init[0] > Tf)
+    eY = (Y - pY).abs().amax(dim=0)[unfrozen]
+    eT = ((T - pT).abs() / pT)[unfrozen]
+    gT, gY = T.cpu().numpy()[idx], Y.cpu().numpy()[:, idx].T
+    cT_, cY_ = cpu_final
+    tight = {"cells": len(tight_ref), "max_dY": 0.0, "max_rel_dT": 0.0}
+    for j, mf, Tt in tight_ref:
+        tight["max_dY"] = max(tight["max_dY"], float(np.abs(gY[j] - mf).max()))
+        tight["max_rel_dT"] = max(tight["max_rel_dT"], float(abs(gT[j] - Tt) / Tt))
+    total = float(lat.sum())
+    return {
+        "cell_updates_per_s": n * nsteps / (total * 1e-3), "speedup_vs_plain": plain_ms / total,
+        "ms_per_split_step": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                              "first": float(lat[0]), "last": float(lat[-1])},
+        "accepted_fraction_of_unfrozen_cells": {"mean": float(np.mean(acc_frac)), "first_step": acc_frac[0],
+                                                "last_step": acc_frac[-1]},
+        "final_fields_vs_plain_gpu": {"cells": int(unfrozen.sum()), "max_abs_dY": float(eY.max()),
+                                      "max_rel_dT": float(eT.max())},
+        "final_fields_vs_cpu_reference": {"cells": int(len(idx)), "max_abs_dY": float(np.abs(gY - cY_).max()),
+                                          "max_rel_dT": float((np.abs(gT - cT_) / cT_).max())},
+        "final_fields_vs_tight_integration": tight,
+        "calibration": cal,
+        "training": {"samples": tr["samples"], "heldout": tr["heldout"], "epochs": 30,
+                     "state_pool": int(PT.shape[0]), "sample_generation_s": tr["sample_generation_s"],
+                     "train_s": tr["train_s"], "setup_s_total": t_setup,
+                     "heldout_median_max_dY": float(np.median(tr["eY"])),
+                     "heldout_p99_max_dY": float(np.percentile(tr["eY"], 99))},
+        "timing": "wall clock around each split step with the device synchronised, against the plain line's "
+                  "CUDA-graph replay time",
+    }
+
+
+def train_surrogate(rc, n_train, epochs, error_epochs, batch, seed=7, cells=None, dt_range=(0.5e-6, 2.0e-6)):
     """The surrogate of `rc` trained on n_train samples that the FP64 update generates (5% held out),
-    with its error model.  Returns (sg, X, Y, train rows, held-out rows, info)."""
+    with its error model; `cells` and `dt_range` as for generate_samples (default: the H2-air cells).
+    Returns (sg, X, Y, train rows, held-out rows, info)."""
     import torch
     from gdtk_gb300.surrogate import ChemSurrogate, generate_samples
     dev = torch.device("cuda", 0)
     sync = torch.cuda.synchronize
     sg = ChemSurrogate(rc, width=256, depth=4, seed=0)
-    X, Yt, valid, t_gen = generate_samples(rc, sg, n_train, seed=seed)
+    X, Yt, valid, t_gen = generate_samples(rc, sg, n_train, seed=seed, cells=cells, dt_range=dt_range)
     rows = torch.nonzero(valid).flatten().to(torch.int32)
     g = torch.Generator(device=dev)
     g.manual_seed(0)
