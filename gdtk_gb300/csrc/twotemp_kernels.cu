@@ -1,7 +1,7 @@
 // twotemp_kernels.cu -- the multi-temperature thermochemical reactor for a two-temperature gas, one
-// thread per cell, with the reference's operations (library exp/pow/log) compiled with FMA contraction:
-// results differ from the reference's evaluation order in rounding only (tested to 1e-8 in Y, 1e-7
-// relative in T, T_ve and p), and the contraction makes the update about 16% faster.
+// thread per cell, compiled with FMA contraction and with the rate constants and equilibrium constants
+// in log form (one exp where the reference takes pows and an exp): results differ from the reference's
+// evaluation order in rounding only (tested to 1e-8 in Y, 1e-7 relative in T, T_ve and p).
 //
 // kinetics/multi_temperature_thermochemical_reactor.d:137-294 (opCall) and :334-431 (Cash-Karp RKF
 // on the concentrations and u_ve), with
@@ -124,13 +124,15 @@ __device__ __forceinline__ double pow_int(double x, int n) {   // small positive
     return r;
 }
 
-// An Arrhenius (at T) or Park (at T^s T_ve^(1-s)) rate constant from the record's A, n, C, s.
-__device__ double base_rc(int model, const double* d, double T, double Tve) {
+// An Arrhenius (at T) or Park (at T_e = T^s T_ve^(1-s)) rate constant from the record's A, n, C, s, in log
+// form: A exp(n ln T_e - C / T_e) with ln T_e = s ln T + (1 - s) ln T_ve from the logs of the subcycle
+// (rate_constant.d:72-75, 364-393 evaluate the same expression with three pow calls and an exp).
+__device__ double base_rc(int model, const double* d, double T, double lnT, double lnTve) {
     if (model == RATE_PARK) {
-        const double Te = pow(T, d[RD_S]) * pow(Tve, 1.0 - d[RD_S]);
-        return d[0] * pow(Te, d[1]) * exp(-d[2] / Te);
+        const double lnTe = d[RD_S] * lnT + (1.0 - d[RD_S]) * lnTve;
+        return d[0] * exp(d[1] * lnTe - d[2] / exp(lnTe));
     }
-    return d[0] * pow(T, d[1]) * exp(-d[2] / T);
+    return d[0] * exp(d[1] * lnT - d[2] / T);
 }
 
 // rate_constant.d:397-404
@@ -142,10 +144,10 @@ __device__ __forceinline__ double Q_mt(double T, double D, double theta) {
 
 // Forward rate constant of reaction ir at (T, T_ve): Arrhenius, Park, or the (modified) Marrone-Treanor
 // non-equilibrium factor times the underlying one (rate_constant.d:438-447, 541-554).
-__device__ double forward_rc(const int* r, const double* d, double T, double Tve) {
+__device__ double forward_rc(const int* r, const double* d, double T, double Tve, double lnT, double lnTve) {
     const int model = r[RX_FRC];
-    if (model != RATE_MT && model != RATE_MMT) return base_rc(model, d, T, Tve);
-    const double kEQ = base_rc(r[RX_BASE], d, T, Tve);
+    if (model != RATE_MT && model != RATE_MMT) return base_rc(model, d, T, lnT, lnTve);
+    const double kEQ = base_rc(r[RX_BASE], d, T, lnT, lnTve);
     const double TD = d[RD_MT_TD], th = d[RD_MT_THETA];
     if (model == RATE_MT) {
         const double U = d[RD_MT_U];
@@ -175,7 +177,8 @@ struct Reactor2T {
         double T = Tq;
         if (T < m.T_lower()) T = m.T_lower();
         if (T > m.T_upper()) T = m.T_upper();
-        const double logT = log(T);
+        const double logT = log(T), logTve = log(Tve);
+        const double lnPRT = log(P_atm / (R_universal * T));
         for (int i = 0; i < m.nsp; ++i) gs[i] = cea_h(m, i, T, logT, err) - T * cea_s(m, i, T, logT, err);
         for (int ir = 0; ir < m.nr; ++ir) {
             const int* r = m.rx(ir);
@@ -188,15 +191,15 @@ struct Reactor2T {
                     dG += nu * gs[isp] * m.sp(isp)[SP_M];
                     nuSum += nu;
                 }
-                const double K_p = exp(-dG / (R_universal * T));
-                Kc = K_p * pow(P_atm / (R_universal * T), nuSum);
+                // K_p (P_atm / R T)^sum(nu) as one exponential (reaction.d:26-52)
+                Kc = exp(fma(nuSum, lnPRT, -dG / (R_universal * T)));
             }
             if (r[RX_FRC] != RATE_FROM_EQ) {
-                kf[ir] = forward_rc(r, d, T, Tve);
-                kb[ir] = (r[RX_BRC] == RATE_FROM_EQ) ? forward_rc(r, d, T, T) / Kc
-                                                     : d[3] * pow(T, d[4]) * exp(-d[5] / T);
+                kf[ir] = forward_rc(r, d, T, Tve, logT, logTve);
+                kb[ir] = (r[RX_BRC] == RATE_FROM_EQ) ? forward_rc(r, d, T, T, logT, logT) / Kc
+                                                     : d[3] * exp(d[4] * logT - d[5] / T);
             } else {
-                kb[ir] = d[3] * pow(T, d[4]) * exp(-d[5] / T);
+                kb[ir] = d[3] * exp(d[4] * logT - d[5] / T);
                 kf[ir] = kb[ir] * Kc;   // the backward rate constant at the state itself (reaction.d:131)
             }
         }

@@ -173,6 +173,25 @@ def test_frozen_and_bad_cells(park5):
 
 
 @pytest.mark.parametrize("kernel", sorted(KERNELS))
+def test_temperature_edges_match_the_oracle(j92, kernel):
+    # The fast kernel compares doubles on their bit patterns (rate-constant clamp, curve segment and blend
+    # window, the mixture-coefficient range, the extrapolation beyond the curves): cells that start exactly
+    # on, just below and just above each of those edges take the oracle's branch.  J92: T limits 300 K and
+    # 50,000 K; CEA breaks 200 / 1000 / 6000 K with blend windows [800, 1200] and [5500, 6500]; the
+    # mixture-coefficient range ends at 5,500 K.
+    from gdtk_gb300.workloads import h2air_cells
+    rc, orc = j92
+    edges = [150.0, 199.99999, 200.0, 250.0, 300.0, 300.00001, 799.99999, 800.0, 800.00001, 1199.99999, 1200.0,
+             1200.00001, 5499.99999, 5500.0, 5500.00001, 6499.99999, 6500.0, 6500.00001]
+    per = 4
+    T, p, Y = h2air_cells(rc.species_names, rc.mol_masses, len(edges) * per, seed=23, gas_file=rc.gmodel.file_name)
+    T = np.repeat(np.array(edges), per)
+    p = np.full(T.shape, 1.0e5)
+    g, o, _, _ = run_pair(rc, orc, T, p, Y, 1.0e-7, kernel=kernel)
+    assert_parity(g, o, min_same_path=0.9)
+
+
+@pytest.mark.parametrize("kernel", sorted(KERNELS))
 def test_failure_restores_state_and_retry(tmp_path, kernel):
     # A mechanism allowed only 3 subcycles cannot finish 1e-6 s from a fresh start: both the
     # first try and the dt_chem = -1 retry hit maxSubcycles; the cell is left as it was.
