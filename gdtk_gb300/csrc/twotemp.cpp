@@ -120,8 +120,10 @@ struct Reactor2TObj {
     int n_i = 0, n_d = 0;
     Species2T* d_sp = nullptr;
     Eem2T* d_eem = nullptr;
+    unsigned* d_counter = nullptr;   // work counter of the update's persistent launch
     int sm_count = 0;
     ~Reactor2TObj() {
+        if (d_counter) cudaFree(d_counter);
         if (d_i) cudaFree(d_i);
         if (d_d) cudaFree(d_d);
         if (d_sp) cudaFree(d_sp);
@@ -208,6 +210,7 @@ extern "C" int chem_reactor2t_new(const char* gas_file, const char* chem_file, c
         ck(cudaMalloc(&r->d_d, pm.D.size() * sizeof(double)), "cudaMalloc");
         ck(cudaMalloc(&r->d_sp, sp.size() * sizeof(Species2T)), "cudaMalloc");
         ck(cudaMalloc(&r->d_eem, std::max<size_t>(1, eem.size()) * sizeof(Eem2T)), "cudaMalloc");
+        ck(cudaMalloc(&r->d_counter, sizeof(unsigned)), "cudaMalloc");
         ck(cudaMemcpy(r->d_i, pm.I.data(), pm.I.size() * sizeof(int), cudaMemcpyHostToDevice), "cudaMemcpy");
         ck(cudaMemcpy(r->d_d, pm.D.data(), pm.D.size() * sizeof(double), cudaMemcpyHostToDevice), "cudaMemcpy");
         ck(cudaMemcpy(r->d_sp, sp.data(), sp.size() * sizeof(Species2T), cudaMemcpyHostToDevice), "cudaMemcpy");
@@ -257,6 +260,7 @@ extern "C" int chem_reactor2t_update_cells(int h, int ncell, const double* rho, 
         a.tol = r.mh.errTol; a.max_subcycles = r.mh.maxSubcycles; a.max_attempts = r.mh.maxAttempts;
         a.ncell = ncell; a.rho = rho; a.T = T; a.Tve = T_ve; a.p = p; a.massf = massf; a.u = u; a.u_ve = u_ve;
         a.dt_chem = dt_chem; a.status = status; a.t_interval = t_interval; a.steps = steps;
+        a.counter = r.d_counter;
         ck(launch_two_temperature_update(a, r.sm_count, (cudaStream_t)stream), "two-temperature update launch");
         return 0;
     });

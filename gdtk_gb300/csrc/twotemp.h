@@ -61,6 +61,7 @@ struct TwoTArgs {
     int* status;       // may be null
     double t_interval;
     unsigned long long* steps;   // optional: total RKF step attempts
+    unsigned* counter;           // work counter of the persistent launch (zeroed by the launcher)
 };
 
 // p, T, T_ve, Y -> rho, u, u_ve (two_temperature_gas.d:84-92).

@@ -306,6 +306,12 @@ struct Reactor2T {
     }
 };
 
+// One thread per cell in a persistent grid.  All 32 lanes of a warp stay in the loop until the warp is out
+// of work, and every loop iteration is one RKF attempt (preceded, where a lane starts a cell or a subcycle,
+// by that work) for every lane that holds a cell; lanes whose cell is done take the next cells from a
+// work counter, one atomic per warp.  Cells of uneven attempt counts then keep the lanes busy, where a
+// fixed cell per thread would leave a warp's lanes idle until its slowest cell finishes.  The operations
+// per cell are those of the subcycle and attempt loops of multi_temperature_thermochemical_reactor.d:137-294.
 __global__ void __launch_bounds__(128) two_temperature_update_kernel(const TwoTArgs a) {
     Reactor2T R;
     R.g.m.bind(a.mech_i, a.mech_d);
@@ -317,47 +323,79 @@ __global__ void __launch_bounds__(128) two_temperature_update_kernel(const TwoTA
     R.max_subcycles = a.max_subcycles;
     R.max_attempts = a.max_attempts;
     const MechView& m = R.g.m;
-    const int nsp = m.nsp, nr = m.nr, nv = nsp + 1;
+    const int nsp = m.nsp, nv = nsp + 1;
+    const double tI = a.t_interval;
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
     unsigned long long my_steps = 0;
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < a.ncell; c += gridDim.x * blockDim.x) {
-        double Y0[GDTK_MAX_SPECIES], Y[GDTK_MAX_SPECIES], y0[NV], yOut[NV], yT[NV], K[6][NV], yErr[NV];
-        double kf[GDTK_MAX_REACTIONS], kb[GDTK_MAX_REACTIONS], wf[GDTK_MAX_REACTIONS], wb[GDTK_MAX_REACTIONS];
-        double q[GDTK_MAX_SPECIES], L[GDTK_MAX_SPECIES], gs[GDTK_MAX_SPECIES], lt[MAX_EEM], ga[MAX_EEM], gv[MAX_EEM];
-        double molef[GDTK_MAX_SPECIES], numden[GDTK_MAX_SPECIES];
-        const double rho = a.rho[c];
-        double T = a.T[c], Tve = a.Tve[c], p = a.p[c];
-        for (int i = 0; i < nsp; ++i) { Y0[i] = a.massf[(size_t)i * a.ncell + c]; Y[i] = Y0[i]; }
-        int fail = 0, err = 0;
-        if (isnan(rho) || rho <= 0.0) fail = CELL_BAD_INPUT;
-        double dt_suggest = a.dt_chem[c], dtSave = dt_suggest, u = 0.0, u_ve = 0.0;
-        const double tI = a.t_interval;
-        if (!fail) {
-            const double u_total = R.g.e_tr_mix(Y, T) + R.g.e_ve_mix(Y, Tve, err);
-            double t = 0.0, h;
-            for (int i = 0; i < nsp; ++i) {
-                const double v = Y[i] * rho / m.sp(i)[SP_M];
-                y0[i] = v < 1.0e-30 ? 0.0 : v;   // gas_model.d:237-256
-            }
-            y0[nsp] = R.g.e_ve_mix(Y, Tve, err);
-            R.rate_constants(T, Tve, kf, kb, gs, err);
-            if (dt_suggest > tI) {
-                h = tI;
-            } else if (dt_suggest <= 0.0) {   // reaction_mechanism.d:161-203
-                R.split_rates(y0, kf, kb, wf, wb, q, L);
-                double min_dt = 1.0e6;
-                for (int i = 0; i < nsp; ++i) {
-                    if (y0[i] > 0.0 && fabs(q[i] - L[i]) > 1.0e-30) {
-                        const double dt = (q[i] > 10000.0 * L[i]) ? y0[i] / (L[i] + 1.0e-50) : fabs(y0[i] / (q[i] - L[i]));
-                        min_dt = fmin(min_dt, dt);
-                    }
+    double Y[GDTK_MAX_SPECIES], y0[NV], yOut[NV], yT[NV], K[6][NV], yErr[NV];
+    double kf[GDTK_MAX_REACTIONS], kb[GDTK_MAX_REACTIONS], wf[GDTK_MAX_REACTIONS], wb[GDTK_MAX_REACTIONS];
+    double q[GDTK_MAX_SPECIES], L[GDTK_MAX_SPECIES], gs[GDTK_MAX_SPECIES], lt[MAX_EEM], ga[MAX_EEM], gv[MAX_EEM];
+    double molef[GDTK_MAX_SPECIES], numden[GDTK_MAX_SPECIES];
+    int c = 0, phase = 0, cycle = 0, attempt = 0, fail = 0, err = 0;
+    bool have = false, alive = true;
+    double rho = 0.0, T = 0.0, Tve = 0.0, p = 0.0, t = 0.0, h = 0.0, dt_suggest = 0.0, dtSave = 0.0;
+    double u_total = 0.0, u = 0.0, u_ve = 0.0;
+    while (true) {
+        const unsigned need = __ballot_sync(FULL, alive && !have);
+        if (need) {   // refill: one atomic per warp for all lanes that need a cell
+            const int leader = __ffs(need) - 1;
+            unsigned base = 0;
+            if (lane == leader) base = atomicAdd(a.counter, (unsigned)__popc(need));
+            base = __shfl_sync(FULL, base, leader);
+            if (alive && !have) {
+                const unsigned pos = base + __popc(need & ((1u << lane) - 1u));
+                if (pos >= (unsigned)a.ncell) {
+                    alive = false;
+                } else {
+                    c = (int)pos;
+                    have = true;
+                    phase = 0;
                 }
-                h = fmax(fmin(1.0e-3 * min_dt, 1.0e-10), 1.0e-15);
-            } else {
-                h = dt_suggest;
             }
-            int cycle = 0;
-            for (; cycle < R.max_subcycles && !fail; ++cycle) {
-                // subcycle's rate constants, relaxation times and exchange terms on the gas state
+        }
+        if (!__any_sync(FULL, alive || have)) break;
+        if (have) {
+            bool done = false;
+            if (phase == 0) {   // the cell's state and first step size
+                rho = a.rho[c];
+                T = a.T[c]; Tve = a.Tve[c]; p = a.p[c];
+                for (int i = 0; i < nsp; ++i) Y[i] = a.massf[(size_t)i * a.ncell + c];
+                fail = 0; err = 0;
+                dt_suggest = a.dt_chem[c]; dtSave = dt_suggest; u = 0.0; u_ve = 0.0;
+                if (isnan(rho) || rho <= 0.0) {
+                    fail = CELL_BAD_INPUT;
+                } else {
+                    u_total = R.g.e_tr_mix(Y, T) + R.g.e_ve_mix(Y, Tve, err);
+                    t = 0.0;
+                    for (int i = 0; i < nsp; ++i) {
+                        const double v = Y[i] * rho / m.sp(i)[SP_M];
+                        y0[i] = v < 1.0e-30 ? 0.0 : v;   // gas_model.d:237-256
+                    }
+                    y0[nsp] = R.g.e_ve_mix(Y, Tve, err);
+                    R.rate_constants(T, Tve, kf, kb, gs, err);
+                    if (dt_suggest > tI) {
+                        h = tI;
+                    } else if (dt_suggest <= 0.0) {   // reaction_mechanism.d:161-203
+                        R.split_rates(y0, kf, kb, wf, wb, q, L);
+                        double min_dt = 1.0e6;
+                        for (int i = 0; i < nsp; ++i) {
+                            if (y0[i] > 0.0 && fabs(q[i] - L[i]) > 1.0e-30) {
+                                const double dt = (q[i] > 10000.0 * L[i]) ? y0[i] / (L[i] + 1.0e-50)
+                                                                          : fabs(y0[i] / (q[i] - L[i]));
+                                min_dt = fmin(min_dt, dt);
+                            }
+                        }
+                        h = fmax(fmin(1.0e-3 * min_dt, 1.0e-10), 1.0e-15);
+                    } else {
+                        h = dt_suggest;
+                    }
+                    cycle = 0;
+                    phase = 1;
+                    if (R.max_subcycles <= 0) fail = CELL_MAX_SUBCYCLES;
+                }
+            }
+            if (!fail && phase == 1) {   // a subcycle's rate constants, relaxation times and exchange terms
                 R.rate_constants(T, Tve, kf, kb, gs, err);
                 double mol = 0.0;
                 for (int i = 0; i < nsp; ++i) mol += Y[i] / m.sp(i)[SP_M];
@@ -381,100 +419,106 @@ __global__ void __launch_bounds__(128) two_temperature_update_kernel(const TwoTA
                 }
                 dtSave = dt_suggest;
                 h = fmin(h, tI - t);
-                int attempt = 0;
-                for (; attempt < R.max_attempts; ++attempt) {
-                    // Cash-Karp (multi_temperature_thermochemical_reactor.d:334-431)
-                    const double a21 = 1. / 5., a31 = 3. / 40., a32 = 9. / 40., a41 = 3. / 10., a42 = -9. / 10.,
-                                 a43 = 6. / 5., a51 = -11. / 54., a52 = 5. / 2., a53 = -70. / 27., a54 = 35. / 27.,
-                                 a61 = 1631. / 55296., a62 = 175. / 512., a63 = 575. / 13824.,
-                                 a64 = 44275. / 110592., a65 = 253. / 4096.;
-                    const double b51 = 37. / 378., b53 = 250. / 621., b54 = 125. / 594., b56 = 512. / 1771.,
-                                 b41 = 2825. / 27648., b43 = 18575. / 48384., b44 = 13525. / 55296.,
-                                 b45 = 277. / 14336., b46 = 1.0 / 4.0;
-                    R.rates(y0, kf, kb, lt, ga, gv, rho, wf, wb, q, L, K[0]);
-                    for (int i = 0; i < nv; ++i) yT[i] = y0[i] + h * a21 * K[0][i];
-                    R.rates(yT, kf, kb, lt, ga, gv, rho, wf, wb, q, L, K[1]);
-                    for (int i = 0; i < nv; ++i) yT[i] = y0[i] + h * (a31 * K[0][i] + a32 * K[1][i]);
-                    R.rates(yT, kf, kb, lt, ga, gv, rho, wf, wb, q, L, K[2]);
-                    for (int i = 0; i < nv; ++i) yT[i] = y0[i] + h * (a41 * K[0][i] + a42 * K[1][i] + a43 * K[2][i]);
-                    R.rates(yT, kf, kb, lt, ga, gv, rho, wf, wb, q, L, K[3]);
-                    for (int i = 0; i < nv; ++i)
-                        yT[i] = y0[i] + h * (a51 * K[0][i] + a52 * K[1][i] + a53 * K[2][i] + a54 * K[3][i]);
-                    R.rates(yT, kf, kb, lt, ga, gv, rho, wf, wb, q, L, K[4]);
-                    for (int i = 0; i < nv; ++i)
-                        yT[i] = y0[i] + h * (a61 * K[0][i] + a62 * K[1][i] + a63 * K[2][i] + a64 * K[3][i] +
-                                             a65 * K[4][i]);
-                    R.rates(yT, kf, kb, lt, ga, gv, rho, wf, wb, q, L, K[5]);
-                    for (int i = 0; i < nv; ++i)
-                        yOut[i] = y0[i] + h * (b51 * K[0][i] + b53 * K[2][i] + b54 * K[3][i] + b56 * K[5][i]);
-                    for (int i = 0; i < nv; ++i)
-                        yErr[i] = yOut[i] - (y0[i] + h * (b41 * K[0][i] + b43 * K[2][i] + b44 * K[3][i] +
-                                                          b45 * K[4][i] + b46 * K[5][i]));
-                    double e2 = 0.0;
-                    for (int i = 0; i < nv; ++i) {
-                        const double sk = R.tol + R.tol * fmax(fabs(y0[i]), fabs(yOut[i]));
-                        e2 += (yErr[i] / sk) * (yErr[i] / sk);
-                    }
-                    const double en = sqrt(e2 / nv);
-                    bool ok;
-                    if (en <= 1.0) {
-                        double scale = (en == 0.0) ? 10.0 : 0.9 * pow(en, -0.2);
-                        if (en != 0.0) scale = fmin(fmax(scale, 0.2), 10.0);
-                        dt_suggest = scale * h;
-                        ok = true;
-                    } else {
-                        dt_suggest = fmax(0.9 * pow(en, -0.2), 0.2) * h;
-                        ok = false;
-                    }
-                    ++my_steps;
-                    bool passed = true;
-                    if (ok) {
-                        double tot = 0.0;
-                        for (int i = 0; i < nsp; ++i) {
-                            const double v = yOut[i] * m.sp(i)[SP_M] / rho;
-                            Y[i] = v < 1.0e-30 ? 0.0 : v;   // conc2massf (gas_model.d:258-271)
-                            tot += Y[i];
-                        }
-                        if (fabs(tot - 1.0) > ALLOWABLE_MASSF_ERROR) passed = false;
-                    }
-                    if (ok && passed) {
-                        t += h;
-                        for (int i = 0; i < nv; ++i) y0[i] = yOut[i];
-                        const double hMax = h * (1.0 + 10.0 / 100.0);
-                        if (dt_suggest > h) h = fmin(dt_suggest, hMax);
-                        break;
-                    }
-                    h /= 10.0;
-                    if (h < H_MIN) { fail = CELL_H_MIN; break; }
+                attempt = 0;
+                phase = 2;
+                if (R.max_attempts <= 0) fail = CELL_MAX_ATTEMPTS;
+            }
+            if (!fail && phase == 2) {   // one Cash-Karp attempt (multi_temperature_thermochemical_reactor.d:334-431)
+                const double a21 = 1. / 5., a31 = 3. / 40., a32 = 9. / 40., a41 = 3. / 10., a42 = -9. / 10.,
+                             a43 = 6. / 5., a51 = -11. / 54., a52 = 5. / 2., a53 = -70. / 27., a54 = 35. / 27.,
+                             a61 = 1631. / 55296., a62 = 175. / 512., a63 = 575. / 13824.,
+                             a64 = 44275. / 110592., a65 = 253. / 4096.;
+                const double b51 = 37. / 378., b53 = 250. / 621., b54 = 125. / 594., b56 = 512. / 1771.,
+                             b41 = 2825. / 27648., b43 = 18575. / 48384., b44 = 13525. / 55296.,
+                             b45 = 277. / 14336., b46 = 1.0 / 4.0;
+                R.rates(y0, kf, kb, lt, ga, gv, rho, wf, wb, q, L, K[0]);
+                for (int i = 0; i < nv; ++i) yT[i] = y0[i] + h * a21 * K[0][i];
+                R.rates(yT, kf, kb, lt, ga, gv, rho, wf, wb, q, L, K[1]);
+                for (int i = 0; i < nv; ++i) yT[i] = y0[i] + h * (a31 * K[0][i] + a32 * K[1][i]);
+                R.rates(yT, kf, kb, lt, ga, gv, rho, wf, wb, q, L, K[2]);
+                for (int i = 0; i < nv; ++i) yT[i] = y0[i] + h * (a41 * K[0][i] + a42 * K[1][i] + a43 * K[2][i]);
+                R.rates(yT, kf, kb, lt, ga, gv, rho, wf, wb, q, L, K[3]);
+                for (int i = 0; i < nv; ++i)
+                    yT[i] = y0[i] + h * (a51 * K[0][i] + a52 * K[1][i] + a53 * K[2][i] + a54 * K[3][i]);
+                R.rates(yT, kf, kb, lt, ga, gv, rho, wf, wb, q, L, K[4]);
+                for (int i = 0; i < nv; ++i)
+                    yT[i] = y0[i] + h * (a61 * K[0][i] + a62 * K[1][i] + a63 * K[2][i] + a64 * K[3][i] +
+                                         a65 * K[4][i]);
+                R.rates(yT, kf, kb, lt, ga, gv, rho, wf, wb, q, L, K[5]);
+                for (int i = 0; i < nv; ++i)
+                    yOut[i] = y0[i] + h * (b51 * K[0][i] + b53 * K[2][i] + b54 * K[3][i] + b56 * K[5][i]);
+                for (int i = 0; i < nv; ++i)
+                    yErr[i] = yOut[i] - (y0[i] + h * (b41 * K[0][i] + b43 * K[2][i] + b44 * K[3][i] +
+                                                      b45 * K[4][i] + b46 * K[5][i]));
+                double e2 = 0.0;
+                for (int i = 0; i < nv; ++i) {
+                    const double sk = R.tol + R.tol * fmax(fabs(y0[i]), fabs(yOut[i]));
+                    e2 += (yErr[i] / sk) * (yErr[i] / sk);
                 }
-                if (fail) break;
-                if (attempt == R.max_attempts) { fail = CELL_MAX_ATTEMPTS; break; }
-                u_ve = y0[nsp];
-                u = u_total - u_ve;
-                if (!R.g.from_rhou(rho, u, u_ve, Y, T, Tve, p)) { fail = CELL_NEWTON_FAIL; break; }
-                if (t >= tI) {
-                    if (cycle == 0) dtSave = dt_suggest;
-                    break;
+                const double en = sqrt(e2 / nv);
+                bool ok;
+                if (en <= 1.0) {
+                    double scale = (en == 0.0) ? 10.0 : 0.9 * pow(en, -0.2);
+                    if (en != 0.0) scale = fmin(fmax(scale, 0.2), 10.0);
+                    dt_suggest = scale * h;
+                    ok = true;
+                } else {
+                    dt_suggest = fmax(0.9 * pow(en, -0.2), 0.2) * h;
+                    ok = false;
+                }
+                ++my_steps;
+                bool passed = true;
+                if (ok) {
+                    double tot = 0.0;
+                    for (int i = 0; i < nsp; ++i) {
+                        const double v = yOut[i] * m.sp(i)[SP_M] / rho;
+                        Y[i] = v < 1.0e-30 ? 0.0 : v;   // conc2massf (gas_model.d:258-271)
+                        tot += Y[i];
+                    }
+                    if (fabs(tot - 1.0) > ALLOWABLE_MASSF_ERROR) passed = false;
+                }
+                if (ok && passed) {   // the attempt ends the subcycle
+                    t += h;
+                    for (int i = 0; i < nv; ++i) y0[i] = yOut[i];
+                    const double hMax = h * (1.0 + 10.0 / 100.0);
+                    if (dt_suggest > h) h = fmin(dt_suggest, hMax);
+                    u_ve = y0[nsp];
+                    u = u_total - u_ve;
+                    if (!R.g.from_rhou(rho, u, u_ve, Y, T, Tve, p)) {
+                        fail = CELL_NEWTON_FAIL;
+                    } else if (t >= tI) {
+                        if (cycle == 0) dtSave = dt_suggest;
+                        done = true;
+                    } else if (++cycle == R.max_subcycles) {
+                        fail = CELL_MAX_SUBCYCLES;
+                    } else {
+                        phase = 1;
+                    }
+                } else {
+                    h /= 10.0;
+                    if (h < H_MIN) fail = CELL_H_MIN;
+                    else if (++attempt == R.max_attempts) fail = CELL_MAX_ATTEMPTS;
                 }
             }
-            if (!fail && cycle == R.max_subcycles) fail = CELL_MAX_SUBCYCLES;
-            if (!fail && err) fail = CELL_CEA_RANGE;
+            if (done && err) { fail = CELL_CEA_RANGE; done = false; }
+            if (fail) {
+                if (a.status) a.status[c] = fail;
+                have = false;
+            } else if (done) {
+                double tot = 0.0;
+                for (int i = 0; i < nsp; ++i) tot += Y[i];
+                for (int i = 0; i < nsp; ++i) a.massf[(size_t)i * a.ncell + c] = Y[i] / tot;
+                a.T[c] = T;
+                a.Tve[c] = Tve;
+                a.p[c] = p;
+                if (a.u) a.u[c] = u;
+                if (a.u_ve) a.u_ve[c] = u_ve;
+                a.dt_chem[c] = dtSave;
+                if (a.status) a.status[c] = CELL_OK;
+                have = false;
+            }
         }
-        if (fail) {
-            if (a.status) a.status[c] = fail;
-            continue;
-        }
-        double tot = 0.0;
-        for (int i = 0; i < nsp; ++i) tot += Y[i];
-        for (int i = 0; i < nsp; ++i) a.massf[(size_t)i * a.ncell + c] = Y[i] / tot;
-        a.T[c] = T;
-        a.Tve[c] = Tve;
-        a.p[c] = p;
-        if (a.u) a.u[c] = u;
-        if (a.u_ve) a.u_ve[c] = u_ve;
-        a.dt_chem[c] = dtSave;
-        if (a.status) a.status[c] = CELL_OK;
-        (void)nr;
+        __syncwarp(FULL);
     }
     if (a.steps && my_steps) atomicAdd(a.steps, my_steps);
 }
@@ -509,8 +553,20 @@ int grid_for_cells(int n, int block, int sm_count) {
 
 cudaError_t launch_two_temperature_update(const TwoTArgs& a, int sm_count, cudaStream_t s) {
     if (a.ncell <= 0) return cudaSuccess;
-    if (a.neem > MAX_EEM) return cudaErrorInvalidValue;
-    two_temperature_update_kernel<<<grid_for_cells(a.ncell, 128, sm_count), 128, 0, s>>>(a);
+    if (a.neem > MAX_EEM || !a.counter) return cudaErrorInvalidValue;
+    // a persistent grid: as many blocks as are resident at once, the cells taken from the work counter
+    static int per_sm = 0;
+    if (per_sm <= 0) {
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, two_temperature_update_kernel, 128, 0);
+        if (e != cudaSuccess) return e;
+        if (per_sm < 1) per_sm = 1;
+    }
+    long long grid = (long long)sm_count * per_sm;
+    const long long want = ((long long)a.ncell + 127) / 128;
+    if (grid > want) grid = want;
+    cudaError_t e = cudaMemsetAsync(a.counter, 0, sizeof(unsigned), s);
+    if (e != cudaSuccess) return e;
+    two_temperature_update_kernel<<<(unsigned)(grid < 1 ? 1 : grid), 128, 0, s>>>(a);
     return cudaGetLastError();
 }
 
