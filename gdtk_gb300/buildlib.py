@@ -19,6 +19,7 @@ NVCC = os.environ.get("NVCC", "nvcc")
 
 SOURCES = [
     ("chem_kernels.cu", ["--fmad=false"]),
+    ("chem_warp.cu", []),
     ("twotemp_kernels.cu", []),
     ("twotemp.cpp", []),
     ("codegen.cpp", []),
@@ -32,7 +33,7 @@ SOURCES = [
     ("mechanism.cpp", []),
     ("lua_table.cpp", []),
 ]
-HEADERS = ["chem_types.h", "chem_launch.h", "cea_thermo.h", "lua_table.h", "mechanism.h", "codegen.h", "fast_exp.h",
+HEADERS = ["chem_kernels.cu", "chem_types.h", "chem_launch.h", "cea_thermo.h", "lua_table.h", "mechanism.h", "codegen.h", "fast_exp.h",
            "chem_fast.cuh", "mix_thermo.cuh", "api_internal.h", "mlp_launch.h", "surrogate_launch.h", "twotemp.h"]
 # sources compiled at run time by NVRTC, embedded in the library as string literals
 EMBEDDED = [("kFastCuhSource", "chem_fast.cuh"), ("kFastExpSource", "fast_exp.h")]

@@ -21,12 +21,19 @@
 //   gas/thermo/therm_perf_gas_mix.d    GibbsFreeEnergies 354-364, update_temperature_from_energy 426-468
 //   gas/gas_model.d                    massf2conc 237-253, conc2massf 255-271, rates2source 273-279
 //   lmr/fluidfvcell.d                  thermochemical_increment 883-997 (caller contract)
+//
+// The one-warp-per-cell update (the last section) is compiled separately, from chem_warp.cu with
+// GDTK_WARP_TU = 1 and FMA contraction; this translation unit (GDTK_WARP_TU = 0) holds the rest.
 #include <cuda_runtime.h>
 
 #include "chem_types.h"
 #include "chem_launch.h"
 #include "cea_thermo.h"
 #include "mix_thermo.cuh"
+
+#ifndef GDTK_WARP_TU
+#define GDTK_WARP_TU 0
+#endif
 
 namespace gdtk {
 namespace {
@@ -400,6 +407,7 @@ __device__ void stage_mechanism(const int* gi, const double* gd, int ni, int nd,
     __syncthreads();
 }
 
+#if !GDTK_WARP_TU
 // ---------------------------------------------------------------- the chemistry update
 template <int METHOD>
 __global__ void __launch_bounds__(256) chem_update_kernel(ChemUpdateArgs a) {
@@ -725,8 +733,10 @@ __global__ void order_scatter(const float* key, int n, int* hist, int* order) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         order[atomicAdd(&hist[order_bucket(key[i])], 1)] = i;
 }
+#endif   // !GDTK_WARP_TU
 
 
+#if GDTK_WARP_TU
 // ---------------------------------------------------------------- one warp per cell (large mechanisms)
 // The reference-order update (chem_update_kernel above) with one warp integrating one cell: species
 // and reactions are spread over the lanes, and the cell's vectors live in the warp's share of shared
@@ -1272,9 +1282,11 @@ __global__ void __launch_bounds__(512) chem_warp_kernel(ChemUpdateArgs a, WarpTa
         __syncwarp();
     }
 }
+#endif   // GDTK_WARP_TU
 
 }  // namespace
 
+#if !GDTK_WARP_TU
 cudaError_t launch_bucket_order(const float* key, int n, int* order, int* hist, int sm_count, cudaStream_t stream) {
     if (n <= 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(hist, 0, ORDER_BUCKETS * sizeof(int), stream);
@@ -1287,8 +1299,11 @@ cudaError_t launch_bucket_order(const float* key, int n, int* order, int* hist, 
     return cudaGetLastError();
 }
 
+#endif   // !GDTK_WARP_TU
+
 // ---------------------------------------------------------------- host-side launchers
 
+#if GDTK_WARP_TU
 int chem_warp_doubles(int nsp, int nr, int neff, int method, int nslot) {
     WarpLayout l;
     l.make(nsp, nr, neff, method, nslot);
@@ -1330,6 +1345,7 @@ cudaError_t launch_chem_update_warp(const ChemUpdateArgs& a, int method, const W
     return cudaGetLastError();
 }
 
+#else
 int chem_scratch_doubles(int nsp, int nr, int neff, int method) {
     Layout l;
     l.make(nsp, nr, neff, method);
@@ -1400,5 +1416,7 @@ cudaError_t launch_gas_service(const GasServiceArgs& a, int sm_count, cudaStream
     cudaError_t f = cudaFreeAsync(buf, stream);
     return e != cudaSuccess ? e : f;
 }
+
+#endif   // GDTK_WARP_TU
 
 }  // namespace gdtk
