@@ -1,7 +1,8 @@
 // twotemp_kernels.cu -- the multi-temperature thermochemical reactor for a two-temperature gas, one
-// thread per cell, compiled with FMA contraction and with the rate constants and equilibrium constants
-// in log form (one exp where the reference takes pows and an exp): results differ from the reference's
-// evaluation order in rounding only (tested to 1e-8 in Y, 1e-7 relative in T, T_ve and p).
+// thread per cell, compiled with FMA contraction, with the rate constants and equilibrium constants in
+// log form (one exp where the reference takes pows and an exp) and the rate, relaxation and coupling
+// exponentials by Tang's table method: results differ from the reference's evaluation order in rounding
+// only (tested to 1e-8 in Y, 1e-7 relative in T, T_ve and p).
 //
 // kinetics/multi_temperature_thermochemical_reactor.d:137-294 (opCall) and :334-431 (Cash-Karp RKF
 // on the concentrations and u_ve), with
@@ -25,6 +26,7 @@
 
 #include "cea_thermo.h"
 #include "chem_types.h"
+#include "fast_exp.h"
 #include "twotemp.h"
 
 namespace gdtk {
@@ -43,6 +45,12 @@ constexpr double H_MIN = 1.0e-15;             // multi_temperature_thermochemica
 constexpr double ALLOWABLE_MASSF_ERROR = 1.0e-3;
 constexpr int NV = GDTK_MAX_SPECIES + 1;
 constexpr int MAX_EEM = 64;
+
+// exp by Tang's table method (fast_exp.h, within 1.3 ulp): 9 FP64 operations where the library's takes
+// about 20 FMA slots on this GPU.  The update kernel stages the table in shared memory once per block.
+__device__ const double kExp2Table[GDTK_EXP2_TABLE_SIZE] = GDTK_EXP2_TABLE_INIT;
+__shared__ double s_exp2[GDTK_EXP2_TABLE_SIZE];
+__device__ __forceinline__ double ex(double x) { return gdtk_exp(x, s_exp2); }
 
 struct Gas2T {
     MechView m;
@@ -130,15 +138,15 @@ __device__ __forceinline__ double pow_int(double x, int n) {   // small positive
 __device__ double base_rc(int model, const double* d, double T, double lnT, double lnTve) {
     if (model == RATE_PARK) {
         const double lnTe = d[RD_S] * lnT + (1.0 - d[RD_S]) * lnTve;
-        return d[0] * exp(d[1] * lnTe - d[2] / exp(lnTe));
+        return d[0] * ex(d[1] * lnTe - d[2] / ex(lnTe));
     }
-    return d[0] * exp(d[1] * lnT - d[2] / T);
+    return d[0] * ex(d[1] * lnT - d[2] / T);
 }
 
 // rate_constant.d:397-404
 __device__ __forceinline__ double Q_mt(double T, double D, double theta) {
-    const double num = 1 - exp(-D / T);
-    const double den = 1 - exp(-theta / T);
+    const double num = 1 - ex(-D / T);
+    const double den = 1 - ex(-theta / T);
     return num / den;
 }
 
@@ -192,14 +200,14 @@ struct Reactor2T {
                     nuSum += nu;
                 }
                 // K_p (P_atm / R T)^sum(nu) as one exponential (reaction.d:26-52)
-                Kc = exp(fma(nuSum, lnPRT, -dG / (R_universal * T)));
+                Kc = ex(fma(nuSum, lnPRT, -dG / (R_universal * T)));
             }
             if (r[RX_FRC] != RATE_FROM_EQ) {
                 kf[ir] = forward_rc(r, d, T, Tve, logT, logTve);
                 kb[ir] = (r[RX_BRC] == RATE_FROM_EQ) ? forward_rc(r, d, T, T, logT, logT) / Kc
-                                                     : d[3] * exp(d[4] * logT - d[5] / T);
+                                                     : d[3] * ex(d[4] * logT - d[5] / T);
             } else {
-                kb[ir] = d[3] * exp(d[4] * logT - d[5] / T);
+                kb[ir] = d[3] * ex(d[4] * logT - d[5] / T);
                 kf[ir] = kb[ir] * Kc;   // the backward rate constant at the state itself (reaction.d:131)
             }
         }
@@ -240,10 +248,12 @@ struct Reactor2T {
     }
 
     // Relaxation time of a Landau-Teller mechanism (relaxation_time.d:27-175); -1 for a rare collider.
-    __device__ double tau(const Eem2T& e, double T, double p, const double* molef, const double* numden) const {
+    // T13 = T^(-1/3), formed once per subcycle.
+    __device__ double tau(const Eem2T& e, double T, double T13, double p, const double* molef,
+                          const double* numden) const {
         if (molef[e.q] <= SMALL_MOLE_FRACTION) return -1.0;
         const double pBath = molef[e.q] * p / P_atm;
-        const double t_mw = (1.0 / pBath) * exp(e.a * (pow(T, -1. / 3.) - e.b) - 18.42);
+        const double t_mw = (1.0 / pBath) * ex(e.a * (T13 - e.b) - 18.42);
         if (e.rt == RT_MILLIKAN_WHITE) return t_mw;
         const double sigma = (e.rt == RT_PARK_HTC) ? e.sigma : e.sigma * (50e3 / T) * (50e3 / T);
         const double cs = sqrt(8.0 * Boltzmann * T / PI_D / e.mu);
@@ -255,8 +265,8 @@ struct Reactor2T {
         if (fabs(iG) < IGAMMA_SWITCH)
             return 0.5 * (D - Th * R_universal) + iG * (Th * Th * R_universal * R_universal - D * D) / 12.0 / R_universal;
         if (iG > IGAMMA_OVERFLOW)
-            return R_universal * Th / (exp(Th * iG) - 1.0) - D * exp(-D / R_universal * iG);
-        return R_universal * Th / (exp(Th * iG) - 1.0) - D / (exp(D / R_universal * iG) - 1.0);
+            return R_universal * Th / (ex(Th * iG) - 1.0) - D * ex(-D / R_universal * iG);
+        return R_universal * Th / (ex(Th * iG) - 1.0) - D / (ex(D / R_universal * iG) - 1.0);
     }
 
     // Energy brought in (ga) and removed (gv) per dissociation at (T, T_ve), J/mol
@@ -269,14 +279,14 @@ struct Reactor2T {
         } else if (e.coupling == CPL_MARRONE_TREANOR) {
             gv = L_knab(1. / Tv - 1. / T - 1. / e.U, e.D, th);
             const double T_F_inv = -1. / e.U;
-            ga = R_universal * th / (exp(th * T_F_inv) - 1.) - e.D / (exp(e.D / R_universal * T_F_inv) - 1.);
+            ga = R_universal * th / (ex(th * T_F_inv) - 1.) - e.D / (ex(e.D / R_universal * T_F_inv) - 1.);
         } else {
             const double TD = e.D;
             const double Uinv = e.aU / T + 1 / e.Ustar;
             double T_F_inv = 1. / Tv - 1. / T - Uinv;
-            gv = R_universal * (th / (exp(th * T_F_inv) - 1.) - TD / (exp(TD * T_F_inv) - 1.)) + e.nb * R_universal * TD;
+            gv = R_universal * (th / (ex(th * T_F_inv) - 1.) - TD / (ex(TD * T_F_inv) - 1.)) + e.nb * R_universal * TD;
             T_F_inv = -e.aU / T - 1 / e.Ustar;
-            ga = R_universal * (th / (exp(th * T_F_inv) - 1.) - TD / (exp(TD * T_F_inv) - 1.));
+            ga = R_universal * (th / (ex(th * T_F_inv) - 1.) - TD / (ex(TD * T_F_inv) - 1.));
         }
     }
 
@@ -313,6 +323,8 @@ struct Reactor2T {
 // fixed cell per thread would leave a warp's lanes idle until its slowest cell finishes.  The operations
 // per cell are those of the subcycle and attempt loops of multi_temperature_thermochemical_reactor.d:137-294.
 __global__ void __launch_bounds__(128) two_temperature_update_kernel(const TwoTArgs a) {
+    for (int k = threadIdx.x; k < GDTK_EXP2_TABLE_SIZE; k += blockDim.x) s_exp2[k] = kExp2Table[k];
+    __syncthreads();
     Reactor2T R;
     R.g.m.bind(a.mech_i, a.mech_d);
     R.g.sp = a.species;
@@ -403,14 +415,14 @@ __global__ void __launch_bounds__(128) two_temperature_update_kernel(const TwoTA
                     molef[i] = (Y[i] / m.sp(i)[SP_M]) / mol;
                     numden[i] = Avogadro * Y[i] * rho / m.sp(i)[SP_M];
                 }
-                const double logT = log(T), logTve = log(Tve);
+                const double logT = log(T), logTve = log(Tve), T13 = ex(logT * (-1. / 3.));
                 for (int k = 0; k < R.neem; ++k) {
                     const Eem2T& e = R.eem[k];
                     lt[k] = 0.0;
                     ga[k] = 0.0;
                     gv[k] = 0.0;
                     if (e.kind == EEM_LANDAU_TELLER) {
-                        const double tk = R.tau(e, T, p, molef, numden);
+                        const double tk = R.tau(e, T, T13, p, molef, numden);
                         if (tk >= 0.0)
                             lt[k] = Y[e.p] * (R.g.e_ve(e.p, T, logT, err) - R.g.e_ve(e.p, Tve, logTve, err)) / tk;
                     } else {
