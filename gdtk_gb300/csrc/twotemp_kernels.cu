@@ -42,6 +42,7 @@ constexpr double SMALL_MOLE_FRACTION = 1.0e-15;   // gas_model.d:42
 constexpr double IGAMMA_SWITCH = 1.0e-7;      // exchange_chemistry_coupling.d:24
 constexpr double IGAMMA_OVERFLOW = 0.001;     // exchange_chemistry_coupling.d:25
 constexpr double H_MIN = 1.0e-15;             // multi_temperature_thermochemical_reactor.d:31
+constexpr double LN_PATM_R = 0x1.2d0f0af013269p+3;   // ln(P_atm / R_universal) = 9.408086270233257
 constexpr double ALLOWABLE_MASSF_ERROR = 1.0e-3;
 constexpr int NV = GDTK_MAX_SPECIES + 1;
 constexpr int MAX_EEM = 64;
@@ -70,8 +71,8 @@ struct Gas2T {
         if (i == electron) return 0.0;
         return sp[i].cp_tr * (T - T_REF) + sp[i].h_f - R(i) * T;
     }
-    __device__ double e_ve_mix(const double* Y, double Tve, int& err) const {
-        const double lt = log(Tve);
+    __device__ double e_ve_mix(const double* Y, double Tve, int& err) const { return e_ve_mix(Y, Tve, log(Tve), err); }
+    __device__ double e_ve_mix(const double* Y, double Tve, double lt, int& err) const {
         double e = 0.0;
         for (int i = 0; i < m.nsp; ++i) e += Y[i] * e_ve(i, Tve, lt, err);
         return e;
@@ -104,17 +105,23 @@ struct Gas2T {
         }
         T = (u + sumA) / sumB;
         int err = 0;
-        double Tg = Tve;
-        double f = e_ve_mix(Y, Tg, err) - u_ve;
+        double Tg = Tve, lg = log(Tve);
+        double f = e_ve_mix(Y, Tg, lg, err) - u_ve;
         if (fabs(f) >= 1e-5) {
             int count = 0;
             double dT = 0.0;
             for (int it = 0; it < 40; ++it) {
                 const double Cv = cv_ve_mix(Y, Tg, err);
                 dT = -f / Cv;
+                // ln(Tg + dT) = ln Tg + log1p(x), x = dT / Tg: the Taylor series to x^6 when |x| < 2^-10 (its
+                // truncation is below 2^-60 |x|), else a fresh log
+                const double x = dT / Tg;
                 Tg += dT;
                 if (fabs(dT) < 1.0e-9) break;
-                f = e_ve_mix(Y, Tg, err) - u_ve;
+                lg = (fabs(x) < 0x1p-10)
+                         ? lg + x * fma(x, fma(x, fma(x, fma(x, fma(x, -1.0 / 6.0, 0.2), -0.25), 1.0 / 3.0), -0.5), 1.0)
+                         : log(Tg);
+                f = e_ve_mix(Y, Tg, lg, err) - u_ve;
                 ++count;
             }
             if (count == 40 && fabs(dT) > 1e-3) return false;
@@ -180,13 +187,14 @@ struct Reactor2T {
     int max_subcycles, max_attempts;
 
     // reaction.d:94-143 (multi-temperature branch) at the clamped T; gs: Gibbs scratch [nsp]
-    __device__ void rate_constants(double Tq, double Tve, double* kf, double* kb, double* gs, int& err) const {
+    // logTq, logTve: ln Tq and ln T_ve (Tq unclamped), which the caller needs as well.
+    __device__ void rate_constants(double Tq, double Tve, double logTq, double logTve, double* kf, double* kb,
+                                   double* gs, int& err) const {
         const MechView& m = g.m;
-        double T = Tq;
-        if (T < m.T_lower()) T = m.T_lower();
-        if (T > m.T_upper()) T = m.T_upper();
-        const double logT = log(T), logTve = log(Tve);
-        const double lnPRT = log(P_atm / (R_universal * T));
+        double T = Tq, logT = logTq;
+        if (T < m.T_lower()) { T = m.T_lower(); logT = log(T); }
+        if (T > m.T_upper()) { T = m.T_upper(); logT = log(T); }
+        const double lnPRT = LN_PATM_R - logT;   // ln(P_atm / R T)
         for (int i = 0; i < m.nsp; ++i) gs[i] = cea_h(m, i, T, logT, err) - T * cea_s(m, i, T, logT, err);
         for (int ir = 0; ir < m.nr; ++ir) {
             const int* r = m.rx(ir);
@@ -385,7 +393,7 @@ __global__ void __launch_bounds__(128) two_temperature_update_kernel(const TwoTA
                         y0[i] = v < 1.0e-30 ? 0.0 : v;   // gas_model.d:237-256
                     }
                     y0[nsp] = R.g.e_ve_mix(Y, Tve, err);
-                    R.rate_constants(T, Tve, kf, kb, gs, err);
+                    R.rate_constants(T, Tve, log(T), log(Tve), kf, kb, gs, err);
                     if (dt_suggest > tI) {
                         h = tI;
                     } else if (dt_suggest <= 0.0) {   // reaction_mechanism.d:161-203
@@ -408,14 +416,14 @@ __global__ void __launch_bounds__(128) two_temperature_update_kernel(const TwoTA
                 }
             }
             if (!fail && phase == 1) {   // a subcycle's rate constants, relaxation times and exchange terms
-                R.rate_constants(T, Tve, kf, kb, gs, err);
+                const double logT = log(T), logTve = log(Tve), T13 = ex(logT * (-1. / 3.));
+                R.rate_constants(T, Tve, logT, logTve, kf, kb, gs, err);
                 double mol = 0.0;
                 for (int i = 0; i < nsp; ++i) mol += Y[i] / m.sp(i)[SP_M];
                 for (int i = 0; i < nsp; ++i) {
                     molef[i] = (Y[i] / m.sp(i)[SP_M]) / mol;
                     numden[i] = Avogadro * Y[i] * rho / m.sp(i)[SP_M];
                 }
-                const double logT = log(T), logTve = log(Tve), T13 = ex(logT * (-1. / 3.));
                 for (int k = 0; k < R.neem; ++k) {
                     const Eem2T& e = R.eem[k];
                     lt[k] = 0.0;
