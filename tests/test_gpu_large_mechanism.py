@@ -179,3 +179,31 @@ def test_acetylene_block_batch_equals_per_block_updates(c2h2):
     for a, b in zip(graphed, single):
         for key in ("T", "p", "massf", "dt_chem", "status"):
             assert torch.equal(a[key], b[key]), key
+
+
+def test_acetylene_results_do_not_depend_on_the_schedule(c2h2):
+    # Warps take cells from a work counter, so which warp integrates a cell depends on the batch's order
+    # and on timing; a cell's result must not.  The same cells in reversed order give bitwise the same
+    # states, statuses and work counters.
+    torch = torch_cuda()
+    rc, _ = c2h2
+    n = 512
+    T, p, Y = _premixed_cells(rc.species_names, rc.mol_masses, n, seed=47, majors=ACETYLENE,
+                              T_range=(1150.0, 2500.0), logp=(4.0, 5.5))
+
+    def run(order):
+        dT, dp, dY = to_dev(torch, T[order], p[order], Y[:, order])
+        rho, u = rc.thermo_from_pT(dp, dT, dY)
+        dtc = torch.full((n,), -1.0, dtype=torch.float64, device="cuda")
+        st = torch.zeros(n, dtype=torch.int32, device="cuda")
+        cnt = torch.zeros((6, n), dtype=torch.int32, device="cuda")
+        rc.update(rho, u, dT, dp, dY, dtc, 1.0e-6, status=st, cell_counters=cnt)
+        torch.cuda.synchronize()
+        back = np.argsort(order)
+        return [a.cpu().numpy()[..., back] for a in (dT, dp, dY, dtc, st, cnt)]
+
+    fwd = run(np.arange(n))
+    rev = run(np.arange(n)[::-1].copy())
+    for a, b, name in zip(fwd, rev, ("T", "p", "Y", "dt_chem", "status", "counters")):
+        assert np.array_equal(a, b), name
+    assert (fwd[4] == 0).all()
