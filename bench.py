@@ -1199,7 +1199,7 @@ def main():
     totals = torch.zeros(6, dtype=torch.int64, device=dev)
     stream = torch.cuda.current_stream()
     tuned = None
-    if n <= 65536 and not (rc.nsp > 32 or rc.nr > 128):
+    if n <= 16384 and not (rc.nsp > 32 or rc.nr > 128):
         # a small batch at one thread per cell fills a fraction of the GPU's lanes: the autotuner also tries
         # one warp per cell and the launch shapes, on this workload's own cells (before the timed region)
         from gdtk_gb300 import autotune
