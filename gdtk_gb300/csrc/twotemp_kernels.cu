@@ -300,9 +300,9 @@ struct Reactor2T {
 
     // dy/dt at y (species rates and the energy exchange into u_ve); lt[k]: the Landau-Teller term of
     // mechanism k on this subcycle's state (0 for others); ga[k], gv[k]: its Marrone-Treanor G_appear and
-    // G_vanish on that state.
+    // G_vanish on that state; rrho = 1 / rho.
     __device__ void rates(const double* y, const double* kf, const double* kb, const double* lt, const double* ga,
-                          const double* gv, double rho, double* wf, double* wb, double* q, double* L,
+                          const double* gv, double rrho, double* wf, double* wb, double* q, double* L,
                           double* out) const {
         const int nsp = g.m.nsp;
         split_rates(y, kf, kb, wf, wb, q, L);
@@ -317,7 +317,7 @@ struct Reactor2T {
                 const double f = wf[e.reaction], b = wb[e.reaction];
                 const double prod = nu > 0 ? nu * f : (nu < 0 ? -nu * b : 0.0);
                 const double loss = nu > 0 ? nu * b : (nu < 0 ? -nu * f : 0.0);
-                rate += (prod * ga[k] - loss * gv[k]) / rho;
+                rate += (prod * ga[k] - loss * gv[k]) * rrho;
             }
         }
         out[nsp] = rate;
@@ -354,7 +354,7 @@ __global__ void __launch_bounds__(128) two_temperature_update_kernel(const TwoTA
     double molef[GDTK_MAX_SPECIES], numden[GDTK_MAX_SPECIES];
     int c = 0, phase = 0, cycle = 0, attempt = 0, fail = 0, err = 0;
     bool have = false, alive = true;
-    double rho = 0.0, T = 0.0, Tve = 0.0, p = 0.0, t = 0.0, h = 0.0, dt_suggest = 0.0, dtSave = 0.0;
+    double rho = 0.0, rrho = 0.0, T = 0.0, Tve = 0.0, p = 0.0, t = 0.0, h = 0.0, dt_suggest = 0.0, dtSave = 0.0;
     double u_total = 0.0, u = 0.0, u_ve = 0.0;
     while (true) {
         const unsigned need = __ballot_sync(FULL, alive && !have);
@@ -379,6 +379,7 @@ __global__ void __launch_bounds__(128) two_temperature_update_kernel(const TwoTA
             bool done = false;
             if (phase == 0) {   // the cell's state and first step size
                 rho = a.rho[c];
+                rrho = 1.0 / rho;
                 T = a.T[c]; Tve = a.Tve[c]; p = a.p[c];
                 for (int i = 0; i < nsp; ++i) Y[i] = a.massf[(size_t)i * a.ncell + c];
                 fail = 0; err = 0;
@@ -419,10 +420,13 @@ __global__ void __launch_bounds__(128) two_temperature_update_kernel(const TwoTA
                 const double logT = log(T), logTve = log(Tve), T13 = ex(logT * (-1. / 3.));
                 R.rate_constants(T, Tve, logT, logTve, kf, kb, gs, err);
                 double mol = 0.0;
-                for (int i = 0; i < nsp; ++i) mol += Y[i] / m.sp(i)[SP_M];
+                // 1 / M_i = R_i / R_universal
+                for (int i = 0; i < nsp; ++i) mol += Y[i] * (m.sp(i)[SP_R] * (1.0 / R_universal));
+                const double rmol = 1.0 / mol;
                 for (int i = 0; i < nsp; ++i) {
-                    molef[i] = (Y[i] / m.sp(i)[SP_M]) / mol;
-                    numden[i] = Avogadro * Y[i] * rho / m.sp(i)[SP_M];
+                    const double n_i = Y[i] * (m.sp(i)[SP_R] * (1.0 / R_universal));
+                    molef[i] = n_i * rmol;
+                    numden[i] = Avogadro * rho * n_i;
                 }
                 for (int k = 0; k < R.neem; ++k) {
                     const Eem2T& e = R.eem[k];
@@ -451,20 +455,20 @@ __global__ void __launch_bounds__(128) two_temperature_update_kernel(const TwoTA
                 const double b51 = 37. / 378., b53 = 250. / 621., b54 = 125. / 594., b56 = 512. / 1771.,
                              b41 = 2825. / 27648., b43 = 18575. / 48384., b44 = 13525. / 55296.,
                              b45 = 277. / 14336., b46 = 1.0 / 4.0;
-                R.rates(y0, kf, kb, lt, ga, gv, rho, wf, wb, q, L, K[0]);
+                R.rates(y0, kf, kb, lt, ga, gv, rrho, wf, wb, q, L, K[0]);
                 for (int i = 0; i < nv; ++i) yT[i] = y0[i] + h * a21 * K[0][i];
-                R.rates(yT, kf, kb, lt, ga, gv, rho, wf, wb, q, L, K[1]);
+                R.rates(yT, kf, kb, lt, ga, gv, rrho, wf, wb, q, L, K[1]);
                 for (int i = 0; i < nv; ++i) yT[i] = y0[i] + h * (a31 * K[0][i] + a32 * K[1][i]);
-                R.rates(yT, kf, kb, lt, ga, gv, rho, wf, wb, q, L, K[2]);
+                R.rates(yT, kf, kb, lt, ga, gv, rrho, wf, wb, q, L, K[2]);
                 for (int i = 0; i < nv; ++i) yT[i] = y0[i] + h * (a41 * K[0][i] + a42 * K[1][i] + a43 * K[2][i]);
-                R.rates(yT, kf, kb, lt, ga, gv, rho, wf, wb, q, L, K[3]);
+                R.rates(yT, kf, kb, lt, ga, gv, rrho, wf, wb, q, L, K[3]);
                 for (int i = 0; i < nv; ++i)
                     yT[i] = y0[i] + h * (a51 * K[0][i] + a52 * K[1][i] + a53 * K[2][i] + a54 * K[3][i]);
-                R.rates(yT, kf, kb, lt, ga, gv, rho, wf, wb, q, L, K[4]);
+                R.rates(yT, kf, kb, lt, ga, gv, rrho, wf, wb, q, L, K[4]);
                 for (int i = 0; i < nv; ++i)
                     yT[i] = y0[i] + h * (a61 * K[0][i] + a62 * K[1][i] + a63 * K[2][i] + a64 * K[3][i] +
                                          a65 * K[4][i]);
-                R.rates(yT, kf, kb, lt, ga, gv, rho, wf, wb, q, L, K[5]);
+                R.rates(yT, kf, kb, lt, ga, gv, rrho, wf, wb, q, L, K[5]);
                 for (int i = 0; i < nv; ++i)
                     yOut[i] = y0[i] + h * (b51 * K[0][i] + b53 * K[2][i] + b54 * K[3][i] + b56 * K[5][i]);
                 for (int i = 0; i < nv; ++i)
@@ -491,7 +495,7 @@ __global__ void __launch_bounds__(128) two_temperature_update_kernel(const TwoTA
                 if (ok) {
                     double tot = 0.0;
                     for (int i = 0; i < nsp; ++i) {
-                        const double v = yOut[i] * m.sp(i)[SP_M] / rho;
+                        const double v = yOut[i] * m.sp(i)[SP_M] * rrho;
                         Y[i] = v < 1.0e-30 ? 0.0 : v;   // conc2massf (gas_model.d:258-271)
                         tot += Y[i];
                     }
