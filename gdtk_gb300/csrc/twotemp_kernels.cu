@@ -142,40 +142,40 @@ __device__ __forceinline__ double pow_int(double x, int n) {   // small positive
 // An Arrhenius (at T) or Park (at T_e = T^s T_ve^(1-s)) rate constant from the record's A, n, C, s, in log
 // form: A exp(n ln T_e - C / T_e) with ln T_e = s ln T + (1 - s) ln T_ve from the logs of the subcycle
 // (rate_constant.d:72-75, 364-393 evaluate the same expression with three pow calls and an exp).
-__device__ double base_rc(int model, const double* d, double T, double lnT, double lnTve) {
+// Temperatures enter as reciprocals (rT = 1 / T), formed once per subcycle where the reference divides.
+__device__ double base_rc(int model, const double* d, double rT, double lnT, double lnTve) {
     if (model == RATE_PARK) {
         const double lnTe = d[RD_S] * lnT + (1.0 - d[RD_S]) * lnTve;
-        return d[0] * ex(d[1] * lnTe - d[2] / ex(lnTe));
+        return d[0] * ex(d[1] * lnTe - d[2] * ex(-lnTe));
     }
-    return d[0] * ex(d[1] * lnT - d[2] / T);
+    return d[0] * ex(d[1] * lnT - d[2] * rT);
 }
 
-// rate_constant.d:397-404
-__device__ __forceinline__ double Q_mt(double T, double D, double theta) {
-    const double num = 1 - ex(-D / T);
-    const double den = 1 - ex(-theta / T);
+// rate_constant.d:397-404 at the temperature whose reciprocal is rT
+__device__ __forceinline__ double Q_mt(double rT, double D, double theta) {
+    const double num = 1 - ex(-D * rT);
+    const double den = 1 - ex(-theta * rT);
     return num / den;
 }
 
 // Forward rate constant of reaction ir at (T, T_ve): Arrhenius, Park, or the (modified) Marrone-Treanor
 // non-equilibrium factor times the underlying one (rate_constant.d:438-447, 541-554).
-__device__ double forward_rc(const int* r, const double* d, double T, double Tve, double lnT, double lnTve) {
+__device__ double forward_rc(const int* r, const double* d, double rT, double rTve, double lnT, double lnTve) {
     const int model = r[RX_FRC];
-    if (model != RATE_MT && model != RATE_MMT) return base_rc(model, d, T, lnT, lnTve);
-    const double kEQ = base_rc(r[RX_BASE], d, T, lnT, lnTve);
+    if (model != RATE_MT && model != RATE_MMT) return base_rc(model, d, rT, lnT, lnTve);
+    const double kEQ = base_rc(r[RX_BASE], d, rT, lnT, lnTve);
     const double TD = d[RD_MT_TD], th = d[RD_MT_THETA];
     if (model == RATE_MT) {
-        const double U = d[RD_MT_U];
-        const double Gamma = 1. / (1. / Tve - 1. / T - 1. / U);
-        const double Q_T = Q_mt(T, TD, th), Q_Gamma = Q_mt(Gamma, TD, th), Q_Tv = Q_mt(Tve, TD, th),
-                     Q_U = Q_mt(-U, TD, th);
+        const double rU = 1. / d[RD_MT_U];
+        const double rGamma = rTve - rT - rU;   // 1 / Gamma
+        const double Q_T = Q_mt(rT, TD, th), Q_Gamma = Q_mt(rGamma, TD, th), Q_Tv = Q_mt(rTve, TD, th),
+                     Q_U = Q_mt(-rU, TD, th);
         return kEQ * Q_T * Q_Gamma / (Q_Tv * Q_U);
     }
-    const double Tinv = 1. / T, Tvinv = 1. / Tve;
-    const double Uinv = d[RD_MT_U] * Tinv + 1. / d[RD_MT_USTAR];
-    const double U = 1. / Uinv;
-    const double TF = 1. / (Tvinv - Tinv - Uinv);
-    const double Q_T = Q_mt(T, TD, th), Q_TF = Q_mt(TF, TD, th), Q_Tv = Q_mt(Tve, TD, th), Q_U = Q_mt(-U, TD, th);
+    const double Uinv = d[RD_MT_U] * rT + 1. / d[RD_MT_USTAR];
+    const double rTF = rTve - rT - Uinv;   // 1 / T_F
+    const double Q_T = Q_mt(rT, TD, th), Q_TF = Q_mt(rTF, TD, th), Q_Tv = Q_mt(rTve, TD, th),
+                 Q_U = Q_mt(-Uinv, TD, th);
     return d[RD_MT_NB] * kEQ * Q_T * Q_TF / (Q_Tv * Q_U);
 }
 
@@ -195,11 +195,12 @@ struct Reactor2T {
         if (T < m.T_lower()) { T = m.T_lower(); logT = log(T); }
         if (T > m.T_upper()) { T = m.T_upper(); logT = log(T); }
         const double lnPRT = LN_PATM_R - logT;   // ln(P_atm / R T)
+        const double rT = 1.0 / T, rTve = 1.0 / Tve;
         for (int i = 0; i < m.nsp; ++i) gs[i] = cea_h(m, i, T, logT, err) - T * cea_s(m, i, T, logT, err);
         for (int ir = 0; ir < m.nr; ++ir) {
             const int* r = m.rx(ir);
             const double* d = m.rxd(ir);
-            double Kc = 1.0;
+            double lnKc = 0.0;
             if (r[RX_FRC] == RATE_FROM_EQ || r[RX_BRC] == RATE_FROM_EQ) {
                 double dG = 0.0, nuSum = 0.0;
                 for (int k = 0; k < r[RX_NPART]; ++k) {
@@ -207,16 +208,16 @@ struct Reactor2T {
                     dG += nu * gs[isp] * m.sp(isp)[SP_M];
                     nuSum += nu;
                 }
-                // K_p (P_atm / R T)^sum(nu) as one exponential (reaction.d:26-52)
-                Kc = ex(fma(nuSum, lnPRT, -dG / (R_universal * T)));
+                // ln of K_p (P_atm / R T)^sum(nu) (reaction.d:26-52)
+                lnKc = fma(nuSum, lnPRT, -dG * (rT * (1.0 / R_universal)));
             }
             if (r[RX_FRC] != RATE_FROM_EQ) {
-                kf[ir] = forward_rc(r, d, T, Tve, logT, logTve);
-                kb[ir] = (r[RX_BRC] == RATE_FROM_EQ) ? forward_rc(r, d, T, T, logT, logT) / Kc
-                                                     : d[3] * ex(d[4] * logT - d[5] / T);
+                kf[ir] = forward_rc(r, d, rT, rTve, logT, logTve);
+                kb[ir] = (r[RX_BRC] == RATE_FROM_EQ) ? forward_rc(r, d, rT, rT, logT, logT) * ex(-lnKc)
+                                                     : d[3] * ex(d[4] * logT - d[5] * rT);
             } else {
-                kb[ir] = d[3] * ex(d[4] * logT - d[5] / T);
-                kf[ir] = kb[ir] * Kc;   // the backward rate constant at the state itself (reaction.d:131)
+                kb[ir] = d[3] * ex(d[4] * logT - d[5] * rT);
+                kf[ir] = kb[ir] * ex(lnKc);   // the backward rate constant at the state itself (reaction.d:131)
             }
         }
     }
@@ -279,21 +280,22 @@ struct Reactor2T {
 
     // Energy brought in (ga) and removed (gv) per dissociation at (T, T_ve), J/mol
     // (exchange_chemistry_coupling.d:94-126 impartial, 152-174 Marrone-Treanor, 204-220 modified).
-    __device__ static void coupling(const Eem2T& e, double T, double Tv, double& ga, double& gv) {
+    // rT = 1 / T, rTv = 1 / T_v
+    __device__ static void coupling(const Eem2T& e, double rT, double rTv, double& ga, double& gv) {
         const double th = e.Thetav;
         if (e.coupling == CPL_IMPARTIAL) {
             ga = 0.5 * (e.D - th * R_universal);
-            gv = L_knab((T - Tv) / (T * Tv), e.D, th);
+            gv = L_knab(rTv - rT, e.D, th);   // (T - T_v) / (T T_v)
         } else if (e.coupling == CPL_MARRONE_TREANOR) {
-            gv = L_knab(1. / Tv - 1. / T - 1. / e.U, e.D, th);
+            gv = L_knab(rTv - rT - 1. / e.U, e.D, th);
             const double T_F_inv = -1. / e.U;
             ga = R_universal * th / (ex(th * T_F_inv) - 1.) - e.D / (ex(e.D / R_universal * T_F_inv) - 1.);
         } else {
             const double TD = e.D;
-            const double Uinv = e.aU / T + 1 / e.Ustar;
-            double T_F_inv = 1. / Tv - 1. / T - Uinv;
+            const double Uinv = e.aU * rT + 1 / e.Ustar;
+            double T_F_inv = rTv - rT - Uinv;
             gv = R_universal * (th / (ex(th * T_F_inv) - 1.) - TD / (ex(TD * T_F_inv) - 1.)) + e.nb * R_universal * TD;
-            T_F_inv = -e.aU / T - 1 / e.Ustar;
+            T_F_inv = -e.aU * rT - 1 / e.Ustar;
             ga = R_universal * (th / (ex(th * T_F_inv) - 1.) - TD / (ex(TD * T_F_inv) - 1.));
         }
     }
@@ -418,6 +420,7 @@ __global__ void __launch_bounds__(128) two_temperature_update_kernel(const TwoTA
             }
             if (!fail && phase == 1) {   // a subcycle's rate constants, relaxation times and exchange terms
                 const double logT = log(T), logTve = log(Tve), T13 = ex(logT * (-1. / 3.));
+                const double rT = 1.0 / T, rTve = 1.0 / Tve;
                 R.rate_constants(T, Tve, logT, logTve, kf, kb, gs, err);
                 double mol = 0.0;
                 // 1 / M_i = R_i / R_universal
@@ -438,7 +441,7 @@ __global__ void __launch_bounds__(128) two_temperature_update_kernel(const TwoTA
                         if (tk >= 0.0)
                             lt[k] = Y[e.p] * (R.g.e_ve(e.p, T, logT, err) - R.g.e_ve(e.p, Tve, logTve, err)) / tk;
                     } else {
-                        Reactor2T::coupling(e, T, Tve, ga[k], gv[k]);
+                        Reactor2T::coupling(e, rT, rTve, ga[k], gv[k]);
                     }
                 }
                 dtSave = dt_suggest;
