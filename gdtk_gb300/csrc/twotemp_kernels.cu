@@ -53,19 +53,56 @@ __device__ const double kExp2Table[GDTK_EXP2_TABLE_SIZE] = GDTK_EXP2_TABLE_INIT;
 __shared__ double s_exp2[GDTK_EXP2_TABLE_SIZE];
 __device__ __forceinline__ double ex(double x) { return gdtk_exp(x, s_exp2); }
 
+// NASA-9 Cp, h and s of cea_thermo_curves.d:55-137 (cea_thermo.h's segment choice and blending,
+// cea_coeffs) in Horner form with the reciprocal temperature rT = 1 / T: the reference's divisions by T,
+// T^2 and the small integers become multiplications.
+__device__ double cea_Cp_r(const MechView& m, int isp, double T, double rT, int& err) {
+    const double* s = m.sp(isp);
+    if (T < s[SP_TLOW]) return s[SP_CPLOW];
+    if (T > s[SP_THIGH]) return s[SP_CPHIGH];
+    double a[9];
+    if (!cea_coeffs(m, isp, T, a)) { err = CELL_CEA_RANGE; return 0.0; }
+    // Cp/R = a0/T^2 + a1/T + a2 + a3 T + a4 T^2 + a5 T^3 + a6 T^4
+    const double c = fma(rT, fma(a[0], rT, a[1]), a[2]) + T * fma(T, fma(T, fma(T, a[6], a[5]), a[4]), a[3]);
+    return s[SP_R] * c;
+}
+__device__ double cea_h_r(const MechView& m, int isp, double T, double rT, double logT, int& err) {
+    const double* s = m.sp(isp);
+    if (T < s[SP_TLOW]) return s[SP_HLOW] - s[SP_CPLOW] * (s[SP_TLOW] - T);
+    if (T > s[SP_THIGH]) return s[SP_HHIGH] + s[SP_CPHIGH] * (T - s[SP_THIGH]);
+    double a[9];
+    if (!cea_coeffs(m, isp, T, a)) { err = CELL_CEA_RANGE; return 0.0; }
+    // h/R = -a0/T + a1 ln T + a2 T + a3 T^2/2 + a4 T^3/3 + a5 T^4/4 + a6 T^5/5 + a7
+    const double poly = fma(T, fma(T, fma(T, a[6] * 0.2, a[5] * 0.25), a[4] * (1.0 / 3.0)), a[3] * 0.5);
+    const double h = fma(-a[0], rT, fma(a[1], logT, a[7])) + T * fma(T, poly, a[2]);
+    return s[SP_R] * h;
+}
+__device__ double cea_s_r(const MechView& m, int isp, double T, double rT, double logT, int& err) {
+    const double* s = m.sp(isp);
+    if (T < s[SP_TLOW]) return s[SP_SLOW] - s[SP_CPLOW] * log(s[SP_TLOW] / T);
+    if (T > s[SP_THIGH]) return s[SP_SHIGH] + s[SP_CPHIGH] * log(T / s[SP_THIGH]);
+    double a[9];
+    if (!cea_coeffs(m, isp, T, a)) { err = CELL_CEA_RANGE; return 0.0; }
+    // s/R = -a0/(2 T^2) - a1/T + a2 ln T + a3 T + a4 T^2/2 + a5 T^3/3 + a6 T^4/4 + a8
+    const double poly = fma(T, fma(T, a[6] * 0.25, a[5] * (1.0 / 3.0)), a[4] * 0.5);
+    const double v = fma(rT, fma(-0.5 * a[0], rT, -a[1]), fma(a[2], logT, a[8])) + T * fma(T, poly, a[3]);
+    return s[SP_R] * v;
+}
+
 struct Gas2T {
     MechView m;
     const Species2T* sp;
     int electron;
     __device__ double R(int i) const { return m.sp(i)[SP_R]; }
     // two_temperature_gas.d:427-445, 538-545, 558-590
-    __device__ double e_ve(int i, double Tve, double logTve, int& err) const {
+    // rTve = 1 / T_ve, logTve = ln T_ve
+    __device__ double e_ve(int i, double Tve, double rTve, double logTve, int& err) const {
         if (i == electron) return 1.5 * R(i) * Tve;
-        return cea_h(m, i, Tve, logTve, err) - sp[i].cp_tr * (Tve - T_REF) - sp[i].h_f;
+        return cea_h_r(m, i, Tve, rTve, logTve, err) - sp[i].cp_tr * (Tve - T_REF) - sp[i].h_f;
     }
-    __device__ double cv_ve(int i, double Tve, int& err) const {
+    __device__ double cv_ve(int i, double Tve, double rTve, int& err) const {
         if (i == electron) return 1.5 * R(i);
-        return cea_Cp(m, i, Tve, err) - sp[i].cp_tr;
+        return cea_Cp_r(m, i, Tve, rTve, err) - sp[i].cp_tr;
     }
     __device__ double e_tr(int i, double T) const {
         if (i == electron) return 0.0;
@@ -73,8 +110,9 @@ struct Gas2T {
     }
     __device__ double e_ve_mix(const double* Y, double Tve, int& err) const { return e_ve_mix(Y, Tve, log(Tve), err); }
     __device__ double e_ve_mix(const double* Y, double Tve, double lt, int& err) const {
+        const double r = 1.0 / Tve;
         double e = 0.0;
-        for (int i = 0; i < m.nsp; ++i) e += Y[i] * e_ve(i, Tve, lt, err);
+        for (int i = 0; i < m.nsp; ++i) e += Y[i] * e_ve(i, Tve, r, lt, err);
         return e;
     }
     __device__ double e_tr_mix(const double* Y, double T) const {
@@ -85,7 +123,8 @@ struct Gas2T {
     }
     __device__ double cv_ve_mix(const double* Y, double Tve, int& err) const {
         double c = 0.0;
-        for (int i = 0; i < m.nsp; ++i) c += Y[i] * cv_ve(i, Tve, err);
+        const double r = 1.0 / Tve;
+        for (int i = 0; i < m.nsp; ++i) c += Y[i] * cv_ve(i, Tve, r, err);
         return c;
     }
     __device__ double pressure(double rho, const double* Y, double T, double Tve) const {
@@ -196,7 +235,7 @@ struct Reactor2T {
         if (T > m.T_upper()) { T = m.T_upper(); logT = log(T); }
         const double lnPRT = LN_PATM_R - logT;   // ln(P_atm / R T)
         const double rT = 1.0 / T, rTve = 1.0 / Tve;
-        for (int i = 0; i < m.nsp; ++i) gs[i] = cea_h(m, i, T, logT, err) - T * cea_s(m, i, T, logT, err);
+        for (int i = 0; i < m.nsp; ++i) gs[i] = cea_h_r(m, i, T, rT, logT, err) - T * cea_s_r(m, i, T, rT, logT, err);
         for (int ir = 0; ir < m.nr; ++ir) {
             const int* r = m.rx(ir);
             const double* d = m.rxd(ir);
@@ -439,7 +478,7 @@ __global__ void __launch_bounds__(128) two_temperature_update_kernel(const TwoTA
                     if (e.kind == EEM_LANDAU_TELLER) {
                         const double tk = R.tau(e, T, T13, p, molef, numden);
                         if (tk >= 0.0)
-                            lt[k] = Y[e.p] * (R.g.e_ve(e.p, T, logT, err) - R.g.e_ve(e.p, Tve, logTve, err)) / tk;
+                            lt[k] = Y[e.p] * (R.g.e_ve(e.p, T, rT, logT, err) - R.g.e_ve(e.p, Tve, rTve, logTve, err)) / tk;
                     } else {
                         Reactor2T::coupling(e, rT, rTve, ga[k], gv[k]);
                     }
