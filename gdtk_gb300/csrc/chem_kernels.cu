@@ -34,6 +34,9 @@
 #ifndef GDTK_WARP_TU
 #define GDTK_WARP_TU 0
 #endif
+#if GDTK_WARP_TU
+#include "fast_exp.h"
+#endif
 
 namespace gdtk {
 namespace {
@@ -1023,22 +1026,37 @@ __device__ bool w_rkf_step(const WarpCtx& w, const double* y0, double h, double*
     return false;
 }
 
+// alpha = N(s) / D(s), s = p h: chemistry_update.d:599-604's rational function of r = 1 / (p h + eps) with
+// numerator and denominator multiplied by s^3 (no division by s, so the reference's eps, which guards its
+// 1 / (p h), changes nothing above s = 1e-34); s is capped at 1e50, where the ratio is 1 to double precision.
+__device__ __forceinline__ void w_alpha_nd(double s, double& N, double& D) {
+    s = fmin(s, 1.0e50);
+    N = fma(s, fma(s, 11.0 + s, 60.0), 180.0);
+    D = fma(s, s, N + 180.0);   // s^3 + 12 s^2 + 60 s + 360
+}
+
+// The alpha-QSS step of chemistry_update.d:533-655 with the predictor and corrector updates multiplied
+// through by D (y + h (N (q - q0) + D (q0 - p_bar y)) / (N h p_bar + D)), so that a species costs two
+// divisions instead of four, by the refined hardware reciprocal (fast_exp.h); sigma as the largest ratio
+// found by cross products, one division per lane.  Mathematically the reference's step, in rounding only
+// different.
 __device__ bool w_aqss_step(const WarpCtx& w, const double* y0, double h, double* yOut, double& hSuggest, double* q,
                             double* L, const double* kf, const double* kb, double* wf, double* wb, double* meff,
                             double* ext, int& nrhs) {
     const MechView& m = w.m;
     const int n = m.nsp;
     const double eps1 = m.eps1(), eps2 = m.eps2(), delta = m.delta();
-    double *q0 = ext, *p0 = ext + n, *yp0 = ext + 2 * n, *yp = ext + 3 * n;
+    double *q0 = ext, *p0 = ext + n, *yp0 = ext + 2 * n, *yp = ext + 3 * n;   // p0 holds p0 / 2
     w_split_rates(w, y0, q, L, kf, kb, wf, wb, meff);
     ++nrhs;
     for (int i = w.lane; i < n; i += 32) {
-        double y = y0[i];
-        double qi = q[i];
-        double pi = L[i] / (y + ZERO_EPS);
-        double a = alpha_of(pi, h);
-        double v = y + (h * (qi - pi * y)) / (1.0 + a * h * pi);
-        q0[i] = qi; p0[i] = pi; yp[i] = v; yp0[i] = v;
+        const double y = y0[i];
+        const double qi = q[i];
+        const double pi = gdtk_div_nr(L[i], y + ZERO_EPS);
+        double N, D;
+        w_alpha_nd(pi * h, N, D);
+        const double v = gdtk_add_div(y, h * (D * fma(-pi, y, qi)), fma(N, h * pi, D));
+        q0[i] = qi; p0[i] = 0.5 * pi; yp[i] = v; yp0[i] = v;
     }
     __syncwarp();
     bool converged = false;
@@ -1047,29 +1065,30 @@ __device__ bool w_aqss_step(const WarpCtx& w, const double* y0, double h, double
         ++nrhs;
         bool conv = true;
         for (int i = w.lane; i < n; i += 32) {
-            double y = y0[i];
-            double pp = L[i] / (yp[i] + ZERO_EPS);
-            double ab = alpha_of(pp, h);
-            double qt = ab * q[i] + (1 - ab) * q0[i];
-            double pb = 0.5 * (p0[i] + pp);
-            double yc = y + (h * (qt - pb * y)) / (1.0 + ab * h * pb);
+            const double y = y0[i];
+            const double pp = gdtk_div_nr(L[i], yp[i] + ZERO_EPS);
+            double N, D;
+            w_alpha_nd(pp * h, N, D);
+            const double pb = fma(0.5, pp, p0[i]);
+            const double yc = gdtk_add_div(y, h * fma(N, q[i] - q0[i], D * fma(-pb, y, q0[i])), fma(N, h * pb, D));
             yp[i] = yc;
             if (!(yc < ZERO_EPS)) {
-                double test = fabs(yc - yp0[i]);
-                if (test >= (eps1 * (yc + delta))) conv = false;
+                const double test = fabs(yc - yp0[i]);
+                if (test >= fma(eps1, yc, eps1 * delta)) conv = false;
             }
         }
         __syncwarp();
         converged = __all_sync(FULL_MASK, conv);
         if (converged) break;
     }
-    double sigma = 0.0;
+    double snum = 0.0, sden = 1.0;   // this lane's largest |yc - yp0| / (eps2 (yc + delta))
     for (int i = w.lane; i < n; i += 32) {
-        double yc = yp[i];
+        const double yc = yp[i];
         if (yc < ZERO_EPS) continue;
-        double test = fabs(yc - yp0[i]) / (eps2 * (yc + delta));
-        if (test > sigma) sigma = test;
+        const double num = fabs(yc - yp0[i]), den = fma(eps2, yc, eps2 * delta);
+        if (num * sden > snum * den) { snum = num; sden = den; }
     }
+    double sigma = snum / sden;
     for (int o = 16; o > 0; o >>= 1) {
         const double other = __shfl_xor_sync(FULL_MASK, sigma, o);
         if (other > sigma) sigma = other;
@@ -1078,10 +1097,10 @@ __device__ bool w_aqss_step(const WarpCtx& w, const double* y0, double h, double
     if (sigma <= 0.0) h_new = 10.0 * h;
     else {
         double x = sigma;
-        x = x - 0.5 * (x * x - sigma) / x;
-        x = x - 0.5 * (x * x - sigma) / x;
-        x = x - 0.5 * (x * x - sigma) / x;
-        h_new = h * ((1.0 / x) + 0.005);
+        x = x - 0.5 * gdtk_div_nr(x * x - sigma, x);
+        x = x - 0.5 * gdtk_div_nr(x * x - sigma, x);
+        x = x - 0.5 * gdtk_div_nr(x * x - sigma, x);
+        h_new = h * (gdtk_div_nr(1.0, x) + 0.005);
     }
     hSuggest = h_new;
     if (converged)
