@@ -110,7 +110,9 @@ struct Gas2T {
     }
     __device__ double e_ve_mix(const double* Y, double Tve, int& err) const { return e_ve_mix(Y, Tve, log(Tve), err); }
     __device__ double e_ve_mix(const double* Y, double Tve, double lt, int& err) const {
-        const double r = 1.0 / Tve;
+        return e_ve_mix(Y, Tve, 1.0 / Tve, lt, err);
+    }
+    __device__ double e_ve_mix(const double* Y, double Tve, double r, double lt, int& err) const {   // r = 1 / Tve
         double e = 0.0;
         for (int i = 0; i < m.nsp; ++i) e += Y[i] * e_ve(i, Tve, r, lt, err);
         return e;
@@ -121,9 +123,9 @@ struct Gas2T {
             if (i != electron) e += Y[i] * e_tr(i, T);
         return e;
     }
-    __device__ double cv_ve_mix(const double* Y, double Tve, int& err) const {
+    __device__ double cv_ve_mix(const double* Y, double Tve, int& err) const { return cv_ve_mix(Y, Tve, 1.0 / Tve, err); }
+    __device__ double cv_ve_mix(const double* Y, double Tve, double r, int& err) const {   // r = 1 / Tve
         double c = 0.0;
-        const double r = 1.0 / Tve;
         for (int i = 0; i < m.nsp; ++i) c += Y[i] * cv_ve(i, Tve, r, err);
         return c;
     }
@@ -144,23 +146,24 @@ struct Gas2T {
         }
         T = (u + sumA) / sumB;
         int err = 0;
-        double Tg = Tve, lg = log(Tve);
-        double f = e_ve_mix(Y, Tg, lg, err) - u_ve;
+        double Tg = Tve, lg = log(Tve), rg = 1.0 / Tve;   // T_ve's iterate, its log and reciprocal
+        double f = e_ve_mix(Y, Tg, rg, lg, err) - u_ve;
         if (fabs(f) >= 1e-5) {
             int count = 0;
             double dT = 0.0;
             for (int it = 0; it < 40; ++it) {
-                const double Cv = cv_ve_mix(Y, Tg, err);
+                const double Cv = cv_ve_mix(Y, Tg, rg, err);
                 dT = -f / Cv;
                 // ln(Tg + dT) = ln Tg + log1p(x), x = dT / Tg: the Taylor series to x^6 when |x| < 2^-10 (its
                 // truncation is below 2^-60 |x|), else a fresh log
-                const double x = dT / Tg;
+                const double x = dT * rg;
                 Tg += dT;
                 if (fabs(dT) < 1.0e-9) break;
                 lg = (fabs(x) < 0x1p-10)
                          ? lg + x * fma(x, fma(x, fma(x, fma(x, fma(x, -1.0 / 6.0, 0.2), -0.25), 1.0 / 3.0), -0.5), 1.0)
                          : log(Tg);
-                f = e_ve_mix(Y, Tg, lg, err) - u_ve;
+                rg = 1.0 / Tg;
+                f = e_ve_mix(Y, Tg, rg, lg, err) - u_ve;
                 ++count;
             }
             if (count == 40 && fabs(dT) > 1e-3) return false;
@@ -470,6 +473,7 @@ __global__ void __launch_bounds__(128) two_temperature_update_kernel(const TwoTA
                     molef[i] = n_i * rmol;
                     numden[i] = Avogadro * rho * n_i;
                 }
+                unsigned have_de = 0;   // species whose e_ve(T) - e_ve(T_ve) is in q (free until the attempt)
                 for (int k = 0; k < R.neem; ++k) {
                     const Eem2T& e = R.eem[k];
                     lt[k] = 0.0;
@@ -477,8 +481,13 @@ __global__ void __launch_bounds__(128) two_temperature_update_kernel(const TwoTA
                     gv[k] = 0.0;
                     if (e.kind == EEM_LANDAU_TELLER) {
                         const double tk = R.tau(e, T, T13, p, molef, numden);
-                        if (tk >= 0.0)
-                            lt[k] = Y[e.p] * (R.g.e_ve(e.p, T, rT, logT, err) - R.g.e_ve(e.p, Tve, rTve, logTve, err)) / tk;
+                        if (tk >= 0.0) {
+                            if (!((have_de >> e.p) & 1u)) {
+                                q[e.p] = R.g.e_ve(e.p, T, rT, logT, err) - R.g.e_ve(e.p, Tve, rTve, logTve, err);
+                                have_de |= 1u << e.p;
+                            }
+                            lt[k] = Y[e.p] * q[e.p] / tk;
+                        }
                     } else {
                         Reactor2T::coupling(e, rT, rTve, ga[k], gv[k]);
                     }
