@@ -20,6 +20,8 @@
 //   * ln T carried with each cell and updated by a log1p series in the Newton iteration, so that
 //     the library log (as costly as about 36 FMAs) runs only at cell start and after large steps;
 //   * divisions by Newton-Raphson refinement of the hardware reciprocal (fast_exp.h);
+//   * compares of doubles on their bit patterns, on the integer pipe (each with the IEEE result), and
+//     the curve-segment blend windows formed once on the host;
 //   * the NASA-9 enthalpy, heat capacity and G/RT in Horner form with coefficients scaled
 //     once on the host (cea_thermo_curves.d:55-137);
 //   * the alpha-QSS predictor/corrector with alpha = N(s)/D(s), s = p h + eps, folded into the
