@@ -750,7 +750,9 @@ __global__ void order_scatter(const float* key, int n, int* hist, int* order) {
 // and thermo read the packed mechanism from global memory (they need not fit in shared memory).
 // Every sum the reference takes over species in order (energies, gas constant, mass-fraction total,
 // RKF error norm) is taken by lane 0 in that order from per-species terms the lanes computed, and q, L
-// gather each species' terms in reaction order, so each value is the reference-order kernel's.
+// gather each species' terms in reaction order, the reference-order kernel's summation order.  This
+// translation unit is compiled with FMA contraction and its alpha-QSS step takes the two-division
+// form (w_aqss_step), so values agree with the reference-order kernel to rounding, not bitwise.
 // Minima and maxima (step estimate, sigma) are order-free.
 constexpr unsigned FULL_MASK = 0xffffffffu;
 
